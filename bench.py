@@ -1,0 +1,376 @@
+"""Benchmark of the GB300 force-evaluation path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload NAME]
+
+Prints ONE JSON line (rank 0).  A step is one integrator step of the
+workload (drift + force evaluation + kick) over the whole particle set.
+
+Workloads (seeded synthetic inputs -- grav_sim publishes no dataset):
+  plummer262144  -- equal-mass Plummer sphere, N = 262,144, G = M = a = 1,
+                    compensated-FP32 direct sum, eps = 0.01, leapfrog,
+                    dt = 1e-3 (the mixed-precision direct-sum workload).
+
+value      particle-steps/s over all ranks, state resident in HBM, device
+           time of K steps from CUDA events on the simulation's stream
+           (L2 flushed by a 256 MiB write before every timed step, outside
+           the step's events).
+e2e        the same metric through launch_simulation_python with host numpy
+           buffers: allocation, host->device copy of x, v, m, K steps and the
+           device->host copy of x, v inside the timed region.
+roofline   dominant kernel (k_direct_sum): 20 FLOP per pair interaction x
+           N(N-1) interactions per launch / mean launch time (CUDA events
+           around the kernel on its stream), against the FP32 FMA peak
+           measured on this GPU by the library's probe.
+cpu_baseline  grav_sim's symmetric pairwise loop (oracle restatement, one
+           thread -- the reference's pairwise has no OpenMP) timed on a
+           bounded slice of rows, extrapolated to a full step.
+Multi-GPU: replicas only (each rank runs the whole workload); value sums
+ranks; time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import importlib.util
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "gravity-simulator_gb300"
+METRIC = "particle-steps/s at ≤1e-3 median accel err vs FP64 sum; learned vs plain BH"
+
+
+def _module(name):
+    key = f"gsgpu_{name}"
+    if key in sys.modules:
+        return sys.modules[key]
+    spec = importlib.util.spec_from_file_location(key, PKG / f"{name}.py")
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[key] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+WORKLOADS = {
+    "plummer262144": dict(n=262144, seed=2, G=1.0, eps=0.01, dt=1e-3, integrator=4,
+                          method=101, flop_per_interaction=20),
+}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_baseline_pairwise(wk, x, m, target_s=12.0):
+    """Time the reference's pairwise loop (oracle restatement, 1 thread) on a
+    bounded slice of outer rows and extrapolate to one full leapfrog step."""
+    sys.path.insert(0, str(ROOT))
+    from oracle import restatement as orc
+    orc.load()
+    n = wk["n"]
+    rows = 64
+    _, pairs = orc.pairwise_slice(x, m, wk["G"], wk["eps"], 0, rows)
+    t0 = time.perf_counter()
+    _, pairs = orc.pairwise_slice(x, m, wk["G"], wk["eps"], 0, rows)
+    dt0 = time.perf_counter() - t0
+    rows = max(64, min(n, int(rows * target_s / max(dt0, 1e-3))))
+    t0 = time.perf_counter()
+    _, pairs = orc.pairwise_slice(x, m, wk["G"], wk["eps"], 0, rows)
+    el = time.perf_counter() - t0
+    pair_rate = pairs / el
+    t_eval = (n * (n - 1) / 2) / pair_rate
+    return {"value": n / t_eval, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+            "sample": f"grav_sim symmetric pairwise loop over outer rows 0..{rows} of N={n} "
+                      f"({pairs} pair evaluations, {el:.1f} s), extrapolated to N(N-1)/2 pairs "
+                      f"per step; kick/drift (O(N)) neglected",
+            "pair_evals_per_s": pair_rate}
+
+
+def accuracy_sample(a_gpu, x, m, G, eps, rows=1024, seed=0):
+    """Median / p99 relative error of GPU accelerations on sampled particles
+    against an FP64 direct sum (numpy, this process)."""
+    rng = np.random.default_rng(seed)
+    idx = rng.choice(x.shape[0], min(rows, x.shape[0]), replace=False)
+    errs = []
+    for i in idx:
+        d = x - x[i]
+        r2 = (d * d).sum(1) + eps * eps
+        r2[i] = np.inf
+        ai = G * (m[:, None] * d / (r2 * np.sqrt(r2))[:, None]).sum(0)
+        errs.append(np.linalg.norm(a_gpu[i] - ai) / np.linalg.norm(ai))
+    errs = np.array(errs)
+    return float(np.median(errs)), float(np.quantile(errs, 0.99))
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    g = _module("gsgpu")
+    wl = _module("workloads")
+    lib = g.load_c_lib()
+    wk = WORKLOADS[args.workload]
+    n = wk["n"]
+    x, v, m = wl.plummer(n, wk["seed"])
+
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.gsgpu_sim_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                                     ctypes.c_double, ctypes.POINTER(g.AccelerationParam),
+                                     ctypes.c_int, ctypes.c_double, ctypes.c_void_p]
+    lib.gsgpu_sim_upload.argtypes = [ctypes.c_void_p, dp, dp, dp]
+    lib.gsgpu_sim_run.argtypes = [ctypes.c_void_p, ctypes.c_int64]
+    lib.gsgpu_sim_download.argtypes = [ctypes.c_void_p, dp, dp]
+    lib.gsgpu_sim_set_force_timing.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.gsgpu_sim_force_timing.argtypes = [ctypes.c_void_p, dp, ctypes.POINTER(ctypes.c_int64)]
+    lib.gsgpu_sim_kernels_per_step.argtypes = [ctypes.c_void_p]
+    lib.gsgpu_sim_destroy.argtypes = [ctypes.c_void_p]
+    lib.gsgpu_sim_download_acceleration.argtypes = [ctypes.c_void_p, dp]
+    lib.gsgpu_measure_fma_peak.argtypes = [ctypes.c_int, dp, dp]
+
+    stream = torch.cuda.Stream()
+    sim = ctypes.c_void_p()
+    p = g.AccelerationParam(wk["method"], 1.0, wk["eps"], -1)
+    rc = lib.gsgpu_sim_create(ctypes.byref(sim), n, wk["G"], ctypes.byref(p), wk["integrator"],
+                              wk["dt"], ctypes.c_void_p(stream.cuda_stream))
+    assert rc == 0, rc
+    assert lib.gsgpu_sim_upload(sim, x.ctypes.data_as(dp), v.ctypes.data_as(dp),
+                                m.ctypes.data_as(dp)) == 0
+    # warm-up (includes the leapfrog half kick and graph capture)
+    assert lib.gsgpu_sim_run(sim, args.warmup) == 0
+    torch.cuda.synchronize()
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    lib.gsgpu_sim_set_force_timing(sim, 1)
+    clocks = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    wall0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)                 # evict L2 between steps (not timed)
+            starts[k].record(stream)
+            assert lib.gsgpu_sim_run(sim, 1) == 0
+            ends[k].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    if world > 1:
+        torch.distributed.barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = float(sum(step_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    force_ms = ctypes.c_double()
+    force_n = ctypes.c_int64()
+    lib.gsgpu_sim_force_timing(sim, ctypes.byref(force_ms), ctypes.byref(force_n))
+    kernels_per_step = lib.gsgpu_sim_kernels_per_step(sim)
+    lib.gsgpu_sim_set_force_timing(sim, 0)
+
+    value = world * n * args.steps / (total_ms / 1e3)
+    interactions = float(n) * (n - 1)
+    mean_force_ms = force_ms.value / max(force_n.value, 1)
+    achieved_tflops = wk["flop_per_interaction"] * interactions / (mean_force_ms / 1e3) / 1e12
+
+    peak = ctypes.c_double()
+    lib.gsgpu_measure_fma_peak(0, ctypes.byref(peak), None)
+
+    # accuracy of the forces of the last step
+    a_host = np.empty((n, 3))
+    torch.cuda.synchronize()
+    assert lib.gsgpu_sim_download_acceleration(sim, a_host.ctypes.data_as(dp)) == 0
+    xs = np.empty((n, 3))
+    vs = np.empty((n, 3))
+    lib.gsgpu_sim_download(sim, xs.ctypes.data_as(dp), vs.ctypes.data_as(dp))
+    med, p99 = accuracy_sample(a_host, xs, m, wk["G"], wk["eps"], rows=512)
+    lib.gsgpu_sim_destroy(sim)
+
+    # end to end through the reference-facing entry point
+    xe, ve, me = x.copy(), v.copy(), m.copy()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g.launch_simulation(lib, xe, ve, me, wk["G"], integrator=wk["integrator"], dt=wk["dt"],
+                        tf=wk["dt"] * args.steps * (1 - 1e-9), method=wk["method"],
+                        softening_length=wk["eps"])
+    e2e_s = time.perf_counter() - t0
+    e2e_val = world * n * args.steps / e2e_s
+
+    traffic = None
+    prof = ROOT / "profiles" / "k_direct_sum_plummer262144.md"
+    if prof.exists():
+        for ln in prof.read_text().splitlines():
+            if ln.startswith("traffic_bytes_per_launch:"):
+                traffic = float(ln.split(":", 1)[1])
+
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "particle-steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 pair terms (Kahan), f64 state",
+        "data": "synthetic (seeded Plummer sphere)",
+        "config": {"workload": f"{args.workload}: Plummer N={n}, compensated-FP32 direct sum, "
+                               f"eps={wk['eps']}, leapfrog dt={wk['dt']}",
+                   "parallelism": f"replicas x{world}", "l2": "flushed between steps (256 MiB write)",
+                   "interactions_per_s": value / n * interactions,
+                   "accuracy": {"median_rel_err": med, "p99_rel_err": p99,
+                                "sample": "512 particles vs FP64 direct sum"}},
+        "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak.value,
+                     "unit": "TFLOP/s", "frac": achieved_tflops / peak.value if peak.value else None,
+                     "traffic": traffic,
+                     "kernel": "k_direct_sum", "mean_launch_ms": mean_force_ms,
+                     "peak_source": "FP32 FMA probe on this GPU (gsgpu_measure_fma_peak), "
+                                    "not in MEASURED_PEAKS.json",
+                     "flop_per_interaction": wk["flop_per_interaction"]},
+        "e2e": {"value": e2e_val, "unit": "particle-steps/s",
+                "h2d_bytes_per_step": (7 * n * 8) / args.steps,
+                "d2h_bytes_per_step": (6 * n * 8) / args.steps,
+                "note": "one launch_simulation_python call of K steps; its copies and setup "
+                        "amortised over the K steps"},
+        "gpu_launches": args.steps * kernels_per_step,
+        "clocks": clk,
+        "wall_s": wall,
+    }
+    if rank == 0:
+        out["cpu_baseline"] = cpu_baseline_pairwise(wk, x, m)
+        print(json.dumps(out), flush=True)
+
+
+def run_reference(args, world, rank, local):
+    if rank != 0:
+        return
+    wl = _module("workloads")
+    wk = WORKLOADS[args.workload]
+    x, v, m = wl.plummer(wk["n"], wk["seed"])
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline_pairwise(wk, x, m, target_s=1.0)
+    for _ in range(args.steps):
+        vals.append(cpu_baseline_pairwise(wk, x, m, target_s=4.0))
+    value = statistics.median(r["value"] for r in vals)
+    out = {
+        "metric": METRIC, "value": value, "unit": "particle-steps/s", "impl": "reference",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * wk["n"] / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Plummer sphere)",
+        "config": {"workload": f"{args.workload}: Plummer N={wk['n']}, grav_sim pairwise "
+                               f"(acceleration.c:177-234) + leapfrog dt={wk['dt']}"},
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+                         "sample": vals[-1]["sample"]},
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="plummer262144", choices=sorted(WORKLOADS))
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank, local)
+        return
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
+    try:
+        run_ours(args, world, rank, local)
+    finally:
+        if world > 1:
+            import torch
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

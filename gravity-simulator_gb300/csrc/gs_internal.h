@@ -1,0 +1,159 @@
+// gs_internal.h -- internal declarations of libgrav_sim_gb300.
+//
+// Host code is C++ over the CUDA runtime; every public entry point is
+// `extern "C"` in include/grav_sim_gb300.h.  Errors travel as grav_sim's
+// ErrorStatus (src/error.h:31-36) with a heap traceback string; CUDA errors
+// and device status words are mapped onto the GRAV_* codes.
+#pragma once
+
+#include "../../include/grav_sim_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <memory>
+#include <vector>
+
+namespace gs {
+
+// Bits of the device status word written by kernels (never a trap).
+enum StatusBits : unsigned {
+    ST_WAIT_TIMEOUT = 1u,     // an mbarrier / flag wait ran out of time
+    ST_TREE_OVERFLOW = 2u,    // node capacity exceeded (host retries larger)
+    ST_STACK_OVERFLOW = 4u,   // walk stack deeper than the octree limit
+    ST_NONFINITE = 8u,        // NaN/Inf seen where the kernel checks
+    ST_BAD_KEY = 16u,         // octant digit out of range while building
+};
+
+// ---- errors ------------------------------------------------------------
+ErrorStatus ok();
+ErrorStatus raise_error(int code, const char *file, int line, const char *func,
+                        const char *fmt, ...)
+#if defined(__GNUC__)
+    __attribute__((format(printf, 5, 6)))
+#endif
+    ;
+ErrorStatus traceback(ErrorStatus st, const char *call, const char *file,
+                      int line, const char *func);
+ErrorStatus cuda_error(cudaError_t e, const char *what, const char *file,
+                       int line, const char *func);
+
+#define GS_RAISE(code, ...) gs::raise_error((code), __FILE__, __LINE__, __func__, __VA_ARGS__)
+#define GS_TRY(call)                                                           \
+    do {                                                                       \
+        ErrorStatus st_ = (call);                                              \
+        if (st_.return_code != GRAV_SUCCESS)                                   \
+            return gs::traceback(st_, #call, __FILE__, __LINE__, __func__);   \
+    } while (0)
+#define GS_CUDA(call)                                                          \
+    do {                                                                       \
+        cudaError_t e_ = (call);                                               \
+        if (e_ != cudaSuccess)                                                 \
+            return gs::cuda_error(e_, #call, __FILE__, __LINE__, __func__);   \
+    } while (0)
+
+// ---- device buffers ----------------------------------------------------
+// Grow-only device allocation owned by an engine or simulation.
+struct DBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DBuf() = default;
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    ~DBuf();
+    ErrorStatus reserve(size_t b);
+    void release();
+    template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+struct DeviceInfo {
+    int id = 0;
+    int sm_count = 0;
+    int cc_major = 0;
+    int cc_minor = 0;
+    char name[256] = {0};
+};
+// Queries the current device once per process; fails when no usable GPU.
+ErrorStatus device_info(const DeviceInfo **out);
+
+// Records CUDA events around the dominant kernel of each force evaluation.
+struct ForceTimer {
+    bool enabled = false;
+    std::vector<cudaEvent_t> ev;   // pairs (start, stop)
+    size_t used = 0;
+    double total_ms = 0.0;
+    int64_t launches = 0;
+    ErrorStatus begin(cudaStream_t s);
+    ErrorStatus end(cudaStream_t s);
+    ErrorStatus collect();   // after the stream is synchronised
+    ~ForceTimer();
+};
+
+// ---- force engines -----------------------------------------------------
+// One engine per (method, N); it owns its scratch memory.  compute() reads
+// FP64 positions and masses on the device and writes FP64 accelerations.
+class Engine {
+  public:
+    virtual ~Engine() {}
+    virtual ErrorStatus setup(int n, double G, const AccelerationParam &p) = 0;
+    virtual ErrorStatus compute(const double *d_x, const double *d_m, double *d_a,
+                                cudaStream_t s, ForceTimer *timer) = 0;
+    // kernels launched by one compute()
+    virtual int kernels_per_eval() const = 0;
+    // true when compute() never synchronises with the host (graph-capturable)
+    virtual bool capturable() const { return true; }
+    // device status word of the engine (may be null)
+    virtual ErrorStatus check_status(cudaStream_t s) { (void)s; return ok(); }
+    // FP64 origin subtracted before positions are rounded to FP32
+    virtual void set_frame_centre(double cx, double cy, double cz)
+    {
+        (void)cx; (void)cy; (void)cz;
+    }
+};
+
+bool is_gpu_method(int method);
+ErrorStatus make_engine(int method, std::unique_ptr<Engine> &out);
+
+std::unique_ptr<Engine> make_direct_engine(bool fp64_reference_order);
+std::unique_ptr<Engine> make_massless_engine();
+std::unique_ptr<Engine> make_barnes_hut_engine(bool compat);
+std::unique_ptr<Engine> make_learned_engine();
+
+// ---- integrator kernels (k_integrate.cu) -------------------------------
+void launch_comp_update(double *y, double *err, const double *d, double dt,
+                        double factor, int len, cudaStream_t s);
+void launch_euler_update(double *x, double *v, double *xe, double *ve,
+                         const double *a, double dt, int len, cudaStream_t s);
+void launch_plain_kick(double *v, const double *a, double coef, double dt, int len,
+                       cudaStream_t s);
+void launch_rk4_stage(double *x, double *v, const double *x0, const double *v0,
+                      const double *xk, const double *vk, double coef, double dt,
+                      int len, cudaStream_t s);
+void launch_rk4_final(double *x, double *v, const double *x0, const double *v0,
+                      double *xe, double *ve, const double *const *xk,
+                      const double *const *vk, double dt, int len, cudaStream_t s);
+void launch_rk_embedded_stage(double *out, const double *y0, const double *const *k,
+                              const double *coef, int nstage, double dt, int len,
+                              cudaStream_t s);
+void launch_rk_embedded_combine(double *y, double *err_comp, double *y1_tmp,
+                                double *err_est, const double *y0,
+                                const double *const *k, const double *w,
+                                const double *wd, int nstage, double dt, int len,
+                                cudaStream_t s);
+void launch_err_norm(const double *x0, const double *v0, const double *x1,
+                     const double *v1, const double *xerr, const double *verr,
+                     double abs_tol, double rel_tol, int len, double *d_sum,
+                     cudaStream_t s);
+
+// ---- diagnostics (k_diag.cu) -------------------------------------------
+ErrorStatus gpu_energy(const double *h_state7, int num_snapshots, int n, double G,
+                       double *h_energy);
+
+// ---- octree (k_octree.cu) ----------------------------------------------
+struct OctreeDevice;   // opaque; owned by a Barnes-Hut engine
+ErrorStatus octree_to_host(const AccelerationParam &p, const System *system,
+                           const double *box_center, double box_width,
+                           LinearOctree *out);
+
+}  // namespace gs

@@ -1,0 +1,653 @@
+// host_sim.cpp -- acceleration(), launch_simulation(), the Python entry point
+// and the device-resident simulation object.
+//
+// The integrator loops follow src/integrator.c (euler :281-454,
+// euler_cromer :456-628, rk4 :630-892, leapfrog :894-1121): the same step
+// count ceil(tf/dt), the same last-step dt clamp (all but rk4), t = steps*dt,
+// one is_exit check per step.  The state (x, v, compensation terms) stays in
+// HBM for the whole run; only the initial state goes host->device and the
+// final state device->host.  A step's kernels are captured once in a CUDA
+// graph and replayed; a clamped last step is launched directly.
+#include "gs_internal.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+namespace gs {
+namespace {
+
+struct Frame {
+    double c[3];
+};
+
+// Centre of the bounding box (the FP64 origin of FP32 pair terms).
+Frame bbox_centre(int n, const double *x)
+{
+    double lo[3] = {x[0], x[1], x[2]}, hi[3] = {x[0], x[1], x[2]};
+    for (int i = 1; i < n; ++i)
+        for (int k = 0; k < 3; ++k) {
+            const double q = x[3 * i + k];
+            lo[k] = q < lo[k] ? q : lo[k];
+            hi[k] = q > hi[k] ? q : hi[k];
+        }
+    Frame f;
+    for (int k = 0; k < 3; ++k) f.c[k] = 0.5 * (lo[k] + hi[k]);
+    return f;
+}
+
+// Per-thread state for host-buffer acceleration() calls.
+struct CallContext {
+    cudaStream_t stream = nullptr;
+    DBuf x, m, a;
+    std::unique_ptr<Engine> engine;
+    int method = -1, n = -1, leaf = 0;
+    double G = 0.0, eps = -1.0, theta = -1.0;
+    ~CallContext()
+    {
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+thread_local std::unique_ptr<CallContext> tl_call;
+
+ErrorStatus call_context(CallContext **out)
+{
+    if (!tl_call) {
+        const DeviceInfo *d = nullptr;
+        GS_TRY(device_info(&d));
+        std::unique_ptr<CallContext> c(new CallContext());
+        GS_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        tl_call = std::move(c);
+    }
+    *out = tl_call.get();
+    return ok();
+}
+
+ErrorStatus check_system(const System *s, bool need_v)
+{
+    if (!s) return GS_RAISE(GRAV_POINTER_ERROR, "System is NULL");
+    if (s->num_particles <= 0)
+        return GS_RAISE(GRAV_VALUE_ERROR, "Number of particles must be positive. Got: %d",
+                        s->num_particles);
+    if (!s->x) return GS_RAISE(GRAV_POINTER_ERROR, "System array x is NULL");
+    if (need_v && !s->v) return GS_RAISE(GRAV_POINTER_ERROR, "System array v is NULL");
+    if (!s->m) return GS_RAISE(GRAV_POINTER_ERROR, "System array m is NULL");
+    return ok();
+}
+
+}  // namespace
+
+// Host-buffer acceleration on the GPU (src/acceleration.c:131-153).
+ErrorStatus accel_host(double *a, const System *system, const AccelerationParam *param_in)
+{
+    if (!a) return GS_RAISE(GRAV_POINTER_ERROR, "Acceleration array is NULL");
+    if (!param_in) return GS_RAISE(GRAV_POINTER_ERROR, "Acceleration parameter pointer is NULL");
+    GS_TRY(check_system(system, false));
+    AccelerationParam p = *param_in;
+    GS_TRY(finalize_acceleration_param(&p));
+    CallContext *c = nullptr;
+    GS_TRY(call_context(&c));
+    const int n = system->num_particles;
+    const bool same = c->engine && c->method == p.method && c->n == n && c->G == system->G &&
+                      c->eps == p.softening_length && c->theta == p.opening_angle &&
+                      c->leaf == p.max_num_particles_per_leaf;
+    if (!same) {
+        c->engine.reset();
+        GS_TRY(make_engine(p.method, c->engine));
+        GS_TRY(c->engine->setup(n, system->G, p));
+        c->method = p.method;
+        c->n = n;
+        c->G = system->G;
+        c->eps = p.softening_length;
+        c->theta = p.opening_angle;
+        c->leaf = p.max_num_particles_per_leaf;
+    }
+    const Frame f = bbox_centre(n, system->x);
+    c->engine->set_frame_centre(f.c[0], f.c[1], f.c[2]);
+    GS_TRY(c->x.reserve((size_t)n * 3 * sizeof(double)));
+    GS_TRY(c->m.reserve((size_t)n * sizeof(double)));
+    GS_TRY(c->a.reserve((size_t)n * 3 * sizeof(double)));
+    GS_CUDA(cudaMemcpyAsync(c->x.p, system->x, (size_t)n * 3 * sizeof(double),
+                            cudaMemcpyHostToDevice, c->stream));
+    GS_CUDA(cudaMemcpyAsync(c->m.p, system->m, (size_t)n * sizeof(double), cudaMemcpyHostToDevice,
+                            c->stream));
+    GS_TRY(c->engine->compute(c->x.as<double>(), c->m.as<double>(), c->a.as<double>(), c->stream,
+                              nullptr));
+    GS_CUDA(cudaMemcpyAsync(a, c->a.p, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                            c->stream));
+    GS_CUDA(cudaStreamSynchronize(c->stream));
+    GS_TRY(c->engine->check_status(c->stream));
+    return ok();
+}
+
+}  // namespace gs
+
+// ---------------------------------------------------------------------------
+// Device-resident simulation.
+// ---------------------------------------------------------------------------
+using namespace gs;
+
+struct gsgpu_sim {
+    int n = 0;
+    double G = 1.0;
+    AccelerationParam p{};
+    int integrator = INTEGRATOR_LEAPFROG;
+    double dt = 0.0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    DBuf x, v, m, a, xe, ve, x0, v0, tmp;
+    DBuf rk[8];   // rk4: vk1..vk4, xk1..xk4
+    std::unique_ptr<Engine> engine;
+    bool primed = false;   // leapfrog: half kick applied
+    double last_dt = 0.0;  // dt of the most recent step
+    cudaGraphExec_t graph = nullptr;
+    double graph_dt = 0.0;
+    bool graph_failed = false;
+    ForceTimer timer;
+    int kernels_last = 0;
+
+    ~gsgpu_sim()
+    {
+        if (graph) cudaGraphExecDestroy(graph);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+
+    size_t bytes3() const { return (size_t)n * 3 * sizeof(double); }
+    int len() const { return 3 * n; }
+
+    ErrorStatus force(double *out)
+    {
+        GS_TRY(engine->compute(x.as<double>(), m.as<double>(), out, stream,
+                               timer.enabled ? &timer : nullptr));
+        return ok();
+    }
+
+    // Leapfrog initial acceleration and half kick (src/integrator.c:962-982).
+    ErrorStatus prime()
+    {
+        if (primed) return ok();
+        if (integrator == INTEGRATOR_LEAPFROG) {
+            GS_TRY(force(a.as<double>()));
+            launch_comp_update(v.as<double>(), ve.as<double>(), a.as<double>(), dt, 0.5, len(),
+                               stream);
+            GS_CUDA(cudaGetLastError());
+        }
+        primed = true;
+        return ok();
+    }
+
+    // Enqueue one step of size h.
+    ErrorStatus step(double h)
+    {
+        const int L = len();
+        switch (integrator) {
+        case INTEGRATOR_EULER:
+            GS_TRY(force(a.as<double>()));
+            launch_euler_update(x.as<double>(), v.as<double>(), xe.as<double>(), ve.as<double>(),
+                                a.as<double>(), h, L, stream);
+            break;
+        case INTEGRATOR_EULER_CROMER:
+            GS_TRY(force(a.as<double>()));
+            launch_comp_update(v.as<double>(), ve.as<double>(), a.as<double>(), h, 1.0, L, stream);
+            launch_comp_update(x.as<double>(), xe.as<double>(), v.as<double>(), h, 1.0, L, stream);
+            break;
+        case INTEGRATOR_RK4: {
+            double *vk[4], *xk[4];
+            for (int s = 0; s < 4; ++s) {
+                vk[s] = rk[s].as<double>();
+                xk[s] = rk[4 + s].as<double>();
+            }
+            GS_CUDA(cudaMemcpyAsync(x0.p, x.p, bytes3(), cudaMemcpyDeviceToDevice, stream));
+            GS_CUDA(cudaMemcpyAsync(v0.p, v.p, bytes3(), cudaMemcpyDeviceToDevice, stream));
+            const double coef[4] = {0.0, 0.5, 0.5, 1.0};
+            for (int s = 0; s < 4; ++s) {
+                if (s > 0)
+                    launch_rk4_stage(x.as<double>(), v.as<double>(), x0.as<double>(),
+                                     v0.as<double>(), xk[s - 1], vk[s - 1], coef[s], h, L, stream);
+                GS_TRY(force(vk[s]));
+                GS_CUDA(cudaMemcpyAsync(xk[s], v.p, bytes3(), cudaMemcpyDeviceToDevice, stream));
+            }
+            const double *cx[4] = {xk[0], xk[1], xk[2], xk[3]};
+            const double *cv[4] = {vk[0], vk[1], vk[2], vk[3]};
+            launch_rk4_final(x.as<double>(), v.as<double>(), x0.as<double>(), v0.as<double>(),
+                             xe.as<double>(), ve.as<double>(), cx, cv, h, L, stream);
+            GS_CUDA(cudaMemcpyAsync(a.p, vk[3], bytes3(), cudaMemcpyDeviceToDevice, stream));
+            break;
+        }
+        case INTEGRATOR_LEAPFROG:
+            launch_comp_update(x.as<double>(), xe.as<double>(), v.as<double>(), h, 1.0, L, stream);
+            GS_TRY(force(a.as<double>()));
+            launch_comp_update(v.as<double>(), ve.as<double>(), a.as<double>(), h, 1.0, L, stream);
+            break;
+        default:
+            return GS_RAISE(GRAV_NOT_IMPLEMENTED_ERROR, "integrator %d is not built", integrator);
+        }
+        GS_CUDA(cudaGetLastError());
+        last_dt = h;
+        return ok();
+    }
+
+    int kernels_per_step() const
+    {
+        const int f = engine->kernels_per_eval();
+        switch (integrator) {
+        case INTEGRATOR_EULER: return f + 1;
+        case INTEGRATOR_EULER_CROMER: return f + 2;
+        case INTEGRATOR_RK4: return 4 * f + 4;
+        case INTEGRATOR_LEAPFROG: return f + 2;
+        default: return f;
+        }
+    }
+
+    // One step through the CUDA graph when possible.
+    ErrorStatus step_graph(double h)
+    {
+        if (timer.enabled || graph_failed || !engine->capturable()) return step(h);
+        if (!graph || graph_dt != h) {
+            if (graph) {
+                cudaGraphExecDestroy(graph);
+                graph = nullptr;
+            }
+            cudaGraph_t g = nullptr;
+            GS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            ErrorStatus st = step(h);
+            cudaError_t e = cudaStreamEndCapture(stream, &g);
+            if (st.return_code != GRAV_SUCCESS) {
+                if (g) cudaGraphDestroy(g);
+                return st;
+            }
+            if (e != cudaSuccess || !g) {
+                (void)cudaGetLastError();
+                graph_failed = true;
+                return step(h);
+            }
+            e = cudaGraphInstantiate(&graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                (void)cudaGetLastError();
+                graph = nullptr;
+                graph_failed = true;
+                return step(h);
+            }
+            graph_dt = h;
+        }
+        GS_CUDA(cudaGraphLaunch(graph, stream));
+        last_dt = h;
+        return ok();
+    }
+};
+
+namespace gs {
+
+ErrorStatus sim_create(gsgpu_sim **out, int n, double G, const AccelerationParam *param,
+                       int integrator, double dt, cudaStream_t stream)
+{
+    if (!out) return GS_RAISE(GRAV_POINTER_ERROR, "output pointer is NULL");
+    if (!param) return GS_RAISE(GRAV_POINTER_ERROR, "Acceleration parameter pointer is NULL");
+    if (n <= 0) return GS_RAISE(GRAV_VALUE_ERROR, "Number of particles must be positive. Got: %d", n);
+    if (!(dt > 0.0)) return GS_RAISE(GRAV_VALUE_ERROR, "dt must be positive. Got: %g", dt);
+    const DeviceInfo *d = nullptr;
+    GS_TRY(device_info(&d));
+    std::unique_ptr<gsgpu_sim> s(new gsgpu_sim());
+    s->n = n;
+    s->G = G;
+    s->p = *param;
+    GS_TRY(finalize_acceleration_param(&s->p));
+    s->integrator = integrator;
+    s->dt = dt;
+    if (stream) {
+        s->stream = stream;
+    } else {
+        GS_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+        s->own_stream = true;
+    }
+    const size_t b3 = s->bytes3();
+    GS_TRY(s->x.reserve(b3));
+    GS_TRY(s->v.reserve(b3));
+    GS_TRY(s->a.reserve(b3));
+    GS_TRY(s->xe.reserve(b3));
+    GS_TRY(s->ve.reserve(b3));
+    GS_TRY(s->tmp.reserve(b3));
+    GS_TRY(s->m.reserve((size_t)n * sizeof(double)));
+    if (integrator == INTEGRATOR_RK4) {
+        GS_TRY(s->x0.reserve(b3));
+        GS_TRY(s->v0.reserve(b3));
+        for (int k = 0; k < 8; ++k) GS_TRY(s->rk[k].reserve(b3));
+    } else if (integrator != INTEGRATOR_EULER && integrator != INTEGRATOR_EULER_CROMER &&
+               integrator != INTEGRATOR_LEAPFROG) {
+        return GS_RAISE(GRAV_NOT_IMPLEMENTED_ERROR,
+                        "integrator %d has no GPU implementation in this library", integrator);
+    }
+    GS_TRY(make_engine(s->p.method, s->engine));
+    GS_TRY(s->engine->setup(n, G, s->p));
+    *out = s.release();
+    return ok();
+}
+
+ErrorStatus sim_upload(gsgpu_sim *s, const double *x, const double *v, const double *m)
+{
+    if (!s || !x || !v || !m) return GS_RAISE(GRAV_POINTER_ERROR, "NULL argument");
+    const Frame f = bbox_centre(s->n, x);
+    s->engine->set_frame_centre(f.c[0], f.c[1], f.c[2]);
+    GS_CUDA(cudaMemcpyAsync(s->x.p, x, s->bytes3(), cudaMemcpyHostToDevice, s->stream));
+    GS_CUDA(cudaMemcpyAsync(s->v.p, v, s->bytes3(), cudaMemcpyHostToDevice, s->stream));
+    GS_CUDA(cudaMemcpyAsync(s->m.p, m, (size_t)s->n * sizeof(double), cudaMemcpyHostToDevice,
+                            s->stream));
+    GS_CUDA(cudaMemsetAsync(s->xe.p, 0, s->bytes3(), s->stream));
+    GS_CUDA(cudaMemsetAsync(s->ve.p, 0, s->bytes3(), s->stream));
+    GS_CUDA(cudaMemsetAsync(s->a.p, 0, s->bytes3(), s->stream));
+    s->primed = false;
+    s->last_dt = s->dt;
+    if (s->graph) {
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    return ok();
+}
+
+ErrorStatus sim_download(gsgpu_sim *s, double *x, double *v)
+{
+    if (!s) return GS_RAISE(GRAV_POINTER_ERROR, "NULL simulation");
+    if (x)
+        GS_CUDA(cudaMemcpyAsync(x, s->x.p, s->bytes3(), cudaMemcpyDeviceToHost, s->stream));
+    if (v) {
+        if (s->integrator == INTEGRATOR_LEAPFROG && s->primed) {
+            // v_1 from v_{1+1/2} without touching the state (src/integrator.c:1088-1094)
+            GS_CUDA(cudaMemcpyAsync(s->tmp.p, s->v.p, s->bytes3(), cudaMemcpyDeviceToDevice,
+                                    s->stream));
+            launch_plain_kick(s->tmp.as<double>(), s->a.as<double>(), 0.5, s->last_dt, s->len(),
+                              s->stream);
+            GS_CUDA(cudaGetLastError());
+            GS_CUDA(cudaMemcpyAsync(v, s->tmp.p, s->bytes3(), cudaMemcpyDeviceToHost, s->stream));
+        } else {
+            GS_CUDA(cudaMemcpyAsync(v, s->v.p, s->bytes3(), cudaMemcpyDeviceToHost, s->stream));
+        }
+    }
+    GS_CUDA(cudaStreamSynchronize(s->stream));
+    GS_TRY(s->engine->check_status(s->stream));
+    return ok();
+}
+
+// Run the reference's step loop for time tf with an is_exit check per step.
+ErrorStatus sim_run_until(gsgpu_sim *s, double tf, SimulationStatus *status, const bool *is_exit)
+{
+    double dt = s->dt;
+    const int64_t total = (int64_t)std::ceil(tf / dt);
+    GS_TRY(s->prime());
+    double t = 0.0;
+    int64_t steps = 0;
+    const bool clamp = s->integrator != INTEGRATOR_RK4;
+    while (steps < total) {
+        if (clamp && t + dt > tf) dt = tf - t;
+        if (status) status->dt = dt;
+        GS_TRY(s->step_graph(dt));
+        ++steps;
+        t = (double)steps * dt;
+        if ((steps & 31) == 0) {
+            GS_CUDA(cudaStreamSynchronize(s->stream));
+            GS_TRY(s->engine->check_status(s->stream));
+        }
+        if (is_exit && *is_exit) break;
+    }
+    if (status) {
+        status->t = t;
+        status->num_steps = steps;
+    }
+    GS_CUDA(cudaStreamSynchronize(s->stream));
+    return ok();
+}
+
+}  // namespace gs
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+ErrorStatus acceleration(double *a, const System *system,
+                         const AccelerationParam *acceleration_param)
+{
+    return gs::accel_host(a, system, acceleration_param);
+}
+
+int gsgpu_sim_create(gsgpu_sim **out, int num_particles, double G,
+                     const AccelerationParam *acceleration_param, int integrator, double dt,
+                     void *stream)
+{
+    ErrorStatus st = gs::sim_create(out, num_particles, G, acceleration_param, integrator, dt,
+                                    static_cast<cudaStream_t>(stream));
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    return 0;
+}
+
+int gsgpu_sim_upload(gsgpu_sim *sim, const double *x, const double *v, const double *m)
+{
+    ErrorStatus st = gs::sim_upload(sim, x, v, m);
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    return 0;
+}
+
+int gsgpu_sim_run(gsgpu_sim *sim, int64_t num_steps)
+{
+    if (!sim) return GRAV_POINTER_ERROR;
+    ErrorStatus st = sim->prime();
+    for (int64_t k = 0; k < num_steps && st.return_code == GRAV_SUCCESS; ++k)
+        st = sim->step_graph(sim->dt);
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    sim->kernels_last = sim->kernels_per_step();
+    return 0;
+}
+
+int gsgpu_sim_download(gsgpu_sim *sim, double *x, double *v)
+{
+    ErrorStatus st = gs::sim_download(sim, x, v);
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    return 0;
+}
+
+const double *gsgpu_sim_device_acceleration(const gsgpu_sim *sim)
+{
+    return sim ? sim->a.as<double>() : nullptr;
+}
+
+int gsgpu_sim_download_acceleration(gsgpu_sim *sim, double *a)
+{
+    if (!sim || !a) return GRAV_POINTER_ERROR;
+    if (cudaMemcpyAsync(a, sim->a.p, sim->bytes3(), cudaMemcpyDeviceToHost, sim->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(sim->stream) != cudaSuccess) {
+        ErrorStatus st = GS_RAISE(GRAV_FAILURE, "acceleration download failed: %s",
+                                  cudaGetErrorString(cudaGetLastError()));
+        print_and_free_traceback(&st);
+        return GRAV_FAILURE;
+    }
+    return 0;
+}
+
+int gsgpu_sim_set_force_timing(gsgpu_sim *sim, int enable)
+{
+    if (!sim) return GRAV_POINTER_ERROR;
+    sim->timer.enabled = enable != 0;
+    sim->timer.total_ms = 0.0;
+    sim->timer.launches = 0;
+    sim->timer.used = 0;
+    return 0;
+}
+
+int gsgpu_sim_force_timing(const gsgpu_sim *sim, double *total_ms, int64_t *launches)
+{
+    if (!sim) return GRAV_POINTER_ERROR;
+    gsgpu_sim *s = const_cast<gsgpu_sim *>(sim);
+    ErrorStatus st = s->timer.collect();
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    if (total_ms) *total_ms = s->timer.total_ms;
+    if (launches) *launches = s->timer.launches;
+    return 0;
+}
+
+int gsgpu_sim_kernels_per_step(const gsgpu_sim *sim)
+{
+    return sim ? sim->kernels_per_step() : 0;
+}
+
+void gsgpu_sim_destroy(gsgpu_sim *sim) { delete sim; }
+
+// src/grav_sim.c:61-138
+ErrorStatus launch_simulation(System *system, IntegratorParam *integrator_param,
+                              AccelerationParam *acceleration_param, OutputParam *output_param,
+                              SimulationStatus *simulation_status, Settings *settings, double tf)
+{
+    // finalize_system (src/system.c:70-111)
+    if (!system) return GS_RAISE(GRAV_POINTER_ERROR, "System is NULL");
+    if (system->num_particles <= 0)
+        return GS_RAISE(GRAV_VALUE_ERROR, "Number of particles must be positive. Got: %d",
+                        system->num_particles);
+    if (!system->particle_ids)
+        return GS_RAISE(GRAV_POINTER_ERROR, "System array particle_ids is NULL");
+    if (!system->x) return GS_RAISE(GRAV_POINTER_ERROR, "System array x is NULL");
+    if (!system->v) return GS_RAISE(GRAV_POINTER_ERROR, "System array v is NULL");
+    if (!system->m) return GS_RAISE(GRAV_POINTER_ERROR, "System array m is NULL");
+    if (system->G <= 0.0)
+        return GS_RAISE(GRAV_VALUE_ERROR, "Gravitational constant G must be positive. Got: %g",
+                        system->G);
+    if (!acceleration_param)
+        return GS_RAISE(GRAV_POINTER_ERROR, "Acceleration parameter pointer is NULL");
+    GS_TRY(finalize_acceleration_param(acceleration_param));
+    // finalize_integration_param (src/integrator.c:131-189)
+    if (!integrator_param) return GS_RAISE(GRAV_POINTER_ERROR, "integration_param is NULL");
+    const int integ = integrator_param->integrator;
+    if (integ < INTEGRATOR_EULER || integ > INTEGRATOR_WHFAST)
+        return GS_RAISE(GRAV_VALUE_ERROR, "Unknown integrator. Got: %d", integ);
+    const bool fixed = integ == INTEGRATOR_EULER || integ == INTEGRATOR_EULER_CROMER ||
+                       integ == INTEGRATOR_RK4 || integ == INTEGRATOR_LEAPFROG ||
+                       integ == INTEGRATOR_WHFAST;
+    if (fixed && integrator_param->dt <= 0.0)
+        return GS_RAISE(GRAV_VALUE_ERROR, "dt must be positive. Got: %g", integrator_param->dt);
+    if (!fixed && integrator_param->tolerance <= 0.0)
+        return GS_RAISE(GRAV_VALUE_ERROR, "tolerance must be positive. Got: %g",
+                        integrator_param->tolerance);
+    // finalize_output_param (src/output.c:126-239): snapshots are not written
+    // by the GPU library.
+    if (!output_param) return GS_RAISE(GRAV_POINTER_ERROR, "output_param is NULL");
+    if (output_param->method != OUTPUT_METHOD_DISABLED) {
+        if (output_param->method == OUTPUT_METHOD_CSV || output_param->method == OUTPUT_METHOD_HDF5)
+            return GS_RAISE(GRAV_NOT_IMPLEMENTED_ERROR,
+                            "snapshot output (method %d) is not part of the GPU library; "
+                            "use output method 1 (disabled)", output_param->method);
+        return GS_RAISE(GRAV_VALUE_ERROR, "Unknown output method. Got: %d", output_param->method);
+    }
+    if (tf < 0.0) return GS_RAISE(GRAV_VALUE_ERROR, "tf must be non-negative. Got: %g", tf);
+    if (!settings) return GS_RAISE(GRAV_POINTER_ERROR, "settings is NULL");
+    if (!simulation_status) return GS_RAISE(GRAV_POINTER_ERROR, "simulation_status is NULL");
+
+    if (integ != INTEGRATOR_EULER && integ != INTEGRATOR_EULER_CROMER && integ != INTEGRATOR_RK4 &&
+        integ != INTEGRATOR_LEAPFROG)
+        return GS_RAISE(GRAV_NOT_IMPLEMENTED_ERROR,
+                        "integrator %d has no GPU implementation in this library", integ);
+
+    if (settings->verbose >= 2) {
+        const DeviceInfo *d = nullptr;
+        GS_TRY(device_info(&d));
+        std::printf("grav_sim GB300 library: %s (%d SMs), method %d, integrator %d, N = %d\n",
+                    d->name, d->sm_count, acceleration_param->method, integ,
+                    system->num_particles);
+    }
+    if (settings->verbose >= 1) std::fputs("Launching simulation...\n", stdout);
+
+    gsgpu_sim *raw = nullptr;
+    GS_TRY(gs::sim_create(&raw, system->num_particles, system->G, acceleration_param, integ,
+                          integrator_param->dt, nullptr));
+    std::unique_ptr<gsgpu_sim> sim(raw);
+    GS_TRY(gs::sim_upload(sim.get(), system->x, system->v, system->m));
+    simulation_status->t = 0.0;
+    simulation_status->dt = integrator_param->dt;
+    simulation_status->num_steps = 0;
+    GS_TRY(gs::sim_run_until(sim.get(), tf, simulation_status, settings->is_exit_ptr));
+    GS_TRY(gs::sim_download(sim.get(), system->x, system->v));
+    return ok();
+}
+
+// src/python_interface.c:94-193
+int launch_simulation_python(int32_t *num_particles, int32_t *particle_ids, double *x, double *v,
+                             double *m, int32_t **new_particle_ids_ptr, double **new_x_ptr,
+                             double **new_v_ptr, double **new_m_ptr, double G, int32_t integrator,
+                             double dt, double tolerance, double initial_dt,
+                             bool whfast_remove_invalid_particles, int32_t acceleration_method,
+                             double opening_angle, double softening_length,
+                             int32_t max_num_particles_per_leaf, int32_t output_method,
+                             char *output_dir, bool output_initial, double output_interval,
+                             int32_t coordinate_output_dtype, int32_t velocity_output_dtype,
+                             int32_t mass_output_dtype, int32_t verbose, bool enable_progress_bar,
+                             bool *is_exit_ptr, double tf)
+{
+    System system = get_new_system();
+    system.num_particles = num_particles ? *num_particles : 0;
+    system.particle_ids = particle_ids;
+    system.x = x;
+    system.v = v;
+    system.m = m;
+    system.G = G;
+
+    AccelerationParam ap = get_new_acceleration_param();
+    ap.method = acceleration_method;
+    ap.opening_angle = opening_angle;
+    ap.softening_length = softening_length;
+    ap.max_num_particles_per_leaf = max_num_particles_per_leaf;
+
+    IntegratorParam ip = get_new_integrator_param();
+    ip.integrator = integrator;
+    ip.dt = dt;
+    ip.tolerance = tolerance;
+    ip.initial_dt = initial_dt;
+    ip.whfast_remove_invalid_particles = whfast_remove_invalid_particles;
+
+    OutputParam op = get_new_output_param();
+    op.method = output_method;
+    op.output_dir = output_dir;
+    op.output_interval = output_interval;
+    op.output_initial = output_initial;
+    op.coordinate_output_dtype = coordinate_output_dtype;
+    op.velocity_output_dtype = velocity_output_dtype;
+    op.mass_output_dtype = mass_output_dtype;
+
+    SimulationStatus ss;
+    ss.t = 0.0;
+    ss.dt = dt;
+    ss.num_steps = 0;
+
+    Settings settings = get_new_settings();
+    settings.verbose = verbose;
+    settings.enable_progress_bar = enable_progress_bar;
+    if (is_exit_ptr) settings.is_exit_ptr = is_exit_ptr;
+
+    ErrorStatus st = launch_simulation(&system, &ip, &ap, &op, &ss, &settings, tf);
+    if (st.return_code != GRAV_SUCCESS) {
+        st = gs::traceback(st, "launch_simulation(&system, ...)", __FILE__, __LINE__, __func__);
+        print_and_free_traceback(&st);
+        return 1;
+    }
+    if (num_particles) *num_particles = system.num_particles;
+    if (new_particle_ids_ptr) *new_particle_ids_ptr = system.particle_ids;
+    if (new_x_ptr) *new_x_ptr = system.x;
+    if (new_v_ptr) *new_v_ptr = system.v;
+    if (new_m_ptr) *new_m_ptr = system.m;
+    return 0;
+}
+
+}  // extern "C"

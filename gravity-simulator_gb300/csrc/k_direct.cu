@@ -1,0 +1,378 @@
+// k_direct.cu -- direct-sum accelerations on sm_103a.
+//
+// Replaces acceleration_pairwise (src/acceleration.c:177-234).
+//
+// GRAV_GPU_PAIRWISE (compensated FP32):
+//   * positions and masses are packed once per evaluation into a float4
+//     array (x, y, z, m) relative to a fixed frame centre, padded to a whole
+//     number of 1024-particle tiles with massless far-away particles;
+//   * a CTA of 256 threads owns 1024 i-particles (4 per thread, register
+//     blocked) and one contiguous j-chunk; j-tiles of 1024 particles (16 KiB)
+//     stream through a 3-stage shared-memory ring filled by TMA bulk copies
+//     (cp.async.bulk + mbarrier complete_tx), read back as broadcast float4;
+//   * each pair term is 3 FADD + 3 FFMA + rsqrt + 3 FMUL + 3 FFMA in FP32;
+//     each tile's partial sum is added into a Kahan-compensated FP32
+//     accumulator;
+//   * the (i-tile, j-chunk) work units are sized so that their count is a
+//     whole number of waves of resident CTAs (152 SMs x occupancy); partial
+//     sums go to an FP64 scratch array [split][3][N] that a second kernel
+//     reduces in fixed order and scales by G.
+//
+// GRAV_GPU_PAIRWISE_FP64 (reference order): one thread per particle sums the
+// pair terms of all other particles in index order with every FP64 product,
+// sum, sqrt and quotient rounded separately -- the same operations as the
+// reference's symmetric loop applies to that particle, so the result equals
+// the reference's bit for bit where the reference is not FMA-contracted.
+#include "gs_internal.h"
+#include "gs_ptx.cuh"
+
+#include <algorithm>
+#include <cmath>
+
+namespace gs {
+
+constexpr int DS_THREADS = 256;
+constexpr int DS_IPT = 4;
+constexpr int DS_ITILE = DS_THREADS * DS_IPT;  // 1024
+constexpr int DS_JTILE = 1024;                 // 16 KiB of float4
+constexpr int DS_STAGES = 3;
+constexpr int DS_SMEM = DS_STAGES * DS_JTILE * 16;
+static_assert(DS_ITILE == DS_JTILE, "i and j tiles share the padding unit");
+
+// Padding particle: massless and far from everything (its pair terms are 0).
+constexpr float kPadPos = 1.0e15f;
+
+__global__ void k_pack_float4(const double *__restrict__ x, const double *__restrict__ m,
+                              int n, int n_pad, double cx, double cy, double cz,
+                              float4 *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_pad) return;
+    float4 p;
+    if (i < n) {
+        p.x = (float)(x[3 * i + 0] - cx);
+        p.y = (float)(x[3 * i + 1] - cy);
+        p.z = (float)(x[3 * i + 2] - cz);
+        p.w = (float)m[i];
+    } else {
+        p = make_float4(kPadPos, kPadPos, kPadPos, 0.0f);
+    }
+    out[i] = p;
+}
+
+template <bool SOFT>
+__device__ __forceinline__ void pair_term(const float4 q, float xi, float yi, float zi,
+                                          float eps2, float &ax, float &ay, float &az)
+{
+    const float dx = q.x - xi;
+    const float dy = q.y - yi;
+    const float dz = q.z - zi;
+    float r2 = fmaf(dx, dx, eps2);
+    r2 = fmaf(dy, dy, r2);
+    r2 = fmaf(dz, dz, r2);
+    float ri = rsqrt_approx(r2);
+    if (!SOFT) ri = (r2 > 0.0f) ? ri : 0.0f;   // self term without softening
+    const float mr = q.w * ri;
+    const float ri2 = ri * ri;
+    const float s = mr * ri2;
+    ax = fmaf(dx, s, ax);
+    ay = fmaf(dy, s, ay);
+    az = fmaf(dz, s, az);
+}
+
+template <bool SOFT>
+__global__ void __launch_bounds__(DS_THREADS, 2)
+k_direct_sum(const float4 *__restrict__ pj, int n_pad, int i_tiles, int jt_per_chunk,
+             int jt_total, float eps2, double *__restrict__ partial,
+             unsigned *__restrict__ status)
+{
+    extern __shared__ __align__(128) unsigned char ds_smem[];
+    float4 *sj = reinterpret_cast<float4 *>(ds_smem);
+    __shared__ __align__(8) uint64_t full_bar[DS_STAGES];
+
+    const int itile = blockIdx.x % i_tiles;
+    const int split = blockIdx.x / i_tiles;
+    const int jt0 = split * jt_per_chunk;
+    const int ntiles = min(jt_total, jt0 + jt_per_chunk) - jt0;
+
+    float xi[DS_IPT], yi[DS_IPT], zi[DS_IPT];
+#pragma unroll
+    for (int k = 0; k < DS_IPT; ++k) {
+        const float4 p = pj[itile * DS_ITILE + k * DS_THREADS + threadIdx.x];
+        xi[k] = p.x;
+        yi[k] = p.y;
+        zi[k] = p.z;
+    }
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < DS_STAGES; ++s) mbar_init(&full_bar[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int pre = min(DS_STAGES, ntiles);
+        for (int s = 0; s < pre; ++s) {
+            mbar_expect_tx(&full_bar[s], DS_JTILE * 16);
+            bulk_g2s(sj + s * DS_JTILE, pj + (size_t)(jt0 + s) * DS_JTILE, DS_JTILE * 16,
+                     &full_bar[s]);
+        }
+    }
+
+    float sx[DS_IPT], sy[DS_IPT], sz[DS_IPT], cx[DS_IPT], cy[DS_IPT], cz[DS_IPT];
+#pragma unroll
+    for (int k = 0; k < DS_IPT; ++k) {
+        sx[k] = sy[k] = sz[k] = 0.0f;
+        cx[k] = cy[k] = cz[k] = 0.0f;
+    }
+
+    int issued = min(DS_STAGES, ntiles);
+    int t = 0;
+    for (; t < ntiles; ++t) {
+        const int st = t % DS_STAGES;
+        const unsigned parity = (unsigned)(t / DS_STAGES) & 1u;
+        const bool ready = mbar_wait(&full_bar[st], parity);
+        if (!__syncthreads_and(ready)) {
+            if (threadIdx.x == 0) atomicOr(status, ST_WAIT_TIMEOUT);
+            break;
+        }
+        const float4 *tile = sj + st * DS_JTILE;
+        float ax[DS_IPT], ay[DS_IPT], az[DS_IPT];
+#pragma unroll
+        for (int k = 0; k < DS_IPT; ++k) ax[k] = ay[k] = az[k] = 0.0f;
+#pragma unroll 8
+        for (int j = 0; j < DS_JTILE; ++j) {
+            const float4 q = tile[j];
+#pragma unroll
+            for (int k = 0; k < DS_IPT; ++k)
+                pair_term<SOFT>(q, xi[k], yi[k], zi[k], eps2, ax[k], ay[k], az[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < DS_IPT; ++k) {
+            kahan_add(sx[k], cx[k], ax[k]);
+            kahan_add(sy[k], cy[k], ay[k]);
+            kahan_add(sz[k], cz[k], az[k]);
+        }
+        __syncthreads();   // every thread is done with stage st
+        if (threadIdx.x == 0 && issued < ntiles) {
+            mbar_expect_tx(&full_bar[st], DS_JTILE * 16);
+            bulk_g2s(sj + st * DS_JTILE, pj + (size_t)(jt0 + issued) * DS_JTILE, DS_JTILE * 16,
+                     &full_bar[st]);
+            ++issued;
+        }
+    }
+    if (t < ntiles) {
+        // Timed out: let copies already issued land before the CTA exits.
+        if (threadIdx.x == 0) {
+            for (int u = t; u < issued; ++u)
+                (void)mbar_wait(&full_bar[u % DS_STAGES], (unsigned)(u / DS_STAGES) & 1u);
+        }
+        __syncthreads();
+        return;
+    }
+
+    const size_t plane = (size_t)n_pad;
+    double *out = partial + (size_t)split * 3 * plane;
+#pragma unroll
+    for (int k = 0; k < DS_IPT; ++k) {
+        const size_t i = (size_t)itile * DS_ITILE + k * DS_THREADS + threadIdx.x;
+        out[0 * plane + i] = (double)sx[k] - (double)cx[k];
+        out[1 * plane + i] = (double)sy[k] - (double)cy[k];
+        out[2 * plane + i] = (double)sz[k] - (double)cz[k];
+    }
+}
+
+// a_i = G * sum_s partial[s][.][i], summed in split order.
+__global__ void k_reduce_splits(const double *__restrict__ partial, int splits, int n,
+                                int n_pad, double G, double *__restrict__ a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t plane = (size_t)n_pad;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int s = 0; s < splits; ++s) {
+        const double *p = partial + (size_t)s * 3 * plane;
+        s0 += p[i];
+        s1 += p[plane + i];
+        s2 += p[2 * plane + i];
+    }
+    a[3 * i + 0] = G * s0;
+    a[3 * i + 1] = G * s1;
+    a[3 * i + 2] = G * s2;
+}
+
+// FP64, reference operation order (see file comment).
+constexpr int RF_THREADS = 128;
+
+__global__ void __launch_bounds__(RF_THREADS)
+k_direct_fp64_reference_order(const double *__restrict__ x, const double *__restrict__ m,
+                              int n, double G, double eps2, double *__restrict__ a)
+{
+    __shared__ double sx[RF_THREADS], sy[RF_THREADS], sz[RF_THREADS], sm[RF_THREADS];
+    const int i = blockIdx.x * RF_THREADS + threadIdx.x;
+    double x0 = 0.0, x1 = 0.0, x2 = 0.0;
+    if (i < n) {
+        x0 = x[3 * i + 0];
+        x1 = x[3 * i + 1];
+        x2 = x[3 * i + 2];
+    }
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    for (int base = 0; base < n; base += RF_THREADS) {
+        const int j = base + threadIdx.x;
+        if (j < n) {
+            sx[threadIdx.x] = x[3 * j + 0];
+            sy[threadIdx.x] = x[3 * j + 1];
+            sz[threadIdx.x] = x[3 * j + 2];
+            sm[threadIdx.x] = m[j];
+        }
+        __syncthreads();
+        const int cnt = min(RF_THREADS, n - base);
+        if (i < n) {
+            for (int jj = 0; jj < cnt; ++jj) {
+                if (base + jj == i) continue;
+                const double r0 = __dsub_rn(x0, sx[jj]);
+                const double r1 = __dsub_rn(x1, sy[jj]);
+                const double r2 = __dsub_rn(x2, sz[jj]);
+                const double s = __dadd_rn(
+                    __dadd_rn(__dadd_rn(__dmul_rn(r0, r0), __dmul_rn(r1, r1)), __dmul_rn(r2, r2)),
+                    eps2);
+                const double rn = __dsqrt_rn(s);
+                const double t = __ddiv_rn(G, __dmul_rn(__dmul_rn(rn, rn), rn));
+                const double mj = sm[jj];
+                a0 = __dsub_rn(a0, __dmul_rn(__dmul_rn(t, r0), mj));
+                a1 = __dsub_rn(a1, __dmul_rn(__dmul_rn(t, r1), mj));
+                a2 = __dsub_rn(a2, __dmul_rn(__dmul_rn(t, r2), mj));
+            }
+        }
+        __syncthreads();
+    }
+    if (i < n) {
+        a[3 * i + 0] = a0;
+        a[3 * i + 1] = a1;
+        a[3 * i + 2] = a2;
+    }
+}
+
+// ------------------------------------------------------------------------
+namespace {
+
+class DirectEngine final : public Engine {
+  public:
+    explicit DirectEngine(bool fp64) : fp64_(fp64) {}
+
+    ErrorStatus setup(int n, double G, const AccelerationParam &p) override
+    {
+        n_ = n;
+        G_ = G;
+        eps_ = p.softening_length;
+        if (fp64_) return ok();
+        const DeviceInfo *dev = nullptr;
+        GS_TRY(device_info(&dev));
+        n_pad_ = ((n + DS_JTILE - 1) / DS_JTILE) * DS_JTILE;
+        i_tiles_ = n_pad_ / DS_ITILE;
+        jt_total_ = n_pad_ / DS_JTILE;
+        int per_sm = 0;
+        GS_CUDA(cudaFuncSetAttribute(k_direct_sum<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     DS_SMEM));
+        GS_CUDA(cudaFuncSetAttribute(k_direct_sum<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     DS_SMEM));
+        GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_direct_sum<true>, DS_THREADS,
+                                                              DS_SMEM));
+        per_sm = std::max(per_sm, 1);
+        const long slots = (long)dev->sm_count * per_sm;
+        // Choose the j-split count: minimise (waves x tiles per unit) with a
+        // small per-unit overhead, so the last wave is (nearly) full.
+        int best_s = 1;
+        double best_cost = 1e300;
+        const int max_s = std::min(jt_total_, 64);
+        for (int s = 1; s <= max_s; ++s) {
+            const int chunk = (jt_total_ + s - 1) / s;
+            const int used = (jt_total_ + chunk - 1) / chunk;   // non-empty splits
+            const long units = (long)i_tiles_ * used;
+            const long waves = (units + slots - 1) / slots;
+            const double cost = (double)waves * (chunk + 0.25);
+            if (cost < best_cost - 1e-9) {
+                best_cost = cost;
+                best_s = used;
+                jt_per_chunk_ = chunk;
+            }
+        }
+        splits_ = best_s;
+        GS_TRY(pj_.reserve((size_t)n_pad_ * sizeof(float4)));
+        GS_TRY(partial_.reserve((size_t)splits_ * 3 * n_pad_ * sizeof(double)));
+        GS_TRY(status_.reserve(sizeof(unsigned)));
+        GS_CUDA(cudaMemset(status_.p, 0, sizeof(unsigned)));
+        return ok();
+    }
+
+    void set_frame_centre(double cx, double cy, double cz) override
+    {
+        c_[0] = cx;
+        c_[1] = cy;
+        c_[2] = cz;
+    }
+
+    ErrorStatus compute(const double *d_x, const double *d_m, double *d_a, cudaStream_t s,
+                        ForceTimer *timer) override
+    {
+        if (fp64_) {
+            const int grid = (n_ + RF_THREADS - 1) / RF_THREADS;
+            if (timer) GS_TRY(timer->begin(s));
+            k_direct_fp64_reference_order<<<grid, RF_THREADS, 0, s>>>(d_x, d_m, n_, G_, eps_ * eps_,
+                                                                      d_a);
+            GS_CUDA(cudaGetLastError());
+            if (timer) GS_TRY(timer->end(s));
+            return ok();
+        }
+        k_pack_float4<<<(n_pad_ + 255) / 256, 256, 0, s>>>(d_x, d_m, n_, n_pad_, c_[0], c_[1], c_[2],
+                                                           pj_.as<float4>());
+        GS_CUDA(cudaGetLastError());
+        const float eps2 = (float)(eps_ * eps_);
+        const int grid = i_tiles_ * splits_;
+        if (timer) GS_TRY(timer->begin(s));
+        if (eps2 > 0.0f)
+            k_direct_sum<true><<<grid, DS_THREADS, DS_SMEM, s>>>(
+                pj_.as<float4>(), n_pad_, i_tiles_, jt_per_chunk_, jt_total_, eps2,
+                partial_.as<double>(), status_.as<unsigned>());
+        else
+            k_direct_sum<false><<<grid, DS_THREADS, DS_SMEM, s>>>(
+                pj_.as<float4>(), n_pad_, i_tiles_, jt_per_chunk_, jt_total_, eps2,
+                partial_.as<double>(), status_.as<unsigned>());
+        GS_CUDA(cudaGetLastError());
+        if (timer) GS_TRY(timer->end(s));
+        k_reduce_splits<<<(n_ + 255) / 256, 256, 0, s>>>(partial_.as<double>(), splits_, n_, n_pad_,
+                                                         G_, d_a);
+        GS_CUDA(cudaGetLastError());
+        return ok();
+    }
+
+    int kernels_per_eval() const override { return fp64_ ? 1 : 3; }
+
+    ErrorStatus check_status(cudaStream_t s) override
+    {
+        if (fp64_) return ok();
+        unsigned h = 0;
+        GS_CUDA(cudaMemcpyAsync(&h, status_.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+        GS_CUDA(cudaStreamSynchronize(s));
+        if (h & ST_WAIT_TIMEOUT)
+            return GS_RAISE(GRAV_FAILURE, "direct-sum kernel: shared-memory tile wait timed out");
+        return ok();
+    }
+
+    int splits() const { return splits_; }
+
+  private:
+    bool fp64_;
+    int n_ = 0, n_pad_ = 0, i_tiles_ = 0, jt_total_ = 0, jt_per_chunk_ = 1, splits_ = 1;
+    double G_ = 1.0, eps_ = 0.0;
+    double c_[3] = {0.0, 0.0, 0.0};
+    DBuf pj_, partial_, status_;
+};
+
+}  // namespace
+
+std::unique_ptr<Engine> make_direct_engine(bool fp64_reference_order)
+{
+    return std::unique_ptr<Engine>(new DirectEngine(fp64_reference_order));
+}
+
+}  // namespace gs

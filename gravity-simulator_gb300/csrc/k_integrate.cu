@@ -1,0 +1,163 @@
+// k_integrate.cu -- FP64 kick / drift / stage updates of grav_sim's
+// fixed-step integrators (src/integrator.c), one thread per array element.
+//
+// Every FP64 operation is an explicitly rounded intrinsic (__dmul_rn,
+// __dadd_rn, __dsub_rn) in the order of the reference's C expressions, so
+// no product is fused into an FMA: given the same accelerations the state
+// after a step equals the reference's bit for bit (the reference compiled
+// without FMA contraction).  These kernels are HBM-bound: a compensated
+// update reads y, err, d and writes y, err (40 B per element).
+#include "gs_internal.h"
+#include "gs_ptx.cuh"
+
+namespace gs {
+
+namespace {
+constexpr int TPB = 256;
+inline int blocks(int len) { return (len + TPB - 1) / TPB; }
+}  // namespace
+
+// y, err updated with d * (factor * dt) ... see launch_comp_update.
+__global__ void k_comp_update(double *__restrict__ y, double *__restrict__ err,
+                              const double *__restrict__ d, double h, int len)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= len) return;
+    double yy = y[k], ee = err[k];
+    comp_update(yy, ee, d[k], h);
+    y[k] = yy;
+    err[k] = ee;
+}
+
+// Leapfrog initial half kick: err += (0.5 * a) * dt (src/integrator.c:978).
+__global__ void k_comp_update_scaled(double *__restrict__ y, double *__restrict__ err,
+                                     const double *__restrict__ d, double coef, double dt,
+                                     int len)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= len) return;
+    const double y0 = y[k];
+    double e = __dadd_rn(err[k], __dmul_rn(__dmul_rn(coef, d[k]), dt));
+    const double yn = __dadd_rn(y0, e);
+    e = __dadd_rn(e, __dsub_rn(y0, yn));
+    y[k] = yn;
+    err[k] = e;
+}
+
+void launch_comp_update(double *y, double *err, const double *d, double dt, double factor,
+                        int len, cudaStream_t s)
+{
+    if (len <= 0) return;
+    if (factor == 1.0)
+        k_comp_update<<<blocks(len), TPB, 0, s>>>(y, err, d, dt, len);
+    else
+        k_comp_update_scaled<<<blocks(len), TPB, 0, s>>>(y, err, d, factor, dt, len);
+}
+
+// src/integrator.c:382-395 (euler): both updates use the state at the start
+// of the step.
+__global__ void k_euler(double *__restrict__ x, double *__restrict__ v, double *__restrict__ xe,
+                        double *__restrict__ ve, const double *__restrict__ a, double dt, int len)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= len) return;
+    const double x0 = x[k], v0 = v[k];
+    double ex = __dadd_rn(xe[k], __dmul_rn(v0, dt));
+    double ev = __dadd_rn(ve[k], __dmul_rn(a[k], dt));
+    const double xn = __dadd_rn(x0, ex);
+    const double vn = __dadd_rn(v0, ev);
+    ex = __dadd_rn(ex, __dsub_rn(x0, xn));
+    ev = __dadd_rn(ev, __dsub_rn(v0, vn));
+    x[k] = xn;
+    v[k] = vn;
+    xe[k] = ex;
+    ve[k] = ev;
+}
+
+void launch_euler_update(double *x, double *v, double *xe, double *ve, const double *a, double dt,
+                         int len, cudaStream_t s)
+{
+    if (len <= 0) return;
+    k_euler<<<blocks(len), TPB, 0, s>>>(x, v, xe, ve, a, dt, len);
+}
+
+// v -= (coef * a) * dt, uncompensated (src/integrator.c:1088-1094).
+__global__ void k_plain_kick(double *__restrict__ v, const double *__restrict__ a, double coef,
+                             double dt, int len)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= len) return;
+    v[k] = __dsub_rn(v[k], __dmul_rn(__dmul_rn(coef, a[k]), dt));
+}
+
+void launch_plain_kick(double *v, const double *a, double coef, double dt, int len, cudaStream_t s)
+{
+    if (len <= 0) return;
+    k_plain_kick<<<blocks(len), TPB, 0, s>>>(v, a, coef, dt, len);
+}
+
+// src/integrator.c:746-793: x = x0 + (coef * xk) * dt, v likewise.
+__global__ void k_rk4_stage(double *__restrict__ x, double *__restrict__ v,
+                            const double *__restrict__ x0, const double *__restrict__ v0,
+                            const double *__restrict__ xk, const double *__restrict__ vk,
+                            double coef, double dt, int len)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= len) return;
+    x[k] = __dadd_rn(x0[k], __dmul_rn(__dmul_rn(coef, xk[k]), dt));
+    v[k] = __dadd_rn(v0[k], __dmul_rn(__dmul_rn(coef, vk[k]), dt));
+}
+
+void launch_rk4_stage(double *x, double *v, const double *x0, const double *v0, const double *xk,
+                      const double *vk, double coef, double dt, int len, cudaStream_t s)
+{
+    if (len <= 0) return;
+    k_rk4_stage<<<blocks(len), TPB, 0, s>>>(x, v, x0, v0, xk, vk, coef, dt, len);
+}
+
+// src/integrator.c:806-819: compensated combine of the four stages,
+// increment = ((((k1 + 2 k2) + 2 k3) + k4) * dt) / 6.
+__device__ __forceinline__ double rk4_incr(double k1, double k2, double k3, double k4, double dt)
+{
+    const double s = __dadd_rn(__dadd_rn(__dadd_rn(k1, __dmul_rn(2.0, k2)), __dmul_rn(2.0, k3)), k4);
+    return __ddiv_rn(__dmul_rn(s, dt), 6.0);
+}
+
+struct Rk4Ptrs {
+    const double *xk[4];
+    const double *vk[4];
+};
+
+__global__ void k_rk4_final(double *__restrict__ x, double *__restrict__ v,
+                            const double *__restrict__ x0, const double *__restrict__ v0,
+                            double *__restrict__ xe, double *__restrict__ ve, Rk4Ptrs p, double dt,
+                            int len)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= len) return;
+    double ev = __dadd_rn(ve[k], rk4_incr(p.vk[0][k], p.vk[1][k], p.vk[2][k], p.vk[3][k], dt));
+    double ex = __dadd_rn(xe[k], rk4_incr(p.xk[0][k], p.xk[1][k], p.xk[2][k], p.xk[3][k], dt));
+    const double vn = __dadd_rn(v0[k], ev);
+    const double xn = __dadd_rn(x0[k], ex);
+    ev = __dadd_rn(ev, __dsub_rn(v0[k], vn));
+    ex = __dadd_rn(ex, __dsub_rn(x0[k], xn));
+    v[k] = vn;
+    x[k] = xn;
+    ve[k] = ev;
+    xe[k] = ex;
+}
+
+void launch_rk4_final(double *x, double *v, const double *x0, const double *v0, double *xe,
+                      double *ve, const double *const *xk, const double *const *vk, double dt,
+                      int len, cudaStream_t s)
+{
+    if (len <= 0) return;
+    Rk4Ptrs p;
+    for (int i = 0; i < 4; ++i) {
+        p.xk[i] = xk[i];
+        p.vk[i] = vk[i];
+    }
+    k_rk4_final<<<blocks(len), TPB, 0, s>>>(x, v, x0, v0, xe, ve, p, dt, len);
+}
+
+}  // namespace gs

@@ -1,0 +1,271 @@
+"""ctypes mirror of grav_sim's C interface for the GB300 library.
+
+The product is ``libgrav_sim_gb300.so`` (built in this directory by
+``__graft_entry__.build()``).  It exports the same C symbols and struct
+layouts as grav_sim's ``libgrav_sim`` (src/acceleration.h:20-26,
+src/system.h:12-20, src/error.h:31-36, src/linear_octree.h:20-57,
+src/python_interface.c:94-304), so this module mirrors grav_sim's own
+ctypes layer (grav_sim/utils.py:12-58, grav_sim/simulator.py:22-143):
+the same struct definitions, the same restypes, the same
+thread + ``is_exit`` launch and the same ``RuntimeError`` on failure.
+
+The GPU path is chosen through ``AccelerationParam.method`` with the GPU
+method codes below; the CPU codes 1-3 of the reference are rejected by this
+library with GRAV_VALUE_ERROR (there is no CPU fallback).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+import time
+from pathlib import Path
+from queue import Queue
+from typing import Optional
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_NAME = "libgrav_sim_gb300.so"
+
+# grav_sim error codes (src/error.h:14-21)
+GRAV_SUCCESS = 0
+GRAV_VALUE_ERROR = 2
+GRAV_POINTER_ERROR = 3
+GRAV_MEMORY_ERROR = 4
+GRAV_OS_ERROR = 5
+GRAV_NOT_IMPLEMENTED_ERROR = 6
+
+# Reference CPU method codes (src/acceleration.h:16-18); rejected here.
+ACCELERATION_METHOD_PAIRWISE = 1
+ACCELERATION_METHOD_MASSLESS = 2
+ACCELERATION_METHOD_BARNES_HUT = 3
+
+# GPU method codes of this library (same AccelerationParam.method field).
+METHOD_GPU_PAIRWISE = 101          # compensated-FP32 direct sum
+METHOD_GPU_MASSLESS = 102          # FP64 massive/massless direct sum
+METHOD_GPU_BARNES_HUT = 103        # FP32 walk, true leaf multipoles
+METHOD_GPU_BH_LEARNED = 104        # theta-cheap walk + learned MLP residual
+METHOD_GPU_PAIRWISE_FP64 = 111     # FP64 direct sum in the reference's order
+METHOD_GPU_BARNES_HUT_COMPAT = 113 # FP32 walk reproducing the reference's tree quirks
+
+# Integrator codes (src/integrator.h:17-26)
+INTEGRATOR_EULER = 1
+INTEGRATOR_EULER_CROMER = 2
+INTEGRATOR_RK4 = 3
+INTEGRATOR_LEAPFROG = 4
+INTEGRATOR_RKF45 = 5
+INTEGRATOR_DOPRI = 6
+INTEGRATOR_DVERK = 7
+INTEGRATOR_RKF78 = 8
+INTEGRATOR_IAS15 = 9
+INTEGRATOR_WHFAST = 10
+
+# Output codes (src/output.h:13-19)
+OUTPUT_METHOD_DISABLED = 1
+OUTPUT_METHOD_CSV = 2
+OUTPUT_METHOD_HDF5 = 3
+OUTPUT_DTYPE_FLOAT = 1
+OUTPUT_DTYPE_DOUBLE = 2
+
+c_double_p = ctypes.POINTER(ctypes.c_double)
+c_int_p = ctypes.POINTER(ctypes.c_int32)
+c_int64_p = ctypes.POINTER(ctypes.c_int64)
+
+
+class System(ctypes.Structure):
+    """src/system.h:12-20"""
+    _fields_ = [
+        ("num_particles", ctypes.c_int),
+        ("particle_ids", c_int_p),
+        ("x", c_double_p),
+        ("v", c_double_p),
+        ("m", c_double_p),
+        ("G", ctypes.c_double),
+    ]
+
+
+class AccelerationParam(ctypes.Structure):
+    """src/acceleration.h:20-26"""
+    _fields_ = [
+        ("method", ctypes.c_int),
+        ("opening_angle", ctypes.c_double),
+        ("softening_length", ctypes.c_double),
+        ("max_num_particles_per_leaf", ctypes.c_int),
+    ]
+
+
+class ErrorStatus(ctypes.Structure):
+    """src/error.h:31-36 (returned by value)"""
+    _fields_ = [
+        ("return_code", ctypes.c_int),
+        ("traceback", ctypes.c_void_p),
+        ("traceback_code_", ctypes.c_int),
+    ]
+
+
+class LinearOctree(ctypes.Structure):
+    """src/linear_octree.h:20-57"""
+    _fields_ = [
+        ("box_width", ctypes.c_double),
+        ("num_internal_nodes", ctypes.c_int),
+        ("particle_morton_indices_deepest_level", c_int64_p),
+        ("sorted_indices", c_int_p),
+        ("tree_num_particles", c_int_p),
+        ("tree_num_internal_children", c_int_p),
+        ("tree_first_particle_sorted_idx", c_int_p),
+        ("tree_first_internal_children_idx", c_int_p),
+        ("tree_mass", c_double_p),
+        ("tree_center_of_mass_x", c_double_p),
+        ("tree_center_of_mass_y", c_double_p),
+        ("tree_center_of_mass_z", c_double_p),
+    ]
+
+
+def library_path() -> Path:
+    return HERE / LIB_NAME
+
+
+def load_c_lib(c_lib_path: Optional[str | os.PathLike] = None) -> ctypes.CDLL:
+    """Load the GB300 library (grav_sim/utils.py:12-35).  Fails loudly when
+    the CUDA library has not been built: there is no fallback."""
+    path = Path(c_lib_path) if c_lib_path else library_path()
+    if not path.exists():
+        raise FileNotFoundError(
+            f"{path} not found: build it with __graft_entry__.build()")
+    lib = ctypes.CDLL(str(path))
+    initialize_c_lib(lib)
+    return lib
+
+
+def initialize_c_lib(lib: ctypes.CDLL) -> None:
+    """Restypes of grav_sim/utils.py:38-58 plus the entry points used here."""
+    lib.launch_simulation_python.restype = ctypes.c_int
+    lib.compute_energy_python.restype = None
+    lib.compute_linear_momentum_python.restype = None
+    lib.compute_angular_momentum_python.restype = None
+    lib.load_built_in_system_python.restype = ctypes.c_int
+    lib.free_memory_int32.restype = None
+    lib.free_memory_double.restype = None
+    lib.keplerian_to_cartesian_python.restype = None
+    lib.acceleration.restype = ErrorStatus
+    lib.acceleration.argtypes = [c_double_p, ctypes.POINTER(System),
+                                 ctypes.POINTER(AccelerationParam)]
+    lib.free_traceback.restype = None
+    lib.free_traceback.argtypes = [ctypes.POINTER(ErrorStatus)]
+    if hasattr(lib, "construct_octree"):
+        lib.construct_octree.restype = ErrorStatus
+        lib.construct_octree.argtypes = [
+            ctypes.POINTER(LinearOctree), ctypes.POINTER(System),
+            ctypes.POINTER(AccelerationParam), c_double_p, ctypes.c_double]
+        lib.free_linear_octree.restype = None
+        lib.free_linear_octree.argtypes = [ctypes.POINTER(LinearOctree)]
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(c_double_p)
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(c_int_p)
+
+
+def make_system(x: np.ndarray, m: np.ndarray, G: float,
+                v: Optional[np.ndarray] = None,
+                ids: Optional[np.ndarray] = None):
+    """Wrap numpy arrays (C-contiguous float64 / int32) as a System without a
+    copy, like src/python_interface.c:127-134.  Returns (system, keepalive)."""
+    n = int(m.shape[0])
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(n, 3)
+    m = np.ascontiguousarray(m, dtype=np.float64)
+    v = np.zeros_like(x) if v is None else np.ascontiguousarray(v, dtype=np.float64).reshape(n, 3)
+    ids = np.arange(n, dtype=np.int32) if ids is None else np.ascontiguousarray(ids, dtype=np.int32)
+    s = System(n, _ip(ids), _dp(x), _dp(v), _dp(m), float(G))
+    return s, (x, v, m, ids)
+
+
+def take_traceback(lib: ctypes.CDLL, st: ErrorStatus) -> str:
+    text = ""
+    if st.traceback:
+        text = ctypes.string_at(st.traceback).decode("utf-8", "replace")
+        lib.free_traceback(ctypes.byref(st))
+    return text
+
+
+class GravError(RuntimeError):
+    def __init__(self, code: int, traceback: str):
+        super().__init__(f"grav_sim error {code}: {traceback}")
+        self.code = code
+        self.traceback = traceback
+
+
+def acceleration(lib: ctypes.CDLL, x: np.ndarray, m: np.ndarray, G: float,
+                 method: int, opening_angle: float = 1.0,
+                 softening_length: float = 0.0,
+                 max_num_particles_per_leaf: int = -1) -> np.ndarray:
+    """Call ``acceleration(a, system, param)`` (src/acceleration.h:53-57)
+    with host buffers and return a as an (N, 3) array."""
+    system, keep = make_system(x, m, G)
+    a = np.empty((system.num_particles, 3), dtype=np.float64)
+    p = AccelerationParam(int(method), float(opening_angle),
+                          float(softening_length), int(max_num_particles_per_leaf))
+    st = lib.acceleration(_dp(a), ctypes.byref(system), ctypes.byref(p))
+    if st.return_code != GRAV_SUCCESS:
+        raise GravError(st.return_code, take_traceback(lib, st))
+    del keep
+    return a
+
+
+def launch_simulation(lib: ctypes.CDLL, x: np.ndarray, v: np.ndarray,
+                      m: np.ndarray, G: float, *, integrator: int, dt: float,
+                      tf: float, method: int, opening_angle: float = 1.0,
+                      softening_length: float = 0.0,
+                      max_num_particles_per_leaf: int = -1,
+                      tolerance: float = -1.0, initial_dt: float = -1.0,
+                      whfast_remove_invalid_particles: bool = True,
+                      ids: Optional[np.ndarray] = None, verbose: int = 0,
+                      is_exit: Optional[ctypes.c_bool] = None):
+    """Mirror of Simulator.launch_simulation (grav_sim/simulator.py:22-143):
+    runs ``launch_simulation_python`` on a worker thread, raises
+    RuntimeError when it returns non-zero, and returns the (possibly
+    shrunk) (ids, x, v, m) arrays.  x and v are updated in place."""
+    n = int(m.shape[0])
+    num = ctypes.c_int32(n)
+    ids = np.arange(n, dtype=np.int32) if ids is None else ids
+    new_ids = c_int_p()
+    new_x = c_double_p()
+    new_v = c_double_p()
+    new_m = c_double_p()
+    flag = ctypes.c_bool(False) if is_exit is None else is_exit
+    q: Queue = Queue()
+
+    def run(*args):
+        q.put(lib.launch_simulation_python(*args))
+
+    args = (
+        ctypes.byref(num), _ip(ids), _dp(x), _dp(v), _dp(m),
+        ctypes.byref(new_ids), ctypes.byref(new_x), ctypes.byref(new_v),
+        ctypes.byref(new_m), ctypes.c_double(G), ctypes.c_int32(integrator),
+        ctypes.c_double(dt), ctypes.c_double(tolerance),
+        ctypes.c_double(initial_dt), ctypes.c_bool(whfast_remove_invalid_particles),
+        ctypes.c_int32(method), ctypes.c_double(opening_angle),
+        ctypes.c_double(softening_length), ctypes.c_int32(max_num_particles_per_leaf),
+        ctypes.c_int32(OUTPUT_METHOD_DISABLED), b"", ctypes.c_bool(False),
+        ctypes.c_double(0.0), ctypes.c_int32(OUTPUT_DTYPE_DOUBLE),
+        ctypes.c_int32(OUTPUT_DTYPE_DOUBLE), ctypes.c_int32(OUTPUT_DTYPE_DOUBLE),
+        ctypes.c_int32(verbose), ctypes.c_bool(False), ctypes.byref(flag),
+        ctypes.c_double(tf),
+    )
+    th = threading.Thread(target=run, args=args)
+    th.start()
+    while th.is_alive():
+        time.sleep(0.002)
+    th.join()
+    ret = q.get()
+    if ret != 0:
+        raise RuntimeError("Simulation failed. Please check the C library traceback.")
+    k = num.value
+    return (np.ctypeslib.as_array(new_ids, shape=(k,)),
+            np.ctypeslib.as_array(new_x, shape=(k, 3)),
+            np.ctypeslib.as_array(new_v, shape=(k, 3)),
+            np.ctypeslib.as_array(new_m, shape=(k,)))

@@ -1,0 +1,278 @@
+/*
+ * grav_sim_gb300.h -- C ABI of the GB300-native force-evaluation library.
+ *
+ * libgrav_sim_gb300.so is a drop-in for grav_sim's libgrav_sim on the
+ * force-evaluation hot path.  Struct layouts and entry points below are the
+ * ones grav_sim declares (each cites the declaration it replaces); the GPU
+ * path is selected through the existing AccelerationParam.method field with
+ * the GRAV_GPU_* codes.  The reference's CPU codes (1-3) are rejected with
+ * GRAV_VALUE_ERROR: this library has no CPU fallback.
+ *
+ * All signatures use plain C types and pointers.  Host pointers are host
+ * memory; entry points named gsgpu_* take device pointers where stated.
+ */
+#ifndef GRAV_SIM_GB300_H
+#define GRAV_SIM_GB300_H
+
+#include <stdbool.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error handling (src/error.h:14-36) ---------------------------- */
+#define GRAV_UNKNOWN_ERROR -1
+#define GRAV_SUCCESS 0
+#define GRAV_FAILURE 1
+#define GRAV_VALUE_ERROR 2
+#define GRAV_POINTER_ERROR 3
+#define GRAV_MEMORY_ERROR 4
+#define GRAV_OS_ERROR 5
+#define GRAV_NOT_IMPLEMENTED_ERROR 6
+
+typedef struct ErrorStatus {
+    int return_code;
+    char *traceback;
+    int traceback_code_;
+} ErrorStatus;
+
+/* src/error.h:105 */
+ErrorStatus make_success_error_status(void);
+/* src/error.h:195 */
+void free_traceback(ErrorStatus *error_status);
+/* src/error.h:202 */
+void print_and_free_traceback(ErrorStatus *error_status);
+
+/* ---- system / parameters (src/system.h:12-20, src/acceleration.h:16-26,
+ *      src/common.h:29-56, src/settings.h:11-16) --------------------- */
+typedef struct System {
+    int num_particles;
+    int *particle_ids;
+    double *x;
+    double *v;
+    double *m;
+    double G;
+} System;
+
+#define ACCELERATION_METHOD_PAIRWISE 1
+#define ACCELERATION_METHOD_MASSLESS 2
+#define ACCELERATION_METHOD_BARNES_HUT 3
+
+/* GPU method codes (new; same AccelerationParam.method field). */
+#define GRAV_GPU_PAIRWISE 101           /* compensated-FP32 direct sum */
+#define GRAV_GPU_MASSLESS 102           /* FP64 massive/massless direct sum */
+#define GRAV_GPU_BARNES_HUT 103         /* FP32 walk, true leaf multipoles */
+#define GRAV_GPU_BH_LEARNED 104         /* theta-cheap walk + learned residual */
+#define GRAV_GPU_PAIRWISE_FP64 111      /* FP64 direct sum, reference order */
+#define GRAV_GPU_BARNES_HUT_COMPAT 113  /* FP32 walk, reference tree quirks */
+
+typedef struct AccelerationParam {
+    int method;
+    double opening_angle;
+    double softening_length;
+    int max_num_particles_per_leaf;
+} AccelerationParam;
+
+typedef struct IntegratorParam {
+    int integrator;
+    double dt;
+    double tolerance;
+    double initial_dt;
+    bool whfast_remove_invalid_particles;
+} IntegratorParam;
+
+#define INTEGRATOR_EULER 1
+#define INTEGRATOR_EULER_CROMER 2
+#define INTEGRATOR_RK4 3
+#define INTEGRATOR_LEAPFROG 4
+#define INTEGRATOR_RKF45 5
+#define INTEGRATOR_DOPRI 6
+#define INTEGRATOR_DVERK 7
+#define INTEGRATOR_RKF78 8
+#define INTEGRATOR_IAS15 9
+#define INTEGRATOR_WHFAST 10
+
+typedef struct OutputParam {
+    int method;
+    char *output_dir;
+    bool output_initial;
+    double output_interval;
+    int coordinate_output_dtype;
+    int velocity_output_dtype;
+    int mass_output_dtype;
+    int output_count_;
+} OutputParam;
+
+#define OUTPUT_METHOD_DISABLED 1
+#define OUTPUT_METHOD_CSV 2
+#define OUTPUT_METHOD_HDF5 3
+
+typedef struct SimulationStatus {
+    double t;
+    double dt;
+    int64_t num_steps;
+} SimulationStatus;
+
+typedef struct Settings {
+    int verbose;
+    bool enable_progress_bar;
+    bool *is_exit_ptr;
+} Settings;
+
+/* src/system.h:28 */
+System get_new_system(void);
+/* src/acceleration.h:33 */
+AccelerationParam get_new_acceleration_param(void);
+/* src/acceleration.h:40-42 */
+ErrorStatus finalize_acceleration_param(AccelerationParam *acceleration_param);
+/* src/integrator.h (get_new_integrator_param, integrator.c:119-129) */
+IntegratorParam get_new_integrator_param(void);
+/* src/output.h (get_new_output_param) */
+OutputParam get_new_output_param(void);
+/* src/settings.h:23 */
+Settings get_new_settings(void);
+
+/* ---- acceleration (src/acceleration.h:53-70) ----------------------- */
+
+/* src/acceleration.h:53-57.  a: host array [3N]; system->x, ->m host.  The
+ * GPU method in acceleration_param->method computes a on the GPU. */
+ErrorStatus acceleration(double *a, const System *system,
+                         const AccelerationParam *acceleration_param);
+
+/* src/acceleration.h:66-70.  GPU Barnes-Hut: GRAV_GPU_BARNES_HUT_COMPAT
+ * when acceleration_param->method is the reference's BARNES_HUT code or
+ * GRAV_GPU_BARNES_HUT_COMPAT, else GRAV_GPU_BARNES_HUT. */
+ErrorStatus acceleration_barnes_hut(double *a, const System *system,
+                                    const AccelerationParam *acceleration_param);
+
+/* ---- linear octree (src/linear_octree.h:14-101) -------------------- */
+#define MORTON_MAX_LEVEL 21
+
+typedef struct LinearOctree {
+    double box_width;
+    int num_internal_nodes;
+    int64_t *particle_morton_indices_deepest_level;
+    int *sorted_indices;
+    int *tree_num_particles;
+    int *tree_num_internal_children;
+    int *tree_first_particle_sorted_idx;
+    int *tree_first_internal_children_idx;
+    double *tree_mass;
+    double *tree_center_of_mass_x;
+    double *tree_center_of_mass_y;
+    double *tree_center_of_mass_z;
+} LinearOctree;
+
+/* src/linear_octree.h:64 */
+LinearOctree get_new_linear_octree(void);
+/* src/linear_octree.h:75-81.  Built on the GPU (bounding box, Morton keys,
+ * radix sort, tree, multipoles) and copied into host arrays that
+ * free_linear_octree releases.  Node numbering, keys, order and internal
+ * node mass / centre of mass are those of the reference. */
+ErrorStatus construct_octree(LinearOctree *octree, const System *system,
+                             const AccelerationParam *acceleration_param,
+                             const double *box_center, double box_width);
+/* src/linear_octree.h:88 */
+void free_linear_octree(LinearOctree *octree);
+/* src/linear_octree.h:97-101 */
+bool linear_octree_check_if_included(int64_t morton_index_i,
+                                     int64_t morton_index_j, int level);
+
+/* ---- simulation (src/grav_sim.h:47-55, src/python_interface.c:8-304) */
+
+/* src/grav_sim.h:47-55 */
+ErrorStatus launch_simulation(System *system, IntegratorParam *integrator_param,
+                              AccelerationParam *acceleration_param,
+                              OutputParam *output_param,
+                              SimulationStatus *simulation_status,
+                              Settings *settings, double tf);
+
+/* src/python_interface.c:94-125 */
+int launch_simulation_python(
+    int32_t *num_particles, int32_t *particle_ids, double *x, double *v,
+    double *m, int32_t **new_particle_ids_ptr, double **new_x_ptr,
+    double **new_v_ptr, double **new_m_ptr, double G, int32_t integrator,
+    double dt, double tolerance, double initial_dt,
+    bool whfast_remove_invalid_particles, int32_t acceleration_method,
+    double opening_angle, double softening_length,
+    int32_t max_num_particles_per_leaf, int32_t output_method,
+    char *output_dir, bool output_initial, double output_interval,
+    int32_t coordinate_output_dtype, int32_t velocity_output_dtype,
+    int32_t mass_output_dtype, int32_t verbose, bool enable_progress_bar,
+    bool *is_exit_ptr, double tf);
+
+/* src/python_interface.c:195-201 (FP64 on the GPU) */
+void compute_energy_python(double *energy, double G, const double *sol_state,
+                           int32_t num_snapshots, int32_t num_particles);
+/* src/python_interface.c:245-250 */
+void compute_linear_momentum_python(double *linear_momentum,
+                                    const double *sol_state,
+                                    int32_t num_snapshots, int32_t num_particles);
+/* src/python_interface.c:270-275 */
+void compute_angular_momentum_python(double *angular_momentum,
+                                     const double *sol_state,
+                                     int32_t num_snapshots, int32_t num_particles);
+/* src/utils.h (compute_energy, src/utils.c:27) */
+double compute_energy(const System *system);
+
+/* src/python_interface.c:8-16 */
+void free_memory_int32(int32_t *ptr);
+void free_memory_double(double *ptr);
+/* src/python_interface.c:18-26.  Built-in initial conditions are host
+ * bookkeeping outside this library's scope: returns GRAV_NOT_IMPLEMENTED_ERROR. */
+int32_t load_built_in_system_python(const char *system_name, int *num_particles_ptr,
+                                    int32_t **particle_ids_ptr, double **x_ptr,
+                                    double **v_ptr, double **m_ptr, double *G_ptr);
+/* src/python_interface.c:55-70 */
+void keplerian_to_cartesian_python(double *x, double *y, double *z, double *v_x,
+                                   double *v_y, double *v_z,
+                                   double semi_major_axis, double eccentricity,
+                                   double inclination, double argument_of_periapsis,
+                                   double longitude_of_ascending_node,
+                                   double true_anomaly, double total_mass,
+                                   double G);
+
+/* ---- device-resident simulation (no counterpart in the reference) ----
+ * The same integrator loops as launch_simulation with the state kept in
+ * HBM between calls, for callers that time or steer the GPU loop directly.
+ * `stream` is a cudaStream_t (NULL = the library's own stream). */
+typedef struct gsgpu_sim gsgpu_sim;
+
+int gsgpu_sim_create(gsgpu_sim **out, int num_particles, double G,
+                     const AccelerationParam *acceleration_param,
+                     int integrator, double dt, void *stream);
+/* Host -> device copy of x [3N], v [3N], m [N]; resets compensation terms. */
+int gsgpu_sim_upload(gsgpu_sim *sim, const double *x, const double *v,
+                     const double *m);
+/* Enqueue num_steps integrator steps (asynchronous on the stream). */
+int gsgpu_sim_run(gsgpu_sim *sim, int64_t num_steps);
+/* Device -> host copy of x, v (v synchronised to integer time for leapfrog). */
+int gsgpu_sim_download(gsgpu_sim *sim, double *x, double *v);
+/* Device pointer of the current acceleration array [3N] (FP64). */
+const double *gsgpu_sim_device_acceleration(const gsgpu_sim *sim);
+/* Device -> host copy of the most recent accelerations a [3N]. */
+int gsgpu_sim_download_acceleration(gsgpu_sim *sim, double *a);
+/* Accumulated device time and launch count of the force kernel (CUDA
+ * events on the simulation's stream); enable before gsgpu_sim_run. */
+int gsgpu_sim_set_force_timing(gsgpu_sim *sim, int enable);
+int gsgpu_sim_force_timing(const gsgpu_sim *sim, double *total_ms,
+                           int64_t *launches);
+/* Number of kernels launched by the most recent gsgpu_sim_run step. */
+int gsgpu_sim_kernels_per_step(const gsgpu_sim *sim);
+void gsgpu_sim_destroy(gsgpu_sim *sim);
+
+/* Library / device information: fills name (NUL-terminated, <= len). */
+int gsgpu_device_info(char *name, int len, int *sm_count, int *cc_major,
+                      int *cc_minor);
+
+/* FMA-throughput probe of the running GPU (fp64 = 0: FP32, 1: FP64):
+ * TFLOP/s at 2 FLOP per FMA, best of 5 launches.  No counterpart in the
+ * reference; it supplies the FP32/FP64 pipe peaks of the rooflines. */
+int gsgpu_measure_fma_peak(int fp64, double *tflops, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GRAV_SIM_GB300_H */

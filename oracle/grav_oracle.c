@@ -1,0 +1,634 @@
+/*
+ * grav_oracle.c -- CPU restatement of grav_sim's force-evaluation hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY (see grav_oracle.h).  Compiled with
+ * -ffp-contract=off: every product and sum is rounded on its own, in the
+ * order the reference's C expressions evaluate them.
+ */
+#include "grav_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------ */
+/* Direct sums                                                          */
+/* ------------------------------------------------------------------ */
+
+/* src/acceleration.c:177-234.  For the pair (i<j) the reference forms
+ * R = x_i - x_j, |R| = sqrt(R.R + eps^2), t = G/|R|^3, then
+ * a_i -= (t R) m_j and a_j += (t R) m_i. */
+void orc_pairwise(int n, const double *x, const double *m, double G,
+                  double eps, double *a)
+{
+    for (int k = 0; k < 3 * n; ++k) a[k] = 0.0;
+    const double eps2 = eps * eps;
+    for (int i = 0; i < n; ++i) {
+        const double mi = m[i];
+        for (int j = i + 1; j < n; ++j) {
+            double r0 = x[3 * i + 0] - x[3 * j + 0];
+            double r1 = x[3 * i + 1] - x[3 * j + 1];
+            double r2 = x[3 * i + 2] - x[3 * j + 2];
+            double s = r0 * r0 + r1 * r1 + r2 * r2 + eps2;
+            double rn = sqrt(s);
+            double t = G / (rn * rn * rn);
+            double mj = m[j];
+            double t0 = t * r0, t1 = t * r1, t2 = t * r2;
+            a[3 * i + 0] -= t0 * mj;
+            a[3 * i + 1] -= t1 * mj;
+            a[3 * i + 2] -= t2 * mj;
+            a[3 * j + 0] += t0 * mi;
+            a[3 * j + 1] += t1 * mi;
+            a[3 * j + 2] += t2 * mi;
+        }
+    }
+}
+
+/* The reference's symmetric loop (src/acceleration.c:198-231) restricted to
+ * outer rows [i_begin, i_end): every pair (i, j>i) of those rows is
+ * evaluated once and updates both a_i and a_j.  A bounded slice of the
+ * reference's own work, used to time it without running all N(N-1)/2 pairs.
+ * Returns the number of pair evaluations performed. */
+int64_t orc_pairwise_slice(int n, const double *x, const double *m, double G,
+                           double eps, int i_begin, int i_end, double *a)
+{
+    int64_t pairs = 0;
+    for (int k = 0; k < 3 * n; ++k) a[k] = 0.0;
+    const double eps2 = eps * eps;
+    for (int i = i_begin; i < i_end && i < n; ++i) {
+        const double mi = m[i];
+        for (int j = i + 1; j < n; ++j) {
+            double r0 = x[3 * i + 0] - x[3 * j + 0];
+            double r1 = x[3 * i + 1] - x[3 * j + 1];
+            double r2 = x[3 * i + 2] - x[3 * j + 2];
+            double rn = sqrt(r0 * r0 + r1 * r1 + r2 * r2 + eps2);
+            double t = G / (rn * rn * rn);
+            double mj = m[j];
+            double t0 = t * r0, t1 = t * r1, t2 = t * r2;
+            a[3 * i + 0] -= t0 * mj;
+            a[3 * i + 1] -= t1 * mj;
+            a[3 * i + 2] -= t2 * mj;
+            a[3 * j + 0] += t0 * mi;
+            a[3 * j + 1] += t1 * mi;
+            a[3 * j + 2] += t2 * mi;
+        }
+        pairs += n - 1 - i;
+    }
+    return pairs;
+}
+
+/* src/acceleration.c:236-367.  Massive particles (m != 0) interact
+ * symmetrically; each massless particle feels every massive one.  The
+ * massless term reads m[i] where i counts massive particles (:357-359). */
+int orc_massless(int n, const double *x, const double *m, double G,
+                 double eps, double *a)
+{
+    for (int k = 0; k < 3 * n; ++k) a[k] = 0.0;
+    int *heavy = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    int *light = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    if (!heavy || !light) { free(heavy); free(light); return 4; }
+    int nh = 0, nl = 0;
+    for (int i = 0; i < n; ++i) {
+        if (m[i] != 0.0) heavy[nh++] = i; else light[nl++] = i;
+    }
+    const double eps2 = eps * eps;
+    for (int p = 0; p < nh; ++p) {
+        const int i = heavy[p];
+        const double mi = m[i];
+        for (int q = p + 1; q < nh; ++q) {
+            const int j = heavy[q];
+            const double mj = m[j];
+            double r0 = x[3 * i + 0] - x[3 * j + 0];
+            double r1 = x[3 * i + 1] - x[3 * j + 1];
+            double r2 = x[3 * i + 2] - x[3 * j + 2];
+            double rn = sqrt(r0 * r0 + r1 * r1 + r2 * r2 + eps2);
+            double t = G / (rn * rn * rn);
+            double t0 = t * r0, t1 = t * r1, t2 = t * r2;
+            a[3 * i + 0] -= t0 * mj;
+            a[3 * i + 1] -= t1 * mj;
+            a[3 * i + 2] -= t2 * mj;
+            a[3 * j + 0] += t0 * mi;
+            a[3 * j + 1] += t1 * mi;
+            a[3 * j + 2] += t2 * mi;
+        }
+    }
+    for (int p = 0; p < nh; ++p) {
+        const int i = heavy[p];
+        for (int q = 0; q < nl; ++q) {
+            const int j = light[q];
+            double r0 = x[3 * i + 0] - x[3 * j + 0];
+            double r1 = x[3 * i + 1] - x[3 * j + 1];
+            double r2 = x[3 * i + 2] - x[3 * j + 2];
+            double rn = sqrt(r0 * r0 + r1 * r1 + r2 * r2 + eps2);
+            double t = G / (rn * rn * rn);
+            a[3 * j + 0] += t * r0 * m[p];
+            a[3 * j + 1] += t * r1 * m[p];
+            a[3 * j + 2] += t * r2 * m[p];
+        }
+    }
+    free(heavy);
+    free(light);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Linear octree                                                        */
+/* ------------------------------------------------------------------ */
+
+/* src/linear_octree.c:113-146 */
+void orc_bbox(int n, const double *x, double center[3], double *width)
+{
+    double lo[3] = {x[0], x[1], x[2]};
+    double hi[3] = {x[0], x[1], x[2]};
+    for (int i = 1; i < n; ++i) {
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fmin(lo[k], x[3 * i + k]);
+            hi[k] = fmax(hi[k], x[3 * i + k]);
+        }
+    }
+    for (int k = 0; k < 3; ++k) center[k] = (hi[k] + lo[k]) / 2.0;
+    double w = fmax(fmax(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+    *width = w;
+}
+
+/* Interleave the low 21 bits of v with two zero bits between each bit. */
+static int64_t spread21(int64_t v)
+{
+    uint64_t u = (uint64_t)v & 0x1fffffULL;
+    uint64_t out = 0;
+    for (int b = 0; b < 21; ++b) out |= ((u >> b) & 1ULL) << (3 * b);
+    return (int64_t)out;
+}
+
+/* src/linear_octree.c:159-202.  The normalised coordinate is converted to
+ * an integer by C truncation, so a particle at the box maximum gives 2^21,
+ * which the 21-bit mask turns into 0. */
+void orc_morton(int n, const double *x, const double center[3], double width,
+                int64_t *keys)
+{
+    for (int i = 0; i < n; ++i) {
+        int64_t c[3];
+        for (int k = 0; k < 3; ++k) {
+            double u = (x[3 * i + k] - center[k]) / width + 0.5;
+            c[k] = (int64_t)(u * (double)(1 << 21));
+        }
+        keys[i] = spread21(c[0]) | (spread21(c[1]) << 1) | (spread21(c[2]) << 2);
+    }
+}
+
+/* src/linear_octree.c:216-326: stable LSD radix sort, 9-bit digits. */
+int orc_radix_sort(int n, int64_t *keys, int *idx)
+{
+    const int bits = 9, radix = 1 << 9;
+    const int passes = (3 * ORC_MORTON_MAX_LEVEL + bits - 1) / bits;
+    int64_t *k2 = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
+    int *i2 = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    int *cnt = (int *)malloc(sizeof(int) * radix);
+    if (!k2 || !i2 || !cnt) { free(k2); free(i2); free(cnt); return 4; }
+    int64_t *src_k = keys, *dst_k = k2;
+    int *src_i = idx, *dst_i = i2;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = p * bits;
+        memset(cnt, 0, sizeof(int) * radix);
+        for (int j = 0; j < n; ++j) cnt[(src_k[j] >> shift) & (radix - 1)]++;
+        int run = 0;
+        for (int d = 0; d < radix; ++d) { int c = cnt[d]; cnt[d] = run; run += c; }
+        for (int j = 0; j < n; ++j) {
+            int d = (int)((src_k[j] >> shift) & (radix - 1));
+            int at = cnt[d]++;
+            dst_k[at] = src_k[j];
+            dst_i[at] = src_i[j];
+        }
+        int64_t *tk = src_k; src_k = dst_k; dst_k = tk;
+        int *ti = src_i; src_i = dst_i; dst_i = ti;
+    }
+    if (src_k != keys) {
+        memcpy(keys, src_k, sizeof(int64_t) * (size_t)n);
+        memcpy(idx, src_i, sizeof(int) * (size_t)n);
+    }
+    free(k2); free(i2); free(cnt);
+    return 0;
+}
+
+static int tree_reserve(OrcTree *t, int need)
+{
+    if (need <= t->capacity) return 0;
+    int cap = t->capacity > 0 ? t->capacity : 64;
+    while (cap < need) cap *= 2;
+#define GROW(field, type, per)                                               \
+    do {                                                                     \
+        type *p_ = (type *)realloc(t->field, sizeof(type) * (size_t)cap * per); \
+        if (!p_) return 4;                                                   \
+        t->field = p_;                                                       \
+    } while (0)
+    GROW(num_particles, int, 1);
+    GROW(num_children, int, 1);
+    GROW(first_particle, int, 1);
+    GROW(first_child, int, 1);
+    GROW(depth, int, 1);
+    GROW(mass, double, 1);
+    GROW(com, double, 3);
+#undef GROW
+    t->capacity = cap;
+    return 0;
+}
+
+/* Octant digit of a deepest-level key at a given depth (1..21). */
+static int octant_at(int64_t key, int depth)
+{
+    return (int)((key >> (3 * (ORC_MORTON_MAX_LEVEL - depth))) & 7);
+}
+
+/* Append the non-empty octants of node `nd` (depth d) as consecutive new
+ * nodes, octant order (src/linear_octree.c:342-393 counts, :406-576 append). */
+static int expand_node(OrcTree *t, int nd)
+{
+    const int d = t->depth[nd];
+    const int begin = t->first_particle[nd];
+    const int end = begin + t->num_particles[nd];
+    int j = begin;
+    int first = -1, count = 0;
+    while (j < end) {
+        const int oct = octant_at(t->keys[j], d + 1);
+        int k = j;
+        while (k < end && octant_at(t->keys[k], d + 1) == oct) ++k;
+        if (tree_reserve(t, t->num_nodes + 1)) return 4;
+        const int c = t->num_nodes++;
+        if (first < 0) first = c;
+        ++count;
+        t->num_particles[c] = k - j;
+        t->first_particle[c] = j;
+        t->num_children[c] = 0;
+        t->first_child[c] = -1;
+        t->depth[c] = d + 1;
+        t->mass[c] = 0.0;
+        t->com[3 * c + 0] = t->com[3 * c + 1] = t->com[3 * c + 2] = 0.0;
+        j = k;
+    }
+    t->first_child[nd] = first;
+    t->num_children[nd] = count;
+    return 0;
+}
+
+/* src/linear_octree.c:590-823 (tree build) and :825-962 (driver). */
+int orc_build_tree(int n, const double *x, const double *m, int leaf_max,
+                   int compat, OrcTree *t)
+{
+    memset(t, 0, sizeof(*t));
+    if (n < 1) return 2;
+    orc_bbox(n, x, t->center, &t->box_width);
+    t->keys = (int64_t *)malloc(sizeof(int64_t) * (size_t)n);
+    t->sorted_indices = (int *)malloc(sizeof(int) * (size_t)n);
+    if (!t->keys || !t->sorted_indices) return 4;
+    for (int i = 0; i < n; ++i) t->sorted_indices[i] = i;
+    orc_morton(n, x, t->center, t->box_width, t->keys);
+    if (orc_radix_sort(n, t->keys, t->sorted_indices)) return 4;
+    if (tree_reserve(t, n > 64 ? n : 64)) return 4;
+
+    t->num_nodes = 1;
+    t->num_particles[0] = n;
+    t->first_particle[0] = 0;
+    t->num_children[0] = 0;
+    t->first_child[0] = -1;
+    t->depth[0] = 0;
+    t->mass[0] = 0.0;
+    t->com[0] = t->com[1] = t->com[2] = 0.0;
+
+    /* Pre-order walk over internal nodes; each internal node is expanded
+     * when first reached, so children of a node are numbered contiguously
+     * in the order the nodes are expanded.  Sums are carried up on exit. */
+    struct Frame { int node; int next; double msum; double s[3]; } st[ORC_MORTON_MAX_LEVEL + 2];
+    int top = 0;
+    if (expand_node(t, 0)) return 4;
+    st[0].node = 0; st[0].next = 0; st[0].msum = 0.0;
+    st[0].s[0] = st[0].s[1] = st[0].s[2] = 0.0;
+    for (;;) {
+        struct Frame *f = &st[top];
+        const int nd = f->node;
+        if (f->next < t->num_children[nd]) {
+            const int c = t->first_child[nd] + f->next;
+            const int cnt = t->num_particles[c];
+            if (cnt <= leaf_max || t->depth[c] >= ORC_MORTON_MAX_LEVEL) {
+                double lm = 0.0, ls[3] = {0.0, 0.0, 0.0};
+                for (int q = 0; q < cnt; ++q) {
+                    const int pid = t->sorted_indices[t->first_particle[c] + q];
+                    const double mp = m[pid];
+                    f->msum += mp;
+                    for (int k = 0; k < 3; ++k) f->s[k] += mp * x[3 * pid + k];
+                    lm += mp;
+                    for (int k = 0; k < 3; ++k) ls[k] += mp * x[3 * pid + k];
+                }
+                if (!compat) {
+                    t->mass[c] = lm;
+                    for (int k = 0; k < 3; ++k) t->com[3 * c + k] = ls[k] / lm;
+                }
+                f->next++;
+                continue;
+            }
+            if (expand_node(t, c)) return 4;
+            ++top;
+            st[top].node = c; st[top].next = 0; st[top].msum = 0.0;
+            st[top].s[0] = st[top].s[1] = st[top].s[2] = 0.0;
+            continue;
+        }
+        /* all children of nd done */
+        t->mass[nd] = f->msum;
+        for (int k = 0; k < 3; ++k) t->com[3 * nd + k] = f->s[k] / f->msum;
+        if (top == 0) break;
+        struct Frame *p = &st[top - 1];
+        p->msum += f->msum;
+        for (int k = 0; k < 3; ++k) p->s[k] += f->s[k];
+        p->next++;
+        --top;
+    }
+    return 0;
+}
+
+void orc_free_tree(OrcTree *t)
+{
+    free(t->keys); free(t->sorted_indices); free(t->num_particles);
+    free(t->num_children); free(t->first_particle); free(t->first_child);
+    free(t->depth); free(t->mass); free(t->com);
+    memset(t, 0, sizeof(*t));
+}
+
+/* src/acceleration_barnes_hut.c:78-248.  Per particle (sorted order), a
+ * depth-first scan of the children of each opened node: a cell that does
+ * not contain the particle and satisfies (w_c)^2 < theta^2 |R|^2 adds its
+ * monopole; otherwise a leaf adds its particles (skipping the particle
+ * itself) and an internal node is opened. */
+void orc_bh_walk(int n, const double *x, const double *m, double G,
+                 double eps, double theta, const OrcTree *t, int compat,
+                 double *a, int64_t *counts)
+{
+    const double eps2 = eps * eps;
+    const double th2 = theta * theta;
+    const double box_length = t->box_width * 2.0;
+    for (int s = 0; s < n; ++s) {
+        const int id = t->sorted_indices[s];
+        const int64_t key_i = compat ? t->keys[id] : t->keys[s];
+        const double xi0 = x[3 * id + 0], xi1 = x[3 * id + 1], xi2 = x[3 * id + 2];
+        double ax = 0.0, ay = 0.0, az = 0.0;
+        int64_t n_cell = 0, n_pp = 0;
+        struct { int node; int next; } st[ORC_MORTON_MAX_LEVEL + 2];
+        int top = 0;
+        st[0].node = 0; st[0].next = 0;
+        int level = 1;
+        for (;;) {
+            const int nd = st[top].node;
+            if (st[top].next < t->num_children[nd]) {
+                const int c = t->first_child[nd] + st[top].next;
+                const int first = t->first_particle[c];
+                const int64_t key_c = compat ? t->keys[t->sorted_indices[first]]
+                                             : t->keys[first];
+                const int sh = 3 * (ORC_MORTON_MAX_LEVEL - level);
+                const int inside = (key_i >> sh) == (key_c >> sh);
+                if (!inside) {
+                    const double r0 = xi0 - t->com[3 * c + 0];
+                    const double r1 = xi1 - t->com[3 * c + 1];
+                    const double r2 = xi2 - t->com[3 * c + 2];
+                    const double bl = box_length / (double)(2 << level);
+                    const double ns = r0 * r0 + r1 * r1 + r2 * r2;
+                    if (bl * bl < th2 * ns) {
+                        const double rn = sqrt(ns + eps2);
+                        const double tv = G * t->mass[c] / (rn * rn * rn);
+                        ax -= tv * r0; ay -= tv * r1; az -= tv * r2;
+                        ++n_cell;
+                        st[top].next++;
+                        continue;
+                    }
+                }
+                if (t->num_children[c] <= 0) {
+                    const int cnt = t->num_particles[c];
+                    for (int q = 0; q < cnt; ++q) {
+                        const int pj = t->sorted_indices[first + q];
+                        if (pj == id) continue;
+                        const double r0 = xi0 - x[3 * pj + 0];
+                        const double r1 = xi1 - x[3 * pj + 1];
+                        const double r2 = xi2 - x[3 * pj + 2];
+                        const double rn = sqrt(r0 * r0 + r1 * r1 + r2 * r2 + eps2);
+                        const double tv = G * m[pj] / (rn * rn * rn);
+                        ax -= tv * r0; ay -= tv * r1; az -= tv * r2;
+                        ++n_pp;
+                    }
+                    st[top].next++;
+                    continue;
+                }
+                ++top;
+                st[top].node = c; st[top].next = 0;
+                ++level;
+                continue;
+            }
+            if (top == 0) break;
+            --top;
+            st[top].next++;
+            --level;
+        }
+        a[3 * id + 0] = ax; a[3 * id + 1] = ay; a[3 * id + 2] = az;
+        if (counts) { counts[2 * id] = n_cell; counts[2 * id + 1] = n_pp; }
+    }
+}
+
+int orc_barnes_hut(int n, const double *x, const double *m, double G,
+                   double eps, double theta, int leaf_max, int compat,
+                   double *a)
+{
+    OrcTree t;
+    int rc = orc_build_tree(n, x, m, leaf_max, compat, &t);
+    if (rc == 0) orc_bh_walk(n, x, m, G, eps, theta, &t, compat, a, NULL);
+    orc_free_tree(&t);
+    return rc;
+}
+
+/* ------------------------------------------------------------------ */
+/* Integrators                                                          */
+/* ------------------------------------------------------------------ */
+
+void orc_comp_update(int len, double *y, double *err, const double *d,
+                     double dt)
+{
+    for (int k = 0; k < len; ++k) {
+        const double y0 = y[k];
+        err[k] += d[k] * dt;
+        y[k] = y0 + err[k];
+        err[k] += y0 - y[k];
+    }
+}
+
+static int accel_of(int method, int n, const double *x, const double *m,
+                    double G, double eps, double *a)
+{
+    if (method == 1) { orc_pairwise(n, x, m, G, eps, a); return 0; }
+    if (method == 2) return orc_massless(n, x, m, G, eps, a);
+    return 2;
+}
+
+/* src/integrator.c:281-454 (euler), :456-628 (euler_cromer),
+ * :630-892 (rk4), :894-1121 (leapfrog). */
+int orc_fixed_step_run(int integrator, int method, int n, double *x, double *v,
+                       const double *m, double G, double eps, double dt,
+                       double tf)
+{
+    const int L = 3 * n;
+    double *a = (double *)calloc((size_t)L * 11 + 1, sizeof(double));
+    if (!a) return 4;
+    double *xe = a + L, *ve = a + 2 * L, *x0 = a + 3 * L, *v0 = a + 4 * L;
+    double *k1 = a + 5 * L, *k2 = a + 6 * L, *k3 = a + 7 * L, *k4 = a + 8 * L;
+    double *vk = a + 9 * L, *tmp = a + 10 * L;
+    (void)tmp;
+    int rc = 0;
+    const int64_t steps = (int64_t)ceil(tf / dt);
+    double t = 0.0;
+    double h = dt;
+    if (integrator == 4) {
+        if ((rc = accel_of(method, n, x, m, G, eps, a))) goto done;
+        for (int k = 0; k < L; ++k) {
+            const double y0 = v[k];
+            ve[k] += 0.5 * a[k] * h;
+            v[k] = y0 + ve[k];
+            ve[k] += y0 - v[k];
+        }
+    }
+    for (int64_t s = 0; s < steps; ++s) {
+        if (integrator != 3 && t + h > tf) h = tf - t;
+        if (integrator == 1) {
+            memcpy(x0, x, sizeof(double) * L);
+            memcpy(v0, v, sizeof(double) * L);
+            if ((rc = accel_of(method, n, x, m, G, eps, a))) goto done;
+            for (int k = 0; k < L; ++k) {
+                xe[k] += v[k] * h;
+                ve[k] += a[k] * h;
+                x[k] = x0[k] + xe[k];
+                v[k] = v0[k] + ve[k];
+                xe[k] += x0[k] - x[k];
+                ve[k] += v0[k] - v[k];
+            }
+        } else if (integrator == 2) {
+            /* src/integrator.c:557-569: kick v with a(x), then drift x with
+             * the new v, both compensated. */
+            if ((rc = accel_of(method, n, x, m, G, eps, a))) goto done;
+            orc_comp_update(L, v, ve, a, h);
+            orc_comp_update(L, x, xe, v, h);
+        } else if (integrator == 3) {
+            memcpy(x0, x, sizeof(double) * L);
+            memcpy(v0, v, sizeof(double) * L);
+            if ((rc = accel_of(method, n, x, m, G, eps, k1))) goto done;
+            memcpy(vk, v, sizeof(double) * L);                 /* xk1 */
+            double *xk1 = vk;
+            double *xk2 = (double *)malloc(sizeof(double) * (size_t)L * 3);
+            if (!xk2) { rc = 4; goto done; }
+            double *xk3 = xk2 + L, *xk4 = xk2 + 2 * L;
+            for (int k = 0; k < L; ++k) {
+                x[k] = x0[k] + 0.5 * xk1[k] * h;
+                v[k] = v0[k] + 0.5 * k1[k] * h;
+            }
+            if ((rc = accel_of(method, n, x, m, G, eps, k2))) { free(xk2); goto done; }
+            memcpy(xk2, v, sizeof(double) * L);
+            for (int k = 0; k < L; ++k) {
+                x[k] = x0[k] + 0.5 * xk2[k] * h;
+                v[k] = v0[k] + 0.5 * k2[k] * h;
+            }
+            if ((rc = accel_of(method, n, x, m, G, eps, k3))) { free(xk2); goto done; }
+            memcpy(xk3, v, sizeof(double) * L);
+            for (int k = 0; k < L; ++k) {
+                x[k] = x0[k] + xk3[k] * h;
+                v[k] = v0[k] + k3[k] * h;
+            }
+            if ((rc = accel_of(method, n, x, m, G, eps, k4))) { free(xk2); goto done; }
+            memcpy(xk4, v, sizeof(double) * L);
+            for (int k = 0; k < L; ++k) {
+                ve[k] += (k1[k] + 2 * k2[k] + 2 * k3[k] + k4[k]) * h / 6.0;
+                xe[k] += (xk1[k] + 2 * xk2[k] + 2 * xk3[k] + xk4[k]) * h / 6.0;
+                v[k] = v0[k] + ve[k];
+                x[k] = x0[k] + xe[k];
+                ve[k] += v0[k] - v[k];
+                xe[k] += x0[k] - x[k];
+            }
+            free(xk2);
+        } else if (integrator == 4) {
+            orc_comp_update(L, x, xe, v, h);
+            if ((rc = accel_of(method, n, x, m, G, eps, a))) goto done;
+            orc_comp_update(L, v, ve, a, h);
+        } else {
+            rc = 2;
+            goto done;
+        }
+        t = (double)(s + 1) * h;
+    }
+    if (integrator == 4) {
+        for (int k = 0; k < L; ++k) v[k] -= 0.5 * a[k] * h;
+    }
+done:
+    free(a);
+    return rc;
+}
+
+/* ------------------------------------------------------------------ */
+/* Diagnostics                                                          */
+/* ------------------------------------------------------------------ */
+
+static double norm3(const double *p)
+{
+    return sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+}
+
+/* src/utils.c:27-59 */
+double orc_energy(int n, const double *x, const double *v, const double *m,
+                  double G)
+{
+    double e = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double vn = norm3(&v[3 * i]);
+        e += 0.5 * m[i] * vn * vn;
+        for (int j = i + 1; j < n; ++j) {
+            double r[3];
+            for (int k = 0; k < 3; ++k) r[k] = x[3 * i + k] - x[3 * j + k];
+            e -= G * m[i] * m[j] / norm3(r);
+        }
+    }
+    return e;
+}
+
+/* src/python_interface.c:245-268 */
+double orc_linear_momentum(int n, const double *v, const double *m)
+{
+    double p = 0.0;
+    for (int i = 0; i < n; ++i)
+        p += m[i] * (v[3 * i] + v[3 * i + 1] + v[3 * i + 2]);
+    return p;
+}
+
+/* src/python_interface.c:270-304 */
+double orc_angular_momentum(int n, const double *x, const double *v,
+                            const double *m)
+{
+    double L = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double *r = &x[3 * i], *u = &v[3 * i];
+        const double c0 = r[1] * u[2] - r[2] * u[1];
+        const double c1 = r[2] * u[0] - r[0] * u[2];
+        const double c2 = r[0] * u[1] - r[1] * u[0];
+        L += m[i] * (c0 + c1 + c2);
+    }
+    return L;
+}
+
+void orc_direct_rows(int n, const double *x, const double *m, double G,
+                     double eps, int nrows, const int *rows, double *a_rows)
+{
+    const double eps2 = eps * eps;
+    for (int r = 0; r < nrows; ++r) {
+        const int i = rows[r];
+        double ax = 0.0, ay = 0.0, az = 0.0;
+        for (int j = 0; j < n; ++j) {
+            if (j == i) continue;
+            const double d0 = x[3 * j + 0] - x[3 * i + 0];
+            const double d1 = x[3 * j + 1] - x[3 * i + 1];
+            const double d2 = x[3 * j + 2] - x[3 * i + 2];
+            const double r2 = d0 * d0 + d1 * d1 + d2 * d2 + eps2;
+            const double inv = 1.0 / (r2 * sqrt(r2));
+            ax += m[j] * inv * d0; ay += m[j] * inv * d1; az += m[j] * inv * d2;
+        }
+        a_rows[3 * r + 0] = G * ax; a_rows[3 * r + 1] = G * ay; a_rows[3 * r + 2] = G * az;
+    }
+}

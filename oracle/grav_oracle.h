@@ -1,0 +1,114 @@
+/*
+ * grav_oracle.h -- CPU restatement of grav_sim's force-evaluation hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA
+ * product: tests/, __graft_entry__.smoke() and the cpu_baseline leg of
+ * bench.py may load it; the product library never does.
+ *
+ * Every function restates (in FP64, serial, no FMA contraction) the
+ * algorithm of the grav_sim file:line named in its comment.  The
+ * restatement is pinned against the reference itself (compiled from its own
+ * sources into oracle/_ref/) and against the committed golden vectors in
+ * tests/golden/.
+ */
+#ifndef GRAV_ORACLE_H
+#define GRAV_ORACLE_H
+
+#include <stdint.h>
+
+#define ORC_MORTON_MAX_LEVEL 21
+
+/* src/acceleration.c:177-234 (symmetric i<j loop, Plummer softening) */
+void orc_pairwise(int n, const double *x, const double *m, double G,
+                  double eps, double *a);
+
+/* src/acceleration.c:198-231 restricted to outer rows [i_begin, i_end);
+ * returns the number of pair evaluations (for timing bounded samples). */
+int64_t orc_pairwise_slice(int n, const double *x, const double *m, double G,
+                           double eps, int i_begin, int i_end, double *a);
+
+/* src/acceleration.c:236-367, including the m[i] loop-index mass read at
+ * :357-359 (the reference reads the mass of the i-th particle in array order,
+ * not of the i-th massive particle). */
+int orc_massless(int n, const double *x, const double *m, double G,
+                 double eps, double *a);
+
+/* src/linear_octree.c:113-146 */
+void orc_bbox(int n, const double *x, double center[3], double *width);
+
+/* src/linear_octree.c:159-202 (normalise, truncate, 21-bit mask, spread) */
+void orc_morton(int n, const double *x, const double center[3], double width,
+                int64_t *keys);
+
+/* src/linear_octree.c:216-326: stable LSD radix sort of keys with their
+ * indices (9-bit digits, ceil(63/9) passes). */
+int orc_radix_sort(int n, int64_t *keys, int *idx);
+
+/* Node arrays of the linear octree, in the reference's node numbering
+ * (src/linear_octree.h:20-57). */
+typedef struct OrcTree {
+    double box_width;
+    double center[3];
+    int num_nodes;
+    int capacity;
+    int64_t *keys;          /* sorted Morton keys            [n] */
+    int *sorted_indices;    /* particle id at sorted slot    [n] */
+    int *num_particles;     /* [num_nodes] */
+    int *num_children;      /* [num_nodes], 0 for leaves */
+    int *first_particle;    /* [num_nodes] */
+    int *first_child;       /* [num_nodes], -1 for leaves */
+    int *depth;             /* [num_nodes] */
+    double *mass;           /* [num_nodes] */
+    double *com;            /* [num_nodes*3] */
+} OrcTree;
+
+/* src/linear_octree.c:825-962 (construct_octree) with the tree build of
+ * :342-823.  compat=1 keeps the reference's zero leaf mass/centre of mass
+ * (:567-570, :662-677); compat=0 gives leaves their true mass and centre of
+ * mass, summed over their particles in sorted order. */
+int orc_build_tree(int n, const double *x, const double *m, int leaf_max,
+                   int compat, OrcTree *tree);
+void orc_free_tree(OrcTree *tree);
+
+/* src/acceleration_barnes_hut.c:78-248.  compat=1 reproduces the reference's
+ * cell-membership test, which indexes the sorted key array by particle id
+ * (:120, :145); compat=0 uses each particle's own sorted key.  If counts is
+ * not NULL it receives, per particle, the number of accepted cells (counts[2i])
+ * and of leaf particle-particle terms (counts[2i+1]). */
+void orc_bh_walk(int n, const double *x, const double *m, double G,
+                 double eps, double theta, const OrcTree *tree, int compat,
+                 double *a, int64_t *counts);
+
+/* Whole Barnes-Hut evaluation: build + walk (src/acceleration_barnes_hut.c:33-76). */
+int orc_barnes_hut(int n, const double *x, const double *m, double G,
+                   double eps, double theta, int leaf_max, int compat,
+                   double *a);
+
+/* Compensated kick/drift of src/integrator.c:1009-1018 and :1030-1039:
+ *   err += d*dt; y_new = y + err; err += y - y_new. */
+void orc_comp_update(int len, double *y, double *err, const double *d,
+                     double dt);
+
+/* Fixed-step integrators of src/integrator.c driven by the FP64 pairwise
+ * sum (method 1) or the massless sum (method 2): integrator codes 1 euler,
+ * 2 euler-cromer, 3 rk4, 4 leapfrog.  Reproduces total_num_steps =
+ * ceil(tf/dt), the last-step dt clamp and t = steps*dt. */
+int orc_fixed_step_run(int integrator, int method, int n, double *x, double *v,
+                       const double *m, double G, double eps, double dt,
+                       double tf);
+
+/* src/utils.c:27-59 (kinetic + unsoftened pairwise potential energy). */
+double orc_energy(int n, const double *x, const double *v, const double *m,
+                  double G);
+
+/* src/python_interface.c:245-304, component sums as the reference forms them. */
+double orc_linear_momentum(int n, const double *v, const double *m);
+double orc_angular_momentum(int n, const double *x, const double *v,
+                            const double *m);
+
+/* Exact FP64 direct sum in a fixed j order, used as the ground truth for
+ * relative-error statistics (not a reference restatement). */
+void orc_direct_rows(int n, const double *x, const double *m, double G,
+                     double eps, int nrows, const int *rows, double *a_rows);
+
+#endif

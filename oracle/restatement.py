@@ -1,0 +1,221 @@
+"""ctypes wrapper of the C restatement (oracle/grav_oracle.c).
+
+TEST INFRASTRUCTURE ONLY.  ``load()`` builds liboracle.so with the Makefile
+beside this file when it is missing (gcc, a second or two).
+"""
+from __future__ import annotations
+
+import ctypes
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+
+dp = ctypes.POINTER(ctypes.c_double)
+ip = ctypes.POINTER(ctypes.c_int32)
+lp = ctypes.POINTER(ctypes.c_int64)
+
+_lib = None
+
+
+def build() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB
+
+
+class OrcTree(ctypes.Structure):
+    _fields_ = [
+        ("box_width", ctypes.c_double),
+        ("center", ctypes.c_double * 3),
+        ("num_nodes", ctypes.c_int),
+        ("capacity", ctypes.c_int),
+        ("keys", lp),
+        ("sorted_indices", ip),
+        ("num_particles", ip),
+        ("num_children", ip),
+        ("first_particle", ip),
+        ("first_child", ip),
+        ("depth", ip),
+        ("mass", dp),
+        ("com", dp),
+    ]
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    src = HERE / "grav_oracle.c"
+    if not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
+        build()
+    lib = ctypes.CDLL(str(LIB))
+    lib.orc_pairwise.argtypes = [ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double, dp]
+    lib.orc_pairwise_slice.argtypes = [ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_int, ctypes.c_int, dp]
+    lib.orc_pairwise_slice.restype = ctypes.c_int64
+    lib.orc_massless.argtypes = [ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double, dp]
+    lib.orc_bbox.argtypes = [ctypes.c_int, dp, dp, dp]
+    lib.orc_morton.argtypes = [ctypes.c_int, dp, dp, ctypes.c_double, lp]
+    lib.orc_radix_sort.argtypes = [ctypes.c_int, lp, ip]
+    lib.orc_build_tree.argtypes = [ctypes.c_int, dp, dp, ctypes.c_int, ctypes.c_int,
+                                   ctypes.POINTER(OrcTree)]
+    lib.orc_free_tree.argtypes = [ctypes.POINTER(OrcTree)]
+    lib.orc_bh_walk.argtypes = [ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double,
+                                ctypes.c_double, ctypes.POINTER(OrcTree), ctypes.c_int,
+                                dp, lp]
+    lib.orc_barnes_hut.argtypes = [ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_int, ctypes.c_int, dp]
+    lib.orc_fixed_step_run.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp,
+                                       ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_double]
+    lib.orc_energy.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_double]
+    lib.orc_energy.restype = ctypes.c_double
+    lib.orc_linear_momentum.argtypes = [ctypes.c_int, dp, dp]
+    lib.orc_linear_momentum.restype = ctypes.c_double
+    lib.orc_angular_momentum.argtypes = [ctypes.c_int, dp, dp, dp]
+    lib.orc_angular_momentum.restype = ctypes.c_double
+    lib.orc_direct_rows.argtypes = [ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_int, ip, dp]
+    _lib = lib
+    return lib
+
+
+def _d(a):
+    return a.ctypes.data_as(dp)
+
+
+def _c(a, dt=np.float64):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def pairwise(x, m, G, eps):
+    x, m = _c(x), _c(m)
+    a = np.empty((m.size, 3))
+    load().orc_pairwise(m.size, _d(x), _d(m), G, eps, _d(a))
+    return a
+
+
+def pairwise_slice(x, m, G, eps, i_begin, i_end):
+    """Run the reference's symmetric loop for outer rows [i_begin, i_end);
+    returns (a, pair evaluations)."""
+    x, m = _c(x), _c(m)
+    a = np.empty((m.size, 3))
+    pairs = load().orc_pairwise_slice(m.size, _d(x), _d(m), G, eps, i_begin, i_end, _d(a))
+    return a, int(pairs)
+
+
+def massless(x, m, G, eps):
+    x, m = _c(x), _c(m)
+    a = np.empty((m.size, 3))
+    rc = load().orc_massless(m.size, _d(x), _d(m), G, eps, _d(a))
+    assert rc == 0
+    return a
+
+
+def bbox(x):
+    x = _c(x)
+    c = np.empty(3)
+    w = ctypes.c_double()
+    load().orc_bbox(x.shape[0], _d(x), _d(c), ctypes.byref(w))
+    return c, w.value
+
+
+def morton(x, center, width):
+    x = _c(x)
+    k = np.empty(x.shape[0], dtype=np.int64)
+    load().orc_morton(x.shape[0], _d(x), _d(_c(center)), width, k.ctypes.data_as(lp))
+    return k
+
+
+def radix_sort(keys):
+    k = _c(keys, np.int64).copy()
+    idx = np.arange(k.size, dtype=np.int32)
+    load().orc_radix_sort(k.size, k.ctypes.data_as(lp), idx.ctypes.data_as(ip))
+    return k, idx
+
+
+def build_tree(x, m, leaf_max, compat):
+    """Return a dict of numpy copies of the oracle's node arrays."""
+    x, m = _c(x), _c(m)
+    t = OrcTree()
+    rc = load().orc_build_tree(m.size, _d(x), _d(m), leaf_max, int(compat), ctypes.byref(t))
+    assert rc == 0, rc
+    nn, n = t.num_nodes, m.size
+    out = dict(
+        box_width=t.box_width, center=np.array(t.center[:]), num_nodes=nn,
+        keys=np.ctypeslib.as_array(t.keys, (n,)).copy(),
+        sorted_indices=np.ctypeslib.as_array(t.sorted_indices, (n,)).copy(),
+        num_particles=np.ctypeslib.as_array(t.num_particles, (nn,)).copy(),
+        num_children=np.ctypeslib.as_array(t.num_children, (nn,)).copy(),
+        first_particle=np.ctypeslib.as_array(t.first_particle, (nn,)).copy(),
+        first_child=np.ctypeslib.as_array(t.first_child, (nn,)).copy(),
+        depth=np.ctypeslib.as_array(t.depth, (nn,)).copy(),
+        mass=np.ctypeslib.as_array(t.mass, (nn,)).copy(),
+        com=np.ctypeslib.as_array(t.com, (nn * 3,)).copy().reshape(nn, 3),
+    )
+    load().orc_free_tree(ctypes.byref(t))
+    return out
+
+
+def barnes_hut(x, m, G, eps, theta, leaf_max, compat):
+    x, m = _c(x), _c(m)
+    a = np.empty((m.size, 3))
+    rc = load().orc_barnes_hut(m.size, _d(x), _d(m), G, eps, theta, leaf_max, int(compat), _d(a))
+    assert rc == 0
+    return a
+
+
+def bh_counts(x, m, G, eps, theta, leaf_max, compat):
+    """Per-particle (accepted cells, leaf pair terms) of the walk."""
+    x, m = _c(x), _c(m)
+    t = OrcTree()
+    lib = load()
+    assert lib.orc_build_tree(m.size, _d(x), _d(m), leaf_max, int(compat), ctypes.byref(t)) == 0
+    a = np.empty((m.size, 3))
+    cnt = np.empty((m.size, 2), dtype=np.int64)
+    lib.orc_bh_walk(m.size, _d(x), _d(m), G, eps, theta, ctypes.byref(t), int(compat),
+                    _d(a), cnt.ctypes.data_as(lp))
+    lib.orc_free_tree(ctypes.byref(t))
+    return a, cnt
+
+
+def fixed_step_run(integrator, method, x, v, m, G, eps, dt, tf):
+    x, v, m = _c(x).copy(), _c(v).copy(), _c(m)
+    rc = load().orc_fixed_step_run(integrator, method, m.size, _d(x), _d(v), _d(m),
+                                   G, eps, dt, tf)
+    assert rc == 0, rc
+    return x, v
+
+
+def energy(x, v, m, G):
+    x, v, m = _c(x), _c(v), _c(m)
+    return load().orc_energy(m.size, _d(x), _d(v), _d(m), G)
+
+
+def linear_momentum(v, m):
+    v, m = _c(v), _c(m)
+    return load().orc_linear_momentum(m.size, _d(v), _d(m))
+
+
+def angular_momentum(x, v, m):
+    x, v, m = _c(x), _c(v), _c(m)
+    return load().orc_angular_momentum(m.size, _d(x), _d(v), _d(m))
+
+
+def direct_rows(x, m, G, eps, rows):
+    x, m = _c(x), _c(m)
+    rows = _c(rows, np.int32)
+    a = np.empty((rows.size, 3))
+    load().orc_direct_rows(m.size, _d(x), _d(m), G, eps, rows.size,
+                           rows.ctypes.data_as(ip), _d(a))
+    return a
+
+
+def rel_err(a, b):
+    """Per-particle |a - b| / |b|."""
+    num = np.linalg.norm(np.asarray(a) - np.asarray(b), axis=1)
+    den = np.linalg.norm(np.asarray(b), axis=1)
+    return num / np.where(den > 0, den, 1.0)

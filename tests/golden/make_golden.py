@@ -1,0 +1,134 @@
+"""Generate the golden vectors under tests/golden/ from grav_sim itself.
+
+grav_sim ships no tests, fixtures or known-answer vectors for its hot path,
+so the vectors are made by running the reference C library -- compiled from
+its own sources by ``make -C oracle ref`` into oracle/_ref/ -- on seeded
+inputs.  Run on a machine where the reference sources are present:
+
+    python tests/golden/make_golden.py
+
+Outputs (compressed .npz, a few hundred KB in total):
+  pairwise.npz       acceleration_pairwise   (src/acceleration.c:177-234)
+  massless.npz       acceleration_massless   (src/acceleration.c:236-367)
+  octree.npz         construct_octree        (src/linear_octree.c:825-962)
+  barnes_hut.npz     acceleration_barnes_hut (src/acceleration_barnes_hut.c:33-248)
+  integrators.npz    euler / euler_cromer / rk4 / leapfrog (src/integrator.c)
+  leapfrog_plummer1024.npz  leapfrog + pairwise, N=1024, dt=1e-3, 1000 steps
+  energy.npz         compute_energy_python   (src/python_interface.c:195-243)
+"""
+from __future__ import annotations
+
+import importlib.util
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+OUT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+from oracle import reference as ref  # noqa: E402
+
+spec = importlib.util.spec_from_file_location("wl", ROOT / "gravity-simulator_gb300" / "workloads.py")
+wl = importlib.util.module_from_spec(spec)
+spec.loader.exec_module(wl)
+
+
+def pairwise_cases():
+    cases = {}
+    for n in (1, 2, 3, 17, 1024):
+        x, v, m = wl.plummer(n, 100 + n)
+        cases[f"plummer{n}"] = (x, m, 1.0, 0.01)
+    # unsoftened
+    x, v, m = wl.plummer(64, 5)
+    cases["plummer64_eps0"] = (x, m, 1.0, 0.0)
+    # coincident pairs with softening
+    x, v, m = wl.plummer(40, 6)
+    x[1] = x[0]
+    x[7] = x[3]
+    cases["coincident"] = (x, m, 1.0, 0.05)
+    # collinear, unequal masses, G != 1
+    t = np.linspace(-3.0, 5.0, 33)
+    x = np.stack([t, 0.5 * t, -2.0 * t], axis=1)
+    m = np.linspace(0.5, 2.0, 33)
+    cases["collinear"] = (x, m, 0.7, 0.01)
+    return cases
+
+
+def main():
+    assert ref.build() or ref.available(), "reference sources not found"
+    out = {}
+    for name, (x, m, G, eps) in pairwise_cases().items():
+        a = ref.acceleration(x, m, G, 1, eps=eps)
+        out[f"{name}/x"], out[f"{name}/m"] = x, m
+        out[f"{name}/G"], out[f"{name}/eps"], out[f"{name}/a"] = np.float64(G), np.float64(eps), a
+    np.savez_compressed(OUT / "pairwise.npz", **out)
+
+    out = {}
+    x, v, m = wl.plummer(300, 11)
+    m1 = m.copy()
+    m1[100:] = 0.0                      # massive first
+    m2 = m.copy()
+    m2[1::4] = 0.0                      # interleaved (loop-index mass read)
+    for name, mm in (("massive_first", m1), ("interleaved", m2)):
+        out[f"{name}/x"], out[f"{name}/m"] = x, mm
+        out[f"{name}/a"] = ref.acceleration(x, mm, 1.0, 2, eps=0.01)
+    np.savez_compressed(OUT / "massless.npz", **out)
+
+    out = {}
+    tree_cases = {}
+    x, v, m = wl.plummer(3000, 21)
+    for leaf in (1, 8, 64):
+        tree_cases[f"plummer3000_leaf{leaf}"] = (x, m, leaf)
+    # particles on the bounding-box maximum (2^21 wraps to 0) and duplicates
+    x2, v2, m2 = wl.plummer(500, 22)
+    x2[10] = x2.max(axis=0)
+    x2[11] = x2.min(axis=0)
+    x2[20:40] = x2[5]                   # 21 coincident particles -> level-21 leaf
+    tree_cases["edges_leaf1"] = (x2, m2, 1)
+    tree_cases["edges_leaf4"] = (x2, m2, 4)
+    tree_cases["single"] = (np.array([[0.3, -0.2, 0.1]]), np.array([1.0]), 1)
+    tree_cases["pair"] = (np.array([[0.0, 0.0, 0.0], [1.0, 0.5, -0.25]]), np.array([1.0, 2.0]), 1)
+    g = wl.galaxy_pair(4096, 4)
+    tree_cases["galaxy4096_leaf1"] = (g[0], g[2], 1)
+    for name, (xx, mm, leaf) in tree_cases.items():
+        t = ref.octree(xx, mm, leaf)
+        out[f"{name}/x"], out[f"{name}/m"], out[f"{name}/leaf"] = xx, mm, np.int64(leaf)
+        for k in ("keys", "sorted_indices", "num_particles", "num_children", "first_particle",
+                  "first_child", "mass", "com"):
+            out[f"{name}/{k}"] = t[k]
+        out[f"{name}/box_width"] = np.float64(t["box_width"])
+    np.savez_compressed(OUT / "octree.npz", **out)
+
+    out = {}
+    for name in ("plummer3000_leaf1", "plummer3000_leaf8", "edges_leaf1", "galaxy4096_leaf1"):
+        xx, mm, leaf = tree_cases[name]
+        out[f"{name}/x"], out[f"{name}/m"], out[f"{name}/leaf"] = xx, mm, np.int64(leaf)
+        for th in (0.5, 1.0):
+            out[f"{name}/a_theta{th}"] = ref.acceleration(xx, mm, 1.0, 3, theta=th, eps=0.01,
+                                                          leaf=leaf)
+    np.savez_compressed(OUT / "barnes_hut.npz", **out)
+
+    out = {}
+    x, v, m = wl.plummer(64, 31)
+    out["x"], out["v"], out["m"] = x, v, m
+    for integ in (1, 2, 3, 4):
+        _, xr, vr, _ = ref.launch(x, v, m, 1.0, integ, 1e-3, 0.0995, 1, eps=0.01)
+        out[f"int{integ}/x"], out[f"int{integ}/v"] = xr, vr
+    np.savez_compressed(OUT / "integrators.npz", **out)
+
+    x, v, m = wl.plummer(1024, 1)
+    _, xr, vr, _ = ref.launch(x, v, m, 1.0, 4, 1e-3, 1.0, 1, eps=0.01)
+    np.savez_compressed(OUT / "leapfrog_plummer1024.npz", x0=x, v0=v, m=m, x=xr, v=vr,
+                        e0=ref.energy_python(x, v, m, 1.0), e1=ref.energy_python(xr, vr, m, 1.0))
+
+    x, v, m = wl.plummer(777, 41)
+    np.savez_compressed(OUT / "energy.npz", x=x, v=v, m=m, G=np.float64(1.3),
+                        e=ref.energy_python(x, v, m, 1.3))
+    for f in sorted(OUT.glob("*.npz")):
+        print(f.name, f.stat().st_size)
+
+
+if __name__ == "__main__":
+    main()

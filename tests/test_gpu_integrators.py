@@ -1,0 +1,93 @@
+"""Integrator loops on the GPU through launch_simulation_python.
+
+With the FP64 reference-order direct sum (111) the whole run -- force,
+compensated kicks and drifts, dt clamp, final velocity synchronisation --
+must equal grav_sim's run bit for bit (FP64 integrator steps, tolerance 0).
+With the compensated-FP32 force (101) the final state agrees to the
+accuracy of the force, and the energy drift matches the reference's.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("integ", [1, 2, 3, 4])
+def test_fixed_step_bitexact_golden(lib, g, integ):
+    d = golden("integrators")
+    x, v = d["x"].copy(), d["v"].copy()
+    _, xo, vo, _ = g.launch_simulation(lib, x, v, d["m"].copy(), 1.0, integrator=integ, dt=1e-3,
+                                       tf=0.0995, method=g.METHOD_GPU_PAIRWISE_FP64,
+                                       softening_length=0.01)
+    assert np.array_equal(xo, d[f"int{integ}/x"])
+    assert np.array_equal(vo, d[f"int{integ}/v"])
+
+
+def test_leapfrog_plummer1024_1000_steps_bitexact(lib, g):
+    d = golden("leapfrog_plummer1024")
+    x, v = d["x0"].copy(), d["v0"].copy()
+    _, xo, vo, _ = g.launch_simulation(lib, x, v, d["m"].copy(), 1.0, integrator=4, dt=1e-3,
+                                       tf=1.0, method=g.METHOD_GPU_PAIRWISE_FP64,
+                                       softening_length=0.01)
+    assert np.array_equal(xo, d["x"]) and np.array_equal(vo, d["v"])
+
+
+def test_leapfrog_plummer1024_fp32_force(lib, g, orc):
+    d = golden("leapfrog_plummer1024")
+    x, v = d["x0"].copy(), d["v0"].copy()
+    _, xo, vo, _ = g.launch_simulation(lib, x, v, d["m"].copy(), 1.0, integrator=4, dt=1e-3,
+                                       tf=1.0, method=g.METHOD_GPU_PAIRWISE,
+                                       softening_length=0.01)
+    dx = np.linalg.norm(xo - d["x"], axis=1)
+    assert np.median(dx) < 1e-6 and dx.max() < 1e-3
+    e0, e_ref = float(d["e0"]), float(d["e1"])
+    e_gpu = orc.energy(xo, vo, d["m"], 1.0)
+    drift_ref = abs(e_ref - e0) / abs(e0)
+    drift_gpu = abs(e_gpu - e0) / abs(e0)
+    print(f"relative energy drift: gpu {drift_gpu:.3g} reference {drift_ref:.3g}")
+    assert drift_gpu < 5 * drift_ref + 1e-7
+
+
+@pytest.mark.parametrize("integ", [1, 2, 3, 4])
+def test_oracle_random_tf_clamp(lib, g, orc, wl, integ):
+    """tf not a multiple of dt: the last step is clamped (all but rk4)."""
+    x, v, m = wl.plummer(300, 90 + integ)
+    _, xo, vo, _ = g.launch_simulation(lib, x.copy(), v.copy(), m, 1.0, integrator=integ,
+                                       dt=2e-3, tf=0.0371, method=g.METHOD_GPU_PAIRWISE_FP64,
+                                       softening_length=0.02)
+    xr, vr = orc.fixed_step_run(integ, 1, x, v, m, 1.0, 0.02, 2e-3, 0.0371)
+    assert np.array_equal(xo, xr) and np.array_equal(vo, vr)
+
+
+def test_is_exit_stops_after_one_step(lib, g, orc, wl):
+    x, v, m = wl.plummer(200, 5)
+    flag = ctypes.c_bool(True)
+    _, xo, vo, _ = g.launch_simulation(lib, x.copy(), v.copy(), m, 1.0, integrator=4, dt=1e-3,
+                                       tf=1.0, method=g.METHOD_GPU_PAIRWISE_FP64,
+                                       softening_length=0.01, is_exit=flag)
+    xr, vr = orc.fixed_step_run(4, 1, x, v, m, 1.0, 0.01, 1e-3, 1e-3)
+    assert np.array_equal(xo, xr) and np.array_equal(vo, vr)
+
+
+def test_energy_diagnostics(lib, g, orc):
+    d = golden("energy")
+    n = d["m"].size
+    state = np.ascontiguousarray(np.concatenate([d["m"][:, None], d["x"], d["v"]], 1))
+    e = np.empty(1)
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.compute_energy_python(e.ctypes.data_as(dp), ctypes.c_double(float(d["G"])),
+                              state.ctypes.data_as(dp), ctypes.c_int32(1), ctypes.c_int32(n))
+    assert abs(e[0] - float(d["e"])) <= 1e-13 * abs(float(d["e"]))
+    p = np.empty(1)
+    lib.compute_linear_momentum_python(p.ctypes.data_as(dp), state.ctypes.data_as(dp),
+                                       ctypes.c_int32(1), ctypes.c_int32(n))
+    assert abs(p[0] - orc.linear_momentum(d["v"], d["m"])) <= 1e-13
+    L = np.empty(1)
+    lib.compute_angular_momentum_python(L.ctypes.data_as(dp), state.ctypes.data_as(dp),
+                                        ctypes.c_int32(1), ctypes.c_int32(n))
+    Lr = orc.angular_momentum(d["x"], d["v"], d["m"])
+    assert abs(L[0] - Lr) <= 1e-12 * max(1.0, abs(Lr))

@@ -1,0 +1,114 @@
+"""The oracle (C restatement) against grav_sim's own outputs.
+
+CPU only.  The golden vectors were produced by the reference library
+compiled from its own sources (tests/golden/make_golden.py); where that
+library is present on this machine the restatement is also compared with it
+on fresh seeded inputs.  Everything here is bit-exact: the restatement
+performs the reference's FP64 operations in the reference's order.
+"""
+import numpy as np
+import pytest
+
+from conftest import cases, golden
+from oracle import reference
+
+
+def test_pairwise_golden(orc):
+    for name, c in cases(golden("pairwise")).items():
+        a = orc.pairwise(c["x"], c["m"], float(c["G"]), float(c["eps"]))
+        assert np.array_equal(a, c["a"]), name
+
+
+def test_massless_golden(orc):
+    for name, c in cases(golden("massless")).items():
+        a = orc.massless(c["x"], c["m"], 1.0, 0.01)
+        assert np.array_equal(a, c["a"]), name
+
+
+TREE_KEYS = ("keys", "sorted_indices", "num_particles", "num_children", "first_particle",
+             "first_child")
+
+
+def test_octree_golden(orc):
+    for name, c in cases(golden("octree")).items():
+        t = orc.build_tree(c["x"], c["m"], int(c["leaf"]), True)
+        assert t["box_width"] == float(c["box_width"]), name
+        for k in TREE_KEYS:
+            assert np.array_equal(t[k], c[k]), (name, k)
+        internal = c["num_children"] > 0
+        assert np.array_equal(t["mass"][internal], c["mass"][internal]), name
+        assert np.array_equal(t["com"][internal], c["com"][internal]), name
+
+
+def test_octree_quirks(orc):
+    """Bounding-box maximum wraps to Morton coordinate 0; duplicates stop at
+    level 21 as one leaf."""
+    c = cases(golden("octree"))["edges_leaf1"]
+    t = orc.build_tree(c["x"], c["m"], 1, True)
+    center, width = orc.bbox(c["x"])
+    keys = orc.morton(c["x"], center, width)
+    k10 = int(keys[10])
+    # along the axis of largest extent the maximum normalises to 1.0, i.e.
+    # 2^21 after scaling, which the 21-bit mask wraps to 0
+    w = int(np.argmax(c["x"].max(axis=0) - c["x"].min(axis=0)))
+    assert k10 & (0x1249249249249249 << w) == 0
+    assert k10 != 0
+    deep = (t["depth"] == 21) & (t["num_children"] == 0)
+    assert deep.any() and t["num_particles"][deep].max() >= 21
+
+
+def test_barnes_hut_golden(orc):
+    for name, c in cases(golden("barnes_hut")).items():
+        for th in (0.5, 1.0):
+            a = orc.barnes_hut(c["x"], c["m"], 1.0, 0.01, th, int(c["leaf"]), True)
+            assert np.array_equal(a, c[f"a_theta{th}"]), (name, th)
+
+
+def test_integrators_golden(orc):
+    d = golden("integrators")
+    for integ in (1, 2, 3, 4):
+        xo, vo = orc.fixed_step_run(integ, 1, d["x"], d["v"], d["m"], 1.0, 0.01, 1e-3, 0.0995)
+        assert np.array_equal(xo, d[f"int{integ}/x"]), integ
+        assert np.array_equal(vo, d[f"int{integ}/v"]), integ
+
+
+def test_leapfrog_plummer1024_golden(orc):
+    d = golden("leapfrog_plummer1024")
+    xo, vo = orc.fixed_step_run(4, 1, d["x0"], d["v0"], d["m"], 1.0, 0.01, 1e-3, 1.0)
+    assert np.array_equal(xo, d["x"]) and np.array_equal(vo, d["v"])
+    e1 = orc.energy(xo, vo, d["m"], 1.0)
+    assert abs(e1 - float(d["e1"])) <= 1e-13 * abs(float(d["e1"]))
+
+
+def test_energy_golden(orc):
+    d = golden("energy")
+    e = orc.energy(d["x"], d["v"], d["m"], float(d["G"]))
+    assert e == float(d["e"])
+
+
+@pytest.mark.skipif(not reference.available(), reason="reference library not built here")
+def test_restatement_vs_reference_fresh(orc, wl):
+    rng = np.random.default_rng(1234)
+    for trial in range(3):
+        n = int(rng.integers(50, 2500))
+        x, v, m = wl.plummer(n, 500 + trial)
+        m = m * rng.uniform(0.5, 1.5, n)
+        assert np.array_equal(orc.pairwise(x, m, 1.0, 0.02), reference.acceleration(x, m, 1.0, 1, eps=0.02))
+        leaf = int(rng.integers(1, 9))
+        tr = reference.octree(x, m, leaf)
+        to = orc.build_tree(x, m, leaf, True)
+        for k in TREE_KEYS:
+            assert np.array_equal(tr[k], to[k]), (trial, k)
+        th = float(rng.uniform(0.3, 1.2))
+        assert np.array_equal(orc.barnes_hut(x, m, 1.0, 0.01, th, leaf, True),
+                              reference.acceleration(x, m, 1.0, 3, theta=th, eps=0.01, leaf=leaf))
+
+
+def test_fixed_mode_tree_is_more_accurate(orc, wl):
+    """With true leaf multipoles and own keys (fixed mode) the walk is far
+    closer to the direct sum than the reference's walk (zero-mass leaves)."""
+    x, v, m = wl.plummer(4000, 9)
+    exact = orc.pairwise(x, m, 1.0, 0.01)
+    e_ref = np.median(orc.rel_err(orc.barnes_hut(x, m, 1.0, 0.01, 0.5, 1, True), exact))
+    e_fix = np.median(orc.rel_err(orc.barnes_hut(x, m, 1.0, 0.01, 0.5, 1, False), exact))
+    assert e_fix < 5e-3 < e_ref
