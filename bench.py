@@ -64,6 +64,9 @@ def _module(name):
 WORKLOADS = {
     "plummer262144": dict(n=262144, seed=2, G=1.0, eps=0.01, dt=1e-3, integrator=4,
                           method=101, flop_per_interaction=20),
+    # small case of the same kernel, for profiler captures
+    "plummer65536": dict(n=65536, seed=2, G=1.0, eps=0.01, dt=1e-3, integrator=4,
+                         method=101, flop_per_interaction=20),
 }
 
 

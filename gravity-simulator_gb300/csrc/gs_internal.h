@@ -110,6 +110,15 @@ class Engine {
     {
         (void)cx; (void)cy; (void)cz;
     }
+    // Interactions of the most recent compute(): out[0] cell (monopole)
+    // terms, out[1] particle-particle terms.  Synchronises the stream.
+    virtual ErrorStatus interaction_counts(cudaStream_t s, long long out[2])
+    {
+        (void)s;
+        out[0] = 0;
+        out[1] = 0;
+        return ok();
+    }
 };
 
 bool is_gpu_method(int method);

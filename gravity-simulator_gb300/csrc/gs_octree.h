@@ -1,0 +1,60 @@
+// gs_octree.h -- device linear octree shared by the tree build (k_octree.cu)
+// and the Barnes-Hut walk (k_walk.cu).
+#pragma once
+
+#include "gs_internal.h"
+#include "gs_radix.h"
+
+namespace gs {
+
+constexpr int OCT_MAX_LEVEL = 21;   // MORTON_MAX_LEVEL (src/linear_octree.h:14)
+
+// Device counters / small state of one build (ints unless noted).
+enum OctCtr {
+    CTR_NODES = 0,      // nodes created (root included)
+    CTR_INTERNAL = 1,   // internal (expanded) nodes
+    CTR_STATUS = 2,     // StatusBits
+    CTR_N = 3,          // particle count (for device-count kernels)
+    CTR_LVL = 8,        // CTR_LVL + d: first internal index of depth d (d = 0..22)
+    CTR_SIZE = 40
+};
+
+struct OctreeDevice {
+    int n = 0;
+    int cap_nodes = 0;   // node capacity
+    int leaf_max = 1;
+    bool compat = true;
+
+    DBuf ctr;                 // int[CTR_SIZE]
+    DBuf frame;               // double[8]: cx, cy, cz, width, box_length
+    DBuf bbox_part;           // double[blocks * 6]
+    DBuf keys, sidx;          // uint64[n] sorted Morton keys, int[n] particle ids
+    // construction lists (unordered)
+    DBuf nd_start, nd_count, nd_depth, nd_parent, nd_rank, nd_int;   // int[cap]
+    DBuf in_node, in_nchild, in_fc, in_id;                           // int[cap]
+    DBuf in_key;                                                     // uint64[cap]
+    DBuf in_order;                                                   // int[cap]
+    DBuf scan_tiles;                                                 // unsigned[...]
+    // final node arrays in the reference's numbering
+    DBuf t_np, t_nc, t_fp, t_fc, t_depth, t_int;                     // int[cap]
+    DBuf t_mass;                                                     // double[cap]
+    DBuf t_com;                                                      // double[3*cap]
+    DBuf in_sum;                                                     // double[4*cap]
+    // walk arrays (frame-centred double-float positions)
+    DBuf w_na, w_nb;          // float4[cap]: (com_hi, mass), (com_lo, 0)
+    DBuf w_nc;                // int4[cap]: (first_child, num_children, first_particle, count)
+    DBuf w_nkey;              // uint64[cap]: key used by the cell-membership test
+    DBuf w_pa, w_pb;          // float4[n] in sorted order: (x_hi, m), (x_lo, 0)
+    RadixSorter sorter;
+
+    ErrorStatus setup(int n, int leaf_max, bool compat);
+    // Builds the tree from device x [3n] and m [n].  box_center/box_width
+    // (host values) replace the bounding box when box_width > 0.
+    ErrorStatus build(const double *d_x, const double *d_m, cudaStream_t s,
+                      const double *box_center = nullptr, double box_width = -1.0);
+    int launches_per_build() const;
+    // Host copies: number of nodes, status word.
+    ErrorStatus read_counts(cudaStream_t s, int *nodes, unsigned *status);
+};
+
+}  // namespace gs

@@ -51,7 +51,11 @@ struct CallContext {
     }
 };
 
+}  // namespace
+
 thread_local std::unique_ptr<CallContext> tl_call;
+
+namespace {
 
 ErrorStatus call_context(CallContext **out)
 {
@@ -504,6 +508,30 @@ int gsgpu_sim_force_timing(const gsgpu_sim *sim, double *total_ms, int64_t *laun
 int gsgpu_sim_kernels_per_step(const gsgpu_sim *sim)
 {
     return sim ? sim->kernels_per_step() : 0;
+}
+
+int gsgpu_sim_interaction_counts(gsgpu_sim *sim, long long *counts)
+{
+    if (!sim || !counts) return GRAV_POINTER_ERROR;
+    ErrorStatus st = sim->engine->interaction_counts(sim->stream, counts);
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    return 0;
+}
+
+int gsgpu_last_interaction_counts(long long *counts)
+{
+    if (!counts) return GRAV_POINTER_ERROR;
+    counts[0] = counts[1] = 0;
+    if (!gs::tl_call || !gs::tl_call->engine) return 0;
+    ErrorStatus st = gs::tl_call->engine->interaction_counts(gs::tl_call->stream, counts);
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    return 0;
 }
 
 void gsgpu_sim_destroy(gsgpu_sim *sim) { delete sim; }

@@ -11,7 +11,7 @@
 //     stream through a 3-stage shared-memory ring filled by TMA bulk copies
 //     (cp.async.bulk + mbarrier complete_tx), read back as broadcast float4;
 //   * each pair term is 3 FADD + 3 FFMA + rsqrt + 3 FMUL + 3 FFMA in FP32;
-//     each tile's partial sum is added into a Kahan-compensated FP32
+//     each partial sum of 128 pair terms is added into a Kahan-compensated FP32
 //     accumulator;
 //   * the (i-tile, j-chunk) work units are sized so that their count is a
 //     whole number of waves of resident CTAs (152 SMs x occupancy); partial
@@ -37,6 +37,7 @@ constexpr int DS_ITILE = DS_THREADS * DS_IPT;  // 1024
 constexpr int DS_JTILE = 1024;                 // 16 KiB of float4
 constexpr int DS_STAGES = 3;
 constexpr int DS_SMEM = DS_STAGES * DS_JTILE * 16;
+constexpr int DS_KAHAN_CHUNK = 128;            // plain FP32 partials of 128 terms
 static_assert(DS_ITILE == DS_JTILE, "i and j tiles share the padding unit");
 
 // Padding particle: massless and far from everything (its pair terms are 0).
@@ -136,21 +137,23 @@ k_direct_sum(const float4 *__restrict__ pj, int n_pad, int i_tiles, int jt_per_c
             break;
         }
         const float4 *tile = sj + st * DS_JTILE;
-        float ax[DS_IPT], ay[DS_IPT], az[DS_IPT];
+        for (int j0 = 0; j0 < DS_JTILE; j0 += DS_KAHAN_CHUNK) {
+            float ax[DS_IPT], ay[DS_IPT], az[DS_IPT];
 #pragma unroll
-        for (int k = 0; k < DS_IPT; ++k) ax[k] = ay[k] = az[k] = 0.0f;
+            for (int k = 0; k < DS_IPT; ++k) ax[k] = ay[k] = az[k] = 0.0f;
 #pragma unroll 8
-        for (int j = 0; j < DS_JTILE; ++j) {
-            const float4 q = tile[j];
+            for (int j = j0; j < j0 + DS_KAHAN_CHUNK; ++j) {
+                const float4 q = tile[j];
 #pragma unroll
-            for (int k = 0; k < DS_IPT; ++k)
-                pair_term<SOFT>(q, xi[k], yi[k], zi[k], eps2, ax[k], ay[k], az[k]);
-        }
+                for (int k = 0; k < DS_IPT; ++k)
+                    pair_term<SOFT>(q, xi[k], yi[k], zi[k], eps2, ax[k], ay[k], az[k]);
+            }
 #pragma unroll
-        for (int k = 0; k < DS_IPT; ++k) {
-            kahan_add(sx[k], cx[k], ax[k]);
-            kahan_add(sy[k], cy[k], ay[k]);
-            kahan_add(sz[k], cz[k], az[k]);
+            for (int k = 0; k < DS_IPT; ++k) {
+                kahan_add(sx[k], cx[k], ax[k]);
+                kahan_add(sy[k], cy[k], ay[k]);
+                kahan_add(sz[k], cz[k], az[k]);
+            }
         }
         __syncthreads();   // every thread is done with stage st
         if (threadIdx.x == 0 && issued < ntiles) {

@@ -1,0 +1,613 @@
+// k_octree.cu -- GPU construction of grav_sim's linear octree.
+//
+// Replaces construct_octree and its helpers (src/linear_octree.c:113-962).
+// Results equal the reference's: bounding box, Morton keys, sorted order,
+// node numbering and topology bit for bit; internal-node mass and centre of
+// mass bit for bit (FP64, reference summation order, no FMA contraction).
+//
+//   bounding box   k_bbox_partial + k_bbox_final: exact FP64 min/max.
+//   Morton keys    k_morton: (x - c)/w + 0.5 in FP64, truncation to int64,
+//                  21-bit mask (a coordinate at the box maximum wraps to 0,
+//                  as in the reference), bit interleave.
+//   sort           RadixSorter (stable LSD, 8-bit digits) of (key, id).
+//   topology       level-synchronous: k_tree_expand(d) splits every internal
+//                  node of depth d into its non-empty octants (binary search
+//                  on the sorted keys), appending children to an unordered
+//                  node list; a child is internal when it holds more than
+//                  leaf_max particles and is above depth 21.
+//   numbering      the reference numbers nodes in creation order: all
+//                  children of a node get consecutive ids when the node is
+//                  expanded, and nodes are expanded in depth-first pre-order.
+//                  Pre-order of internal nodes is the order of (first
+//                  particle, depth), so internal nodes are radix-sorted by
+//                  that key and an exclusive scan of their child counts gives
+//                  each one's first-child id; a node's id is then its
+//                  parent's first-child id plus its octant rank.
+//   multipoles     bottom-up, one launch per depth: an internal node adds,
+//                  child by child in octant order, the particles of leaf
+//                  children (sorted order) and the running sums of internal
+//                  children -- the reference's order (:652-735).  Leaves keep
+//                  mass 0 and centre of mass 0 in compat mode (the
+//                  reference's behaviour); otherwise they get their own sums.
+// Every count the kernels need is read from device memory, so a whole build
+// is graph-capturable.  Node-capacity overflow sets ST_TREE_OVERFLOW.
+#include "gs_octree.h"
+#include "gs_ptx.cuh"
+
+namespace gs {
+
+constexpr int OT_THREADS = 256;
+constexpr int BBOX_BLOCKS = 512;
+constexpr int SCAN_TILE = 4096;
+
+__device__ __forceinline__ double dmin(double a, double b) { return fmin(a, b); }
+__device__ __forceinline__ double dmax(double a, double b) { return fmax(a, b); }
+
+__global__ void __launch_bounds__(OT_THREADS)
+k_bbox_partial(const double *__restrict__ x, int n, double *__restrict__ part)
+{
+    __shared__ double s[6][OT_THREADS];
+    double lo[3], hi[3];
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = x[k];
+        hi[k] = x[k];
+    }
+    for (int i = blockIdx.x * OT_THREADS + threadIdx.x; i < n; i += gridDim.x * OT_THREADS) {
+        for (int k = 0; k < 3; ++k) {
+            const double q = x[3 * i + k];
+            lo[k] = dmin(lo[k], q);
+            hi[k] = dmax(hi[k], q);
+        }
+    }
+    for (int k = 0; k < 3; ++k) {
+        s[k][threadIdx.x] = lo[k];
+        s[3 + k][threadIdx.x] = hi[k];
+    }
+    __syncthreads();
+    for (int w = OT_THREADS / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            for (int k = 0; k < 3; ++k) {
+                s[k][threadIdx.x] = dmin(s[k][threadIdx.x], s[k][threadIdx.x + w]);
+                s[3 + k][threadIdx.x] = dmax(s[3 + k][threadIdx.x], s[3 + k][threadIdx.x + w]);
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 6) part[blockIdx.x * 6 + threadIdx.x] = s[threadIdx.x][0];
+}
+
+// src/linear_octree.c:138-145 (and :856-867 when a box is given)
+__global__ void k_bbox_final(const double *__restrict__ part, int blocks, double ocx, double ocy,
+                             double ocz, double owidth, double *__restrict__ frame)
+{
+    if (threadIdx.x != 0) return;
+    double lo[3], hi[3];
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = part[k];
+        hi[k] = part[3 + k];
+    }
+    for (int b = 1; b < blocks; ++b)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = dmin(lo[k], part[6 * b + k]);
+            hi[k] = dmax(hi[k], part[6 * b + 3 + k]);
+        }
+    double c[3], w;
+    if (owidth > 0.0) {
+        c[0] = ocx;
+        c[1] = ocy;
+        c[2] = ocz;
+        w = owidth;
+    } else {
+        for (int k = 0; k < 3; ++k) c[k] = __ddiv_rn(__dadd_rn(hi[k], lo[k]), 2.0);
+        w = dmax(dmax(__dsub_rn(hi[0], lo[0]), __dsub_rn(hi[1], lo[1])), __dsub_rn(hi[2], lo[2]));
+    }
+    frame[0] = c[0];
+    frame[1] = c[1];
+    frame[2] = c[2];
+    frame[3] = w;
+    frame[4] = __dmul_rn(w, 2.0);
+}
+
+// 21 low bits of v spread to every third bit (magic-number interleave).
+__device__ __forceinline__ uint64_t spread3(uint64_t v)
+{
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x001f00000000ffffull;
+    v = (v | (v << 16)) & 0x001f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+// src/linear_octree.c:159-202
+__global__ void k_morton(const double *__restrict__ x, int n, const double *__restrict__ frame,
+                         uint64_t *__restrict__ keys, int *__restrict__ sidx)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double w = frame[3];
+    uint64_t k = 0;
+    for (int d = 0; d < 3; ++d) {
+        const double u = __dadd_rn(__ddiv_rn(__dsub_rn(x[3 * i + d], frame[d]), w), 0.5);
+        const long long q = __double2ll_rz(__dmul_rn(u, 2097152.0));
+        k |= spread3((uint64_t)q) << d;
+    }
+    keys[i] = k;
+    sidx[i] = i;
+}
+
+__global__ void k_tree_init(int *__restrict__ ctr, int n, int *__restrict__ nd_start,
+                            int *__restrict__ nd_count, int *__restrict__ nd_depth,
+                            int *__restrict__ nd_parent, int *__restrict__ nd_rank,
+                            int *__restrict__ nd_int, int *__restrict__ in_node)
+{
+    if (threadIdx.x != 0) return;
+    ctr[CTR_NODES] = 1;
+    ctr[CTR_INTERNAL] = 1;
+    ctr[CTR_STATUS] = 0;
+    ctr[CTR_N] = n;
+    ctr[CTR_LVL + 0] = 0;
+    ctr[CTR_LVL + 1] = 1;
+    nd_start[0] = 0;
+    nd_count[0] = n;
+    nd_depth[0] = 0;
+    nd_parent[0] = -1;
+    nd_rank[0] = 0;
+    nd_int[0] = 0;
+    in_node[0] = 0;
+}
+
+// First index in [lo, hi) whose octant digit at `shift` exceeds o.
+__device__ __forceinline__ int octant_end(const uint64_t *__restrict__ keys, int lo, int hi,
+                                          int shift, int o)
+{
+    while (lo < hi) {
+        const int mid = lo + ((hi - lo) >> 1);
+        const int dig = (int)((keys[mid] >> shift) & 7ull);
+        if (dig <= o)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// src/linear_octree.c:342-576 for all internal nodes of depth d at once.
+__global__ void __launch_bounds__(OT_THREADS)
+k_tree_expand(int d, int leaf_max, int cap, const uint64_t *__restrict__ keys, int *__restrict__ ctr,
+              int *__restrict__ nd_start, int *__restrict__ nd_count, int *__restrict__ nd_depth,
+              int *__restrict__ nd_parent, int *__restrict__ nd_rank, int *__restrict__ nd_int,
+              int *__restrict__ in_node, int *__restrict__ in_nchild)
+{
+    const int lo = ctr[CTR_LVL + d];
+    const int hi = ctr[CTR_LVL + d + 1];
+    const int cd = d + 1;
+    const int shift = 3 * (OCT_MAX_LEVEL - cd);
+    for (int ii = lo + blockIdx.x * OT_THREADS + threadIdx.x; ii < hi;
+         ii += gridDim.x * OT_THREADS) {
+        const int q = in_node[ii];
+        const int s = nd_start[q];
+        const int e = s + nd_count[q];
+        int ends[8];
+        int nch = 0;
+        int prev = s;
+        for (int o = 0; o < 8; ++o) {
+            ends[o] = octant_end(keys, prev, e, shift, o);
+            if (ends[o] > prev) ++nch;
+            prev = ends[o];
+        }
+        const int base = atomicAdd(&ctr[CTR_NODES], nch);
+        if (base + nch > cap) {
+            atomicOr((unsigned *)&ctr[CTR_STATUS], ST_TREE_OVERFLOW);
+            in_nchild[ii] = 0;
+            continue;
+        }
+        int r = 0;
+        prev = s;
+        for (int o = 0; o < 8; ++o) {
+            const int cnt = ends[o] - prev;
+            if (cnt > 0) {
+                const int c = base + r;
+                nd_start[c] = prev;
+                nd_count[c] = cnt;
+                nd_depth[c] = cd;
+                nd_parent[c] = ii;
+                nd_rank[c] = r;
+                int slot = -1;
+                if (cnt > leaf_max && cd < OCT_MAX_LEVEL) {
+                    slot = atomicAdd(&ctr[CTR_INTERNAL], 1);
+                    if (slot >= cap) {
+                        atomicOr((unsigned *)&ctr[CTR_STATUS], ST_TREE_OVERFLOW);
+                        slot = -1;
+                    } else {
+                        in_node[slot] = c;
+                    }
+                }
+                nd_int[c] = slot;
+                ++r;
+            }
+            prev = ends[o];
+        }
+        in_nchild[ii] = nch;
+    }
+}
+
+__global__ void k_tree_mark(int d, int *__restrict__ ctr)
+{
+    if (threadIdx.x == 0) ctr[CTR_LVL + d + 2] = ctr[CTR_INTERNAL];
+}
+
+// Sort key of an internal node: pre-order = (first particle, depth).
+__global__ void k_internal_keys(const int *__restrict__ ctr, const int *__restrict__ in_node,
+                                const int *__restrict__ nd_start, const int *__restrict__ nd_depth,
+                                uint64_t *__restrict__ in_key, int *__restrict__ in_order)
+{
+    const int ni = ctr[CTR_INTERNAL];
+    for (int ii = blockIdx.x * blockDim.x + threadIdx.x; ii < ni; ii += gridDim.x * blockDim.x) {
+        const int q = in_node[ii];
+        in_key[ii] = ((uint64_t)nd_start[q] << 5) | (uint64_t)nd_depth[q];
+        in_order[ii] = ii;
+    }
+}
+
+// Tile sums of child counts in pre-order.
+__global__ void __launch_bounds__(OT_THREADS)
+k_fc_tile_sums(const int *__restrict__ ctr, const int *__restrict__ in_order,
+               const int *__restrict__ in_nchild, unsigned *__restrict__ tile_sum)
+{
+    __shared__ unsigned red[OT_THREADS];
+    const int ni = ctr[CTR_INTERNAL];
+    const int base = blockIdx.x * SCAN_TILE;
+    unsigned s = 0;
+    for (int k = threadIdx.x; k < SCAN_TILE; k += OT_THREADS) {
+        const int e = base + k;
+        if (e < ni) s += (unsigned)in_nchild[in_order[e]];
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = OT_THREADS / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = red[0];
+}
+
+__global__ void __launch_bounds__(1024) k_scan_small(unsigned *__restrict__ v, int len)
+{
+    __shared__ unsigned part[1024];
+    const int per = (len + 1023) / 1024;
+    const int b = threadIdx.x * per;
+    const int e = min(len, b + per);
+    unsigned s = 0;
+    for (int i = b; i < e; ++i) s += v[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        const unsigned t = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += t;
+        __syncthreads();
+    }
+    unsigned run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
+    for (int i = b; i < e; ++i) {
+        const unsigned c = v[i];
+        v[i] = run;
+        run += c;
+    }
+}
+
+// First-child id of each internal node: 1 + exclusive scan in pre-order.
+__global__ void __launch_bounds__(OT_THREADS)
+k_fc_apply(const int *__restrict__ ctr, const int *__restrict__ in_order,
+           const int *__restrict__ in_nchild, const unsigned *__restrict__ tile_off,
+           int *__restrict__ in_fc)
+{
+    constexpr int PER = SCAN_TILE / OT_THREADS;   // 16 consecutive per thread
+    __shared__ unsigned part[OT_THREADS];
+    const int ni = ctr[CTR_INTERNAL];
+    const int base = blockIdx.x * SCAN_TILE + threadIdx.x * PER;
+    unsigned v[PER];
+    unsigned s = 0;
+    for (int k = 0; k < PER; ++k) {
+        const int e = base + k;
+        v[k] = e < ni ? (unsigned)in_nchild[in_order[e]] : 0u;
+        s += v[k];
+    }
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < OT_THREADS; off <<= 1) {
+        const unsigned t = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += t;
+        __syncthreads();
+    }
+    unsigned run = tile_off[blockIdx.x] + (threadIdx.x ? part[threadIdx.x - 1] : 0u);
+    for (int k = 0; k < PER; ++k) {
+        const int e = base + k;
+        if (e < ni) in_fc[in_order[e]] = 1 + (int)run;
+        run += v[k];
+    }
+}
+
+// Final node arrays by id.
+__global__ void k_tree_number(const int *__restrict__ ctr, int compat,
+                              const int *__restrict__ nd_start, const int *__restrict__ nd_count,
+                              const int *__restrict__ nd_depth, const int *__restrict__ nd_parent,
+                              const int *__restrict__ nd_rank, const int *__restrict__ nd_int,
+                              const int *__restrict__ in_nchild, const int *__restrict__ in_fc,
+                              int *__restrict__ in_id, int *__restrict__ t_np,
+                              int *__restrict__ t_nc, int *__restrict__ t_fp,
+                              int *__restrict__ t_fc, int *__restrict__ t_depth,
+                              int *__restrict__ t_int, double *__restrict__ t_mass,
+                              double *__restrict__ t_com)
+{
+    const int nn = min(ctr[CTR_NODES], 0x7fffffff);
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nn; q += gridDim.x * blockDim.x) {
+        const int id = (q == 0) ? 0 : in_fc[nd_parent[q]] + nd_rank[q];
+        t_np[id] = nd_count[q];
+        t_fp[id] = nd_start[q];
+        t_depth[id] = nd_depth[q];
+        const int ii = nd_int[q];
+        t_int[id] = ii;
+        if (ii >= 0) {
+            t_nc[id] = in_nchild[ii];
+            t_fc[id] = in_fc[ii];
+            in_id[ii] = id;
+        } else {
+            t_nc[id] = 0;
+            t_fc[id] = -1;
+            if (compat) {
+                t_mass[id] = 0.0;
+                t_com[3 * id + 0] = 0.0;
+                t_com[3 * id + 1] = 0.0;
+                t_com[3 * id + 2] = 0.0;
+            }
+        }
+    }
+}
+
+// Running sums of the particles of one leaf, sorted order (reference :667-674).
+__device__ __forceinline__ void add_particles(const double *__restrict__ x,
+                                              const double *__restrict__ m,
+                                              const int *__restrict__ sidx, int first, int count,
+                                              double &M, double &S0, double &S1, double &S2)
+{
+    for (int p = first; p < first + count; ++p) {
+        const int pid = sidx[p];
+        const double mp = m[pid];
+        M = __dadd_rn(M, mp);
+        S0 = __dadd_rn(S0, __dmul_rn(mp, x[3 * pid + 0]));
+        S1 = __dadd_rn(S1, __dmul_rn(mp, x[3 * pid + 1]));
+        S2 = __dadd_rn(S2, __dmul_rn(mp, x[3 * pid + 2]));
+    }
+}
+
+// Internal nodes of depth d (reference :652-735).
+__global__ void k_multipole_level(int d, const int *__restrict__ ctr, const double *__restrict__ x,
+                                  const double *__restrict__ m, const int *__restrict__ sidx,
+                                  const int *__restrict__ in_id, const int *__restrict__ in_fc,
+                                  const int *__restrict__ in_nchild, const int *__restrict__ t_np,
+                                  const int *__restrict__ t_nc, const int *__restrict__ t_fp,
+                                  const int *__restrict__ t_int, double *__restrict__ in_sum,
+                                  double *__restrict__ t_mass, double *__restrict__ t_com)
+{
+    const int lo = ctr[CTR_LVL + d];
+    const int hi = ctr[CTR_LVL + d + 1];
+    for (int ii = lo + blockIdx.x * blockDim.x + threadIdx.x; ii < hi;
+         ii += gridDim.x * blockDim.x) {
+        double M = 0.0, S0 = 0.0, S1 = 0.0, S2 = 0.0;
+        const int fc = in_fc[ii];
+        const int nch = in_nchild[ii];
+        for (int c = fc; c < fc + nch; ++c) {
+            if (t_nc[c] > 0) {
+                const double *cs = in_sum + 4 * (size_t)t_int[c];
+                M = __dadd_rn(M, cs[0]);
+                S0 = __dadd_rn(S0, cs[1]);
+                S1 = __dadd_rn(S1, cs[2]);
+                S2 = __dadd_rn(S2, cs[3]);
+            } else {
+                add_particles(x, m, sidx, t_fp[c], t_np[c], M, S0, S1, S2);
+            }
+        }
+        double *ws = in_sum + 4 * (size_t)ii;
+        ws[0] = M;
+        ws[1] = S0;
+        ws[2] = S1;
+        ws[3] = S2;
+        const int id = in_id[ii];
+        t_mass[id] = M;
+        t_com[3 * id + 0] = __ddiv_rn(S0, M);
+        t_com[3 * id + 1] = __ddiv_rn(S1, M);
+        t_com[3 * id + 2] = __ddiv_rn(S2, M);
+    }
+}
+
+// Leaves with their own mass and centre of mass (non-compat trees).
+__global__ void k_leaf_multipoles(const int *__restrict__ ctr, const double *__restrict__ x,
+                                  const double *__restrict__ m, const int *__restrict__ sidx,
+                                  const int *__restrict__ t_np, const int *__restrict__ t_nc,
+                                  const int *__restrict__ t_fp, double *__restrict__ t_mass,
+                                  double *__restrict__ t_com)
+{
+    const int nn = ctr[CTR_NODES];
+    for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < nn; id += gridDim.x * blockDim.x) {
+        if (t_nc[id] > 0) continue;
+        double M = 0.0, S0 = 0.0, S1 = 0.0, S2 = 0.0;
+        add_particles(x, m, sidx, t_fp[id], t_np[id], M, S0, S1, S2);
+        t_mass[id] = M;
+        t_com[3 * id + 0] = __ddiv_rn(S0, M);
+        t_com[3 * id + 1] = __ddiv_rn(S1, M);
+        t_com[3 * id + 2] = __ddiv_rn(S2, M);
+    }
+}
+
+__device__ __forceinline__ void split_df(double v, float &hi, float &lo)
+{
+    hi = __double2float_rn(v);
+    lo = __double2float_rn(__dsub_rn(v, (double)hi));
+}
+
+// Frame-centred double-float copies for the FP32 walk.
+__global__ void k_walk_nodes(const int *__restrict__ ctr, int compat, const double *__restrict__ frame,
+                             const uint64_t *__restrict__ keys, const int *__restrict__ sidx,
+                             const int *__restrict__ t_np, const int *__restrict__ t_nc,
+                             const int *__restrict__ t_fp, const int *__restrict__ t_fc,
+                             const double *__restrict__ t_mass, const double *__restrict__ t_com,
+                             float4 *__restrict__ na, float4 *__restrict__ nb, int4 *__restrict__ nc,
+                             uint64_t *__restrict__ nkey)
+{
+    const int nn = ctr[CTR_NODES];
+    const double c0 = frame[0], c1 = frame[1], c2 = frame[2];
+    for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < nn; id += gridDim.x * blockDim.x) {
+        float h0, l0, h1, l1, h2, l2;
+        split_df(__dsub_rn(t_com[3 * id + 0], c0), h0, l0);
+        split_df(__dsub_rn(t_com[3 * id + 1], c1), h1, l1);
+        split_df(__dsub_rn(t_com[3 * id + 2], c2), h2, l2);
+        na[id] = make_float4(h0, h1, h2, (float)t_mass[id]);
+        nb[id] = make_float4(l0, l1, l2, 0.0f);
+        const int fp = t_fp[id];
+        nc[id] = make_int4(t_fc[id], t_nc[id], fp, t_np[id]);
+        // the reference's membership test reads keys[sorted_indices[first]]
+        // from the sorted key array (src/acceleration_barnes_hut.c:145)
+        nkey[id] = compat ? keys[sidx[fp]] : keys[fp];
+    }
+}
+
+__global__ void k_walk_particles(int n, const double *__restrict__ frame, const double *__restrict__ x,
+                                 const double *__restrict__ m, const int *__restrict__ sidx,
+                                 float4 *__restrict__ pa, float4 *__restrict__ pb)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int id = sidx[p];
+    float h0, l0, h1, l1, h2, l2;
+    split_df(__dsub_rn(x[3 * id + 0], frame[0]), h0, l0);
+    split_df(__dsub_rn(x[3 * id + 1], frame[1]), h1, l1);
+    split_df(__dsub_rn(x[3 * id + 2], frame[2]), h2, l2);
+    pa[p] = make_float4(h0, h1, h2, (float)m[id]);
+    pb[p] = make_float4(l0, l1, l2, 0.0f);
+}
+
+// ------------------------------------------------------------------------
+ErrorStatus OctreeDevice::setup(int n_, int leaf_max_, bool compat_)
+{
+    n = n_;
+    leaf_max = leaf_max_;
+    compat = compat_;
+    int cap = 4 * n + 4096;
+    if (cap < n) return GS_RAISE(GRAV_VALUE_ERROR, "too many particles for the octree: %d", n);
+    cap_nodes = cap;
+    const size_t ci = (size_t)cap * sizeof(int);
+    GS_TRY(ctr.reserve(CTR_SIZE * sizeof(int)));
+    GS_TRY(frame.reserve(8 * sizeof(double)));
+    GS_TRY(bbox_part.reserve((size_t)BBOX_BLOCKS * 6 * sizeof(double)));
+    GS_TRY(keys.reserve((size_t)n * sizeof(uint64_t)));
+    GS_TRY(sidx.reserve((size_t)n * sizeof(int)));
+    DBuf *ints[] = {&nd_start, &nd_count, &nd_depth, &nd_parent, &nd_rank, &nd_int, &in_node,
+                    &in_nchild, &in_fc, &in_id, &in_order, &t_np, &t_nc, &t_fp, &t_fc, &t_depth,
+                    &t_int};
+    for (DBuf *b : ints) GS_TRY(b->reserve(ci));
+    GS_TRY(in_key.reserve((size_t)cap * sizeof(uint64_t)));
+    GS_TRY(scan_tiles.reserve((size_t)((cap + SCAN_TILE - 1) / SCAN_TILE + 1) * sizeof(unsigned)));
+    GS_TRY(t_mass.reserve((size_t)cap * sizeof(double)));
+    GS_TRY(t_com.reserve((size_t)cap * 3 * sizeof(double)));
+    GS_TRY(in_sum.reserve((size_t)cap * 4 * sizeof(double)));
+    GS_TRY(w_na.reserve((size_t)cap * sizeof(float4)));
+    GS_TRY(w_nb.reserve((size_t)cap * sizeof(float4)));
+    GS_TRY(w_nc.reserve((size_t)cap * sizeof(int4)));
+    GS_TRY(w_nkey.reserve((size_t)cap * sizeof(uint64_t)));
+    GS_TRY(w_pa.reserve((size_t)n * sizeof(float4)));
+    GS_TRY(w_pb.reserve((size_t)n * sizeof(float4)));
+    GS_TRY(sorter.reserve(std::max(n, cap)));
+    return ok();
+}
+
+int OctreeDevice::launches_per_build() const
+{
+    // bbox 2, morton 1, sort, init 1, levels 2*21, keys 1, sort, fc 3,
+    // number 1, multipoles 21 (+1 leaves), walk arrays 2
+    return 2 + 1 + RadixSorter::launches(63) + 1 + 42 + 1 + RadixSorter::launches(36) + 3 + 1 +
+           21 + (compat ? 0 : 1) + 2;
+}
+
+ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream_t s,
+                                const double *box_center, double box_width)
+{
+    const int nb = std::min(BBOX_BLOCKS, std::max(1, (n + OT_THREADS - 1) / OT_THREADS));
+    k_bbox_partial<<<nb, OT_THREADS, 0, s>>>(d_x, n, bbox_part.as<double>());
+    const bool own_box = box_center && box_width > 0.0;
+    k_bbox_final<<<1, 32, 0, s>>>(bbox_part.as<double>(), nb, own_box ? box_center[0] : 0.0,
+                                  own_box ? box_center[1] : 0.0, own_box ? box_center[2] : 0.0,
+                                  own_box ? box_width : -1.0, frame.as<double>());
+    const int pb = (n + OT_THREADS - 1) / OT_THREADS;
+    k_morton<<<pb, OT_THREADS, 0, s>>>(d_x, n, frame.as<double>(), keys.as<uint64_t>(),
+                                       sidx.as<int>());
+    k_tree_init<<<1, 32, 0, s>>>(ctr.as<int>(), n, nd_start.as<int>(), nd_count.as<int>(),
+                                 nd_depth.as<int>(), nd_parent.as<int>(), nd_rank.as<int>(),
+                                 nd_int.as<int>(), in_node.as<int>());
+    GS_CUDA(cudaGetLastError());
+    GS_TRY(sorter.sort(keys.as<uint64_t>(), sidx.as<int>(), ctr.as<int>() + CTR_N, 63, s));
+
+    const DeviceInfo *dev = nullptr;
+    GS_TRY(device_info(&dev));
+    const int grid = dev->sm_count * 8;
+    for (int d = 0; d < OCT_MAX_LEVEL; ++d) {
+        k_tree_expand<<<grid, OT_THREADS, 0, s>>>(
+            d, leaf_max, cap_nodes, keys.as<uint64_t>(), ctr.as<int>(), nd_start.as<int>(),
+            nd_count.as<int>(), nd_depth.as<int>(), nd_parent.as<int>(), nd_rank.as<int>(),
+            nd_int.as<int>(), in_node.as<int>(), in_nchild.as<int>());
+        k_tree_mark<<<1, 32, 0, s>>>(d, ctr.as<int>());
+    }
+    GS_CUDA(cudaGetLastError());
+    k_internal_keys<<<grid, OT_THREADS, 0, s>>>(ctr.as<int>(), in_node.as<int>(), nd_start.as<int>(),
+                                                nd_depth.as<int>(), in_key.as<uint64_t>(),
+                                                in_order.as<int>());
+    GS_TRY(sorter.sort(in_key.as<uint64_t>(), in_order.as<int>(), ctr.as<int>() + CTR_INTERNAL, 36,
+                       s));
+    const int tiles = (cap_nodes + SCAN_TILE - 1) / SCAN_TILE;
+    k_fc_tile_sums<<<tiles, OT_THREADS, 0, s>>>(ctr.as<int>(), in_order.as<int>(),
+                                                in_nchild.as<int>(), scan_tiles.as<unsigned>());
+    k_scan_small<<<1, 1024, 0, s>>>(scan_tiles.as<unsigned>(), tiles);
+    k_fc_apply<<<tiles, OT_THREADS, 0, s>>>(ctr.as<int>(), in_order.as<int>(), in_nchild.as<int>(),
+                                            scan_tiles.as<unsigned>(), in_fc.as<int>());
+    k_tree_number<<<grid, OT_THREADS, 0, s>>>(
+        ctr.as<int>(), compat ? 1 : 0, nd_start.as<int>(), nd_count.as<int>(), nd_depth.as<int>(),
+        nd_parent.as<int>(), nd_rank.as<int>(), nd_int.as<int>(), in_nchild.as<int>(),
+        in_fc.as<int>(), in_id.as<int>(), t_np.as<int>(), t_nc.as<int>(), t_fp.as<int>(),
+        t_fc.as<int>(), t_depth.as<int>(), t_int.as<int>(), t_mass.as<double>(),
+        t_com.as<double>());
+    GS_CUDA(cudaGetLastError());
+    for (int d = OCT_MAX_LEVEL - 1; d >= 0; --d) {
+        k_multipole_level<<<grid, OT_THREADS, 0, s>>>(
+            d, ctr.as<int>(), d_x, d_m, sidx.as<int>(), in_id.as<int>(), in_fc.as<int>(),
+            in_nchild.as<int>(), t_np.as<int>(), t_nc.as<int>(), t_fp.as<int>(), t_int.as<int>(),
+            in_sum.as<double>(), t_mass.as<double>(), t_com.as<double>());
+    }
+    if (!compat)
+        k_leaf_multipoles<<<grid, OT_THREADS, 0, s>>>(ctr.as<int>(), d_x, d_m, sidx.as<int>(),
+                                                      t_np.as<int>(), t_nc.as<int>(),
+                                                      t_fp.as<int>(), t_mass.as<double>(),
+                                                      t_com.as<double>());
+    k_walk_nodes<<<grid, OT_THREADS, 0, s>>>(
+        ctr.as<int>(), compat ? 1 : 0, frame.as<double>(), keys.as<uint64_t>(), sidx.as<int>(),
+        t_np.as<int>(), t_nc.as<int>(), t_fp.as<int>(), t_fc.as<int>(), t_mass.as<double>(),
+        t_com.as<double>(), w_na.as<float4>(), w_nb.as<float4>(), w_nc.as<int4>(),
+        w_nkey.as<uint64_t>());
+    k_walk_particles<<<pb, OT_THREADS, 0, s>>>(n, frame.as<double>(), d_x, d_m, sidx.as<int>(),
+                                               w_pa.as<float4>(), w_pb.as<float4>());
+    GS_CUDA(cudaGetLastError());
+    return ok();
+}
+
+ErrorStatus OctreeDevice::read_counts(cudaStream_t s, int *nodes, unsigned *status)
+{
+    int h[3];
+    GS_CUDA(cudaMemcpyAsync(h, ctr.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+    GS_CUDA(cudaStreamSynchronize(s));
+    if (nodes) *nodes = h[CTR_NODES];
+    if (status) *status = (unsigned)h[CTR_STATUS];
+    return ok();
+}
+
+}  // namespace gs

@@ -265,7 +265,8 @@ def launch_simulation(lib: ctypes.CDLL, x: np.ndarray, v: np.ndarray,
     if ret != 0:
         raise RuntimeError("Simulation failed. Please check the C library traceback.")
     k = num.value
-    return (np.ctypeslib.as_array(new_ids, shape=(k,)),
-            np.ctypeslib.as_array(new_x, shape=(k, 3)),
-            np.ctypeslib.as_array(new_v, shape=(k, 3)),
-            np.ctypeslib.as_array(new_m, shape=(k,)))
+    # The C side returns the caller's own buffers (src/python_interface.c:186-190),
+    # possibly compacted to k particles; hand back views of the numpy arrays
+    # that own that memory so they stay alive with the result.
+    assert ctypes.addressof(new_x.contents) == x.ctypes.data
+    return (ids[:k], x.reshape(-1, 3)[:k], v.reshape(-1, 3)[:k], m[:k])

@@ -260,6 +260,12 @@ int gsgpu_sim_force_timing(const gsgpu_sim *sim, double *total_ms,
                            int64_t *launches);
 /* Number of kernels launched by the most recent gsgpu_sim_run step. */
 int gsgpu_sim_kernels_per_step(const gsgpu_sim *sim);
+/* Interactions of the most recent force evaluation: counts[0] cell
+ * (monopole) terms, counts[1] particle-particle terms (tree methods; both 0
+ * for the direct sums, whose count is N(N-1)). */
+int gsgpu_sim_interaction_counts(gsgpu_sim *sim, long long *counts);
+/* The same for the calling thread's most recent acceleration() call. */
+int gsgpu_last_interaction_counts(long long *counts);
 void gsgpu_sim_destroy(gsgpu_sim *sim);
 
 /* Library / device information: fills name (NUL-terminated, <= len). */

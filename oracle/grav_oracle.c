@@ -359,7 +359,7 @@ void orc_free_tree(OrcTree *t)
  * itself) and an internal node is opened. */
 void orc_bh_walk(int n, const double *x, const double *m, double G,
                  double eps, double theta, const OrcTree *t, int compat,
-                 double *a, int64_t *counts)
+                 double *a, int64_t *counts, double *absum)
 {
     const double eps2 = eps * eps;
     const double th2 = theta * theta;
@@ -368,7 +368,7 @@ void orc_bh_walk(int n, const double *x, const double *m, double G,
         const int id = t->sorted_indices[s];
         const int64_t key_i = compat ? t->keys[id] : t->keys[s];
         const double xi0 = x[3 * id + 0], xi1 = x[3 * id + 1], xi2 = x[3 * id + 2];
-        double ax = 0.0, ay = 0.0, az = 0.0;
+        double ax = 0.0, ay = 0.0, az = 0.0, mag = 0.0;
         int64_t n_cell = 0, n_pp = 0;
         struct { int node; int next; } st[ORC_MORTON_MAX_LEVEL + 2];
         int top = 0;
@@ -393,6 +393,7 @@ void orc_bh_walk(int n, const double *x, const double *m, double G,
                         const double rn = sqrt(ns + eps2);
                         const double tv = G * t->mass[c] / (rn * rn * rn);
                         ax -= tv * r0; ay -= tv * r1; az -= tv * r2;
+                        mag += fabs(tv) * sqrt(ns);
                         ++n_cell;
                         st[top].next++;
                         continue;
@@ -409,6 +410,7 @@ void orc_bh_walk(int n, const double *x, const double *m, double G,
                         const double rn = sqrt(r0 * r0 + r1 * r1 + r2 * r2 + eps2);
                         const double tv = G * m[pj] / (rn * rn * rn);
                         ax -= tv * r0; ay -= tv * r1; az -= tv * r2;
+                        mag += fabs(tv) * sqrt(r0 * r0 + r1 * r1 + r2 * r2);
                         ++n_pp;
                     }
                     st[top].next++;
@@ -426,6 +428,7 @@ void orc_bh_walk(int n, const double *x, const double *m, double G,
         }
         a[3 * id + 0] = ax; a[3 * id + 1] = ay; a[3 * id + 2] = az;
         if (counts) { counts[2 * id] = n_cell; counts[2 * id + 1] = n_pp; }
+        if (absum) absum[id] = mag;
     }
 }
 
@@ -435,7 +438,7 @@ int orc_barnes_hut(int n, const double *x, const double *m, double G,
 {
     OrcTree t;
     int rc = orc_build_tree(n, x, m, leaf_max, compat, &t);
-    if (rc == 0) orc_bh_walk(n, x, m, G, eps, theta, &t, compat, a, NULL);
+    if (rc == 0) orc_bh_walk(n, x, m, G, eps, theta, &t, compat, a, NULL, NULL);
     orc_free_tree(&t);
     return rc;
 }
@@ -611,6 +614,26 @@ double orc_angular_momentum(int n, const double *x, const double *v,
         L += m[i] * (c0 + c1 + c2);
     }
     return L;
+}
+
+void orc_abs_sum_rows(int n, const double *x, const double *m, double G,
+                      double eps, int nrows, const int *rows, double *out)
+{
+    const double eps2 = eps * eps;
+    for (int r = 0; r < nrows; ++r) {
+        const int i = rows[r];
+        double s = 0.0;
+        for (int j = 0; j < n; ++j) {
+            if (j == i) continue;
+            const double d0 = x[3 * j + 0] - x[3 * i + 0];
+            const double d1 = x[3 * j + 1] - x[3 * i + 1];
+            const double d2 = x[3 * j + 2] - x[3 * i + 2];
+            const double q = d0 * d0 + d1 * d1 + d2 * d2;
+            const double r2 = q + eps2;
+            if (r2 > 0.0) s += m[j] * sqrt(q) / (r2 * sqrt(r2));
+        }
+        out[r] = G * s;
+    }
 }
 
 void orc_direct_rows(int n, const double *x, const double *m, double G,

@@ -74,10 +74,11 @@ void orc_free_tree(OrcTree *tree);
  * cell-membership test, which indexes the sorted key array by particle id
  * (:120, :145); compat=0 uses each particle's own sorted key.  If counts is
  * not NULL it receives, per particle, the number of accepted cells (counts[2i])
- * and of leaf particle-particle terms (counts[2i+1]). */
+ * and of leaf particle-particle terms (counts[2i+1]); if absum is not NULL it
+ * receives the sum of the magnitudes of the particle's terms. */
 void orc_bh_walk(int n, const double *x, const double *m, double G,
                  double eps, double theta, const OrcTree *tree, int compat,
-                 double *a, int64_t *counts);
+                 double *a, int64_t *counts, double *absum);
 
 /* Whole Barnes-Hut evaluation: build + walk (src/acceleration_barnes_hut.c:33-76). */
 int orc_barnes_hut(int n, const double *x, const double *m, double G,
@@ -110,5 +111,10 @@ double orc_angular_momentum(int n, const double *x, const double *v,
  * relative-error statistics (not a reference restatement). */
 void orc_direct_rows(int n, const double *x, const double *m, double G,
                      double eps, int nrows, const int *rows, double *a_rows);
+
+/* Sum of pair-term magnitudes, A_i = G sum_j m_j |r_ij| / (r_ij^2+eps^2)^1.5:
+ * the scale against which the rounding of FP32 pair terms is bounded. */
+void orc_abs_sum_rows(int n, const double *x, const double *m, double G,
+                      double eps, int nrows, const int *rows, double *out);
 
 #endif

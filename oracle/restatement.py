@@ -65,7 +65,7 @@ def load():
     lib.orc_free_tree.argtypes = [ctypes.POINTER(OrcTree)]
     lib.orc_bh_walk.argtypes = [ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double,
                                 ctypes.c_double, ctypes.POINTER(OrcTree), ctypes.c_int,
-                                dp, lp]
+                                dp, lp, dp]
     lib.orc_barnes_hut.argtypes = [ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_int, ctypes.c_int, dp]
     lib.orc_fixed_step_run.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp,
@@ -79,6 +79,8 @@ def load():
     lib.orc_angular_momentum.restype = ctypes.c_double
     lib.orc_direct_rows.argtypes = [ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_int, ip, dp]
+    lib.orc_abs_sum_rows.argtypes = [ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_int, ip, dp]
     _lib = lib
     return lib
 
@@ -169,17 +171,19 @@ def barnes_hut(x, m, G, eps, theta, leaf_max, compat):
 
 
 def bh_counts(x, m, G, eps, theta, leaf_max, compat):
-    """Per-particle (accepted cells, leaf pair terms) of the walk."""
+    """Walk with diagnostics: (a, per-particle [accepted cells, leaf pair
+    terms], per-particle sum of term magnitudes)."""
     x, m = _c(x), _c(m)
     t = OrcTree()
     lib = load()
     assert lib.orc_build_tree(m.size, _d(x), _d(m), leaf_max, int(compat), ctypes.byref(t)) == 0
     a = np.empty((m.size, 3))
     cnt = np.empty((m.size, 2), dtype=np.int64)
+    mag = np.empty(m.size)
     lib.orc_bh_walk(m.size, _d(x), _d(m), G, eps, theta, ctypes.byref(t), int(compat),
-                    _d(a), cnt.ctypes.data_as(lp))
+                    _d(a), cnt.ctypes.data_as(lp), _d(mag))
     lib.orc_free_tree(ctypes.byref(t))
-    return a, cnt
+    return a, cnt, mag
 
 
 def fixed_step_run(integrator, method, x, v, m, G, eps, dt, tf):
@@ -212,6 +216,16 @@ def direct_rows(x, m, G, eps, rows):
     load().orc_direct_rows(m.size, _d(x), _d(m), G, eps, rows.size,
                            rows.ctypes.data_as(ip), _d(a))
     return a
+
+
+def abs_sum_rows(x, m, G, eps, rows=None):
+    """A_i = G sum_j m_j |r_ij| / (r_ij^2 + eps^2)^1.5 for the given rows."""
+    x, m = _c(x), _c(m)
+    rows = np.arange(m.size, dtype=np.int32) if rows is None else _c(rows, np.int32)
+    out = np.empty(rows.size)
+    load().orc_abs_sum_rows(m.size, _d(x), _d(m), G, eps, rows.size,
+                            rows.ctypes.data_as(ip), _d(out))
+    return out
 
 
 def rel_err(a, b):

