@@ -24,6 +24,9 @@ struct OctreeDevice {
     int cap_nodes = 0;   // node capacity
     int leaf_max = 1;
     bool compat = true;
+    bool quad = false;   // traceless quadrupoles about the centre of mass
+    DBuf t_quad;         // double[6*cap]: xx, xy, xz, yy, yz, zz
+    DBuf w_nq;           // float4[2*cap]: (xx, xy, xz, yy), (yz, zz, 0, 0)
 
     DBuf ctr;                 // int[CTR_SIZE]
     DBuf frame;               // double[8]: cx, cy, cz, width, box_length
@@ -47,7 +50,7 @@ struct OctreeDevice {
     DBuf w_pa, w_pb;          // float4[n] in sorted order: (x_hi, m), (x_lo, 0)
     RadixSorter sorter;
 
-    ErrorStatus setup(int n, int leaf_max, bool compat);
+    ErrorStatus setup(int n, int leaf_max, bool compat, bool quad = false);
     // Builds the tree from device x [3n] and m [n].  box_center/box_width
     // (host values) replace the bounding box when box_width > 0.
     ErrorStatus build(const double *d_x, const double *d_m, cudaStream_t s,

@@ -423,22 +423,81 @@ __global__ void k_multipole_level(int d, const int *__restrict__ ctr, const doub
     }
 }
 
-// Leaves with their own mass and centre of mass (non-compat trees).
+// Leaves with their own mass and centre of mass (non-compat trees), and,
+// when q is not null, their quadrupole sum_p m (3 d d^T - |d|^2 I) about it.
 __global__ void k_leaf_multipoles(const int *__restrict__ ctr, const double *__restrict__ x,
                                   const double *__restrict__ m, const int *__restrict__ sidx,
                                   const int *__restrict__ t_np, const int *__restrict__ t_nc,
                                   const int *__restrict__ t_fp, double *__restrict__ t_mass,
-                                  double *__restrict__ t_com)
+                                  double *__restrict__ t_com, double *__restrict__ q)
 {
     const int nn = ctr[CTR_NODES];
     for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < nn; id += gridDim.x * blockDim.x) {
         if (t_nc[id] > 0) continue;
         double M = 0.0, S0 = 0.0, S1 = 0.0, S2 = 0.0;
         add_particles(x, m, sidx, t_fp[id], t_np[id], M, S0, S1, S2);
+        const double c0 = __ddiv_rn(S0, M), c1 = __ddiv_rn(S1, M), c2 = __ddiv_rn(S2, M);
         t_mass[id] = M;
-        t_com[3 * id + 0] = __ddiv_rn(S0, M);
-        t_com[3 * id + 1] = __ddiv_rn(S1, M);
-        t_com[3 * id + 2] = __ddiv_rn(S2, M);
+        t_com[3 * id + 0] = c0;
+        t_com[3 * id + 1] = c1;
+        t_com[3 * id + 2] = c2;
+        if (q) {
+            double Q[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+            for (int p = t_fp[id]; p < t_fp[id] + t_np[id]; ++p) {
+                const int pid = sidx[p];
+                const double mp = m[pid];
+                const double d0 = x[3 * pid] - c0, d1 = x[3 * pid + 1] - c1, d2 = x[3 * pid + 2] - c2;
+                const double r2 = d0 * d0 + d1 * d1 + d2 * d2;
+                Q[0] += mp * (3.0 * d0 * d0 - r2);
+                Q[1] += mp * 3.0 * d0 * d1;
+                Q[2] += mp * 3.0 * d0 * d2;
+                Q[3] += mp * (3.0 * d1 * d1 - r2);
+                Q[4] += mp * 3.0 * d1 * d2;
+                Q[5] += mp * (3.0 * d2 * d2 - r2);
+            }
+            for (int k = 0; k < 6; ++k) q[6 * (size_t)id + k] = Q[k];
+        }
+    }
+}
+
+// Quadrupoles of the internal nodes of depth d from their children by the
+// parallel-axis shift: Q = sum_c [Q_c + M_c (3 s s^T - |s|^2 I)], s = com_c - com.
+__global__ void k_quadrupole_level(int d, const int *__restrict__ ctr, const int *__restrict__ in_id,
+                                   const int *__restrict__ in_fc, const int *__restrict__ in_nchild,
+                                   const double *__restrict__ t_mass,
+                                   const double *__restrict__ t_com, double *__restrict__ q)
+{
+    const int lo = ctr[CTR_LVL + d];
+    const int hi = ctr[CTR_LVL + d + 1];
+    for (int ii = lo + blockIdx.x * blockDim.x + threadIdx.x; ii < hi;
+         ii += gridDim.x * blockDim.x) {
+        const int id = in_id[ii];
+        const double c0 = t_com[3 * id], c1 = t_com[3 * id + 1], c2 = t_com[3 * id + 2];
+        double Q[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int c = in_fc[ii]; c < in_fc[ii] + in_nchild[ii]; ++c) {
+            const double Mc = t_mass[c];
+            const double s0 = t_com[3 * c] - c0, s1 = t_com[3 * c + 1] - c1, s2 = t_com[3 * c + 2] - c2;
+            const double r2 = s0 * s0 + s1 * s1 + s2 * s2;
+            const double *qc = q + 6 * (size_t)c;
+            Q[0] += qc[0] + Mc * (3.0 * s0 * s0 - r2);
+            Q[1] += qc[1] + Mc * 3.0 * s0 * s1;
+            Q[2] += qc[2] + Mc * 3.0 * s0 * s2;
+            Q[3] += qc[3] + Mc * (3.0 * s1 * s1 - r2);
+            Q[4] += qc[4] + Mc * 3.0 * s1 * s2;
+            Q[5] += qc[5] + Mc * (3.0 * s2 * s2 - r2);
+        }
+        for (int k = 0; k < 6; ++k) q[6 * (size_t)id + k] = Q[k];
+    }
+}
+
+__global__ void k_walk_quads(const int *__restrict__ ctr, const double *__restrict__ q,
+                             float4 *__restrict__ nq)
+{
+    const int nn = ctr[CTR_NODES];
+    for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < nn; id += gridDim.x * blockDim.x) {
+        const double *Q = q + 6 * (size_t)id;
+        nq[2 * (size_t)id] = make_float4((float)Q[0], (float)Q[1], (float)Q[2], (float)Q[3]);
+        nq[2 * (size_t)id + 1] = make_float4((float)Q[4], (float)Q[5], 0.0f, 0.0f);
     }
 }
 
@@ -490,11 +549,12 @@ __global__ void k_walk_particles(int n, const double *__restrict__ frame, const 
 }
 
 // ------------------------------------------------------------------------
-ErrorStatus OctreeDevice::setup(int n_, int leaf_max_, bool compat_)
+ErrorStatus OctreeDevice::setup(int n_, int leaf_max_, bool compat_, bool quad_)
 {
     n = n_;
     leaf_max = leaf_max_;
     compat = compat_;
+    quad = quad_ && !compat_;
     int cap = 4 * n + 4096;
     if (cap < n) return GS_RAISE(GRAV_VALUE_ERROR, "too many particles for the octree: %d", n);
     cap_nodes = cap;
@@ -519,6 +579,10 @@ ErrorStatus OctreeDevice::setup(int n_, int leaf_max_, bool compat_)
     GS_TRY(w_nkey.reserve((size_t)cap * sizeof(uint64_t)));
     GS_TRY(w_pa.reserve((size_t)n * sizeof(float4)));
     GS_TRY(w_pb.reserve((size_t)n * sizeof(float4)));
+    if (quad) {
+        GS_TRY(t_quad.reserve((size_t)cap * 6 * sizeof(double)));
+        GS_TRY(w_nq.reserve((size_t)cap * 2 * sizeof(float4)));
+    }
     GS_TRY(sorter.reserve(std::max(n, cap)));
     return ok();
 }
@@ -526,9 +590,9 @@ ErrorStatus OctreeDevice::setup(int n_, int leaf_max_, bool compat_)
 int OctreeDevice::launches_per_build() const
 {
     // bbox 2, morton 1, sort, init 1, levels 2*21, keys 1, sort, fc 3,
-    // number 1, multipoles 21 (+1 leaves), walk arrays 2
+    // number 1, multipoles 21 (+1 leaves), walk arrays 2 (+ quadrupoles 21 + 1)
     return 2 + 1 + RadixSorter::launches(63) + 1 + 42 + 1 + RadixSorter::launches(36) + 3 + 1 +
-           21 + (compat ? 0 : 1) + 2;
+           21 + (compat ? 0 : 1) + 2 + (quad ? 22 : 0);
 }
 
 ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream_t s,
@@ -578,17 +642,24 @@ ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream
         t_fc.as<int>(), t_depth.as<int>(), t_int.as<int>(), t_mass.as<double>(),
         t_com.as<double>());
     GS_CUDA(cudaGetLastError());
+    if (!compat)
+        k_leaf_multipoles<<<grid, OT_THREADS, 0, s>>>(
+            ctr.as<int>(), d_x, d_m, sidx.as<int>(), t_np.as<int>(), t_nc.as<int>(),
+            t_fp.as<int>(), t_mass.as<double>(), t_com.as<double>(),
+            quad ? t_quad.as<double>() : nullptr);
     for (int d = OCT_MAX_LEVEL - 1; d >= 0; --d) {
         k_multipole_level<<<grid, OT_THREADS, 0, s>>>(
             d, ctr.as<int>(), d_x, d_m, sidx.as<int>(), in_id.as<int>(), in_fc.as<int>(),
             in_nchild.as<int>(), t_np.as<int>(), t_nc.as<int>(), t_fp.as<int>(), t_int.as<int>(),
             in_sum.as<double>(), t_mass.as<double>(), t_com.as<double>());
+        if (quad)
+            k_quadrupole_level<<<grid, OT_THREADS, 0, s>>>(
+                d, ctr.as<int>(), in_id.as<int>(), in_fc.as<int>(), in_nchild.as<int>(),
+                t_mass.as<double>(), t_com.as<double>(), t_quad.as<double>());
     }
-    if (!compat)
-        k_leaf_multipoles<<<grid, OT_THREADS, 0, s>>>(ctr.as<int>(), d_x, d_m, sidx.as<int>(),
-                                                      t_np.as<int>(), t_nc.as<int>(),
-                                                      t_fp.as<int>(), t_mass.as<double>(),
-                                                      t_com.as<double>());
+    if (quad)
+        k_walk_quads<<<grid, OT_THREADS, 0, s>>>(ctr.as<int>(), t_quad.as<double>(),
+                                                 w_nq.as<float4>());
     k_walk_nodes<<<grid, OT_THREADS, 0, s>>>(
         ctr.as<int>(), compat ? 1 : 0, frame.as<double>(), keys.as<uint64_t>(), sidx.as<int>(),
         t_np.as<int>(), t_nc.as<int>(), t_fp.as<int>(), t_fc.as<int>(), t_mass.as<double>(),

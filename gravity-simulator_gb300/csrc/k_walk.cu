@@ -38,6 +38,7 @@ constexpr int WK_STACK = OCT_MAX_LEVEL + 2;
 struct WalkArgs {
     const float4 *na;
     const float4 *nb;
+    const float4 *nq;       // quadrupoles (2 float4 per node) or null
     const int4 *nc;
     const uint64_t *nkey;
     const double *ncom;     // FP64 centre of mass [3*nodes] (exact opening test)
@@ -65,6 +66,7 @@ __device__ __forceinline__ void add3(float &sx, float &cx, float &sy, float &cy,
     kahan_add(sz, cz, pz);
 }
 
+template <bool QUAD>
 __global__ void __launch_bounds__(WK_THREADS)
 k_bh_walk(WalkArgs A)
 {
@@ -162,8 +164,25 @@ k_bh_walk(WalkArgs A)
                 if (accept) {
                     const float r2 = ns + A.eps2;
                     const float ri = rsqrt_approx(r2);
-                    const float sc = ca.w * ri * ri * ri;
-                    add3(sx, cx, sy, cy, sz, cz, dx * sc, dy * sc, dz * sc);
+                    const float ri2 = ri * ri;
+                    const float ri3 = ri2 * ri;
+                    const float sc = ca.w * ri3;
+                    float px = dx * sc, py = dy * sc, pz = dz * sc;
+                    if (QUAD) {
+                        // d = com - x = -R:  G [-Q d / r^5 + 2.5 (d.Q.d) d / r^7]
+                        const float4 q0 = A.nq[2 * c];
+                        const float4 q1 = A.nq[2 * c + 1];
+                        const float qx = q0.x * dx + q0.y * dy + q0.z * dz;
+                        const float qy = q0.y * dx + q0.w * dy + q1.x * dz;
+                        const float qz = q0.z * dx + q1.x * dy + q1.y * dz;
+                        const float dqd = dx * qx + dy * qy + dz * qz;
+                        const float ri5 = ri3 * ri2;
+                        const float f = 2.5f * dqd * ri5 * ri2;
+                        px += f * dx - qx * ri5;
+                        py += f * dy - qy * ri5;
+                        pz += f * dz - qz * ri5;
+                    }
+                    add3(sx, cx, sy, cy, sz, cz, px, py, pz);
                     ++n_cell;
                     dec = 1;
                 }
@@ -231,7 +250,7 @@ namespace {
 
 class BarnesHutEngine final : public Engine {
   public:
-    explicit BarnesHutEngine(bool compat) : compat_(compat) {}
+    BarnesHutEngine(bool compat, bool quad) : compat_(compat), quad_(quad && !compat) {}
 
     ErrorStatus setup(int n, double G, const AccelerationParam &p) override
     {
@@ -239,7 +258,7 @@ class BarnesHutEngine final : public Engine {
         G_ = G;
         eps_ = p.softening_length;
         theta_ = p.opening_angle;
-        GS_TRY(tree_.setup(n, p.max_num_particles_per_leaf, compat_));
+        GS_TRY(tree_.setup(n, p.max_num_particles_per_leaf, compat_, quad_));
         GS_TRY(counters_.reserve(4 * sizeof(unsigned long long)));
         GS_CUDA(cudaMemset(counters_.p, 0, 4 * sizeof(unsigned long long)));
         return ok();
@@ -252,6 +271,7 @@ class BarnesHutEngine final : public Engine {
         WalkArgs w;
         w.na = tree_.w_na.as<float4>();
         w.nb = tree_.w_nb.as<float4>();
+        w.nq = quad_ ? tree_.w_nq.as<float4>() : nullptr;
         w.nc = tree_.w_nc.as<int4>();
         w.nkey = tree_.w_nkey.as<uint64_t>();
         w.ncom = tree_.t_com.as<double>();
@@ -271,7 +291,11 @@ class BarnesHutEngine final : public Engine {
         w.status = reinterpret_cast<unsigned *>(tree_.ctr.as<int>() + CTR_STATUS);
         GS_CUDA(cudaMemsetAsync(counters_.p, 0, 2 * sizeof(unsigned long long), s));
         if (timer) GS_TRY(timer->begin(s));
-        k_bh_walk<<<(n_ + WK_THREADS - 1) / WK_THREADS, WK_THREADS, 0, s>>>(w);
+        const int grid = (n_ + WK_THREADS - 1) / WK_THREADS;
+        if (quad_)
+            k_bh_walk<true><<<grid, WK_THREADS, 0, s>>>(w);
+        else
+            k_bh_walk<false><<<grid, WK_THREADS, 0, s>>>(w);
         GS_CUDA(cudaGetLastError());
         if (timer) GS_TRY(timer->end(s));
         return ok();
@@ -302,7 +326,7 @@ class BarnesHutEngine final : public Engine {
     }
 
   private:
-    bool compat_;
+    bool compat_, quad_;
     int n_ = 0;
     double G_ = 1.0, eps_ = 0.0, theta_ = 1.0;
     OctreeDevice tree_;
@@ -311,9 +335,9 @@ class BarnesHutEngine final : public Engine {
 
 }  // namespace
 
-std::unique_ptr<Engine> make_barnes_hut_engine(bool compat)
+std::unique_ptr<Engine> make_barnes_hut_engine(bool compat, bool quad)
 {
-    return std::unique_ptr<Engine>(new BarnesHutEngine(compat));
+    return std::unique_ptr<Engine>(new BarnesHutEngine(compat, quad));
 }
 
 ErrorStatus accel_host(double *a, const System *system, const AccelerationParam *param_in);

@@ -64,6 +64,7 @@ typedef struct System {
 #define GRAV_GPU_MASSLESS 102           /* FP64 massive/massless direct sum */
 #define GRAV_GPU_BARNES_HUT 103         /* FP32 walk, true leaf multipoles */
 #define GRAV_GPU_BH_LEARNED 104         /* theta-cheap walk + learned residual */
+#define GRAV_GPU_BARNES_HUT_QUAD 105    /* FP32 walk, monopole + quadrupole cells */
 #define GRAV_GPU_PAIRWISE_FP64 111      /* FP64 direct sum, reference order */
 #define GRAV_GPU_BARNES_HUT_COMPAT 113  /* FP32 walk, reference tree quirks */
 

@@ -432,6 +432,107 @@ void orc_bh_walk(int n, const double *x, const double *m, double G,
     }
 }
 
+/* Traceless quadrupole moment of every node about its centre of mass,
+ * Q = sum_p m_p (3 d d^T - |d|^2 I), d = x_p - com, summed directly over the
+ * node's particles; stored (xx, xy, xz, yy, yz, zz).  Not part of grav_sim:
+ * the checker for the quadrupole extension of the walk. */
+void orc_quadrupoles(const OrcTree *t, const double *x, const double *m,
+                     double *q)
+{
+    for (int c = 0; c < t->num_nodes; ++c) {
+        double s[6] = {0, 0, 0, 0, 0, 0};
+        const double *cm = &t->com[3 * c];
+        for (int p = t->first_particle[c]; p < t->first_particle[c] + t->num_particles[c]; ++p) {
+            const int id = t->sorted_indices[p];
+            const double d0 = x[3 * id] - cm[0], d1 = x[3 * id + 1] - cm[1], d2 = x[3 * id + 2] - cm[2];
+            const double r2 = d0 * d0 + d1 * d1 + d2 * d2, mm = m[id];
+            s[0] += mm * (3 * d0 * d0 - r2);
+            s[1] += mm * 3 * d0 * d1;
+            s[2] += mm * 3 * d0 * d2;
+            s[3] += mm * (3 * d1 * d1 - r2);
+            s[4] += mm * 3 * d1 * d2;
+            s[5] += mm * (3 * d2 * d2 - r2);
+        }
+        for (int k = 0; k < 6; ++k) q[6 * c + k] = s[k];
+    }
+}
+
+/* The corrected walk (compat = 0 decisions) with monopole + quadrupole terms
+ * for accepted cells:  a += G [ -M R / r^3 + Q R / r^5 - 2.5 (R.Q.R) R / r^7 ],
+ * R = x_i - com, r^2 = |R|^2 + eps^2.  Leaves add particle terms as usual. */
+void orc_bh_walk_quad(int n, const double *x, const double *m, double G,
+                      double eps, double theta, const OrcTree *t, const double *q,
+                      double *a, double *absum)
+{
+    const double eps2 = eps * eps;
+    const double th2 = theta * theta;
+    const double box_length = t->box_width * 2.0;
+    for (int s = 0; s < n; ++s) {
+        const int id = t->sorted_indices[s];
+        const int64_t key_i = t->keys[s];
+        double acc[3] = {0.0, 0.0, 0.0}, mag = 0.0;
+        struct { int node; int next; } st[ORC_MORTON_MAX_LEVEL + 2];
+        int top = 0, level = 1;
+        st[0].node = 0; st[0].next = 0;
+        for (;;) {
+            const int nd = st[top].node;
+            if (st[top].next < t->num_children[nd]) {
+                const int c = t->first_child[nd] + st[top].next;
+                const int first = t->first_particle[c];
+                const int sh = 3 * (ORC_MORTON_MAX_LEVEL - level);
+                const int inside = (key_i >> sh) == (t->keys[first] >> sh);
+                if (!inside) {
+                    double R[3];
+                    for (int k = 0; k < 3; ++k) R[k] = x[3 * id + k] - t->com[3 * c + k];
+                    const double bl = box_length / (double)(2 << level);
+                    const double ns = R[0] * R[0] + R[1] * R[1] + R[2] * R[2];
+                    if (bl * bl < th2 * ns) {
+                        const double r2 = ns + eps2, ri = 1.0 / sqrt(r2);
+                        const double ri3 = ri * ri * ri, ri5 = ri3 * ri * ri, ri7 = ri5 * ri * ri;
+                        const double *Q = &q[6 * c];
+                        const double QR[3] = {Q[0] * R[0] + Q[1] * R[1] + Q[2] * R[2],
+                                              Q[1] * R[0] + Q[3] * R[1] + Q[4] * R[2],
+                                              Q[2] * R[0] + Q[4] * R[1] + Q[5] * R[2]};
+                        const double RQR = R[0] * QR[0] + R[1] * QR[1] + R[2] * QR[2];
+                        for (int k = 0; k < 3; ++k) {
+                            const double tm = -t->mass[c] * ri3 * R[k];
+                            const double tq = QR[k] * ri5 - 2.5 * RQR * R[k] * ri7;
+                            acc[k] += G * (tm + tq);
+                        }
+                        mag += G * t->mass[c] * ri3 * sqrt(ns);
+                        st[top].next++;
+                        continue;
+                    }
+                }
+                if (t->num_children[c] <= 0) {
+                    for (int p = first; p < first + t->num_particles[c]; ++p) {
+                        const int j = t->sorted_indices[p];
+                        if (j == id) continue;
+                        double R[3];
+                        for (int k = 0; k < 3; ++k) R[k] = x[3 * id + k] - x[3 * j + k];
+                        const double q2 = R[0] * R[0] + R[1] * R[1] + R[2] * R[2];
+                        const double r2 = q2 + eps2, ri = 1.0 / sqrt(r2);
+                        for (int k = 0; k < 3; ++k) acc[k] -= G * m[j] * ri * ri * ri * R[k];
+                        mag += G * m[j] * ri * ri * ri * sqrt(q2);
+                    }
+                    st[top].next++;
+                    continue;
+                }
+                ++top;
+                st[top].node = c; st[top].next = 0;
+                ++level;
+                continue;
+            }
+            if (top == 0) break;
+            --top;
+            st[top].next++;
+            --level;
+        }
+        for (int k = 0; k < 3; ++k) a[3 * id + k] = acc[k];
+        if (absum) absum[id] = mag;
+    }
+}
+
 int orc_barnes_hut(int n, const double *x, const double *m, double G,
                    double eps, double theta, int leaf_max, int compat,
                    double *a)

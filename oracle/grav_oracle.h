@@ -80,6 +80,15 @@ void orc_bh_walk(int n, const double *x, const double *m, double G,
                  double eps, double theta, const OrcTree *tree, int compat,
                  double *a, int64_t *counts, double *absum);
 
+/* Quadrupole extension (not in grav_sim): traceless node quadrupoles about
+ * the centre of mass, q[6*node] = (xx, xy, xz, yy, yz, zz), and the
+ * corrected walk with monopole + quadrupole cell terms. */
+void orc_quadrupoles(const OrcTree *tree, const double *x, const double *m,
+                     double *q);
+void orc_bh_walk_quad(int n, const double *x, const double *m, double G,
+                      double eps, double theta, const OrcTree *tree,
+                      const double *q, double *a, double *absum);
+
 /* Whole Barnes-Hut evaluation: build + walk (src/acceleration_barnes_hut.c:33-76). */
 int orc_barnes_hut(int n, const double *x, const double *m, double G,
                    double eps, double theta, int leaf_max, int compat,

@@ -186,6 +186,26 @@ def bh_counts(x, m, G, eps, theta, leaf_max, compat):
     return a, cnt, mag
 
 
+def bh_quad(x, m, G, eps, theta, leaf_max):
+    """Corrected walk with quadrupole cell terms: (a, per-particle magnitude
+    sum, node quadrupoles [nodes, 6])."""
+    x, m = _c(x), _c(m)
+    lib = load()
+    lib.orc_quadrupoles.argtypes = [ctypes.POINTER(OrcTree), dp, dp, dp]
+    lib.orc_bh_walk_quad.argtypes = [ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_double, ctypes.POINTER(OrcTree), dp, dp, dp]
+    t = OrcTree()
+    assert lib.orc_build_tree(m.size, _d(x), _d(m), leaf_max, 0, ctypes.byref(t)) == 0
+    q = np.empty((t.num_nodes, 6))
+    lib.orc_quadrupoles(ctypes.byref(t), _d(x), _d(m), _d(q))
+    a = np.empty((m.size, 3))
+    mag = np.empty(m.size)
+    lib.orc_bh_walk_quad(m.size, _d(x), _d(m), G, eps, theta, ctypes.byref(t), _d(q), _d(a),
+                         _d(mag))
+    lib.orc_free_tree(ctypes.byref(t))
+    return a, mag, q
+
+
 def fixed_step_run(integrator, method, x, v, m, G, eps, dt, tf):
     x, v, m = _c(x).copy(), _c(v).copy(), _c(m)
     rc = load().orc_fixed_step_run(integrator, method, m.size, _d(x), _d(v), _d(m),

@@ -145,6 +145,20 @@ def test_reference_entry_point_acceleration_barnes_hut(lib, g, orc, wl):
     check_terms(a, a_o, mag)
 
 
+@pytest.mark.parametrize("theta", [0.5, 1.0])
+def test_quadrupole_walk_vs_oracle(lib, g, orc, wl, theta):
+    """GRAV_GPU_BARNES_HUT_QUAD: same opening decisions as the corrected walk,
+    cells add monopole + quadrupole terms; quadrupoles composed bottom-up on
+    the GPU (parallel-axis shifts) against the oracle's direct per-node sums."""
+    x, v, m = wl.galaxy_pair(32768, 12)
+    a = g.acceleration(lib, x, m, 1.0, g.METHOD_GPU_BARNES_HUT_QUAD, opening_angle=theta,
+                       softening_length=0.01, max_num_particles_per_leaf=1)
+    a_o, mag, q = orc.bh_quad(x, m, 1.0, 0.01, theta, 1)
+    _, cnt, _ = orc.bh_counts(x, m, 1.0, 0.01, theta, 1, False)
+    assert gpu_counts(lib) == (int(cnt[:, 0].sum()), int(cnt[:, 1].sum()))
+    check_terms(a, a_o, mag)
+
+
 def test_fixed_walk_accuracy_vs_direct_sum(lib, g, orc, wl):
     """Corrected multipoles: theta=0.5 reaches ~1e-3 median error against the
     FP64 direct sum on the galaxy model (the reference's walk does not)."""
