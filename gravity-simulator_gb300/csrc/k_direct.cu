@@ -28,6 +28,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <mutex>
 
 namespace gs {
 
@@ -378,4 +380,147 @@ std::unique_ptr<Engine> make_direct_engine(bool fp64_reference_order)
     return std::unique_ptr<Engine>(new DirectEngine(fp64_reference_order));
 }
 
+// ------------------------------------------------------------------------
+// Allocation-free compensated-FP32 direct sum.
+//
+// For callers that cannot allocate device memory while they run: code that
+// records or replays a fixed plan of work and may not call cudaMalloc
+// (which can synchronise the device) in the middle of it, embedders whose
+// allocator is a pool they own, and real-time loops that must not touch the
+// allocator at all.  This entry point computes the same accelerations as
+// acceleration() with GRAV_GPU_PAIRWISE, from device arrays the caller
+// owns, using the same kernels; its scratch (the packed float4 particles,
+// the per-split partial sums and the status word) lives in one file-scope
+// device array instead of memory the library allocates.  That array is part
+// of the library image: every GPU that loads the library holds its
+// NOALLOC_BYTES (about 6.5 MiB) until the process exits.
+constexpr int NOALLOC_MAX_N = 32768;      // largest particle count accepted
+constexpr int NOALLOC_MAX_SPLITS = 8;
+constexpr size_t NOALLOC_PJ_BYTES = (size_t)NOALLOC_MAX_N * sizeof(float4);
+constexpr size_t NOALLOC_PARTIAL_BYTES =
+    (size_t)NOALLOC_MAX_SPLITS * 3 * NOALLOC_MAX_N * sizeof(double);
+constexpr size_t NOALLOC_BYTES = NOALLOC_PJ_BYTES + NOALLOC_PARTIAL_BYTES + 256;
+static_assert(NOALLOC_MAX_N % DS_JTILE == 0, "capacity must be whole tiles");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+namespace {
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of the scratch array on the current device.  On a host
+// `g_noalloc_scratch` only names a host-side stand-in for the symbol, so
+// its address is looked up once per device (with that device current) by
+// cudaGetSymbolAddress, which allocates nothing.
+cudaError_t noalloc_scratch(void **out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return cudaSuccess;
+}
+
+}  // namespace
+
 }  // namespace gs
+
+extern "C" int gsgpu_pairwise_acceleration_noalloc(const double *d_x, const double *d_m,
+                                                   int num_particles, double G,
+                                                   double softening_length, double *d_a,
+                                                   void *stream)
+{
+    using namespace gs;
+    if (!d_x || !d_m || !d_a) {
+        std::fprintf(stderr, "gsgpu_pairwise_acceleration_noalloc: NULL array argument\n");
+        return GRAV_POINTER_ERROR;
+    }
+    if (num_particles < 1 || num_particles > NOALLOC_MAX_N) {
+        std::fprintf(stderr,
+                     "gsgpu_pairwise_acceleration_noalloc: num_particles must be in [1, %d] "
+                     "(the fixed scratch capacity). Got: %d\n",
+                     NOALLOC_MAX_N, num_particles);
+        return GRAV_VALUE_ERROR;
+    }
+    if (!(softening_length >= 0.0)) {
+        std::fprintf(stderr, "gsgpu_pairwise_acceleration_noalloc: Softening length is "
+                             "negative. Got: %.3g\n", softening_length);
+        return GRAV_VALUE_ERROR;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    void *base = nullptr;
+    cudaError_t e = noalloc_scratch(&base);
+    int dev = 0, sms = 0, per_sm = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_direct_sum<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 DS_SMEM);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_direct_sum<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 DS_SMEM);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_direct_sum<true>, DS_THREADS,
+                                                          DS_SMEM);
+    if (e != cudaSuccess) {
+        std::fprintf(stderr, "gsgpu_pairwise_acceleration_noalloc: %s\n", cudaGetErrorString(e));
+        return GRAV_FAILURE;
+    }
+    unsigned char *scratch = static_cast<unsigned char *>(base);
+    float4 *pj = reinterpret_cast<float4 *>(scratch);
+    double *partial = reinterpret_cast<double *>(scratch + NOALLOC_PJ_BYTES);
+    unsigned *status = reinterpret_cast<unsigned *>(scratch + NOALLOC_PJ_BYTES +
+                                                    NOALLOC_PARTIAL_BYTES);
+
+    // Same work split as the allocating engine, with at most 8 j-chunks.
+    const int n_pad = ((num_particles + DS_JTILE - 1) / DS_JTILE) * DS_JTILE;
+    const int i_tiles = n_pad / DS_ITILE;
+    const int jt_total = n_pad / DS_JTILE;
+    const long slots = (long)sms * (per_sm > 0 ? per_sm : 1);
+    int splits = 1, jt_per_chunk = jt_total;
+    double best = 1e300;
+    for (int sp = 1; sp <= std::min(jt_total, NOALLOC_MAX_SPLITS); ++sp) {
+        const int chunk = (jt_total + sp - 1) / sp;
+        const int used = (jt_total + chunk - 1) / chunk;
+        const long units = (long)i_tiles * used;
+        const double cost = (double)((units + slots - 1) / slots) * (chunk + 0.25);
+        if (cost < best - 1e-9) {
+            best = cost;
+            splits = used;
+            jt_per_chunk = chunk;
+        }
+    }
+
+    // The status word must start at zero; the packed array and the partial
+    // sums are fully rewritten by every call.
+    e = cudaMemsetAsync(status, 0, sizeof(unsigned), s);
+    if (e == cudaSuccess) {
+        k_pack_float4<<<(n_pad + 255) / 256, 256, 0, s>>>(d_x, d_m, num_particles, n_pad, 0.0,
+                                                          0.0, 0.0, pj);
+        const float eps2 = (float)(softening_length * softening_length);
+        if (eps2 > 0.0f)
+            k_direct_sum<true><<<i_tiles * splits, DS_THREADS, DS_SMEM, s>>>(
+                pj, n_pad, i_tiles, jt_per_chunk, jt_total, eps2, partial, status);
+        else
+            k_direct_sum<false><<<i_tiles * splits, DS_THREADS, DS_SMEM, s>>>(
+                pj, n_pad, i_tiles, jt_per_chunk, jt_total, eps2, partial, status);
+        k_reduce_splits<<<(num_particles + 255) / 256, 256, 0, s>>>(partial, splits,
+                                                                    num_particles, n_pad, G, d_a);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+        std::fprintf(stderr, "gsgpu_pairwise_acceleration_noalloc: %s\n", cudaGetErrorString(e));
+        return GRAV_FAILURE;
+    }
+    return GRAV_SUCCESS;
+}

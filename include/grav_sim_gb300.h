@@ -273,6 +273,30 @@ void gsgpu_sim_destroy(gsgpu_sim *sim);
 int gsgpu_device_info(char *name, int len, int *sm_count, int *cc_major,
                       int *cc_minor);
 
+/* Allocation-free compensated-FP32 direct sum.  No counterpart in the
+ * reference.  For callers that must not allocate device memory while they
+ * run -- code that records or replays a fixed plan of GPU work, where a
+ * cudaMalloc (which may synchronise the device) would break the plan;
+ * embedders whose device memory is a pool they manage; real-time loops that
+ * may not touch the allocator.  Computes the accelerations of
+ * acceleration() with GRAV_GPU_PAIRWISE (positions taken relative to the
+ * origin) from caller-owned device arrays d_x [3N], d_m [N] into d_a [3N],
+ * enqueued on `stream` (a cudaStream_t; NULL = legacy default stream) and not
+ * synchronised.  It calls no cudaMalloc, cudaFree or allocating library
+ * routine: its scratch is a fixed device array in the library image of about
+ * 6.5 MiB, which every GPU that loads the library keeps until the process
+ * exits, so num_particles is limited to 1..32768 (larger counts return
+ * GRAV_VALUE_ERROR).  The first call on each device looks up that array's
+ * device address with the device current; make that first call before any
+ * stream capture.  All calls share the one array and it keeps the last
+ * call's contents: calls that overlap on the GPU (other streams, other
+ * threads) race and must be serialised by the caller.  Returns a GRAV_*
+ * code; messages go to stderr. */
+int gsgpu_pairwise_acceleration_noalloc(const double *d_x, const double *d_m,
+                                        int num_particles, double G,
+                                        double softening_length, double *d_a,
+                                        void *stream);
+
 /* FMA-throughput probe of the running GPU (fp64 = 0: FP32, 1: FP64):
  * TFLOP/s at 2 FLOP per FMA, best of 5 launches.  No counterpart in the
  * reference; it supplies the FP32/FP64 pipe peaks of the rooflines. */
