@@ -46,6 +46,7 @@ METHOD_GPU_PAIRWISE = 101          # compensated-FP32 direct sum
 METHOD_GPU_MASSLESS = 102          # FP64 massive/massless direct sum
 METHOD_GPU_BARNES_HUT = 103        # FP32 walk, true leaf multipoles
 METHOD_GPU_BH_LEARNED = 104        # theta-cheap walk + learned MLP residual
+METHOD_GPU_BARNES_HUT_QUAD = 105   # FP32 walk, monopole + quadrupole cell terms
 METHOD_GPU_PAIRWISE_FP64 = 111     # FP64 direct sum in the reference's order
 METHOD_GPU_BARNES_HUT_COMPAT = 113 # FP32 walk reproducing the reference's tree quirks
 

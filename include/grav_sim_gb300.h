@@ -297,6 +297,35 @@ int gsgpu_pairwise_acceleration_noalloc(const double *d_x, const double *d_m,
                                         double softening_length, double *d_a,
                                         void *stream);
 
+/* Tensor-core self-test (no counterpart in the reference): one 128 x N tile
+ * C = A * B^T through tcgen05 BF16 MMA with FP32 accumulation in TMEM.
+ * hA [128 x K], hB [N x K] are row-major BF16 bit patterns on the host, hC
+ * [128 x N] FP32; the operands are staged K-major or MN-major as selected.
+ * 16 <= N, K <= 128, multiples of 16. */
+int gsgpu_tc_gemm_selftest(int N, int K, int a_mn_major, int b_mn_major,
+                           const uint16_t *hA, const uint16_t *hB, float *hC);
+
+/* ---- learned residual network (no counterpart in the reference) ------
+ * 32 -> 64 -> 64 -> 64 -> 3 MLP with SiLU, BF16 tcgen05 kernels with FP32
+ * accumulation.  Parameters are FP32 (gsgpu_mlp_num_params() floats:
+ * W1[64][32] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[16][64] b4[16],
+ * last-layer rows 3..15 zero).  Features [n][32] and targets / predictions
+ * [n][3] are FP32 host arrays. */
+typedef struct gsgpu_mlp gsgpu_mlp;
+int gsgpu_mlp_num_params(void);
+int gsgpu_mlp_create(gsgpu_mlp **out, unsigned long long seed);
+void gsgpu_mlp_destroy(gsgpu_mlp *mlp);
+int gsgpu_mlp_get_params(gsgpu_mlp *mlp, float *params);
+int gsgpu_mlp_set_params(gsgpu_mlp *mlp, const float *params);
+int gsgpu_mlp_forward(gsgpu_mlp *mlp, const float *features, int n, float *pred);
+/* Gradient of mean_n sum_k (pred_k - target_k)^2 w.r.t. the parameters (no
+ * update); loss_sum receives sum_n sum_k (pred_k - target_k)^2. */
+int gsgpu_mlp_gradients(gsgpu_mlp *mlp, const float *features, const float *target, int n,
+                        float *grad, double *loss_sum);
+/* One Adam step (beta1 0.9, beta2 0.999) with learning rate lr. */
+int gsgpu_mlp_train_step(gsgpu_mlp *mlp, const float *features, const float *target, int n,
+                         float lr, double *loss_sum);
+
 /* FMA-throughput probe of the running GPU (fp64 = 0: FP32, 1: FP64):
  * TFLOP/s at 2 FLOP per FMA, best of 5 launches.  No counterpart in the
  * reference; it supplies the FP32/FP64 pipe peaks of the rooflines. */

@@ -11,7 +11,7 @@ tolerances against the FP64 reference:
     is set by rounding positions to FP32 for the closest pairs, about
     ulp(|x|) / |r_ij|;
   * per-particle relative error |a_i - a_ref,i| / |a_ref,i|: median <= 1e-6
-    and 99th percentile <= 1e-5.
+    and 99th percentile <= 1e-5, over populations of at least 4096 particles.
 """
 import numpy as np
 import pytest
@@ -32,7 +32,9 @@ def check_fp32(a, ref, abs_sum):
     assert np.all(diff <= TOL_ABS_SUM * abs_sum + 1e-300), float(np.max(diff / (abs_sum + 1e-300)))
     mag = np.linalg.norm(ref, axis=1)
     nz = mag > 0
-    if not nz.any():
+    if nz.sum() < 4096:
+        # the relative-error statistics need a population; tiny cases are
+        # held to the per-particle bound above
         return 0.0, 0.0
     rel = diff[nz] / mag[nz]
     med = float(np.median(rel))
