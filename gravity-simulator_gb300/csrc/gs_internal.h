@@ -110,6 +110,16 @@ class Engine {
     {
         (void)cx; (void)cy; (void)cz;
     }
+    // false while the engine is still preparing itself (collecting training
+    // data): its forces are then the fallback method's
+    virtual bool ready() const { return true; }
+    // Engine-specific statistics; returns how many values were written.
+    virtual int report(double *out, int nmax) const
+    {
+        (void)out;
+        (void)nmax;
+        return 0;
+    }
     // Interactions of the most recent compute(): out[0] cell (monopole)
     // terms, out[1] particle-particle terms.  Synchronises the stream.
     virtual ErrorStatus interaction_counts(cudaStream_t s, long long out[2])
@@ -119,6 +129,22 @@ class Engine {
         out[1] = 0;
         return ok();
     }
+};
+
+// Compensated-FP32 direct sum for a list of target particles against all
+// sources (k_direct.cu); positions are taken relative to a device FP64
+// centre d_frame[0..2].  a_rows[3r..3r+2] = acceleration of particle rows[r].
+class DirectRows {
+  public:
+    ErrorStatus setup(int nj, int max_rows);
+    ErrorStatus compute(const double *d_x, const double *d_m, const double *d_frame,
+                        const int *d_rows, int nrows, double G, double eps, double *d_a_rows,
+                        cudaStream_t s, ForceTimer *timer = nullptr);
+    static constexpr int kernels() { return 4; }
+
+  private:
+    int nj_ = 0, nj_pad_ = 0, ni_pad_ = 0, splits_ = 1, jt_per_chunk_ = 1;
+    DBuf pj_, pi_, partial_, status_;
 };
 
 bool is_gpu_method(int method);

@@ -27,6 +27,9 @@ struct OctreeDevice {
     bool quad = false;   // traceless quadrupoles about the centre of mass
     DBuf t_quad;         // double[6*cap]: xx, xy, xz, yy, yz, zz
     DBuf w_nq;           // float4[2*cap]: (xx, xy, xz, yy), (yz, zz, 0, 0)
+    bool links = false;  // parent ids and particle -> leaf map
+    DBuf t_parent;       // int[cap] (-1 for the root)
+    DBuf leaf_of;        // int[n]: leaf id of sorted particle p
 
     DBuf ctr;                 // int[CTR_SIZE]
     DBuf frame;               // double[8]: cx, cy, cz, width, box_length
@@ -59,5 +62,12 @@ struct OctreeDevice {
     // Host copies: number of nodes, status word.
     ErrorStatus read_counts(cudaStream_t s, int *nodes, unsigned *status);
 };
+
+// Barnes-Hut walk of a built tree (k_walk.cu).  counters (2 x u64) receive
+// cell and particle terms (added); gate (device int, may be null) makes the
+// launch return at once when *gate == 0.
+ErrorStatus launch_bh_walk(const OctreeDevice &t, const double *d_x, double theta, double eps,
+                           double G, double *d_a, const int *gate,
+                           unsigned long long *counters, cudaStream_t s);
 
 }  // namespace gs

@@ -521,6 +521,32 @@ int gsgpu_sim_interaction_counts(gsgpu_sim *sim, long long *counts)
     return 0;
 }
 
+int gsgpu_sim_warmup_until_ready(gsgpu_sim *sim, int64_t max_steps, int64_t *steps_taken)
+{
+    if (!sim) return GRAV_POINTER_ERROR;
+    ErrorStatus st = sim->prime();
+    int64_t k = 0;
+    while (st.return_code == GRAV_SUCCESS && !sim->engine->ready() && k < max_steps) {
+        st = sim->step(sim->dt);
+        ++k;
+    }
+    if (st.return_code == GRAV_SUCCESS && cudaStreamSynchronize(sim->stream) != cudaSuccess)
+        st = GS_RAISE(GRAV_FAILURE, "stream synchronisation failed");
+    if (steps_taken) *steps_taken = k;
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    return sim->engine->ready() ? 0 : GRAV_FAILURE;
+}
+
+int gsgpu_sim_report(gsgpu_sim *sim, double *out, int nmax)
+{
+    if (!sim || !out) return -GRAV_POINTER_ERROR;
+    cudaStreamSynchronize(sim->stream);
+    return sim->engine->report(out, nmax);
+}
+
 int gsgpu_last_interaction_counts(long long *counts)
 {
     if (!counts) return GRAV_POINTER_ERROR;

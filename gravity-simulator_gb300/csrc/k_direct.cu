@@ -83,25 +83,24 @@ __device__ __forceinline__ void pair_term(const float4 q, float xi, float yi, fl
     az = fmaf(dz, s, az);
 }
 
+// One (i-tile, j-chunk) work unit: the 1024 i-particles start at pi_tile;
+// partial sums go to partial[split][3][plane] at rows itile*1024 + ...
 template <bool SOFT>
-__global__ void __launch_bounds__(DS_THREADS, 2)
-k_direct_sum(const float4 *__restrict__ pj, int n_pad, int i_tiles, int jt_per_chunk,
-             int jt_total, float eps2, double *__restrict__ partial,
-             unsigned *__restrict__ status)
+__device__ __forceinline__ void direct_sum_unit(const float4 *__restrict__ pi_tile,
+                                                const float4 *__restrict__ pj, int plane,
+                                                int itile, int split, int jt_per_chunk,
+                                                int jt_total, float eps2,
+                                                double *__restrict__ partial,
+                                                unsigned *__restrict__ status, float4 *sj,
+                                                uint64_t *full_bar)
 {
-    extern __shared__ __align__(128) unsigned char ds_smem[];
-    float4 *sj = reinterpret_cast<float4 *>(ds_smem);
-    __shared__ __align__(8) uint64_t full_bar[DS_STAGES];
-
-    const int itile = blockIdx.x % i_tiles;
-    const int split = blockIdx.x / i_tiles;
     const int jt0 = split * jt_per_chunk;
     const int ntiles = min(jt_total, jt0 + jt_per_chunk) - jt0;
 
     float xi[DS_IPT], yi[DS_IPT], zi[DS_IPT];
 #pragma unroll
     for (int k = 0; k < DS_IPT; ++k) {
-        const float4 p = pj[itile * DS_ITILE + k * DS_THREADS + threadIdx.x];
+        const float4 p = pi_tile[k * DS_THREADS + threadIdx.x];
         xi[k] = p.x;
         yi[k] = p.y;
         zi[k] = p.z;
@@ -175,15 +174,47 @@ k_direct_sum(const float4 *__restrict__ pj, int n_pad, int i_tiles, int jt_per_c
         return;
     }
 
-    const size_t plane = (size_t)n_pad;
-    double *out = partial + (size_t)split * 3 * plane;
+    double *out = partial + (size_t)split * 3 * (size_t)plane;
 #pragma unroll
     for (int k = 0; k < DS_IPT; ++k) {
         const size_t i = (size_t)itile * DS_ITILE + k * DS_THREADS + threadIdx.x;
-        out[0 * plane + i] = (double)sx[k] - (double)cx[k];
-        out[1 * plane + i] = (double)sy[k] - (double)cy[k];
-        out[2 * plane + i] = (double)sz[k] - (double)cz[k];
+        out[0 * (size_t)plane + i] = (double)sx[k] - (double)cx[k];
+        out[1 * (size_t)plane + i] = (double)sy[k] - (double)cy[k];
+        out[2 * (size_t)plane + i] = (double)sz[k] - (double)cz[k];
     }
+}
+
+template <bool SOFT>
+__global__ void __launch_bounds__(DS_THREADS, 2)
+k_direct_sum(const float4 *__restrict__ pj, int n_pad, int i_tiles, int jt_per_chunk,
+             int jt_total, float eps2, double *__restrict__ partial,
+             unsigned *__restrict__ status)
+{
+    extern __shared__ __align__(128) unsigned char ds_smem[];
+    __shared__ __align__(8) uint64_t full_bar[DS_STAGES];
+    const int itile = blockIdx.x % i_tiles;
+    const int split = blockIdx.x / i_tiles;
+    direct_sum_unit<SOFT>(pj + (size_t)itile * DS_ITILE, pj, n_pad, itile, split, jt_per_chunk,
+                          jt_total, eps2, partial, status, reinterpret_cast<float4 *>(ds_smem),
+                          full_bar);
+}
+
+// Direct sum for a separate list of target particles pi [ni_pad] (padded to
+// whole 1024-particle tiles) against all sources pj: the sampled rows of the
+// learned method's training targets and per-step judge.
+template <bool SOFT>
+__global__ void __launch_bounds__(DS_THREADS, 2)
+k_direct_rows(const float4 *__restrict__ pi, int ni_pad, const float4 *__restrict__ pj,
+              int i_tiles, int jt_per_chunk, int jt_total, float eps2,
+              double *__restrict__ partial, unsigned *__restrict__ status)
+{
+    extern __shared__ __align__(128) unsigned char ds_smem[];
+    __shared__ __align__(8) uint64_t full_bar[DS_STAGES];
+    const int itile = blockIdx.x % i_tiles;
+    const int split = blockIdx.x / i_tiles;
+    direct_sum_unit<SOFT>(pi + (size_t)itile * DS_ITILE, pj, ni_pad, itile, split, jt_per_chunk,
+                          jt_total, eps2, partial, status, reinterpret_cast<float4 *>(ds_smem),
+                          full_bar);
 }
 
 // a_i = G * sum_s partial[s][.][i], summed in split order.
@@ -378,6 +409,101 @@ class DirectEngine final : public Engine {
 std::unique_ptr<Engine> make_direct_engine(bool fp64_reference_order)
 {
     return std::unique_ptr<Engine>(new DirectEngine(fp64_reference_order));
+}
+
+// ---- direct sum over selected rows ----------------------------------------
+// Sources packed relative to frame[0..2] (a device FP64 centre).
+__global__ void k_pack_frame(const double *__restrict__ x, const double *__restrict__ m, int n,
+                             int n_pad, const double *__restrict__ frame, float4 *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_pad) return;
+    float4 p;
+    if (i < n) {
+        p.x = (float)(x[3 * i + 0] - frame[0]);
+        p.y = (float)(x[3 * i + 1] - frame[1]);
+        p.z = (float)(x[3 * i + 2] - frame[2]);
+        p.w = (float)m[i];
+    } else {
+        p = make_float4(kPadPos, kPadPos, kPadPos, 0.0f);
+    }
+    out[i] = p;
+}
+
+__global__ void k_gather_rows(const float4 *__restrict__ pj, const int *__restrict__ rows,
+                              int nrows, int nrows_pad, float4 *__restrict__ pi)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrows_pad) return;
+    pi[r] = r < nrows ? pj[rows[r]] : make_float4(kPadPos, kPadPos, kPadPos, 0.0f);
+}
+
+ErrorStatus DirectRows::setup(int nj, int max_rows)
+{
+    const DeviceInfo *dev = nullptr;
+    GS_TRY(device_info(&dev));
+    nj_ = nj;
+    nj_pad_ = ((nj + DS_JTILE - 1) / DS_JTILE) * DS_JTILE;
+    ni_pad_ = ((max_rows + DS_ITILE - 1) / DS_ITILE) * DS_ITILE;
+    const int jt_total = nj_pad_ / DS_JTILE;
+    const int i_tiles = ni_pad_ / DS_ITILE;
+    int per_sm = 0;
+    GS_CUDA(cudaFuncSetAttribute(k_direct_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 DS_SMEM));
+    GS_CUDA(cudaFuncSetAttribute(k_direct_rows<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 DS_SMEM));
+    GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_direct_rows<true>, DS_THREADS,
+                                                          DS_SMEM));
+    const long slots = (long)dev->sm_count * std::max(per_sm, 1);
+    double best = 1e300;
+    for (int s = 1; s <= std::min(jt_total, 128); ++s) {
+        const int chunk = (jt_total + s - 1) / s;
+        const int used = (jt_total + chunk - 1) / chunk;
+        const long units = (long)i_tiles * used;
+        const double cost = (double)((units + slots - 1) / slots) * (chunk + 0.25);
+        if (cost < best - 1e-9) {
+            best = cost;
+            splits_ = used;
+            jt_per_chunk_ = chunk;
+        }
+    }
+    GS_TRY(pj_.reserve((size_t)nj_pad_ * sizeof(float4)));
+    GS_TRY(pi_.reserve((size_t)ni_pad_ * sizeof(float4)));
+    GS_TRY(partial_.reserve((size_t)splits_ * 3 * ni_pad_ * sizeof(double)));
+    GS_TRY(status_.reserve(sizeof(unsigned)));
+    GS_CUDA(cudaMemset(status_.p, 0, sizeof(unsigned)));
+    return ok();
+}
+
+ErrorStatus DirectRows::compute(const double *d_x, const double *d_m, const double *d_frame,
+                                const int *d_rows, int nrows, double G, double eps, double *d_a_rows,
+                                cudaStream_t s, ForceTimer *timer)
+{
+    if (nrows <= 0) return ok();
+    if (((nrows + DS_ITILE - 1) / DS_ITILE) * DS_ITILE > ni_pad_)
+        return GS_RAISE(GRAV_VALUE_ERROR, "direct rows: %d rows exceed the prepared %d", nrows, ni_pad_);
+    k_pack_frame<<<(nj_pad_ + 255) / 256, 256, 0, s>>>(d_x, d_m, nj_, nj_pad_, d_frame,
+                                                       pj_.as<float4>());
+    const int nr_pad = ((nrows + DS_ITILE - 1) / DS_ITILE) * DS_ITILE;
+    k_gather_rows<<<(nr_pad + 255) / 256, 256, 0, s>>>(pj_.as<float4>(), d_rows, nrows, nr_pad,
+                                                       pi_.as<float4>());
+    const float eps2 = (float)(eps * eps);
+    const int i_tiles = nr_pad / DS_ITILE;
+    const int jt_total = nj_pad_ / DS_JTILE;
+    if (timer) GS_TRY(timer->begin(s));
+    if (eps2 > 0.0f)
+        k_direct_rows<true><<<i_tiles * splits_, DS_THREADS, DS_SMEM, s>>>(
+            pi_.as<float4>(), ni_pad_, pj_.as<float4>(), i_tiles, jt_per_chunk_, jt_total, eps2,
+            partial_.as<double>(), status_.as<unsigned>());
+    else
+        k_direct_rows<false><<<i_tiles * splits_, DS_THREADS, DS_SMEM, s>>>(
+            pi_.as<float4>(), ni_pad_, pj_.as<float4>(), i_tiles, jt_per_chunk_, jt_total, eps2,
+            partial_.as<double>(), status_.as<unsigned>());
+    if (timer) GS_TRY(timer->end(s));
+    k_reduce_splits<<<(nrows + 255) / 256, 256, 0, s>>>(partial_.as<double>(), splits_, nrows,
+                                                        ni_pad_, G, d_a_rows);
+    GS_CUDA(cudaGetLastError());
+    return ok();
 }
 
 // ------------------------------------------------------------------------

@@ -1,0 +1,460 @@
+// k_learned.cu -- Barnes-Hut with a learned residual (GRAV_GPU_BH_LEARNED).
+//
+// A cheap walk (opening angle theta_cheap, 1.0 by default, monopole +
+// quadrupole cells) is corrected by the residual network of k_mlp.cu:
+//     a = a_cheap + |a_cheap| * net(features) / 100,
+// where the network was trained to predict 100 (a_direct - a_cheap)/|a_cheap|
+// from 32 per-particle features of the tree around the particle.
+//
+// Life cycle of the engine (one engine per simulation):
+//   collection   the first kSnapshots force evaluations return the fallback
+//                walk (theta 0.5, monopole + quadrupole) and record one
+//                training snapshot each: features and direct-sum residuals of
+//                65,536 sampled particles (direct sum in compensated FP32);
+//   training     after the last snapshot, the network is trained on the GPU
+//                by its own tcgen05 forward / backward kernels and Adam; the
+//                last snapshot is held out to measure what the network gains;
+//   inference    cheap walk + features + network + correction, then a judge:
+//                the direct sum of 4,096 particles (a different sample each
+//                step) gives their exact accelerations; when the median
+//                relative error of the corrected accelerations exceeds 1e-3
+//                a device flag turns on the fallback walk for the whole step,
+//                and the judged particles get their exact values in any case.
+// Inference is graph-capturable (the fallback is a gated launch, not a host
+// decision).
+//
+// Features (sorted particle s, its leaf L and the leaf's parent P, cell
+// widths hL and hP = 2 hL, x the particle position, c / M / Q the centre of
+// mass, mass and traceless quadrupole of a node):
+//   0-2  (x - c_L) / hL           3  M_L / M_P          4-6  (c_L - c_P) / hP
+//   7-12 Q_L / (M_L hL^2)        13  ln(M_P / m) / 10  14-16 (x - c_P) / hP
+//  17-22 Q_P / (M_P hP^2)        23  log10(M_P / hP^3) / 5
+//  24-31 |x - c_k| / hP for the children k of P in octant order (0 if absent)
+#include "gs_mlp.h"
+#include "gs_octree.h"
+#include "gs_ptx.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <numeric>
+#include <random>
+#include <vector>
+
+namespace gs {
+
+namespace {
+
+constexpr int kSnapshots = 64;
+constexpr int kSamplesPerSnapshot = 65536;
+constexpr int kJudge = 4096;
+constexpr double kJudgeTol = 1e-3;
+constexpr double kThetaFallback = 0.5;
+constexpr float kResidualScale = 100.0f;
+constexpr int kBatch = 8192;
+constexpr int kEpochs = 24;
+
+}  // namespace
+
+__global__ void k_features(int count, const int *__restrict__ pos, const int *__restrict__ sidx,
+                           const int *__restrict__ leaf_of, const int *__restrict__ t_parent,
+                           const int *__restrict__ t_nc, const int *__restrict__ t_fc,
+                           const int *__restrict__ t_depth, const double *__restrict__ t_mass,
+                           const double *__restrict__ t_com, const double *__restrict__ t_quad,
+                           const double *__restrict__ frame, const double *__restrict__ x,
+                           const double *__restrict__ m, float *__restrict__ feat)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const int s = pos ? pos[k] : k;
+    const int id = sidx[s];
+    const int L = leaf_of[s];
+    int P = t_parent[L];
+    if (P < 0) P = L;
+    const double hL = frame[3] / (double)(1 << min(t_depth[L], 30));
+    const double hP = 2.0 * hL;
+    const double x0 = x[3 * id], x1 = x[3 * id + 1], x2 = x[3 * id + 2];
+    const double *cL = t_com + 3 * (size_t)L;
+    const double *cP = t_com + 3 * (size_t)P;
+    const double ML = fmax(t_mass[L], 1e-300), MP = fmax(t_mass[P], 1e-300);
+    const double *QL = t_quad + 6 * (size_t)L;
+    const double *QP = t_quad + 6 * (size_t)P;
+    float f[MLP_IN];
+    f[0] = (float)((x0 - cL[0]) / hL);
+    f[1] = (float)((x1 - cL[1]) / hL);
+    f[2] = (float)((x2 - cL[2]) / hL);
+    f[3] = (float)(ML / MP);
+    f[4] = (float)((cL[0] - cP[0]) / hP);
+    f[5] = (float)((cL[1] - cP[1]) / hP);
+    f[6] = (float)((cL[2] - cP[2]) / hP);
+    const double nL = 1.0 / (ML * hL * hL), nP = 1.0 / (MP * hP * hP);
+    for (int q = 0; q < 6; ++q) f[7 + q] = (float)(QL[q] * nL);
+    f[13] = m[id] > 0.0 ? (float)(log(MP / m[id]) / 10.0) : 0.0f;
+    f[14] = (float)((x0 - cP[0]) / hP);
+    f[15] = (float)((x1 - cP[1]) / hP);
+    f[16] = (float)((x2 - cP[2]) / hP);
+    for (int q = 0; q < 6; ++q) f[17 + q] = (float)(QP[q] * nP);
+    f[23] = (float)(log10(MP / (hP * hP * hP)) / 5.0);
+    const int nc = t_nc[P], fc = t_fc[P];
+    for (int c = 0; c < 8; ++c) {
+        float d = 0.0f;
+        if (c < nc) {
+            const double *cc = t_com + 3 * (size_t)(fc + c);
+            const double d0 = x0 - cc[0], d1 = x1 - cc[1], d2 = x2 - cc[2];
+            d = (float)(sqrt(d0 * d0 + d1 * d1 + d2 * d2) / hP);
+        }
+        f[24 + c] = d;
+    }
+    float4 *out = reinterpret_cast<float4 *>(feat + (size_t)k * MLP_IN);
+#pragma unroll
+    for (int q = 0; q < MLP_IN / 4; ++q)
+        out[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+}
+
+// Sorted positions and particle ids of a strided sample; when step_ctr is
+// given the offset also moves with the device step counter, so a replayed
+// graph judges a different sample every step.
+__global__ void k_sample(int count, int n, long long offset, long long stride,
+                         const double *__restrict__ step_ctr, const int *__restrict__ sidx,
+                         int *__restrict__ pos, int *__restrict__ ids)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    if (step_ctr) offset += (long long)step_ctr[0] * 7919LL;
+    const int s = (int)((offset + (long long)k * stride) % n);
+    pos[k] = s;
+    ids[k] = sidx[s];
+}
+
+// target = 100 (a_direct - a_cheap) / |a_cheap|
+__global__ void k_targets(int count, const int *__restrict__ ids, const double *__restrict__ a_cheap,
+                          const double *__restrict__ a_exact, float *__restrict__ target)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const int id = ids[k];
+    const double c0 = a_cheap[3 * id], c1 = a_cheap[3 * id + 1], c2 = a_cheap[3 * id + 2];
+    const double mag = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+    const double inv = mag > 0.0 ? kResidualScale / mag : 0.0;
+    target[3 * k] = (float)((a_exact[3 * k] - c0) * inv);
+    target[3 * k + 1] = (float)((a_exact[3 * k + 1] - c1) * inv);
+    target[3 * k + 2] = (float)((a_exact[3 * k + 2] - c2) * inv);
+}
+
+// a += |a| pred / 100 (pred in sorted order)
+__global__ void k_correct(int n, const int *__restrict__ sidx, const float *__restrict__ pred,
+                          double *__restrict__ a)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int id = sidx[s];
+    const double a0 = a[3 * id], a1 = a[3 * id + 1], a2 = a[3 * id + 2];
+    const double f = sqrt(a0 * a0 + a1 * a1 + a2 * a2) / kResidualScale;
+    a[3 * id] = a0 + f * pred[3 * s];
+    a[3 * id + 1] = a1 + f * pred[3 * s + 1];
+    a[3 * id + 2] = a2 + f * pred[3 * s + 2];
+}
+
+// Median relative error of a at the judged particles (radix select on the
+// bit patterns of the non-negative errors); sets the fallback flag and the
+// running statistics [0] last median, [1] steps judged, [2] steps fallen back.
+constexpr int JG_THREADS = 1024;
+__global__ void __launch_bounds__(JG_THREADS)
+k_judge(int J, const int *__restrict__ ids, const double *__restrict__ a,
+        const double *__restrict__ a_exact, double tol, int *__restrict__ flag,
+        double *__restrict__ stats)
+{
+    __shared__ unsigned bits[kJudge];
+    __shared__ int red[JG_THREADS / 32];
+    for (int j = threadIdx.x; j < J; j += JG_THREADS) {
+        const int id = ids[j];
+        const double d0 = a[3 * id] - a_exact[3 * j], d1 = a[3 * id + 1] - a_exact[3 * j + 1],
+                     d2 = a[3 * id + 2] - a_exact[3 * j + 2];
+        const double e0 = a_exact[3 * j], e1 = a_exact[3 * j + 1], e2 = a_exact[3 * j + 2];
+        const double den = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+        const float err = den > 0.0 ? (float)(sqrt(d0 * d0 + d1 * d1 + d2 * d2) / den) : 0.0f;
+        bits[j] = __float_as_uint(err);
+    }
+    __syncthreads();
+    const int k = (J - 1) / 2;
+    unsigned prefix = 0;
+    for (int b = 30; b >= 0; --b) {
+        const unsigned cand = prefix | (1u << b);
+        int c = 0;
+        for (int j = threadIdx.x; j < J; j += JG_THREADS) c += bits[j] < cand ? 1 : 0;
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int t = 0;
+            for (int w = 0; w < JG_THREADS / 32; ++w) t += red[w];
+            red[0] = t;
+        }
+        __syncthreads();
+        if (red[0] <= k) prefix = cand;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double med = (double)__uint_as_float(prefix);
+        const int fb = med > tol ? 1 : 0;
+        *flag = fb;
+        stats[0] = med;
+        stats[1] += 1.0;
+        stats[2] += fb;
+    }
+}
+
+__global__ void k_replace_rows(int J, const int *__restrict__ ids,
+                               const double *__restrict__ a_exact, double *__restrict__ a)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= J) return;
+    const int id = ids[j];
+    a[3 * id] = a_exact[3 * j];
+    a[3 * id + 1] = a_exact[3 * j + 1];
+    a[3 * id + 2] = a_exact[3 * j + 2];
+}
+
+namespace {
+
+class LearnedEngine final : public Engine {
+  public:
+    ErrorStatus setup(int n, double G, const AccelerationParam &p) override
+    {
+        n_ = n;
+        G_ = G;
+        eps_ = p.softening_length;
+        theta_ = p.opening_angle > 0.0 ? p.opening_angle : 1.0;
+        K_ = std::min(kSamplesPerSnapshot, n);
+        J_ = std::min(kJudge, n);
+        GS_CUDA(cudaStreamCreateWithFlags(&own_, cudaStreamNonBlocking));
+        tree_.links = true;
+        GS_TRY(tree_.setup(n, p.max_num_particles_per_leaf, false, true));
+        GS_TRY(mlp_.setup(20261203ull, own_));
+        GS_TRY(rows_.setup(n, std::max(K_, J_)));
+        GS_TRY(a_cheap_.reserve((size_t)n * 3 * sizeof(double)));
+        GS_TRY(feat_.reserve((size_t)n * MLP_IN * sizeof(float)));
+        GS_TRY(pred_.reserve((size_t)n * MLP_OUT * sizeof(float)));
+        GS_TRY(pos_.reserve((size_t)std::max(K_, J_) * sizeof(int)));
+        GS_TRY(ids_.reserve((size_t)std::max(K_, J_) * sizeof(int)));
+        GS_TRY(a_rows_.reserve((size_t)std::max(K_, J_) * 3 * sizeof(double)));
+        GS_TRY(data_feat_.reserve((size_t)kSnapshots * K_ * MLP_IN * sizeof(float)));
+        GS_TRY(data_target_.reserve((size_t)kSnapshots * K_ * MLP_OUT * sizeof(float)));
+        GS_TRY(flag_.reserve(sizeof(int)));
+        GS_TRY(stats_.reserve(4 * sizeof(double)));
+        GS_TRY(counters_.reserve(2 * sizeof(unsigned long long)));
+        GS_CUDA(cudaMemset(flag_.p, 0, sizeof(int)));
+        GS_CUDA(cudaMemset(stats_.p, 0, 4 * sizeof(double)));
+        GS_CUDA(cudaMemset(counters_.p, 0, 2 * sizeof(unsigned long long)));
+        return ok();
+    }
+
+    ~LearnedEngine() override
+    {
+        if (own_) cudaStreamDestroy(own_);
+    }
+
+    bool capturable() const override { return trained_; }
+    bool ready() const override { return trained_; }
+
+    ErrorStatus compute(const double *d_x, const double *d_m, double *d_a, cudaStream_t s,
+                        ForceTimer *timer) override
+    {
+        GS_CUDA(cudaMemsetAsync(counters_.p, 0, 2 * sizeof(unsigned long long), s));
+        GS_TRY(tree_.build(d_x, d_m, s));
+        if (!trained_) {
+            GS_TRY(collect(d_x, d_m, d_a, s));
+            if (snapshots_ == kSnapshots) GS_TRY(train(s));
+            return ok();
+        }
+        unsigned long long *cnt = counters_.as<unsigned long long>();
+        if (timer) GS_TRY(timer->begin(s));
+        GS_TRY(launch_bh_walk(tree_, d_x, theta_, eps_, G_, d_a, nullptr, cnt, s));
+        if (timer) GS_TRY(timer->end(s));
+        GS_TRY(features(nullptr, n_, feat_.as<float>(), d_x, d_m, s));
+        GS_TRY(mlp_.forward(feat_.as<float>(), n_, pred_.as<float>(), s));
+        k_correct<<<(n_ + 255) / 256, 256, 0, s>>>(n_, tree_.sidx.as<int>(), pred_.as<float>(), d_a);
+        // judge on a rotating strided sample
+        const long long stride = std::max(1, n_ / J_);
+        k_sample<<<(J_ + 255) / 256, 256, 0, s>>>(J_, n_, 0, stride, stats_.as<double>() + 1,
+                                                  tree_.sidx.as<int>(), pos_.as<int>(),
+                                                  ids_.as<int>());
+        GS_TRY(rows_.compute(d_x, d_m, tree_.frame.as<double>(), ids_.as<int>(), J_, G_, eps_,
+                             a_rows_.as<double>(), s));
+        k_judge<<<1, JG_THREADS, 0, s>>>(J_, ids_.as<int>(), d_a, a_rows_.as<double>(), kJudgeTol,
+                                         flag_.as<int>(), stats_.as<double>());
+        GS_TRY(launch_bh_walk(tree_, d_x, kThetaFallback, eps_, G_, d_a, flag_.as<int>(), cnt, s));
+        k_replace_rows<<<(J_ + 255) / 256, 256, 0, s>>>(J_, ids_.as<int>(), a_rows_.as<double>(),
+                                                        d_a);
+        GS_CUDA(cudaGetLastError());
+        return ok();
+    }
+
+    int kernels_per_eval() const override
+    {
+        return tree_.launches_per_build() + 1 + 1 + 1 + 1 + 1 + DirectRows::kernels() + 1 + 1 + 1;
+    }
+
+    ErrorStatus check_status(cudaStream_t s) override
+    {
+        int nodes = 0;
+        unsigned st = 0;
+        GS_TRY(tree_.read_counts(s, &nodes, &st));
+        if (st & ST_TREE_OVERFLOW)
+            return GS_RAISE(GRAV_MEMORY_ERROR, "octree node capacity (%d) exceeded", tree_.cap_nodes);
+        if (st & ST_STACK_OVERFLOW)
+            return GS_RAISE(GRAV_FAILURE, "tree walk deeper than the octree depth limit");
+        GS_TRY(mlp_.check(s));
+        return ok();
+    }
+
+    ErrorStatus interaction_counts(cudaStream_t s, long long out[2]) override
+    {
+        unsigned long long h[2] = {0, 0};
+        GS_CUDA(cudaMemcpyAsync(h, counters_.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+        GS_CUDA(cudaStreamSynchronize(s));
+        out[0] = (long long)h[0];
+        out[1] = (long long)h[1];
+        return ok();
+    }
+
+    int report(double *out, int nmax) const override
+    {
+        double v[12] = {trained_ ? 1.0 : 0.0, (double)snapshots_, loss_first_, loss_last_,
+                        hold_before_, hold_after_, 0.0, 0.0, 0.0, theta_, train_seconds_,
+                        (double)adam_steps_};
+        double st[4] = {0, 0, 0, 0};
+        if (stats_.p && cudaMemcpy(st, stats_.p, sizeof(st), cudaMemcpyDeviceToHost) == cudaSuccess) {
+            v[6] = st[0];
+            v[7] = st[1];
+            v[8] = st[2];
+        }
+        const int k = std::min(nmax, 12);
+        for (int i = 0; i < k; ++i) out[i] = v[i];
+        return k;
+    }
+
+  private:
+    ErrorStatus features(const int *pos, int count, float *out, const double *d_x,
+                         const double *d_m, cudaStream_t s)
+    {
+        k_features<<<(count + 127) / 128, 128, 0, s>>>(
+            count, pos, tree_.sidx.as<int>(), tree_.leaf_of.as<int>(), tree_.t_parent.as<int>(),
+            tree_.t_nc.as<int>(), tree_.t_fc.as<int>(), tree_.t_depth.as<int>(),
+            tree_.t_mass.as<double>(), tree_.t_com.as<double>(), tree_.t_quad.as<double>(),
+            tree_.frame.as<double>(), d_x, d_m, out);
+        GS_CUDA(cudaGetLastError());
+        return ok();
+    }
+
+    // One training snapshot; the step's force is the fallback walk.
+    ErrorStatus collect(const double *d_x, const double *d_m, double *d_a, cudaStream_t s)
+    {
+        unsigned long long *cnt = counters_.as<unsigned long long>();
+        GS_TRY(launch_bh_walk(tree_, d_x, theta_, eps_, G_, a_cheap_.as<double>(), nullptr, cnt, s));
+        GS_TRY(launch_bh_walk(tree_, d_x, kThetaFallback, eps_, G_, d_a, nullptr, cnt, s));
+        const long long stride = std::max(1, n_ / K_);
+        const long long offset = ((long long)snapshots_ * 104729LL) % std::max(1LL, stride) +
+                                 (long long)snapshots_ * 31LL;
+        k_sample<<<(K_ + 255) / 256, 256, 0, s>>>(K_, n_, offset, stride, nullptr,
+                                                  tree_.sidx.as<int>(), pos_.as<int>(),
+                                                  ids_.as<int>());
+        GS_TRY(rows_.compute(d_x, d_m, tree_.frame.as<double>(), ids_.as<int>(), K_, G_, eps_,
+                             a_rows_.as<double>(), s));
+        float *f = data_feat_.as<float>() + (size_t)snapshots_ * K_ * MLP_IN;
+        float *t = data_target_.as<float>() + (size_t)snapshots_ * K_ * MLP_OUT;
+        GS_TRY(features(pos_.as<int>(), K_, f, d_x, d_m, s));
+        k_targets<<<(K_ + 255) / 256, 256, 0, s>>>(K_, ids_.as<int>(), a_cheap_.as<double>(),
+                                                   a_rows_.as<double>(), t);
+        GS_CUDA(cudaGetLastError());
+        ++snapshots_;
+        return ok();
+    }
+
+    // Median over samples of |target| and |target - pred| (residual units).
+    ErrorStatus holdout(cudaStream_t s, double *before, double *after)
+    {
+        const float *f = data_feat_.as<float>() + (size_t)(kSnapshots - 1) * K_ * MLP_IN;
+        const float *t = data_target_.as<float>() + (size_t)(kSnapshots - 1) * K_ * MLP_OUT;
+        GS_TRY(mlp_.forward(f, K_, pred_.as<float>(), s));
+        std::vector<float> hp((size_t)K_ * 3), ht((size_t)K_ * 3);
+        GS_CUDA(cudaMemcpyAsync(hp.data(), pred_.p, hp.size() * 4, cudaMemcpyDeviceToHost, s));
+        GS_CUDA(cudaMemcpyAsync(ht.data(), t, ht.size() * 4, cudaMemcpyDeviceToHost, s));
+        GS_CUDA(cudaStreamSynchronize(s));
+        std::vector<double> b(K_), a(K_);
+        for (int k = 0; k < K_; ++k) {
+            double sb = 0, sa = 0;
+            for (int c = 0; c < 3; ++c) {
+                const double tt = ht[3 * k + c], pp = hp[3 * k + c];
+                sb += tt * tt;
+                sa += (tt - pp) * (tt - pp);
+            }
+            b[k] = std::sqrt(sb) / kResidualScale;
+            a[k] = std::sqrt(sa) / kResidualScale;
+        }
+        std::nth_element(b.begin(), b.begin() + K_ / 2, b.end());
+        std::nth_element(a.begin(), a.begin() + K_ / 2, a.end());
+        *before = b[K_ / 2];
+        *after = a[K_ / 2];
+        return ok();
+    }
+
+    ErrorStatus train(cudaStream_t s)
+    {
+        GS_CUDA(cudaStreamSynchronize(s));
+        const auto t0 = std::chrono::steady_clock::now();
+        const int train_samples = (kSnapshots - 1) * K_;
+        const int batches = std::max(1, train_samples / kBatch);
+        const int batch = std::min(kBatch, train_samples);
+        std::mt19937_64 rng(7);
+        std::vector<int> order(batches);
+        std::iota(order.begin(), order.end(), 0);
+        const int total = kEpochs * batches;
+        int step = 0;
+        for (int e = 0; e < kEpochs; ++e) {
+            std::shuffle(order.begin(), order.end(), rng);
+            for (int b = 0; b < batches; ++b, ++step) {
+                const double frac = (double)step / (double)total;
+                const float lr = (float)(1e-5 + 0.5 * (2e-3 - 1e-5) * (1.0 + std::cos(3.14159265358979 * frac)));
+                const size_t off = (size_t)order[b] * batch;
+                GS_TRY(mlp_.train_step(data_feat_.as<float>() + off * MLP_IN,
+                                       data_target_.as<float>() + off * MLP_OUT, batch, lr, s));
+            }
+            double l = 0.0;
+            GS_TRY(mlp_.read_loss(s, &l));
+            const double mse = l / ((double)batches * batch);
+            if (e == 0) loss_first_ = mse;
+            loss_last_ = mse;
+        }
+        adam_steps_ = step;
+        GS_TRY(mlp_.check(s));
+        GS_TRY(holdout(s, &hold_before_, &hold_after_));
+        train_seconds_ =
+            std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        trained_ = true;
+        return ok();
+    }
+
+    int n_ = 0, K_ = 0, J_ = 0;
+    double G_ = 1.0, eps_ = 0.0, theta_ = 1.0;
+    cudaStream_t own_ = nullptr;
+    OctreeDevice tree_;
+    MlpDevice mlp_;
+    DirectRows rows_;
+    DBuf a_cheap_, feat_, pred_, pos_, ids_, a_rows_, data_feat_, data_target_, flag_, stats_,
+        counters_;
+    int snapshots_ = 0;
+    bool trained_ = false;
+    int adam_steps_ = 0;
+    double loss_first_ = 0.0, loss_last_ = 0.0, hold_before_ = 0.0, hold_after_ = 0.0;
+    double train_seconds_ = 0.0;
+};
+
+}  // namespace
+
+std::unique_ptr<Engine> make_learned_engine()
+{
+    return std::unique_ptr<Engine>(new LearnedEngine());
+}
+
+}  // namespace gs

@@ -367,6 +367,28 @@ __global__ void k_tree_number(const int *__restrict__ ctr, int compat,
     }
 }
 
+// Parent id of every node and the leaf of every sorted particle (used by
+// the learned method's features).
+__global__ void k_tree_links(const int *__restrict__ ctr, const int *__restrict__ nd_start,
+                             const int *__restrict__ nd_count, const int *__restrict__ nd_parent,
+                             const int *__restrict__ nd_rank, const int *__restrict__ nd_int,
+                             const int *__restrict__ in_node, const int *__restrict__ in_fc,
+                             int *__restrict__ t_parent, int *__restrict__ leaf_of)
+{
+    const int nn = ctr[CTR_NODES];
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nn; q += gridDim.x * blockDim.x) {
+        int id = 0, parent = -1;
+        if (q != 0) {
+            id = in_fc[nd_parent[q]] + nd_rank[q];
+            const int pq = in_node[nd_parent[q]];
+            parent = (pq == 0) ? 0 : in_fc[nd_parent[pq]] + nd_rank[pq];
+        }
+        t_parent[id] = parent;
+        if (nd_int[q] < 0)
+            for (int p = nd_start[q]; p < nd_start[q] + nd_count[q]; ++p) leaf_of[p] = id;
+    }
+}
+
 // Running sums of the particles of one leaf, sorted order (reference :667-674).
 __device__ __forceinline__ void add_particles(const double *__restrict__ x,
                                               const double *__restrict__ m,
@@ -583,6 +605,10 @@ ErrorStatus OctreeDevice::setup(int n_, int leaf_max_, bool compat_, bool quad_)
         GS_TRY(t_quad.reserve((size_t)cap * 6 * sizeof(double)));
         GS_TRY(w_nq.reserve((size_t)cap * 2 * sizeof(float4)));
     }
+    if (links) {
+        GS_TRY(t_parent.reserve((size_t)cap * sizeof(int)));
+        GS_TRY(leaf_of.reserve((size_t)n * sizeof(int)));
+    }
     GS_TRY(sorter.reserve(std::max(n, cap)));
     return ok();
 }
@@ -592,7 +618,7 @@ int OctreeDevice::launches_per_build() const
     // bbox 2, morton 1, sort, init 1, levels 2*21, keys 1, sort, fc 3,
     // number 1, multipoles 21 (+1 leaves), walk arrays 2 (+ quadrupoles 21 + 1)
     return 2 + 1 + RadixSorter::launches(63) + 1 + 42 + 1 + RadixSorter::launches(36) + 3 + 1 +
-           21 + (compat ? 0 : 1) + 2 + (quad ? 22 : 0);
+           21 + (compat ? 0 : 1) + 2 + (quad ? 22 : 0) + (links ? 1 : 0);
 }
 
 ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream_t s,
@@ -642,6 +668,12 @@ ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream
         t_fc.as<int>(), t_depth.as<int>(), t_int.as<int>(), t_mass.as<double>(),
         t_com.as<double>());
     GS_CUDA(cudaGetLastError());
+    if (links)
+        k_tree_links<<<grid, OT_THREADS, 0, s>>>(ctr.as<int>(), nd_start.as<int>(),
+                                                 nd_count.as<int>(), nd_parent.as<int>(),
+                                                 nd_rank.as<int>(), nd_int.as<int>(),
+                                                 in_node.as<int>(), in_fc.as<int>(),
+                                                 t_parent.as<int>(), leaf_of.as<int>());
     if (!compat)
         k_leaf_multipoles<<<grid, OT_THREADS, 0, s>>>(
             ctr.as<int>(), d_x, d_m, sidx.as<int>(), t_np.as<int>(), t_nc.as<int>(),

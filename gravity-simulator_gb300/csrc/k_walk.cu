@@ -56,6 +56,7 @@ struct WalkArgs {
     double *a;
     unsigned long long *counters;   // [0] accepted cells, [1] leaf pair terms
     unsigned *status;
+    const int *gate;                // when set, the launch runs only if *gate != 0
 };
 
 __device__ __forceinline__ void add3(float &sx, float &cx, float &sy, float &cy, float &sz, float &cz,
@@ -76,6 +77,7 @@ k_bh_walk(WalkArgs A)
     __shared__ float s_w2[WK_STACK];     // (cell width at depth)^2, FP32
     __shared__ double s_w[WK_STACK];     // cell width at depth, FP64 (reference formula)
 
+    if (A.gate && *A.gate == 0) return;   // block-uniform
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     if (threadIdx.x < WK_STACK) {
@@ -289,6 +291,7 @@ class BarnesHutEngine final : public Engine {
         w.a = d_a;
         w.counters = counters_.as<unsigned long long>();
         w.status = reinterpret_cast<unsigned *>(tree_.ctr.as<int>() + CTR_STATUS);
+        w.gate = nullptr;
         GS_CUDA(cudaMemsetAsync(counters_.p, 0, 2 * sizeof(unsigned long long), s));
         if (timer) GS_TRY(timer->begin(s));
         const int grid = (n_ + WK_THREADS - 1) / WK_THREADS;
@@ -338,6 +341,43 @@ class BarnesHutEngine final : public Engine {
 std::unique_ptr<Engine> make_barnes_hut_engine(bool compat, bool quad)
 {
     return std::unique_ptr<Engine>(new BarnesHutEngine(compat, quad));
+}
+
+// Walk of a built (non-compat) tree, for engines that walk one tree several
+// times (the learned method's cheap walk and its gated fallback).
+ErrorStatus launch_bh_walk(const OctreeDevice &t, const double *d_x, double theta, double eps,
+                           double G, double *d_a, const int *gate,
+                           unsigned long long *counters, cudaStream_t s)
+{
+    WalkArgs w;
+    w.na = t.w_na.as<float4>();
+    w.nb = t.w_nb.as<float4>();
+    w.nq = t.quad ? t.w_nq.as<float4>() : nullptr;
+    w.nc = t.w_nc.as<int4>();
+    w.nkey = t.w_nkey.as<uint64_t>();
+    w.ncom = t.t_com.as<double>();
+    w.pa = t.w_pa.as<float4>();
+    w.pb = t.w_pb.as<float4>();
+    w.sidx = t.sidx.as<int>();
+    w.skeys = t.keys.as<uint64_t>();
+    w.x = d_x;
+    w.frame = t.frame.as<double>();
+    w.n = t.n;
+    w.compat = t.compat ? 1 : 0;
+    w.eps2 = (float)(eps * eps);
+    w.theta2 = theta * theta;
+    w.G = G;
+    w.a = d_a;
+    w.counters = counters;
+    w.status = reinterpret_cast<unsigned *>(t.ctr.as<int>() + CTR_STATUS);
+    w.gate = gate;
+    const int grid = (t.n + WK_THREADS - 1) / WK_THREADS;
+    if (t.quad)
+        k_bh_walk<true><<<grid, WK_THREADS, 0, s>>>(w);
+    else
+        k_bh_walk<false><<<grid, WK_THREADS, 0, s>>>(w);
+    GS_CUDA(cudaGetLastError());
+    return ok();
 }
 
 ErrorStatus accel_host(double *a, const System *system, const AccelerationParam *param_in);

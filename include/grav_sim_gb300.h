@@ -267,6 +267,16 @@ int gsgpu_sim_kernels_per_step(const gsgpu_sim *sim);
 int gsgpu_sim_interaction_counts(gsgpu_sim *sim, long long *counts);
 /* The same for the calling thread's most recent acceleration() call. */
 int gsgpu_last_interaction_counts(long long *counts);
+/* Advance the simulation until its force engine is ready (the learned
+ * method collects its training snapshots during its first steps and then
+ * trains); at most max_steps steps.  0 when ready. */
+int gsgpu_sim_warmup_until_ready(gsgpu_sim *sim, int64_t max_steps, int64_t *steps_taken);
+/* Engine statistics; returns the number of values written (learned method:
+ * trained, snapshots, first-epoch loss, last-epoch loss, held-out median
+ * residual before and after the network, last judged median error, steps
+ * judged, steps that fell back, cheap opening angle, training seconds, Adam
+ * steps). */
+int gsgpu_sim_report(gsgpu_sim *sim, double *out, int nmax);
 void gsgpu_sim_destroy(gsgpu_sim *sim);
 
 /* Library / device information: fills name (NUL-terminated, <= len). */
