@@ -24,6 +24,8 @@ enum StatusBits : unsigned {
     ST_STACK_OVERFLOW = 4u,   // walk stack deeper than the octree limit
     ST_NONFINITE = 8u,        // NaN/Inf seen where the kernel checks
     ST_BAD_KEY = 16u,         // octant digit out of range while building
+    ST_NO_PRIMARY = 32u,      // an ensemble system has no particle with id 0
+    ST_CAPACITY = 64u,        // an ensemble system outgrew its sort capacity
 };
 
 // ---- errors ------------------------------------------------------------
@@ -120,6 +122,12 @@ class Engine {
         (void)nmax;
         return 0;
     }
+    // Learned engines: training samples of one snapshot (count written).
+    virtual int dataset(int snap, float *feat, float *target, int count) const
+    {
+        (void)snap; (void)feat; (void)target; (void)count;
+        return 0;
+    }
     // Interactions of the most recent compute(): out[0] cell (monopole)
     // terms, out[1] particle-particle terms.  Synchronises the stream.
     virtual ErrorStatus interaction_counts(cudaStream_t s, long long out[2])
@@ -191,4 +199,19 @@ ErrorStatus octree_to_host(const AccelerationParam &p, const System *system,
                            const double *box_center, double box_width,
                            LinearOctree *out);
 
+}  // namespace gs
+
+// ---- batched ensembles (k_whfast.cu) -----------------------------------
+struct gsgpu_ensemble;
+namespace gs {
+ErrorStatus ensemble_create(gsgpu_ensemble **out, int num_systems, const int *counts, double G,
+                            int integrator, int method, double eps, double dt,
+                            int remove_invalid, cudaStream_t stream);
+ErrorStatus ensemble_upload(gsgpu_ensemble *e, const int *ids, const double *x, const double *v,
+                            const double *m);
+ErrorStatus ensemble_run_until(gsgpu_ensemble *e, double tf, SimulationStatus *status,
+                               const bool *is_exit);
+ErrorStatus ensemble_download(gsgpu_ensemble *e, int *counts, int *ids, double *x, double *v,
+                              double *m);
+void ensemble_destroy(gsgpu_ensemble *e);
 }  // namespace gs

@@ -540,6 +540,14 @@ int gsgpu_sim_warmup_until_ready(gsgpu_sim *sim, int64_t max_steps, int64_t *ste
     return sim->engine->ready() ? 0 : GRAV_FAILURE;
 }
 
+int gsgpu_sim_training_samples(gsgpu_sim *sim, int snapshot, float *features, float *targets,
+                               int count)
+{
+    if (!sim) return -GRAV_POINTER_ERROR;
+    cudaStreamSynchronize(sim->stream);
+    return sim->engine->dataset(snapshot, features, targets, count);
+}
+
 int gsgpu_sim_report(gsgpu_sim *sim, double *out, int nmax)
 {
     if (!sim || !out) return -GRAV_POINTER_ERROR;
@@ -611,9 +619,34 @@ ErrorStatus launch_simulation(System *system, IntegratorParam *integrator_param,
     if (!simulation_status) return GS_RAISE(GRAV_POINTER_ERROR, "simulation_status is NULL");
 
     if (integ != INTEGRATOR_EULER && integ != INTEGRATOR_EULER_CROMER && integ != INTEGRATOR_RK4 &&
-        integ != INTEGRATOR_LEAPFROG)
+        integ != INTEGRATOR_LEAPFROG && integ != INTEGRATOR_WHFAST)
         return GS_RAISE(GRAV_NOT_IMPLEMENTED_ERROR,
                         "integrator %d has no GPU implementation in this library", integ);
+
+    if (integ == INTEGRATOR_WHFAST) {
+        // src/integrator_whfast.c:200-407 as a one-system ensemble; the
+        // arrays are permuted (sort by distance) and compacted (removals) in
+        // place, num_particles shrinking like the reference's.
+        const int n0 = system->num_particles;
+        gsgpu_ensemble *raw = nullptr;
+        GS_TRY(gs::ensemble_create(&raw, 1, &n0, system->G, integ, acceleration_param->method,
+                                   acceleration_param->softening_length, integrator_param->dt,
+                                   integrator_param->whfast_remove_invalid_particles ? 1 : 0,
+                                   nullptr));
+        std::unique_ptr<gsgpu_ensemble, void (*)(gsgpu_ensemble *)> ens(raw, gs::ensemble_destroy);
+        GS_TRY(gs::ensemble_upload(ens.get(), system->particle_ids, system->x, system->v,
+                                   system->m));
+        simulation_status->t = 0.0;
+        simulation_status->dt = integrator_param->dt;
+        simulation_status->num_steps = 0;
+        if (settings->verbose >= 1) std::fputs("Launching simulation...\n", stdout);
+        GS_TRY(gs::ensemble_run_until(ens.get(), tf, simulation_status, settings->is_exit_ptr));
+        int n1 = n0;
+        GS_TRY(gs::ensemble_download(ens.get(), &n1, system->particle_ids, system->x, system->v,
+                                     system->m));
+        system->num_particles = n1;
+        return ok();
+    }
 
     if (settings->verbose >= 2) {
         const DeviceInfo *d = nullptr;

@@ -318,6 +318,19 @@ class LearnedEngine final : public Engine {
         return ok();
     }
 
+    // Copy up to `count` training samples (features, targets) of snapshot `snap`.
+    int dataset(int snap, float *feat, float *target, int count) const override
+    {
+        if (snap < 0 || snap >= snapshots_ || !feat || !target) return 0;
+        const int k = std::min(count, K_);
+        const float *f = data_feat_.as<float>() + (size_t)snap * K_ * MLP_IN;
+        const float *t = data_target_.as<float>() + (size_t)snap * K_ * MLP_OUT;
+        if (cudaMemcpy(feat, f, (size_t)k * MLP_IN * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(target, t, (size_t)k * MLP_OUT * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return 0;
+        return k;
+    }
+
     int report(double *out, int nmax) const override
     {
         double v[12] = {trained_ ? 1.0 : 0.0, (double)snapshots_, loss_first_, loss_last_,

@@ -1,0 +1,904 @@
+// k_whfast.cu -- batched planetary ensembles: WHFast and leapfrog with the
+// massless acceleration, many independent systems of uneven size per launch.
+//
+// Replaces whfast and its helpers (src/integrator_whfast.c:200-1279),
+// system_sort_by_distance / remove_particles (src/system.c:444-577,
+// :1210-1335), and for leapfrog acceleration_massless
+// (src/acceleration.c:236-367) with the kicks / drifts of src/integrator.c.
+//
+// Layout: all systems concatenated; system s owns slots [off[s], off[s+1])
+// of every per-particle array and its first cnt[s] slots are live (WHFast
+// can remove particles).  Every kernel covers all systems in one launch:
+//   k_wh_sort       one CTA per system: sort by distance from the primary
+//                   (bitonic sort of (distance, index) in shared memory,
+//                   ties by index), permute, eta (sequential prefix);
+//   k_wh_seq        one thread per system: removals (compaction), eta,
+//                   Jacobi <-> Cartesian recurrences, massive-body list;
+//   k_wh_drift      one thread per particle: universal-variable Kepler
+//                   solve (Newton, Stumpff series with argument quartering);
+//   k_wh_accel      one thread per particle: interaction accelerations in
+//                   Jacobi form (massless or pairwise variant);
+//   k_wh_kick       v_jac += a dt.
+// Every FP64 operation is an explicitly rounded intrinsic in the
+// reference's expression order, so each system evolves exactly as the
+// reference evolves it (where the reference is not FMA-contracted and does
+// not read its uninitialised a[0] / aux, taken as zero here).
+#include "gs_internal.h"
+#include "gs_ptx.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace gs {
+
+// Ensemble integrator / acceleration variants.
+enum { WH_MASSLESS = 0, WH_PAIRWISE = 1 };
+
+// Largest system of an ensemble: the per-system sort holds 12 bytes per
+// slot of the next power of two in shared memory (192 KiB at 16384).
+constexpr int kEnsembleMaxSystem = 16384;
+
+struct EnsDev {
+    int S;
+    const int *off;      // [S+1]
+    int *cnt;            // [S]
+    const int *sys_of;   // [P]
+    int *ids;
+    double *x, *v, *m, *jx, *jv, *a, *eta;
+    int *hv;             // massive-body list (indices within the system), per system at off[s]
+    int *nh;             // [S]
+    int *rm;             // [P] removal marks
+    int *nrm;            // [S]
+    // scratch for the permutation
+    int *t_ids;
+    double *t_x, *t_v, *t_m;
+    unsigned *status;
+    double G, eps;
+    int variant;
+    int remove_invalid;
+};
+
+__device__ __forceinline__ double dot3(const double *a, const double *b)
+{
+    return __dadd_rn(__dadd_rn(__dmul_rn(a[0], b[0]), __dmul_rn(a[1], b[1])), __dmul_rn(a[2], b[2]));
+}
+
+__device__ __forceinline__ double norm3d(const double *a) { return __dsqrt_rn(dot3(a, a)); }
+
+// ---- sort by distance ----------------------------------------------------
+// Sorts slots of one system by |vec_i - vec_prim| and permutes vec, vel, m,
+// ids; then eta.  Dynamic shared memory: pow2 * (8 + 4) bytes.
+__global__ void k_wh_sort(EnsDev E, double *vec, double *vel, int pow2_max)
+{
+    extern __shared__ __align__(16) unsigned char wh_smem[];
+    const int s = blockIdx.x;
+    const int base = E.off[s];
+    const int n = E.cnt[s];
+    if (n <= 0) return;
+    int P2 = 1;
+    while (P2 < n) P2 <<= 1;
+    if (P2 > pow2_max) {
+        if (threadIdx.x == 0) atomicOr(E.status, ST_CAPACITY);
+        return;
+    }
+    double *key = reinterpret_cast<double *>(wh_smem);
+    int *idx = reinterpret_cast<int *>(wh_smem + (size_t)pow2_max * 8);
+    __shared__ int prim_s;
+    if (threadIdx.x == 0) {
+        int prim = -1;
+        if (E.ids[base] == 0) {
+            prim = 0;
+        } else {
+            for (int i = 0; i < n; ++i)
+                if (E.ids[base + i] == 0) {
+                    prim = i;
+                    break;
+                }
+        }
+        prim_s = prim;
+    }
+    __syncthreads();
+    const int prim = prim_s;
+    if (prim < 0) {
+        if (threadIdx.x == 0) atomicOr(E.status, ST_NO_PRIMARY);
+        return;
+    }
+    const double p0 = vec[3 * (base + prim)], p1 = vec[3 * (base + prim) + 1],
+                 p2 = vec[3 * (base + prim) + 2];
+    for (int i = threadIdx.x; i < P2; i += blockDim.x) {
+        if (i < n) {
+            const double d[3] = {__dsub_rn(vec[3 * (base + i)], p0),
+                                 __dsub_rn(vec[3 * (base + i) + 1], p1),
+                                 __dsub_rn(vec[3 * (base + i) + 2], p2)};
+            key[i] = (i == prim) ? 0.0 : norm3d(d);
+            idx[i] = i;
+        } else {
+            key[i] = __longlong_as_double(0x7ff0000000000000ll);   // +inf pads last
+            idx[i] = 0x7fffffff;
+        }
+    }
+    __syncthreads();
+    // bitonic sort ascending by (key, idx)
+    for (int k = 2; k <= P2; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < P2; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const bool up = (i & k) == 0;
+                    const double ki = key[i], kl = key[l];
+                    const int ii = idx[i], il = idx[l];
+                    const bool gt = (ki > kl) || (ki == kl && ii > il);
+                    if (gt == up) {
+                        key[i] = kl;
+                        key[l] = ki;
+                        idx[i] = il;
+                        idx[l] = ii;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // permute through the scratch arrays
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int src = base + idx[i], dst = base + i;
+        E.t_ids[dst] = E.ids[src];
+        E.t_m[dst] = E.m[src];
+        for (int c = 0; c < 3; ++c) {
+            E.t_x[3 * dst + c] = vec[3 * src + c];
+            E.t_v[3 * dst + c] = vel[3 * src + c];
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int d = base + i;
+        E.ids[d] = E.t_ids[d];
+        E.m[d] = E.t_m[d];
+        for (int c = 0; c < 3; ++c) {
+            vec[3 * d + c] = E.t_x[3 * d + c];
+            vel[3 * d + c] = E.t_v[3 * d + c];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {   // src/integrator_whfast.c:1266-1279
+        double e = E.m[base];
+        E.eta[base] = e;
+        for (int i = 1; i < n; ++i) {
+            e = __dadd_rn(e, E.m[base + i]);
+            E.eta[base + i] = e;
+        }
+    }
+}
+
+// ---- per-system sequential work ---------------------------------------------
+__device__ void wh_massive_list(const EnsDev &E, int base, int n, int s)
+{
+    int k = 0;
+    for (int i = 0; i < n; ++i)
+        if (E.variant == WH_PAIRWISE || E.m[base + i] != 0.0) E.hv[base + k++] = i;
+    E.nh[s] = k;
+}
+
+// mode 0: Cartesian -> Jacobi (initialisation); mode 1: removals, eta,
+// Jacobi -> Cartesian.  Both rebuild the massive-body list.
+__global__ void k_wh_seq(EnsDev E, int mode)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= E.S) return;
+    const int base = E.off[s];
+    int n = E.cnt[s];
+    if (n <= 0) return;
+    double *m = E.m + base, *eta = E.eta + base;
+    double *x = E.x + 3 * base, *v = E.v + 3 * base, *jx = E.jx + 3 * base, *jv = E.jv + 3 * base;
+    if (mode == 0) {
+        // src/integrator_whfast.c:682-724
+        double xc[3], vc[3];
+        for (int k = 0; k < 3; ++k) {
+            xc[k] = __dmul_rn(m[0], x[k]);
+            vc[k] = __dmul_rn(m[0], v[k]);
+        }
+        for (int i = 1; i < n; ++i) {
+            const double ie = eta[i - 1];
+            for (int k = 0; k < 3; ++k) {
+                jx[3 * i + k] = __dsub_rn(x[3 * i + k], __ddiv_rn(xc[k], ie));
+                jv[3 * i + k] = __dsub_rn(v[3 * i + k], __ddiv_rn(vc[k], ie));
+                const double f = __dadd_rn(1.0, __ddiv_rn(m[i], ie));
+                xc[k] = __dadd_rn(__dmul_rn(xc[k], f), __dmul_rn(m[i], jx[3 * i + k]));
+                vc[k] = __dadd_rn(__dmul_rn(vc[k], f), __dmul_rn(m[i], jv[3 * i + k]));
+            }
+        }
+        for (int k = 0; k < 3; ++k) {
+            jx[k] = __ddiv_rn(xc[k], eta[n - 1]);
+            jv[k] = __ddiv_rn(vc[k], eta[n - 1]);
+        }
+    } else {
+        if (E.nrm[s] > 0) {
+            // src/system.c:444-528 and :530-577: stable compaction of the
+            // surviving slots (Cartesian x, v, m, ids, Jacobi x, v), then eta
+            int w = 0;
+            for (int i = 0; i < n; ++i) {
+                if (E.rm[base + i]) {
+                    E.rm[base + i] = 0;
+                    continue;
+                }
+                if (w != i) {
+                    E.ids[base + w] = E.ids[base + i];
+                    m[w] = m[i];
+                    for (int k = 0; k < 3; ++k) {
+                        x[3 * w + k] = x[3 * i + k];
+                        v[3 * w + k] = v[3 * i + k];
+                        jx[3 * w + k] = jx[3 * i + k];
+                        jv[3 * w + k] = jv[3 * i + k];
+                    }
+                }
+                ++w;
+            }
+            n = w;
+            E.cnt[s] = n;
+            E.nrm[s] = 0;
+            double e = m[0];
+            eta[0] = e;
+            for (int i = 1; i < n; ++i) {
+                e = __dadd_rn(e, m[i]);
+                eta[i] = e;
+            }
+        }
+        // src/integrator_whfast.c:726-772
+        double xc[3], vc[3];
+        for (int k = 0; k < 3; ++k) {
+            xc[k] = __dmul_rn(eta[n - 1], jx[k]);
+            vc[k] = __dmul_rn(eta[n - 1], jv[k]);
+        }
+        for (int i = n - 1; i > 0; --i) {
+            for (int k = 0; k < 3; ++k) {
+                xc[k] = __ddiv_rn(__dsub_rn(xc[k], __dmul_rn(m[i], jx[3 * i + k])), eta[i]);
+                vc[k] = __ddiv_rn(__dsub_rn(vc[k], __dmul_rn(m[i], jv[3 * i + k])), eta[i]);
+                x[3 * i + k] = __dadd_rn(jx[3 * i + k], xc[k]);
+                v[3 * i + k] = __dadd_rn(jv[3 * i + k], vc[k]);
+                xc[k] = __dmul_rn(eta[i - 1], xc[k]);
+                vc[k] = __dmul_rn(eta[i - 1], vc[k]);
+            }
+        }
+        for (int k = 0; k < 3; ++k) {
+            x[k] = __ddiv_rn(xc[k], m[0]);
+            v[k] = __ddiv_rn(vc[k], m[0]);
+        }
+    }
+    wh_massive_list(E, base, n, s);
+}
+
+// ---- Kepler drift -------------------------------------------------------------
+// src/integrator_whfast.c:774-815
+__device__ __forceinline__ void stumpff(double z, double &c0, double &c1, double &c2, double &c3)
+{
+    int q = 0;
+    while (fabs(z) > 0.1) {
+        z = __ddiv_rn(z, 4.0);
+        ++q;
+    }
+    double t = __dsub_rn(1.0, __ddiv_rn(z, 210.0));
+    t = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 156.0), t));
+    t = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 110.0), t));
+    t = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 72.0), t));
+    t = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 42.0), t));
+    t = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 20.0), t));
+    double s3 = __ddiv_rn(t, 6.0);
+    double u = __dsub_rn(1.0, __ddiv_rn(z, 182.0));
+    u = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 132.0), u));
+    u = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 90.0), u));
+    u = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 56.0), u));
+    u = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 30.0), u));
+    u = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 12.0), u));
+    double s2 = __ddiv_rn(u, 2.0);
+    double s1 = __dsub_rn(1.0, __dmul_rn(z, s3));
+    double s0 = __dsub_rn(1.0, __dmul_rn(z, s2));
+    while (q > 0) {
+        s3 = __ddiv_rn(__dadd_rn(s2, __dmul_rn(s0, s3)), 4.0);
+        s2 = __ddiv_rn(__dmul_rn(s1, s1), 2.0);
+        s1 = __dmul_rn(s0, s1);
+        s0 = __dsub_rn(__dmul_rn(__dmul_rn(2.0, s0), s0), 1.0);
+        --q;
+    }
+    c0 = s0;
+    c1 = s1;
+    c2 = s2;
+    c3 = s3;
+}
+
+// src/integrator_whfast.c:424-600 for one Jacobi body; returns true when the
+// particle has to be removed.
+__device__ bool kepler_drift(double *jx, double *jv, double gm, double dt)
+{
+    const double xx[3] = {jx[0], jx[1], jx[2]};
+    const double vv[3] = {jv[0], jv[1], jv[2]};
+    const double xn = norm3d(xx);
+    const double vn = norm3d(vv);
+    const double rv = __ddiv_rn(dot3(xx, vv), xn);
+    const double alpha = __dsub_rn(__ddiv_rn(__dmul_rn(2.0, gm), xn), __dmul_rn(vn, vn));
+    double s = __ddiv_rn(dt, xn);
+    double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0;
+    bool conv = false, bad_z = false;
+    const double xrv = __dmul_rn(xn, rv);
+    for (int it = 0; it < 500; ++it) {
+        const double ss = __dmul_rn(s, s);
+        const double z = __dmul_rn(alpha, ss);
+        if (!isfinite(z)) {
+            bad_z = true;
+            break;
+        }
+        stumpff(z, c0, c1, c2, c3);
+        const double sss = __dmul_rn(ss, s);
+        const double F = __dsub_rn(__dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(xn, s), c1),
+                                                       __dmul_rn(__dmul_rn(xrv, ss), c2)),
+                                             __dmul_rn(__dmul_rn(gm, sss), c3)),
+                                   dt);
+        const double dF = __dadd_rn(__dadd_rn(__dmul_rn(xn, c0), __dmul_rn(__dmul_rn(xrv, s), c1)),
+                                    __dmul_rn(__dmul_rn(gm, ss), c2));
+        const double ds = __ddiv_rn(-F, dF);
+        s = __dadd_rn(s, ds);
+        if (fabs(ds) < 1e-12) {
+            conv = true;
+            break;
+        }
+    }
+    const double ss = __dmul_rn(s, s);
+    const double sss = __dmul_rn(ss, s);
+    const double r = __dadd_rn(__dadd_rn(__dmul_rn(xn, c0), __dmul_rn(__dmul_rn(xrv, s), c1)),
+                               __dmul_rn(__dmul_rn(gm, ss), c2));
+    bool remove = false;
+    if (!conv) {
+        const double F = __dsub_rn(__dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(xn, s), c1),
+                                                       __dmul_rn(__dmul_rn(xrv, ss), c2)),
+                                             __dmul_rn(__dmul_rn(gm, sss), c3)),
+                                   dt);
+        const double err = __ddiv_rn(F, r);
+        remove = (err > 1e-5) || bad_z;
+    }
+    const double f = __dsub_rn(1.0, __ddiv_rn(__dmul_rn(__dmul_rn(gm, ss), c2), xn));
+    const double g = __dsub_rn(dt, __dmul_rn(__dmul_rn(gm, sss), c3));
+    const double df = __ddiv_rn(__dmul_rn(__dmul_rn(-gm, s), c1), __dmul_rn(r, xn));
+    const double dg = __dsub_rn(1.0, __ddiv_rn(__dmul_rn(__dmul_rn(gm, ss), c2), r));
+    for (int k = 0; k < 3; ++k) {
+        jx[k] = __dadd_rn(__dmul_rn(f, xx[k]), __dmul_rn(g, vv[k]));
+        jv[k] = __dadd_rn(__dmul_rn(df, xx[k]), __dmul_rn(dg, vv[k]));
+    }
+    return remove;
+}
+
+__global__ void k_wh_drift(EnsDev E, int P, double dt)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int s = E.sys_of[p];
+    const int base = E.off[s];
+    const int i = p - base;
+    if (i == 0 || i >= E.cnt[s]) return;
+    const double gm = __ddiv_rn(__dmul_rn(__dmul_rn(E.G, E.m[base]), E.eta[p]), E.eta[p - 1]);
+    const bool rm = kepler_drift(E.jx + 3 * (size_t)p, E.jv + 3 * (size_t)p, gm, dt);
+    if (rm && E.remove_invalid) {
+        E.rm[p] = 1;
+        atomicAdd(&E.nrm[s], 1);
+    }
+}
+
+// ---- interaction accelerations ---------------------------------------------
+// src/integrator_whfast.c:959-1264 (massless) / :839-957 (pairwise).
+__global__ void k_wh_accel(EnsDev E, int P)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int s = E.sys_of[p];
+    const int base = E.off[s];
+    const int i = p - base;
+    const int n = E.cnt[s];
+    if (i >= n) return;
+    double *a = E.a + 3 * (size_t)p;
+    if (i == 0) {
+        a[0] = a[1] = a[2] = 0.0;
+        return;
+    }
+    const double *x = E.x + 3 * (size_t)base;
+    const double *m = E.m + base;
+    const double *eta = E.eta + base;
+    const int *hv = E.hv + base;
+    const int nh = E.nh[s];
+    const double e3 = __dmul_rn(__dmul_rn(E.eps, E.eps), E.eps);
+    const double G = E.G;
+    const bool massive = (E.variant == WH_PAIRWISE) || m[i] != 0.0;
+    const double xi[3] = {x[3 * i], x[3 * i + 1], x[3 * i + 2]};
+    const double tv[3] = {__dsub_rn(xi[0], x[0]), __dsub_rn(xi[1], x[1]), __dsub_rn(xi[2], x[2])};
+    const double tn = norm3d(tv);
+    const double tc = __dadd_rn(__dmul_rn(__dmul_rn(tn, tn), tn), e3);
+    const double *jxi = E.jx + 3 * (size_t)p;
+    const double jn = norm3d(jxi);
+    const double jc = __dadd_rn(__dmul_rn(__dmul_rn(jn, jn), jn), e3);
+    const double Gm0 = __dmul_rn(G, m[0]);
+    const double pre = massive ? __ddiv_rn(__dmul_rn(Gm0, eta[i]), eta[i - 1]) : Gm0;
+    double acc[3];
+    for (int k = 0; k < 3; ++k)
+        acc[k] = __dmul_rn(pre, __dsub_rn(__ddiv_rn(jxi[k], jc), __ddiv_rn(tv[k], tc)));
+    double aux[3] = {0.0, 0.0, 0.0};
+    for (int q = 1; q < nh; ++q) {
+        const int j = hv[q];
+        if (j >= i) break;
+        const double d[3] = {__dsub_rn(xi[0], x[3 * j]), __dsub_rn(xi[1], x[3 * j + 1]),
+                             __dsub_rn(xi[2], x[3 * j + 2])};
+        const double dn = norm3d(d);
+        const double dc = __dadd_rn(__dmul_rn(__dmul_rn(dn, dn), dn), e3);
+        const double Gm = __dmul_rn(G, m[j]);
+        for (int k = 0; k < 3; ++k) aux[k] = __dadd_rn(aux[k], __ddiv_rn(__dmul_rn(Gm, d[k]), dc));
+    }
+    for (int k = 0; k < 3; ++k)
+        acc[k] = __dsub_rn(acc[k],
+                           massive ? __ddiv_rn(__dmul_rn(aux[k], eta[i]), eta[i - 1]) : aux[k]);
+    aux[0] = aux[1] = aux[2] = 0.0;
+    for (int q = 1; q < nh; ++q) {
+        const int j = hv[q];
+        if (j <= i) continue;
+        const double d[3] = {__dsub_rn(x[3 * j], xi[0]), __dsub_rn(x[3 * j + 1], xi[1]),
+                             __dsub_rn(x[3 * j + 2], xi[2])};
+        const double dn = norm3d(d);
+        const double dc = __dadd_rn(__dmul_rn(__dmul_rn(dn, dn), dn), e3);
+        const double Gm = __dmul_rn(G, m[j]);
+        for (int k = 0; k < 3; ++k) aux[k] = __dadd_rn(aux[k], __ddiv_rn(__dmul_rn(Gm, d[k]), dc));
+    }
+    for (int k = 0; k < 3; ++k) acc[k] = __dadd_rn(acc[k], aux[k]);
+    aux[0] = aux[1] = aux[2] = 0.0;
+    for (int q0 = 0; q0 < nh; ++q0) {
+        const int j = hv[q0];
+        if (j >= i) break;
+        const double Gmj = __dmul_rn(G, m[j]);
+        for (int q1 = q0 + 1; q1 < nh; ++q1) {
+            const int kk = hv[q1];
+            if (kk <= i) continue;
+            const double d[3] = {__dsub_rn(x[3 * kk], x[3 * j]), __dsub_rn(x[3 * kk + 1], x[3 * j + 1]),
+                                 __dsub_rn(x[3 * kk + 2], x[3 * j + 2])};
+            const double dn = norm3d(d);
+            const double dc = __dadd_rn(__dmul_rn(__dmul_rn(dn, dn), dn), e3);
+            const double Gmm = __dmul_rn(Gmj, m[kk]);
+            for (int k = 0; k < 3; ++k)
+                aux[k] = __dadd_rn(aux[k], __ddiv_rn(__dmul_rn(Gmm, d[k]), dc));
+        }
+    }
+    for (int k = 0; k < 3; ++k) a[k] = __dsub_rn(acc[k], __ddiv_rn(aux[k], eta[i - 1]));
+}
+
+__global__ void k_wh_kick(EnsDev E, int P, double h)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int s = E.sys_of[p];
+    if (p - E.off[s] >= E.cnt[s]) return;
+    for (int k = 0; k < 3; ++k)
+        E.jv[3 * (size_t)p + k] = __dadd_rn(E.jv[3 * (size_t)p + k], __dmul_rn(E.a[3 * (size_t)p + k], h));
+}
+
+// ---- leapfrog + massless acceleration (src/acceleration.c:236-367) ---------
+__global__ void k_ens_massless_accel(EnsDev E, int P)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int s = E.sys_of[p];
+    const int base = E.off[s];
+    const int i = p - base;
+    const int n = E.cnt[s];
+    if (i >= n) return;
+    const double *x = E.x + 3 * (size_t)base;
+    const double *m = E.m + base;
+    const int *hv = E.hv + base;
+    const int nh = E.nh[s];
+    const double eps2 = __dmul_rn(E.eps, E.eps);
+    const double xi0 = x[3 * i], xi1 = x[3 * i + 1], xi2 = x[3 * i + 2];
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    // the pairwise variant lists every particle and is the symmetric sum of
+    // src/acceleration.c:177-234 seen from particle i (same term order)
+    if (E.variant == WH_PAIRWISE || m[i] != 0.0) {
+        for (int q = 0; q < nh; ++q) {
+            const int j = hv[q];
+            if (j == i) continue;
+            const double r0 = __dsub_rn(xi0, x[3 * j]), r1 = __dsub_rn(xi1, x[3 * j + 1]),
+                         r2 = __dsub_rn(xi2, x[3 * j + 2]);
+            const double rn = __dsqrt_rn(__dadd_rn(
+                __dadd_rn(__dadd_rn(__dmul_rn(r0, r0), __dmul_rn(r1, r1)), __dmul_rn(r2, r2)), eps2));
+            const double t = __ddiv_rn(E.G, __dmul_rn(__dmul_rn(rn, rn), rn));
+            const double mj = m[j];
+            a0 = __dsub_rn(a0, __dmul_rn(__dmul_rn(t, r0), mj));
+            a1 = __dsub_rn(a1, __dmul_rn(__dmul_rn(t, r1), mj));
+            a2 = __dsub_rn(a2, __dmul_rn(__dmul_rn(t, r2), mj));
+        }
+    } else {
+        for (int q = 0; q < nh; ++q) {
+            const int j = hv[q];
+            const double r0 = __dsub_rn(x[3 * j], xi0), r1 = __dsub_rn(x[3 * j + 1], xi1),
+                         r2 = __dsub_rn(x[3 * j + 2], xi2);
+            const double rn = __dsqrt_rn(__dadd_rn(
+                __dadd_rn(__dadd_rn(__dmul_rn(r0, r0), __dmul_rn(r1, r1)), __dmul_rn(r2, r2)), eps2));
+            const double t = __ddiv_rn(E.G, __dmul_rn(__dmul_rn(rn, rn), rn));
+            const double mq = m[q];   // the reference's loop-index mass read
+            a0 = __dadd_rn(a0, __dmul_rn(__dmul_rn(t, r0), mq));
+            a1 = __dadd_rn(a1, __dmul_rn(__dmul_rn(t, r1), mq));
+            a2 = __dadd_rn(a2, __dmul_rn(__dmul_rn(t, r2), mq));
+        }
+    }
+    E.a[3 * (size_t)p] = a0;
+    E.a[3 * (size_t)p + 1] = a1;
+    E.a[3 * (size_t)p + 2] = a2;
+}
+
+__global__ void k_ens_massive_list(EnsDev E)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= E.S) return;
+    wh_massive_list(E, E.off[s], E.cnt[s], s);
+}
+
+}  // namespace gs
+
+// ---------------------------------------------------------------------------
+// Host side: the ensemble object.
+// ---------------------------------------------------------------------------
+using namespace gs;
+
+struct gsgpu_ensemble {
+    int S = 0, P = 0, max_n = 0, pow2 = 1;
+    int integrator = INTEGRATOR_WHFAST;
+    double dt = 0.0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::vector<int> h_off;
+    DBuf off, cnt, sys_of, ids, x, v, m, jx, jv, a, eta, hv, nh, rm, nrm, t_ids, t_x, t_v, t_m,
+        status, xe, ve;
+    EnsDev E{};
+    bool primed = false;
+    double last_dt = 0.0;
+    cudaGraphExec_t graph = nullptr;
+    double graph_dt = 0.0;
+
+    ~gsgpu_ensemble()
+    {
+        if (graph) cudaGraphExecDestroy(graph);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+
+    int pgrid() const { return (P + 127) / 128; }
+
+    ErrorStatus sort(double *vec, double *vel)
+    {
+        const size_t smem = (size_t)pow2 * 12;
+        const int threads = pow2 >= 256 ? 256 : (pow2 < 32 ? 32 : pow2);
+        k_wh_sort<<<S, threads, smem, stream>>>(E, vec, vel, pow2);
+        GS_CUDA(cudaGetLastError());
+        return ok();
+    }
+
+    ErrorStatus accel()
+    {
+        if (integrator == INTEGRATOR_WHFAST)
+            k_wh_accel<<<pgrid(), 128, 0, stream>>>(E, P);
+        else
+            k_ens_massless_accel<<<pgrid(), 128, 0, stream>>>(E, P);
+        GS_CUDA(cudaGetLastError());
+        return ok();
+    }
+
+    ErrorStatus prime()
+    {
+        if (primed) return ok();
+        if (integrator == INTEGRATOR_WHFAST) {
+            // src/integrator_whfast.c:241-273
+            GS_TRY(sort(E.x, E.v));
+            k_wh_seq<<<(S + 127) / 128, 128, 0, stream>>>(E, 0);
+            GS_TRY(accel());
+            k_wh_kick<<<pgrid(), 128, 0, stream>>>(E, P, 0.5 * dt);
+        } else {
+            k_ens_massive_list<<<(S + 127) / 128, 128, 0, stream>>>(E);
+            GS_TRY(accel());
+            launch_comp_update(E.v, ve.as<double>(), E.a, dt, 0.5, 3 * P, stream);
+        }
+        GS_CUDA(cudaGetLastError());
+        primed = true;
+        return ok();
+    }
+
+    ErrorStatus step(double h)
+    {
+        if (integrator == INTEGRATOR_WHFAST) {
+            // src/integrator_whfast.c:290-343
+            GS_TRY(sort(E.jx, E.jv));
+            k_wh_drift<<<pgrid(), 128, 0, stream>>>(E, P, h);
+            k_wh_seq<<<(S + 127) / 128, 128, 0, stream>>>(E, 1);
+            GS_TRY(accel());
+            k_wh_kick<<<pgrid(), 128, 0, stream>>>(E, P, h);
+        } else {
+            launch_comp_update(E.x, xe.as<double>(), E.v, h, 1.0, 3 * P, stream);
+            GS_TRY(accel());
+            launch_comp_update(E.v, ve.as<double>(), E.a, h, 1.0, 3 * P, stream);
+        }
+        GS_CUDA(cudaGetLastError());
+        last_dt = h;
+        return ok();
+    }
+
+    int kernels_per_step() const { return integrator == INTEGRATOR_WHFAST ? 5 : 3; }
+
+    ErrorStatus step_graph(double h)
+    {
+        if (!graph || graph_dt != h) {
+            if (graph) {
+                cudaGraphExecDestroy(graph);
+                graph = nullptr;
+            }
+            cudaGraph_t g = nullptr;
+            GS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            ErrorStatus st = step(h);
+            cudaError_t e = cudaStreamEndCapture(stream, &g);
+            if (st.return_code != GRAV_SUCCESS) {
+                if (g) cudaGraphDestroy(g);
+                return st;
+            }
+            if (e != cudaSuccess) {
+                (void)cudaGetLastError();
+                return step(h);
+            }
+            e = cudaGraphInstantiate(&graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                (void)cudaGetLastError();
+                graph = nullptr;
+                return step(h);
+            }
+            graph_dt = h;
+        }
+        GS_CUDA(cudaGraphLaunch(graph, stream));
+        last_dt = h;
+        return ok();
+    }
+
+    ErrorStatus check()
+    {
+        unsigned h = 0;
+        GS_CUDA(cudaMemcpyAsync(&h, status.p, sizeof(h), cudaMemcpyDeviceToHost, stream));
+        GS_CUDA(cudaStreamSynchronize(stream));
+        if (h & ST_CAPACITY)
+            return GS_RAISE(GRAV_VALUE_ERROR, "a system exceeds the ensemble's sort capacity");
+        if (h & ST_NO_PRIMARY)
+            return GS_RAISE(GRAV_VALUE_ERROR, "Primary particle ID not found in system");
+        return ok();
+    }
+};
+
+namespace gs {
+
+ErrorStatus ensemble_create(gsgpu_ensemble **out, int num_systems, const int *counts, double G,
+                            int integrator, int method, double eps, double dt,
+                            int remove_invalid, cudaStream_t stream)
+{
+    if (!out || !counts) return GS_RAISE(GRAV_POINTER_ERROR, "NULL argument");
+    if (num_systems <= 0) return GS_RAISE(GRAV_VALUE_ERROR, "num_systems must be positive");
+    if (!(dt > 0.0)) return GS_RAISE(GRAV_VALUE_ERROR, "dt must be positive. Got: %g", dt);
+    if (integrator != INTEGRATOR_WHFAST && integrator != INTEGRATOR_LEAPFROG)
+        return GS_RAISE(GRAV_VALUE_ERROR, "ensembles run WHFast (10) or leapfrog (4). Got: %d",
+                        integrator);
+    if (method != GRAV_GPU_MASSLESS && method != GRAV_GPU_PAIRWISE &&
+        method != GRAV_GPU_PAIRWISE_FP64)
+        return GS_RAISE(GRAV_VALUE_ERROR,
+                        "Invalid acceleration method for WHFast integrator. Only pairwise and "
+                        "massless methods are supported.");
+    const DeviceInfo *d = nullptr;
+    GS_TRY(device_info(&d));
+    std::unique_ptr<gsgpu_ensemble> e(new gsgpu_ensemble());
+    e->S = num_systems;
+    e->integrator = integrator;
+    e->dt = dt;
+    e->h_off.assign(num_systems + 1, 0);
+    for (int s = 0; s < num_systems; ++s) {
+        if (counts[s] <= 0) return GS_RAISE(GRAV_VALUE_ERROR, "system %d is empty", s);
+        e->h_off[s + 1] = e->h_off[s] + counts[s];
+        e->max_n = std::max(e->max_n, counts[s]);
+    }
+    e->P = e->h_off[num_systems];
+    while (e->pow2 < e->max_n) e->pow2 <<= 1;
+    if (e->pow2 > kEnsembleMaxSystem)
+        return GS_RAISE(GRAV_VALUE_ERROR, "systems of more than %d particles are not supported",
+                        kEnsembleMaxSystem);
+    if (stream) {
+        e->stream = stream;
+    } else {
+        GS_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+        e->own_stream = true;
+    }
+    const size_t P = (size_t)e->P, S = (size_t)e->S;
+    GS_TRY(e->off.reserve((S + 1) * sizeof(int)));
+    GS_TRY(e->cnt.reserve(S * sizeof(int)));
+    GS_TRY(e->nh.reserve(S * sizeof(int)));
+    GS_TRY(e->nrm.reserve(S * sizeof(int)));
+    DBuf *ints[] = {&e->sys_of, &e->ids, &e->hv, &e->rm, &e->t_ids};
+    for (DBuf *b : ints) GS_TRY(b->reserve(P * sizeof(int)));
+    DBuf *vec3[] = {&e->x, &e->v, &e->jx, &e->jv, &e->a, &e->t_x, &e->t_v, &e->xe, &e->ve};
+    for (DBuf *b : vec3) GS_TRY(b->reserve(P * 3 * sizeof(double)));
+    GS_TRY(e->m.reserve(P * sizeof(double)));
+    GS_TRY(e->eta.reserve(P * sizeof(double)));
+    GS_TRY(e->t_m.reserve(P * sizeof(double)));
+    GS_TRY(e->status.reserve(sizeof(unsigned)));
+    std::vector<int> sys(P);
+    for (int s = 0; s < num_systems; ++s)
+        for (int p = e->h_off[s]; p < e->h_off[s + 1]; ++p) sys[p] = s;
+    GS_CUDA(cudaMemcpy(e->off.p, e->h_off.data(), (S + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    GS_CUDA(cudaMemcpy(e->cnt.p, counts, S * sizeof(int), cudaMemcpyHostToDevice));
+    GS_CUDA(cudaMemcpy(e->sys_of.p, sys.data(), P * sizeof(int), cudaMemcpyHostToDevice));
+    GS_CUDA(cudaMemset(e->nrm.p, 0, S * sizeof(int)));
+    GS_CUDA(cudaMemset(e->rm.p, 0, P * sizeof(int)));
+    GS_CUDA(cudaMemset(e->status.p, 0, sizeof(unsigned)));
+    GS_CUDA(cudaMemset(e->a.p, 0, P * 3 * sizeof(double)));
+    GS_CUDA(cudaFuncSetAttribute(k_wh_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)std::max<size_t>((size_t)e->pow2 * 12, 48 * 1024)));
+    EnsDev &E = e->E;
+    E.S = e->S;
+    E.off = e->off.as<int>();
+    E.cnt = e->cnt.as<int>();
+    E.sys_of = e->sys_of.as<int>();
+    E.ids = e->ids.as<int>();
+    E.x = e->x.as<double>();
+    E.v = e->v.as<double>();
+    E.m = e->m.as<double>();
+    E.jx = e->jx.as<double>();
+    E.jv = e->jv.as<double>();
+    E.a = e->a.as<double>();
+    E.eta = e->eta.as<double>();
+    E.hv = e->hv.as<int>();
+    E.nh = e->nh.as<int>();
+    E.rm = e->rm.as<int>();
+    E.nrm = e->nrm.as<int>();
+    E.t_ids = e->t_ids.as<int>();
+    E.t_x = e->t_x.as<double>();
+    E.t_v = e->t_v.as<double>();
+    E.t_m = e->t_m.as<double>();
+    E.status = e->status.as<unsigned>();
+    E.G = G;
+    E.eps = eps;
+    E.variant = method == GRAV_GPU_MASSLESS ? WH_MASSLESS : WH_PAIRWISE;
+    E.remove_invalid = remove_invalid ? 1 : 0;
+    *out = e.release();
+    return ok();
+}
+
+ErrorStatus ensemble_upload(gsgpu_ensemble *e, const int *ids, const double *x, const double *v,
+                            const double *m)
+{
+    if (!e || !ids || !x || !v || !m) return GS_RAISE(GRAV_POINTER_ERROR, "NULL argument");
+    const size_t P = (size_t)e->P;
+    GS_CUDA(cudaMemcpyAsync(e->ids.p, ids, P * sizeof(int), cudaMemcpyHostToDevice, e->stream));
+    GS_CUDA(cudaMemcpyAsync(e->x.p, x, P * 3 * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+    GS_CUDA(cudaMemcpyAsync(e->v.p, v, P * 3 * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+    GS_CUDA(cudaMemcpyAsync(e->m.p, m, P * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+    GS_CUDA(cudaMemsetAsync(e->xe.p, 0, P * 3 * sizeof(double), e->stream));
+    GS_CUDA(cudaMemsetAsync(e->ve.p, 0, P * 3 * sizeof(double), e->stream));
+    e->primed = false;
+    return ok();
+}
+
+// The reference's step loop over time tf (same step count and dt clamp).
+ErrorStatus ensemble_run_until(gsgpu_ensemble *e, double tf, SimulationStatus *status,
+                               const bool *is_exit)
+{
+    double dt = e->dt;
+    const int64_t total = (int64_t)std::ceil(tf / dt);
+    GS_TRY(e->prime());
+    double t = 0.0;
+    int64_t steps = 0;
+    while (steps < total) {
+        if (t + dt > tf) dt = tf - t;
+        if (status) status->dt = dt;
+        GS_TRY(e->step_graph(dt));
+        ++steps;
+        t = (double)steps * dt;
+        if ((steps & 31) == 0) GS_TRY(e->check());
+        if (is_exit && *is_exit) break;
+    }
+    if (status) {
+        status->t = t;
+        status->num_steps = steps;
+    }
+    GS_TRY(e->check());
+    return ok();
+}
+
+// Final state: WHFast returns the Cartesian arrays as the reference leaves
+// them; leapfrog synchronises v to integer time (src/integrator.c:1088-1094).
+ErrorStatus ensemble_download(gsgpu_ensemble *e, int *counts, int *ids, double *x, double *v,
+                              double *m)
+{
+    GS_TRY(e->check());
+    const size_t P = (size_t)e->P;
+    double *vsrc = e->E.v;
+    if (e->integrator == INTEGRATOR_LEAPFROG && e->primed && v) {
+        // v at integer time from the half-step state, without touching it
+        GS_CUDA(cudaMemcpyAsync(e->t_v.p, e->v.p, P * 3 * sizeof(double), cudaMemcpyDeviceToDevice,
+                                e->stream));
+        launch_plain_kick(e->E.t_v, e->E.a, 0.5, e->last_dt, 3 * e->P, e->stream);
+        GS_CUDA(cudaGetLastError());
+        vsrc = e->E.t_v;
+    }
+    if (counts) GS_CUDA(cudaMemcpyAsync(counts, e->cnt.p, e->S * sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+    if (ids) GS_CUDA(cudaMemcpyAsync(ids, e->ids.p, P * sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+    if (x) GS_CUDA(cudaMemcpyAsync(x, e->x.p, P * 3 * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    if (v) GS_CUDA(cudaMemcpyAsync(v, vsrc, P * 3 * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    if (m) GS_CUDA(cudaMemcpyAsync(m, e->m.p, P * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    GS_CUDA(cudaStreamSynchronize(e->stream));
+    return ok();
+}
+
+void ensemble_destroy(gsgpu_ensemble *e) { delete e; }
+
+}  // namespace gs
+
+extern "C" {
+
+int gsgpu_ensemble_create(gsgpu_ensemble **out, int num_systems, const int *counts, double G,
+                          int integrator, int acceleration_method, double softening_length,
+                          double dt, int remove_invalid_particles, void *stream)
+{
+    ErrorStatus st = gs::ensemble_create(out, num_systems, counts, G, integrator, acceleration_method,
+                                         softening_length, dt, remove_invalid_particles,
+                                         static_cast<cudaStream_t>(stream));
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    return 0;
+}
+
+int gsgpu_ensemble_upload(gsgpu_ensemble *e, const int *ids, const double *x, const double *v,
+                          const double *m)
+{
+    ErrorStatus st = gs::ensemble_upload(e, ids, x, v, m);
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    return 0;
+}
+
+int gsgpu_ensemble_run(gsgpu_ensemble *e, int64_t num_steps)
+{
+    if (!e) return GRAV_POINTER_ERROR;
+    ErrorStatus st = e->prime();
+    for (int64_t k = 0; k < num_steps && st.return_code == GRAV_SUCCESS; ++k)
+        st = e->step_graph(e->dt);
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    return 0;
+}
+
+int gsgpu_ensemble_run_until(gsgpu_ensemble *e, double tf)
+{
+    if (!e) return GRAV_POINTER_ERROR;
+    ErrorStatus st = gs::ensemble_run_until(e, tf, nullptr, nullptr);
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    return 0;
+}
+
+int gsgpu_ensemble_download(gsgpu_ensemble *e, int *counts, int *ids, double *x, double *v,
+                            double *m)
+{
+    if (!e) return GRAV_POINTER_ERROR;
+    ErrorStatus st = gs::ensemble_download(e, counts, ids, x, v, m);
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    return 0;
+}
+
+int gsgpu_ensemble_kernels_per_step(const gsgpu_ensemble *e) { return e ? e->kernels_per_step() : 0; }
+
+int gsgpu_ensemble_num_particles(const gsgpu_ensemble *e) { return e ? e->P : 0; }
+
+void gsgpu_ensemble_destroy(gsgpu_ensemble *e) { delete e; }
+
+}  // extern "C"

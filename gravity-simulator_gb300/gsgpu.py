@@ -271,3 +271,107 @@ def launch_simulation(lib: ctypes.CDLL, x: np.ndarray, v: np.ndarray,
     # that own that memory so they stay alive with the result.
     assert ctypes.addressof(new_x.contents) == x.ctypes.data
     return (ids[:k], x.reshape(-1, 3)[:k], v.reshape(-1, 3)[:k], m[:k])
+
+
+class Ensemble:
+    """Batched planetary ensembles (``gsgpu_ensemble_*``): many independent
+    systems of uneven size advanced together on the GPU by WHFast
+    (INTEGRATOR_WHFAST) or leapfrog (INTEGRATOR_LEAPFROG) with the massless or
+    pairwise accelerations.  Each system evolves as the reference's
+    ``launch_simulation`` evolves it alone (src/integrator_whfast.c:200-407,
+    src/integrator.c:894-1121).
+
+    ``counts`` gives the particles per system; ``ids``, ``x``, ``v``, ``m``
+    are the systems concatenated, ids system-local with the primary's id 0.
+    """
+
+    def __init__(self, lib: ctypes.CDLL, counts, G: float, *, integrator: int,
+                 method: int, dt: float, softening_length: float = 0.0,
+                 remove_invalid_particles: bool = True):
+        self.lib = lib
+        _init_ensemble_api(lib)
+        self.counts = np.ascontiguousarray(counts, dtype=np.int32)
+        self.num_systems = int(self.counts.shape[0])
+        self.num_particles = int(self.counts.sum())
+        h = ctypes.c_void_p()
+        rc = lib.gsgpu_ensemble_create(
+            ctypes.byref(h), self.num_systems, _ip(self.counts), float(G), int(integrator),
+            int(method), float(softening_length), float(dt), int(bool(remove_invalid_particles)),
+            None)
+        if rc != 0:
+            raise GravError(rc, "gsgpu_ensemble_create failed")
+        self.handle = h
+
+    def _check(self, rc: int, what: str) -> None:
+        if rc != 0:
+            raise GravError(rc, f"{what} failed")
+
+    def upload(self, ids: np.ndarray, x: np.ndarray, v: np.ndarray, m: np.ndarray) -> None:
+        P = self.num_particles
+        self._keep = (np.ascontiguousarray(ids, dtype=np.int32).reshape(P),
+                      np.ascontiguousarray(x, dtype=np.float64).reshape(P, 3),
+                      np.ascontiguousarray(v, dtype=np.float64).reshape(P, 3),
+                      np.ascontiguousarray(m, dtype=np.float64).reshape(P))
+        i, xx, vv, mm = self._keep
+        self._check(self.lib.gsgpu_ensemble_upload(self.handle, _ip(i), _dp(xx), _dp(vv), _dp(mm)),
+                    "gsgpu_ensemble_upload")
+
+    def run(self, num_steps: int) -> None:
+        self._check(self.lib.gsgpu_ensemble_run(self.handle, ctypes.c_int64(int(num_steps))),
+                    "gsgpu_ensemble_run")
+
+    def run_until(self, tf: float) -> None:
+        self._check(self.lib.gsgpu_ensemble_run_until(self.handle, ctypes.c_double(tf)),
+                    "gsgpu_ensemble_run_until")
+
+    def download(self):
+        """Returns (counts, ids, x, v, m); system s occupies the first
+        counts[s] slots of its block (blocks at the original offsets)."""
+        P = self.num_particles
+        counts = np.empty(self.num_systems, dtype=np.int32)
+        ids = np.empty(P, dtype=np.int32)
+        x = np.empty((P, 3))
+        v = np.empty((P, 3))
+        m = np.empty(P)
+        self._check(self.lib.gsgpu_ensemble_download(self.handle, _ip(counts), _ip(ids), _dp(x),
+                                                     _dp(v), _dp(m)),
+                    "gsgpu_ensemble_download")
+        return counts, ids, x, v, m
+
+    def kernels_per_step(self) -> int:
+        return int(self.lib.gsgpu_ensemble_kernels_per_step(self.handle))
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.gsgpu_ensemble_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _init_ensemble_api(lib: ctypes.CDLL) -> None:
+    if getattr(lib, "_ensemble_api", False):
+        return
+    vp = ctypes.c_void_p
+    lib.gsgpu_ensemble_create.restype = ctypes.c_int
+    lib.gsgpu_ensemble_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, c_int_p,
+                                          ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_double, ctypes.c_double, ctypes.c_int, vp]
+    lib.gsgpu_ensemble_upload.restype = ctypes.c_int
+    lib.gsgpu_ensemble_upload.argtypes = [vp, c_int_p, c_double_p, c_double_p, c_double_p]
+    lib.gsgpu_ensemble_run.restype = ctypes.c_int
+    lib.gsgpu_ensemble_run.argtypes = [vp, ctypes.c_int64]
+    lib.gsgpu_ensemble_run_until.restype = ctypes.c_int
+    lib.gsgpu_ensemble_run_until.argtypes = [vp, ctypes.c_double]
+    lib.gsgpu_ensemble_download.restype = ctypes.c_int
+    lib.gsgpu_ensemble_download.argtypes = [vp, c_int_p, c_int_p, c_double_p, c_double_p,
+                                            c_double_p]
+    lib.gsgpu_ensemble_kernels_per_step.restype = ctypes.c_int
+    lib.gsgpu_ensemble_kernels_per_step.argtypes = [vp]
+    lib.gsgpu_ensemble_destroy.restype = None
+    lib.gsgpu_ensemble_destroy.argtypes = [vp]
+    lib._ensemble_api = True

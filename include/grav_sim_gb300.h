@@ -277,7 +277,42 @@ int gsgpu_sim_warmup_until_ready(gsgpu_sim *sim, int64_t max_steps, int64_t *ste
  * judged, steps that fell back, cheap opening angle, training seconds, Adam
  * steps). */
 int gsgpu_sim_report(gsgpu_sim *sim, double *out, int nmax);
+/* Learned method: copy up to `count` training samples of one snapshot
+ * (features [count][32], targets [count][3]); returns the number copied. */
+int gsgpu_sim_training_samples(gsgpu_sim *sim, int snapshot, float *features, float *targets,
+                               int count);
 void gsgpu_sim_destroy(gsgpu_sim *sim);
+
+/* Batched planetary ensembles: many independent systems of uneven size
+ * advanced together, every phase one launch over all systems.  Replaces the
+ * reference's per-system WHFast (src/integrator_whfast.c:200-407, integrator
+ * 10, with its sort by distance src/system.c:1210-1335 and particle removal
+ * src/system.c:444-577) and leapfrog (src/integrator.c:894-1121, integrator
+ * 4) driven by the massless (GRAV_GPU_MASSLESS) or pairwise
+ * (GRAV_GPU_PAIRWISE / GRAV_GPU_PAIRWISE_FP64: FP64, reference order)
+ * accelerations.  Each system evolves bit for bit as the reference evolves
+ * it alone.  counts[s] particles per system (1..16384); arrays are the
+ * systems concatenated, ids system-local with the primary's id 0.  WHFast
+ * removes particles whose Kepler solve fails; downloads then report the new
+ * counts and leave the freed slots at each system's end. */
+typedef struct gsgpu_ensemble gsgpu_ensemble;
+
+int gsgpu_ensemble_create(gsgpu_ensemble **out, int num_systems, const int *counts,
+                          double G, int integrator, int acceleration_method,
+                          double softening_length, double dt,
+                          int remove_invalid_particles, void *stream);
+int gsgpu_ensemble_upload(gsgpu_ensemble *e, const int *ids, const double *x,
+                          const double *v, const double *m);
+/* Enqueue num_steps steps of the creation dt (asynchronous). */
+int gsgpu_ensemble_run(gsgpu_ensemble *e, int64_t num_steps);
+/* The reference's loop to time tf: ceil(tf/dt) steps, the last one clamped. */
+int gsgpu_ensemble_run_until(gsgpu_ensemble *e, double tf);
+/* counts [S], ids [P], x, v [3P], m [P]; any pointer may be NULL. */
+int gsgpu_ensemble_download(gsgpu_ensemble *e, int *counts, int *ids, double *x,
+                            double *v, double *m);
+int gsgpu_ensemble_kernels_per_step(const gsgpu_ensemble *e);
+int gsgpu_ensemble_num_particles(const gsgpu_ensemble *e);
+void gsgpu_ensemble_destroy(gsgpu_ensemble *e);
 
 /* Library / device information: fills name (NUL-terminated, <= len). */
 int gsgpu_device_info(char *name, int len, int *sm_count, int *cc_major,

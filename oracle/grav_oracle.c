@@ -668,6 +668,304 @@ done:
 }
 
 /* ------------------------------------------------------------------ */
+/* WHFast (src/integrator_whfast.c)                                     */
+/* ------------------------------------------------------------------ */
+
+static double norm3v(const double *p)
+{
+    return sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+}
+
+typedef struct { double d; int i; } OrcDist;
+
+static int cmp_dist(const void *a, const void *b)
+{
+    const OrcDist *p = (const OrcDist *)a, *q = (const OrcDist *)b;
+    if (p->d < q->d) return -1;
+    if (p->d > q->d) return 1;
+    return (p->i > q->i) - (p->i < q->i);   /* ties: array order */
+}
+
+/* src/system.c:1210-1335: order particles by |x_i - x_primary| (primary's
+ * distance forced to 0), permuting ids, the given vectors and m. */
+static int sort_by_distance(int n, int *ids, double *xa, double *va, double *m)
+{
+    int prim = -1;
+    if (0 < n && ids[0] == 0) prim = 0;
+    else for (int i = 0; i < n; ++i) if (ids[i] == 0) { prim = i; break; }
+    if (prim < 0) return 2;
+    OrcDist *h = (OrcDist *)malloc(sizeof(OrcDist) * (size_t)n);
+    int *ni = (int *)malloc(sizeof(int) * (size_t)n);
+    double *nx = (double *)malloc(sizeof(double) * 3 * (size_t)n);
+    double *nv = (double *)malloc(sizeof(double) * 3 * (size_t)n);
+    double *nm = (double *)malloc(sizeof(double) * (size_t)n);
+    if (!h || !ni || !nx || !nv || !nm) { free(h); free(ni); free(nx); free(nv); free(nm); return 4; }
+    for (int i = 0; i < n; ++i) {
+        double d[3];
+        for (int k = 0; k < 3; ++k) d[k] = xa[3 * i + k] - xa[3 * prim + k];
+        h[i].d = norm3v(d);
+        h[i].i = i;
+    }
+    h[prim].d = 0.0;
+    qsort(h, (size_t)n, sizeof(OrcDist), cmp_dist);
+    for (int i = 0; i < n; ++i) {
+        const int j = h[i].i;
+        ni[i] = ids[j];
+        for (int k = 0; k < 3; ++k) { nx[3 * i + k] = xa[3 * j + k]; nv[3 * i + k] = va[3 * j + k]; }
+        nm[i] = m[j];
+    }
+    memcpy(ids, ni, sizeof(int) * (size_t)n);
+    memcpy(xa, nx, sizeof(double) * 3 * (size_t)n);
+    memcpy(va, nv, sizeof(double) * 3 * (size_t)n);
+    memcpy(m, nm, sizeof(double) * (size_t)n);
+    free(h); free(ni); free(nx); free(nv); free(nm);
+    return 0;
+}
+
+/* :1266-1279 */
+static void wh_eta(int n, const double *m, double *eta)
+{
+    eta[0] = m[0];
+    for (int i = 1; i < n; ++i) eta[i] = eta[i - 1] + m[i];
+}
+
+/* :682-724 */
+static void wh_cart_to_jac(int n, const double *x, const double *v, const double *m,
+                           const double *eta, double *jx, double *jv)
+{
+    double xc[3], vc[3];
+    for (int k = 0; k < 3; ++k) { xc[k] = m[0] * x[k]; vc[k] = m[0] * v[k]; }
+    for (int i = 1; i < n; ++i) {
+        for (int k = 0; k < 3; ++k) {
+            jx[3 * i + k] = x[3 * i + k] - xc[k] / eta[i - 1];
+            jv[3 * i + k] = v[3 * i + k] - vc[k] / eta[i - 1];
+            xc[k] = xc[k] * (1.0 + m[i] / eta[i - 1]) + m[i] * jx[3 * i + k];
+            vc[k] = vc[k] * (1.0 + m[i] / eta[i - 1]) + m[i] * jv[3 * i + k];
+        }
+    }
+    for (int k = 0; k < 3; ++k) {
+        jx[k] = xc[k] / eta[n - 1];
+        jv[k] = vc[k] / eta[n - 1];
+    }
+}
+
+/* :726-772 */
+static void wh_jac_to_cart(int n, const double *jx, const double *jv, const double *m,
+                           const double *eta, double *x, double *v)
+{
+    double xc[3], vc[3];
+    for (int k = 0; k < 3; ++k) { xc[k] = eta[n - 1] * jx[k]; vc[k] = eta[n - 1] * jv[k]; }
+    for (int i = n - 1; i > 0; --i) {
+        for (int k = 0; k < 3; ++k) {
+            xc[k] = (xc[k] - m[i] * jx[3 * i + k]) / eta[i];
+            vc[k] = (vc[k] - m[i] * jv[3 * i + k]) / eta[i];
+            x[3 * i + k] = jx[3 * i + k] + xc[k];
+            v[3 * i + k] = jv[3 * i + k] + vc[k];
+            xc[k] = eta[i - 1] * xc[k];
+            vc[k] = eta[i - 1] * vc[k];
+        }
+    }
+    for (int k = 0; k < 3; ++k) { x[k] = xc[k] / m[0]; v[k] = vc[k] / m[0]; }
+}
+
+/* :774-815 */
+static void stumpff(double z, double *c0, double *c1, double *c2, double *c3)
+{
+    int q = 0;
+    while (fabs(z) > 0.1) { z /= 4.0; ++q; }
+    double s3 = (1.0 - z / 20.0 * (1.0 - z / 42.0 * (1.0 - z / 72.0 * (1.0 - z / 110.0
+                 * (1.0 - z / 156.0 * (1.0 - z / 210.0)))))) / 6.0;
+    double s2 = (1.0 - z / 12.0 * (1.0 - z / 30.0 * (1.0 - z / 56.0 * (1.0 - z / 90.0
+                 * (1.0 - z / 132.0 * (1.0 - z / 182.0)))))) / 2.0;
+    double s1 = 1.0 - z * s3;
+    double s0 = 1.0 - z * s2;
+    while (q > 0) {
+        s3 = (s2 + s0 * s3) / 4.0;
+        s2 = (s1 * s1) / 2.0;
+        s1 = s0 * s1;
+        s0 = (2.0 * s0 * s0) - 1.0;
+        --q;
+    }
+    *c0 = s0; *c1 = s1; *c2 = s2; *c3 = s3;
+}
+
+/* :424-600: universal-variable Kepler drift of Jacobi body i; returns
+ * 1 when the particle is to be removed (not converged with error above
+ * 1e-5, or non-finite argument), else 0. */
+static int wh_drift_one(double *jx, double *jv, double gm, double dt)
+{
+    const double xx[3] = {jx[0], jx[1], jx[2]};
+    const double vv[3] = {jv[0], jv[1], jv[2]};
+    const double xn = norm3v(xx);
+    const double vn = norm3v(vv);
+    const double rv = (xx[0] * vv[0] + xx[1] * vv[1] + xx[2] * vv[2]) / xn;
+    const double alpha = 2.0 * gm / xn - (vn * vn);
+    double s = dt / xn;
+    double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0;
+    int conv = 0, bad_z = 0;
+    for (int it = 0; it < 500; ++it) {
+        const double z = alpha * (s * s);
+        if (!isfinite(z)) { bad_z = 1; break; }
+        stumpff(z, &c0, &c1, &c2, &c3);
+        const double F = xn * s * c1 + xn * rv * (s * s) * c2 + gm * (s * s * s) * c3 - dt;
+        const double dF = xn * c0 + xn * rv * s * c1 + gm * (s * s) * c2;
+        const double ds = -F / dF;
+        s += ds;
+        if (fabs(ds) < 1e-12) { conv = 1; break; }
+    }
+    const double r = xn * c0 + xn * rv * s * c1 + gm * (s * s) * c2;
+    int remove = 0;
+    if (!conv) {
+        const double err = (xn * s * c1 + xn * rv * (s * s) * c2 + gm * (s * s * s) * c3 - dt) / r;
+        if (err > 1e-5 || bad_z) remove = 1;
+    }
+    const double f = 1.0 - gm * (s * s) * c2 / xn;
+    const double g = dt - gm * (s * s * s) * c3;
+    const double df = -gm * s * c1 / (r * xn);
+    const double dg = 1.0 - gm * (s * s) * c2 / r;
+    for (int k = 0; k < 3; ++k) {
+        jx[k] = f * xx[k] + g * vv[k];
+        jv[k] = df * xx[k] + dg * vv[k];
+    }
+    return remove;
+}
+
+/* :959-1264 (massless variant, aux taken as zero where the reference
+ * reads it uninitialised) and :839-957 (pairwise variant). a[0] is 0. */
+static int wh_accel(int n, const double *x, const double *jx, const double *m,
+                    const double *eta, double G, double eps, int pairwise, double *a)
+{
+    const double e3 = eps * eps * eps;
+    int *hv = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    if (!hv) return 4;
+    int nh = 0;
+    for (int i = 0; i < n; ++i)
+        if (pairwise || m[i] != 0.0) hv[nh++] = i;
+    for (int k = 0; k < 3 * n; ++k) a[k] = 0.0;
+    for (int i = 1; i < n; ++i) {
+        const int massive = pairwise || m[i] != 0.0;
+        double tv[3], aux[3] = {0.0, 0.0, 0.0};
+        for (int k = 0; k < 3; ++k) tv[k] = x[3 * i + k] - x[k];
+        const double tn = norm3v(tv);
+        const double tc = (tn * tn * tn) + e3;
+        const double jn = norm3v(&jx[3 * i]);
+        const double jc = (jn * jn * jn) + e3;
+        for (int k = 0; k < 3; ++k) {
+            const double pre = massive ? G * m[0] * eta[i] / eta[i - 1] : G * m[0];
+            a[3 * i + k] = pre * (jx[3 * i + k] / jc - tv[k] / tc);
+        }
+        /* interior massive bodies j in (0, i) */
+        for (int p = 1; p < nh && hv[p] < i; ++p) {
+            const int j = hv[p];
+            double d[3];
+            for (int k = 0; k < 3; ++k) d[k] = x[3 * i + k] - x[3 * j + k];
+            const double dn = norm3v(d);
+            const double dc = (dn * dn * dn) + e3;
+            for (int k = 0; k < 3; ++k) aux[k] += G * m[j] * d[k] / dc;
+        }
+        for (int k = 0; k < 3; ++k)
+            a[3 * i + k] -= massive ? aux[k] * eta[i] / eta[i - 1] : aux[k];
+        aux[0] = aux[1] = aux[2] = 0.0;
+        /* exterior massive bodies */
+        for (int p = 1; p < nh; ++p) {
+            const int j = hv[p];
+            if (j <= i) continue;
+            double d[3];
+            for (int k = 0; k < 3; ++k) d[k] = x[3 * j + k] - x[3 * i + k];
+            const double dn = norm3v(d);
+            const double dc = (dn * dn * dn) + e3;
+            for (int k = 0; k < 3; ++k) aux[k] += G * m[j] * d[k] / dc;
+        }
+        for (int k = 0; k < 3; ++k) a[3 * i + k] += aux[k];
+        aux[0] = aux[1] = aux[2] = 0.0;
+        /* pairs (interior j incl. 0, exterior k) */
+        for (int p = 0; p < nh && hv[p] < i; ++p) {
+            const int j = hv[p];
+            for (int q = p + 1; q < nh; ++q) {
+                const int kk = hv[q];
+                if (kk <= i) continue;
+                double d[3];
+                for (int k = 0; k < 3; ++k) d[k] = x[3 * kk + k] - x[3 * j + k];
+                const double dn = norm3v(d);
+                const double dc = (dn * dn * dn) + e3;
+                for (int k = 0; k < 3; ++k) aux[k] += G * m[j] * m[kk] * d[k] / dc;
+            }
+        }
+        for (int k = 0; k < 3; ++k) a[3 * i + k] -= aux[k] / eta[i - 1];
+    }
+    free(hv);
+    return 0;
+}
+
+static void remove_rows(int n, const int *rm, int nrm, int width, double *arr)
+{
+    int w = 0, r = 0;
+    for (int i = 0; i < n; ++i) {
+        if (r < nrm && rm[r] == i) { ++r; continue; }
+        for (int k = 0; k < width; ++k) arr[width * w + k] = arr[width * i + k];
+        ++w;
+    }
+}
+
+/* src/integrator_whfast.c:200-407 for one system; *n may shrink when
+ * invalid particles are removed (remove_invalid != 0). */
+int orc_whfast_run(int *n_io, int *ids, double *x, double *v, double *m, double G, double eps,
+                   double dt, double tf, int remove_invalid, int pairwise)
+{
+    int n = *n_io;
+    double *jx = (double *)calloc((size_t)n * 3, sizeof(double));
+    double *jv = (double *)malloc(sizeof(double) * 3 * (size_t)n);
+    double *a = (double *)malloc(sizeof(double) * 3 * (size_t)n);
+    double *eta = (double *)malloc(sizeof(double) * (size_t)n);
+    int *rm = (int *)malloc(sizeof(int) * (size_t)n);
+    int rc = 0;
+    if (!jx || !jv || !a || !eta || !rm) { rc = 4; goto out; }
+    if ((rc = sort_by_distance(n, ids, x, v, m))) goto out;
+    wh_eta(n, m, eta);
+    wh_cart_to_jac(n, x, v, m, eta, jx, jv);
+    if ((rc = wh_accel(n, x, jx, m, eta, G, eps, pairwise, a))) goto out;
+    for (int k = 0; k < 3 * n; ++k) jv[k] += a[k] * (0.5 * dt);
+    {
+        const int64_t steps = (int64_t)ceil(tf / dt);
+        double t = 0.0, h = dt;
+        for (int64_t s = 0; s < steps; ++s) {
+            if (t + h > tf) h = tf - t;
+            if ((rc = sort_by_distance(n, ids, jx, jv, m))) goto out;
+            wh_eta(n, m, eta);
+            int nrm = 0;
+            for (int i = 1; i < n; ++i) {
+                const double gm = G * m[0] * eta[i] / eta[i - 1];
+                if (wh_drift_one(&jx[3 * i], &jv[3 * i], gm, h) && remove_invalid) rm[nrm++] = i;
+            }
+            if (nrm > 0) {
+                int *idsrc = ids;
+                /* compact ids, cartesian x, v, m, then jx, jv (and eta) */
+                int w = 0, r = 0;
+                for (int i = 0; i < n; ++i) {
+                    if (r < nrm && rm[r] == i) { ++r; continue; }
+                    idsrc[w++] = idsrc[i];
+                }
+                remove_rows(n, rm, nrm, 3, x);
+                remove_rows(n, rm, nrm, 3, v);
+                remove_rows(n, rm, nrm, 1, m);
+                remove_rows(n, rm, nrm, 3, jx);
+                remove_rows(n, rm, nrm, 3, jv);
+                n -= nrm;
+                wh_eta(n, m, eta);
+            }
+            wh_jac_to_cart(n, jx, jv, m, eta, x, v);
+            if ((rc = wh_accel(n, x, jx, m, eta, G, eps, pairwise, a))) goto out;
+            for (int k = 0; k < 3 * n; ++k) jv[k] += a[k] * h;
+            t = (double)(s + 1) * h;
+        }
+    }
+out:
+    *n_io = n;
+    free(jx); free(jv); free(a); free(eta); free(rm);
+    return rc;
+}
+
+/* ------------------------------------------------------------------ */
 /* Diagnostics                                                          */
 /* ------------------------------------------------------------------ */
 

@@ -107,6 +107,15 @@ int orc_fixed_step_run(int integrator, int method, int n, double *x, double *v,
                        const double *m, double G, double eps, double dt,
                        double tf);
 
+/* src/integrator_whfast.c:200-407 for one system: sort by distance, eta,
+ * Jacobi transforms, universal-variable Kepler drift, the interaction
+ * accelerations (pairwise=0: the massless variant :959-1264, 1: the
+ * pairwise variant :839-957) and kicks; a[0] and the uninitialised aux of
+ * the reference are taken as zero.  *n shrinks when remove_invalid removes
+ * particles whose Kepler solve failed. */
+int orc_whfast_run(int *n, int *ids, double *x, double *v, double *m, double G,
+                   double eps, double dt, double tf, int remove_invalid, int pairwise);
+
 /* src/utils.c:27-59 (kinetic + unsoftened pairwise potential energy). */
 double orc_energy(int n, const double *x, const double *v, const double *m,
                   double G);

@@ -214,6 +214,22 @@ def fixed_step_run(integrator, method, x, v, m, G, eps, dt, tf):
     return x, v
 
 
+def whfast_run(x, v, m, G, eps, dt, tf, remove_invalid=True, pairwise=False, ids=None):
+    """WHFast for one system; returns (ids, x, v, m) of the survivors."""
+    lib = load()
+    lib.orc_whfast_run.argtypes = [ctypes.POINTER(ctypes.c_int), ip, dp, dp, dp, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_int, ctypes.c_int]
+    x, v, m = _c(x).copy(), _c(v).copy(), _c(m).copy()
+    ids = np.arange(m.size, dtype=np.int32) if ids is None else _c(ids, np.int32).copy()
+    n = ctypes.c_int(m.size)
+    rc = lib.orc_whfast_run(ctypes.byref(n), ids.ctypes.data_as(ip), _d(x), _d(v), _d(m), G, eps,
+                            dt, tf, int(remove_invalid), int(pairwise))
+    assert rc == 0, rc
+    k = n.value
+    return ids[:k], x.reshape(-1, 3)[:k], v.reshape(-1, 3)[:k], m[:k]
+
+
 def energy(x, v, m, G):
     x, v, m = _c(x), _c(v), _c(m)
     return load().orc_energy(m.size, _d(x), _d(v), _d(m), G)

@@ -15,6 +15,8 @@ Outputs (compressed .npz, a few hundred KB in total):
   integrators.npz    euler / euler_cromer / rk4 / leapfrog (src/integrator.c)
   leapfrog_plummer1024.npz  leapfrog + pairwise, N=1024, dt=1e-3, 1000 steps
   energy.npz         compute_energy_python   (src/python_interface.c:195-243)
+  whfast.npz         WHFast, massless / pairwise / softened / removal
+                     (src/integrator_whfast.c:200-407)
 """
 from __future__ import annotations
 
@@ -54,6 +56,53 @@ def pairwise_cases():
     m = np.linspace(0.5, 2.0, 33)
     cases["collinear"] = (x, m, 0.7, 0.01)
     return cases
+
+
+def whfast_systems():
+    """Planetary systems for WHFast: (name, x, v, m, method, eps, dt, tf)."""
+    G = wl.G_AU_MSUN_DAY
+    (x, v, m), = wl.planetary_ensemble(1, 7, max_test=64)
+    sys_ = [("massless", x, v, m, 2, 0.0, 10.0, 365.0),
+            ("pairwise", x, v, m, 1, 0.0, 10.0, 365.0),
+            ("massless_soft", x, v, m, 2, 1e-3, 5.0, 101.0)]
+    # a test particle on a fast hyperbolic orbit: its Kepler solve overflows
+    # (non-finite Stumpff argument) and WHFast removes it
+    xe = np.concatenate([x, [[1.0, 0.2, 0.0]]])
+    ve = np.concatenate([v, [[100.0, 0.0, 0.0]]])
+    me = np.concatenate([m, [0.0]])
+    sys_.append(("escape", xe, ve, me, 2, 0.0, 10.0, 100.0))
+    return G, sys_
+
+
+def whfast_cases():
+    """WHFast (src/integrator_whfast.c) run by the reference.  The reference
+    kicks the primary's Jacobi velocity with an acceleration it never writes
+    (a[0] of a malloc'd array), so a run is kept only when it reproduces the
+    oracle's a[0] = 0 policy; up to five attempts per case.
+    launch_simulation_python (src/python_interface.c:186-190) does not write
+    the shrunken particle count back after removals, so the survivors are the
+    first k slots of the returned arrays, k from the oracle's count."""
+    from oracle import restatement as orc
+    G, systems = whfast_systems()
+    out = {}
+    for name, x, v, m, method, eps, dt, tf in systems:
+        ids0 = np.arange(m.size, dtype=np.int32)
+        oi, ox, ov, om = orc.whfast_run(x, v, m, G, eps, dt, tf, pairwise=(method == 1), ids=ids0)
+        for attempt in range(5):
+            ri, rx, rv, rm = ref.launch(x, v, m, G, 10, dt, tf, method, eps=eps)
+            k = oi.size
+            ri, rx, rv, rm = ri[:k], rx[:k], rv[:k], rm[:k]
+            if (np.array_equal(ri, oi) and np.array_equal(rx, ox) and np.array_equal(rv, ov)
+                    and np.array_equal(rm, om)):
+                break
+        else:
+            raise AssertionError(f"whfast {name}: reference and oracle differ")
+        out[f"{name}/x0"], out[f"{name}/v0"], out[f"{name}/m0"] = x, v, m
+        out[f"{name}/method"], out[f"{name}/eps"] = np.int64(method), np.float64(eps)
+        out[f"{name}/dt"], out[f"{name}/tf"], out[f"{name}/G"] = (np.float64(dt), np.float64(tf),
+                                                                  np.float64(G))
+        out[f"{name}/ids"], out[f"{name}/x"], out[f"{name}/v"], out[f"{name}/m"] = ri, rx, rv, rm
+    return out
 
 
 def main():
@@ -126,6 +175,8 @@ def main():
     x, v, m = wl.plummer(777, 41)
     np.savez_compressed(OUT / "energy.npz", x=x, v=v, m=m, G=np.float64(1.3),
                         e=ref.energy_python(x, v, m, 1.3))
+
+    np.savez_compressed(OUT / "whfast.npz", **whfast_cases())
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -80,6 +80,19 @@ def test_leapfrog_plummer1024_golden(orc):
     assert abs(e1 - float(d["e1"])) <= 1e-13 * abs(float(d["e1"]))
 
 
+def test_whfast_golden(orc):
+    """WHFast restatement against the reference's runs: massless, pairwise,
+    softened, and a removal (hyperbolic escaper), bit for bit."""
+    for name, c in cases(golden("whfast")).items():
+        ids, x, v, m = orc.whfast_run(c["x0"], c["v0"], c["m0"], float(c["G"]), float(c["eps"]),
+                                      float(c["dt"]), float(c["tf"]),
+                                      pairwise=int(c["method"]) == 1)
+        assert np.array_equal(ids, c["ids"]), name
+        assert np.array_equal(x, c["x"]) and np.array_equal(v, c["v"]), name
+        assert np.array_equal(m, c["m"]), name
+    assert cases(golden("whfast"))["escape"]["ids"].size == cases(golden("whfast"))["escape"]["m0"].size - 1
+
+
 def test_energy_golden(orc):
     d = golden("energy")
     e = orc.energy(d["x"], d["v"], d["m"], float(d["G"]))
