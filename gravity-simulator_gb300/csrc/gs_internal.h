@@ -176,18 +176,23 @@ void launch_rk4_stage(double *x, double *v, const double *x0, const double *v0,
 void launch_rk4_final(double *x, double *v, const double *x0, const double *v0,
                       double *xe, double *ve, const double *const *xk,
                       const double *const *vk, double dt, int len, cudaStream_t s);
-void launch_rk_embedded_stage(double *out, const double *y0, const double *const *k,
-                              const double *coef, int nstage, double dt, int len,
-                              cudaStream_t s);
-void launch_rk_embedded_combine(double *y, double *err_comp, double *y1_tmp,
-                                double *err_est, const double *y0,
-                                const double *const *k, const double *w,
-                                const double *wd, int nstage, double dt, int len,
-                                cudaStream_t s);
-void launch_err_norm(const double *x0, const double *v0, const double *x1,
-                     const double *v1, const double *xerr, const double *verr,
-                     double abs_tol, double rel_tol, int len, double *d_sum,
-                     cudaStream_t s);
+void launch_rk_emb_stage(const double *x, const double *v, const double *xe, const double *ve,
+                         const double *vk, double *xk, double *xs, const double *a_row,
+                         int stage, double dt, int len, cudaStream_t s);
+void launch_rk_emb_combine(const double *x, const double *v, const double *xe, const double *ve,
+                           const double *vk, const double *xk, double *x1, double *v1,
+                           double *txe, double *tve, double *terms, const double *w,
+                           const double *dtdw, int stages, double dt, double abs_tol,
+                           double rel_tol, int len, cudaStream_t s);
+
+// ---- embedded Runge-Kutta tableaus (host_rk.cpp) -------------------------
+struct RkTableau {
+    int stages, power, power_test;
+    double a[13][12];   // a[s][i], i < s
+    double b[13], b_hat[13];
+};
+// Integrator codes 5-8; nullptr for any other code.
+const RkTableau *rk_tableau(int integrator);
 
 // ---- diagnostics (k_diag.cu) -------------------------------------------
 ErrorStatus gpu_energy(const double *h_state7, int num_snapshots, int n, double G,

@@ -152,11 +152,152 @@ struct gsgpu_sim {
     bool graph_failed = false;
     ForceTimer timer;
     int kernels_last = 0;
+    // embedded Runge-Kutta (integrators 5-8)
+    double tolerance = -1.0, initial_dt = -1.0;
+    DBuf e_vk, e_xk, e_x1, e_v1, e_txe, e_tve, e_xs, e_terms;
+    double *h_terms = nullptr;   // pinned host copy of the 6N error terms
 
     ~gsgpu_sim()
     {
         if (graph) cudaGraphExecDestroy(graph);
+        if (h_terms) cudaFreeHost(h_terms);
         if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+
+    // src/integrator_rk_embedded.c:346-520 on host copies of x, v and the
+    // GPU accelerations, with the reference's long double intermediates.
+    ErrorStatus rk_emb_initial_dt(int power, double *out)
+    {
+        const size_t L = (size_t)3 * n;
+        std::vector<double> hx(L), hv(L), ha(L), ha1(L), sx(L), sv(L), hx1(L), hv1(L);
+        GS_TRY(force(a.as<double>()));
+        GS_CUDA(cudaMemcpyAsync(hx.data(), x.p, bytes3(), cudaMemcpyDeviceToHost, stream));
+        GS_CUDA(cudaMemcpyAsync(hv.data(), v.p, bytes3(), cudaMemcpyDeviceToHost, stream));
+        GS_CUDA(cudaMemcpyAsync(ha.data(), a.p, bytes3(), cudaMemcpyDeviceToHost, stream));
+        GS_CUDA(cudaStreamSynchronize(stream));
+        GS_TRY(engine->check_status(stream));
+        const double tol = tolerance;
+        for (size_t k = 0; k < L; ++k) {
+            sx[k] = tol + tol * std::fabs(hx[k]);
+            sv[k] = tol + tol * std::fabs(hv[k]);
+        }
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+        for (size_t k = 0; k < L; ++k) {
+            s0 += (hx[k] / sx[k]) * (hx[k] / sx[k]);
+            s0 += (hv[k] / sv[k]) * (hv[k] / sv[k]);
+            s1 += (hv[k] / sx[k]) * (hv[k] / sx[k]);
+            s1 += (ha[k] / sv[k]) * (ha[k] / sv[k]);
+        }
+        const double d0 = std::sqrt(s0 / (n * 6));
+        const double d1 = std::sqrt(s1 / (n * 6));
+        const double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-4 : d0 / d1;
+        for (size_t k = 0; k < L; ++k) {
+            hx1[k] = hx[k] + (dt0 / 100.0) * hv[k];
+            hv1[k] = hv[k] + (dt0 / 100.0) * ha[k];
+        }
+        GS_CUDA(cudaMemcpyAsync(e_xs.p, hx1.data(), bytes3(), cudaMemcpyHostToDevice, stream));
+        GS_TRY(engine->compute(e_xs.as<double>(), m.as<double>(), tmp.as<double>(), stream,
+                               nullptr));
+        GS_CUDA(cudaMemcpyAsync(ha1.data(), tmp.p, bytes3(), cudaMemcpyDeviceToHost, stream));
+        GS_CUDA(cudaStreamSynchronize(stream));
+        GS_TRY(engine->check_status(stream));
+        for (size_t k = 0; k < L; ++k) {
+            s2 += ((hv1[k] - hv[k]) / sx[k]) * ((hv1[k] - hv[k]) / sx[k]);
+            s2 += ((ha1[k] - ha[k]) / sv[k]) * ((ha1[k] - ha[k]) / sv[k]);
+        }
+        const double d2 = std::sqrt(s2 / (n * 6)) / dt0;
+        const double dt1 = std::pow((double)(0.01L / (long double)std::fmax(d1, d2)),
+                                    (double)(1.0L / (long double)(1 + power)));
+        const double dtv = std::fmin((double)(100.0L * (long double)dt0), dt1);
+        *out = dtv * 1e-2;
+        if (*out <= 0.0) return GS_RAISE(GRAV_VALUE_ERROR, "Initial dt is negative");
+        return ok();
+    }
+
+    // src/integrator_rk_embedded.c:522-987: stages and the weighted combine
+    // on the GPU; the RMS error is summed on the host in the reference's
+    // element order from the per-element terms, and the step-size control
+    // (glibc pow) runs on the host, so accept / reject decisions and dt
+    // follow the reference's exactly.
+    ErrorStatus rk_emb_run(double tf, SimulationStatus *status, const bool *is_exit)
+    {
+        const RkTableau *T = rk_tableau(integrator);
+        if (!T) return GS_RAISE(GRAV_VALUE_ERROR, "Invalid integrator method");
+        if (!(tolerance > 0.0))
+            return GS_RAISE(GRAV_VALUE_ERROR, "tolerance must be positive. Got: %g", tolerance);
+        const int S = T->stages, L = len();
+        const int min_power = T->power < T->power_test ? T->power : T->power_test;
+        double dw[13];
+        for (int s = 0; s < S; ++s) dw[s] = T->b[s] - T->b_hat[s];
+        const double fac = std::pow(0.38, 1.0 / (1.0 + (double)min_power));
+        const double fac_max = 6.0, fac_min = 0.33;
+        double h;
+        if (initial_dt > 0.0) {
+            h = initial_dt;
+        } else {
+            GS_TRY(rk_emb_initial_dt(T->power, &h));
+            if (h > tf) h = tf;
+        }
+        double t = 0.0;
+        int64_t steps = 0;
+        if (status) {
+            status->t = 0.0;
+            status->dt = h;
+            status->num_steps = 0;
+        }
+        double *vk = e_vk.as<double>(), *xk = e_xk.as<double>();
+        while (t < tf) {
+            GS_TRY(force(vk));
+            GS_CUDA(cudaMemcpyAsync(xk, v.p, bytes3(), cudaMemcpyDeviceToDevice, stream));
+            for (int s = 1; s < S; ++s) {
+                launch_rk_emb_stage(x.as<double>(), v.as<double>(), xe.as<double>(),
+                                    ve.as<double>(), vk, xk, e_xs.as<double>(), T->a[s], s, h, L,
+                                    stream);
+                GS_CUDA(cudaGetLastError());
+                GS_TRY(engine->compute(e_xs.as<double>(), m.as<double>(), vk + (size_t)s * L,
+                                       stream, timer.enabled ? &timer : nullptr));
+            }
+            double dtdw[13];
+            for (int s = 0; s < S; ++s) dtdw[s] = h * dw[s];
+            launch_rk_emb_combine(x.as<double>(), v.as<double>(), xe.as<double>(),
+                                  ve.as<double>(), vk, xk, e_x1.as<double>(), e_v1.as<double>(),
+                                  e_txe.as<double>(), e_tve.as<double>(), e_terms.as<double>(),
+                                  T->b, dtdw, S, h, tolerance, tolerance, L, stream);
+            GS_CUDA(cudaGetLastError());
+            GS_CUDA(cudaMemcpyAsync(h_terms, e_terms.p, (size_t)2 * L * sizeof(double),
+                                    cudaMemcpyDeviceToHost, stream));
+            GS_CUDA(cudaStreamSynchronize(stream));
+            GS_TRY(engine->check_status(stream));
+            double sum = 0.0;
+            for (int k = 0; k < 2 * L; ++k) sum += h_terms[k];
+            double error = std::sqrt(sum / (n * 3 * 2));
+            if (error <= 1 || h <= tf * 1e-12) {
+                ++steps;
+                t += h;
+                GS_CUDA(cudaMemcpyAsync(x.p, e_x1.p, bytes3(), cudaMemcpyDeviceToDevice, stream));
+                GS_CUDA(cudaMemcpyAsync(v.p, e_v1.p, bytes3(), cudaMemcpyDeviceToDevice, stream));
+                GS_CUDA(cudaMemcpyAsync(xe.p, e_txe.p, bytes3(), cudaMemcpyDeviceToDevice, stream));
+                GS_CUDA(cudaMemcpyAsync(ve.p, e_tve.p, bytes3(), cudaMemcpyDeviceToDevice, stream));
+            }
+            if (error < 1e-10) error = 1e-10;
+            const double dt_new = h * fac / std::pow(error, 1.0 / (1.0 + (double)min_power));
+            if (dt_new > fac_max * h)
+                h *= fac_max;
+            else if (dt_new < fac_min * h)
+                h *= fac_min;
+            else
+                h = dt_new;
+            if (dt_new / tf < 1e-12) h = tf * 1e-12;
+            if (t < tf && t + h > tf) h = tf - t;
+            if (status) {
+                status->t = t;
+                status->dt = h;
+                status->num_steps = steps;
+            }
+            if (is_exit && *is_exit) break;
+        }
+        GS_CUDA(cudaStreamSynchronize(stream));
+        return ok();
     }
 
     size_t bytes3() const { return (size_t)n * 3 * sizeof(double); }
@@ -320,6 +461,14 @@ ErrorStatus sim_create(gsgpu_sim **out, int n, double G, const AccelerationParam
         GS_TRY(s->x0.reserve(b3));
         GS_TRY(s->v0.reserve(b3));
         for (int k = 0; k < 8; ++k) GS_TRY(s->rk[k].reserve(b3));
+    } else if (const RkTableau *T = rk_tableau(integrator)) {
+        GS_TRY(s->e_vk.reserve(b3 * T->stages));
+        GS_TRY(s->e_xk.reserve(b3 * T->stages));
+        DBuf *bufs[] = {&s->e_x1, &s->e_v1, &s->e_txe, &s->e_tve, &s->e_xs};
+        for (DBuf *b : bufs) GS_TRY(b->reserve(b3));
+        GS_TRY(s->e_terms.reserve(2 * b3));
+        GS_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&s->h_terms), 2 * b3,
+                              cudaHostAllocDefault));
     } else if (integrator != INTEGRATOR_EULER && integrator != INTEGRATOR_EULER_CROMER &&
                integrator != INTEGRATOR_LEAPFROG) {
         return GS_RAISE(GRAV_NOT_IMPLEMENTED_ERROR,
@@ -378,6 +527,7 @@ ErrorStatus sim_download(gsgpu_sim *s, double *x, double *v)
 // Run the reference's step loop for time tf with an is_exit check per step.
 ErrorStatus sim_run_until(gsgpu_sim *s, double tf, SimulationStatus *status, const bool *is_exit)
 {
+    if (rk_tableau(s->integrator)) return s->rk_emb_run(tf, status, is_exit);
     double dt = s->dt;
     const int64_t total = (int64_t)std::ceil(tf / dt);
     GS_TRY(s->prime());
@@ -449,6 +599,32 @@ int gsgpu_sim_run(gsgpu_sim *sim, int64_t num_steps)
         return st.return_code;
     }
     sim->kernels_last = sim->kernels_per_step();
+    return 0;
+}
+
+int gsgpu_sim_set_tolerance(gsgpu_sim *sim, double tolerance, double initial_dt)
+{
+    if (!sim) return GRAV_POINTER_ERROR;
+    if (!(tolerance > 0.0)) {
+        ErrorStatus st = GS_RAISE(GRAV_VALUE_ERROR, "tolerance must be positive. Got: %g",
+                                  tolerance);
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    sim->tolerance = tolerance;
+    sim->initial_dt = initial_dt;
+    return 0;
+}
+
+int gsgpu_sim_run_until(gsgpu_sim *sim, double tf)
+{
+    if (!sim) return GRAV_POINTER_ERROR;
+    SimulationStatus ss{};
+    ErrorStatus st = gs::sim_run_until(sim, tf, &ss, nullptr);
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
     return 0;
 }
 
@@ -618,8 +794,7 @@ ErrorStatus launch_simulation(System *system, IntegratorParam *integrator_param,
     if (!settings) return GS_RAISE(GRAV_POINTER_ERROR, "settings is NULL");
     if (!simulation_status) return GS_RAISE(GRAV_POINTER_ERROR, "simulation_status is NULL");
 
-    if (integ != INTEGRATOR_EULER && integ != INTEGRATOR_EULER_CROMER && integ != INTEGRATOR_RK4 &&
-        integ != INTEGRATOR_LEAPFROG && integ != INTEGRATOR_WHFAST)
+    if (integ == INTEGRATOR_IAS15)
         return GS_RAISE(GRAV_NOT_IMPLEMENTED_ERROR,
                         "integrator %d has no GPU implementation in this library", integ);
 
@@ -658,9 +833,12 @@ ErrorStatus launch_simulation(System *system, IntegratorParam *integrator_param,
     if (settings->verbose >= 1) std::fputs("Launching simulation...\n", stdout);
 
     gsgpu_sim *raw = nullptr;
+    // adaptive integrators carry no fixed dt: the creation dt is a placeholder
     GS_TRY(gs::sim_create(&raw, system->num_particles, system->G, acceleration_param, integ,
-                          integrator_param->dt, nullptr));
+                          fixed ? integrator_param->dt : 1.0, nullptr));
     std::unique_ptr<gsgpu_sim> sim(raw);
+    sim->tolerance = integrator_param->tolerance;
+    sim->initial_dt = integrator_param->initial_dt;
     GS_TRY(gs::sim_upload(sim.get(), system->x, system->v, system->m));
     simulation_status->t = 0.0;
     simulation_status->dt = integrator_param->dt;

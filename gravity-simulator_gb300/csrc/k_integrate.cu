@@ -160,4 +160,98 @@ void launch_rk4_final(double *x, double *v, const double *x0, const double *v0, 
     k_rk4_final<<<blocks(len), TPB, 0, s>>>(x, v, x0, v0, xe, ve, p, dt, len);
 }
 
+// ---- embedded Runge-Kutta (src/integrator_rk_embedded.c:721-856) ----------
+// Stage and weight coefficients travel as kernel parameters (at most 13
+// stages); vk / xk are S arrays of len doubles, stage i at offset i * len.
+struct RkEmbCoef {
+    double c[13];    // a[s][0..s-1] for the stage kernel; b for the combine
+    double dc[13];   // dt * (b - b_hat) for the combine
+};
+
+// Stage s: position / velocity at which the next acceleration is taken,
+//   tv = sum_{i<s} a[s][i] vk[i],  tx = sum_{i<s} a[s][i] xk[i]  (from +0.0)
+//   tv = (v + dt tv) + ve,  tx = (x + dt tx) + xe,  xk[s] = tv.
+__global__ void k_rk_emb_stage(const double *__restrict__ x, const double *__restrict__ v,
+                               const double *__restrict__ xe, const double *__restrict__ ve,
+                               const double *__restrict__ vk, double *__restrict__ xk,
+                               double *__restrict__ xs, RkEmbCoef cf, int stage, double dt,
+                               int len)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= len) return;
+    double tv = 0.0, tx = 0.0;
+    for (int i = 0; i < stage; ++i) {
+        tv = __dadd_rn(tv, __dmul_rn(cf.c[i], vk[(size_t)i * len + k]));
+        tx = __dadd_rn(tx, __dmul_rn(cf.c[i], xk[(size_t)i * len + k]));
+    }
+    tv = __dadd_rn(__dadd_rn(v[k], __dmul_rn(dt, tv)), ve[k]);
+    tx = __dadd_rn(__dadd_rn(x[k], __dmul_rn(dt, tx)), xe[k]);
+    xs[k] = tx;
+    xk[(size_t)stage * len + k] = tv;
+}
+
+// Weights, error deltas, compensated x1 / v1 and the two squared scaled
+// error terms of element k, written at terms[2k] (velocity) and
+// terms[2k + 1] (position): the order in which the reference sums them.
+__global__ void k_rk_emb_combine(const double *__restrict__ x, const double *__restrict__ v,
+                                 const double *__restrict__ xe, const double *__restrict__ ve,
+                                 const double *__restrict__ vk, const double *__restrict__ xk,
+                                 double *__restrict__ x1, double *__restrict__ v1,
+                                 double *__restrict__ txe, double *__restrict__ tve,
+                                 double *__restrict__ terms, RkEmbCoef cf, int stages, double dt,
+                                 double abs_tol, double rel_tol, int len)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= len) return;
+    double tv = 0.0, tx = 0.0, dv = 0.0, dx = 0.0;
+    for (int s = 0; s < stages; ++s) {
+        const double a = vk[(size_t)s * len + k], b = xk[(size_t)s * len + k];
+        tv = __dadd_rn(tv, __dmul_rn(cf.c[s], a));
+        tx = __dadd_rn(tx, __dmul_rn(cf.c[s], b));
+        dv = __dadd_rn(dv, __dmul_rn(cf.dc[s], a));
+        dx = __dadd_rn(dx, __dmul_rn(cf.dc[s], b));
+    }
+    const double v0 = v[k], x0 = x[k];
+    double ev = __dadd_rn(ve[k], __dmul_rn(dt, tv));
+    double ex = __dadd_rn(xe[k], __dmul_rn(dt, tx));
+    const double vn = __dadd_rn(v0, ev), xn = __dadd_rn(x0, ex);
+    ev = __dadd_rn(ev, __dsub_rn(v0, vn));
+    ex = __dadd_rn(ex, __dsub_rn(x0, xn));
+    v1[k] = vn;
+    x1[k] = xn;
+    tve[k] = ev;
+    txe[k] = ex;
+    const double sv = __dadd_rn(abs_tol, __dmul_rn(fmax(fabs(v0), fabs(vn)), rel_tol));
+    const double sx = __dadd_rn(abs_tol, __dmul_rn(fmax(fabs(x0), fabs(xn)), rel_tol));
+    const double qv = __ddiv_rn(dv, sv), qx = __ddiv_rn(dx, sx);
+    terms[2 * (size_t)k] = __dmul_rn(qv, qv);
+    terms[2 * (size_t)k + 1] = __dmul_rn(qx, qx);
+}
+
+void launch_rk_emb_stage(const double *x, const double *v, const double *xe, const double *ve,
+                         const double *vk, double *xk, double *xs, const double *a_row,
+                         int stage, double dt, int len, cudaStream_t s)
+{
+    if (len <= 0) return;
+    RkEmbCoef cf{};
+    for (int i = 0; i < stage && i < 13; ++i) cf.c[i] = a_row[i];
+    k_rk_emb_stage<<<blocks(len), TPB, 0, s>>>(x, v, xe, ve, vk, xk, xs, cf, stage, dt, len);
+}
+
+void launch_rk_emb_combine(const double *x, const double *v, const double *xe, const double *ve,
+                           const double *vk, const double *xk, double *x1, double *v1,
+                           double *txe, double *tve, double *terms, const double *w,
+                           const double *dtdw, int stages, double dt, double abs_tol,
+                           double rel_tol, int len, cudaStream_t s)
+{
+    if (len <= 0) return;
+    RkEmbCoef cf{};
+    for (int i = 0; i < stages && i < 13; ++i) {
+        cf.c[i] = w[i];
+        cf.dc[i] = dtdw[i];
+    }
+    k_rk_emb_combine<<<blocks(len), TPB, 0, s>>>(x, v, xe, ve, vk, xk, x1, v1, txe, tve, terms,
+                                                 cf, stages, dt, abs_tol, rel_tol, len);
+}
+
 }  // namespace gs

@@ -246,8 +246,16 @@ int gsgpu_sim_create(gsgpu_sim **out, int num_particles, double G,
 /* Host -> device copy of x [3N], v [3N], m [N]; resets compensation terms. */
 int gsgpu_sim_upload(gsgpu_sim *sim, const double *x, const double *v,
                      const double *m);
-/* Enqueue num_steps integrator steps (asynchronous on the stream). */
+/* Enqueue num_steps integrator steps (asynchronous on the stream); fixed-step
+ * integrators (1-4) only. */
 int gsgpu_sim_run(gsgpu_sim *sim, int64_t num_steps);
+/* The reference's loop to time tf (src/integrator.c, fixed-step: ceil(tf/dt)
+ * steps with the last one clamped; src/integrator_rk_embedded.c:680-930,
+ * integrators 5-8: adaptive steps from the initial dt to tf).  Synchronous. */
+int gsgpu_sim_run_until(gsgpu_sim *sim, double tf);
+/* Embedded Runge-Kutta (integrators 5-8): abs = rel tolerance and the initial
+ * dt (<= 0: the reference's estimate, src/integrator_rk_embedded.c:346-520). */
+int gsgpu_sim_set_tolerance(gsgpu_sim *sim, double tolerance, double initial_dt);
 /* Device -> host copy of x, v (v synchronised to integer time for leapfrog). */
 int gsgpu_sim_download(gsgpu_sim *sim, double *x, double *v);
 /* Device pointer of the current acceleration array [3N] (FP64). */

@@ -668,6 +668,243 @@ done:
 }
 
 /* ------------------------------------------------------------------ */
+/* Embedded Runge-Kutta (src/integrator_rk_embedded.c)                  */
+/* ------------------------------------------------------------------ */
+
+/* The published tableaus as exact rationals {p, q}: the stage matrix as its
+ * lower triangle, row s (s = 1..S-1) holding a[s][0..s-1], then the weights
+ * b[0..S-1] and the comparison weights bt[0..S-1].  Every quotient rounds
+ * to the same double whether formed in double or long double. */
+typedef struct { int p, q; } OrcQ;
+typedef struct { int stages, power, power_test; const OrcQ *a, *b, *bt; } OrcTableau;
+
+static const OrcQ rkf45_a[] = {
+    {1, 4},
+    {3, 32}, {9, 32},
+    {1932, 2197}, {-7200, 2197}, {7296, 2197},
+    {439, 216}, {-8, 1}, {3680, 513}, {-845, 4104},
+    {-8, 27}, {2, 1}, {-3544, 2565}, {1859, 4104}, {-11, 40}};
+static const OrcQ rkf45_b[] = {{25, 216}, {0, 1}, {1408, 2565}, {2197, 4104}, {-1, 5}, {0, 1}};
+static const OrcQ rkf45_bt[] = {{16, 135}, {0, 1}, {6656, 12825}, {28561, 56430}, {-9, 50}, {2, 55}};
+
+static const OrcQ dopri_a[] = {
+    {1, 5},
+    {3, 40}, {9, 40},
+    {44, 45}, {-56, 15}, {32, 9},
+    {19372, 6561}, {-25360, 2187}, {64448, 6561}, {-212, 729},
+    {9017, 3168}, {-355, 33}, {46732, 5247}, {49, 176}, {-5103, 18656},
+    {35, 384}, {0, 1}, {500, 1113}, {125, 192}, {-2187, 6784}, {11, 84}};
+static const OrcQ dopri_b[] = {{35, 384}, {0, 1}, {500, 1113}, {125, 192}, {-2187, 6784},
+                               {11, 84}, {0, 1}};
+static const OrcQ dopri_bt[] = {{5179, 57600}, {0, 1}, {7571, 16695}, {393, 640},
+                                {-92097, 339200}, {187, 2100}, {1, 40}};
+
+static const OrcQ dverk_a[] = {
+    {1, 6},
+    {4, 75}, {16, 75},
+    {5, 6}, {-8, 3}, {5, 2},
+    {-165, 64}, {55, 6}, {-425, 64}, {85, 96},
+    {12, 5}, {-8, 1}, {4015, 612}, {-11, 36}, {88, 255},
+    {-8263, 15000}, {124, 75}, {-643, 680}, {-81, 250}, {2484, 10625}, {0, 1},
+    {3501, 1720}, {-300, 43}, {297275, 52632}, {-319, 2322}, {24068, 84065}, {0, 1},
+    {3850, 26703}};
+static const OrcQ dverk_b[] = {{3, 40}, {0, 1}, {875, 2244}, {23, 72}, {264, 1955}, {0, 1},
+                               {125, 11592}, {43, 616}};
+static const OrcQ dverk_bt[] = {{13, 160}, {0, 1}, {2375, 5984}, {5, 16}, {12, 85}, {3, 44},
+                                {0, 1}, {0, 1}};
+
+static const OrcQ rkf78_a[] = {
+    {2, 27},
+    {1, 36}, {1, 12},
+    {1, 24}, {0, 1}, {1, 8},
+    {5, 12}, {0, 1}, {-25, 16}, {25, 16},
+    {1, 20}, {0, 1}, {0, 1}, {1, 4}, {1, 5},
+    {-25, 108}, {0, 1}, {0, 1}, {125, 108}, {-65, 27}, {125, 54},
+    {31, 300}, {0, 1}, {0, 1}, {0, 1}, {61, 225}, {-2, 9}, {13, 900},
+    {2, 1}, {0, 1}, {0, 1}, {-53, 6}, {704, 45}, {-107, 9}, {67, 90}, {3, 1},
+    {-91, 108}, {0, 1}, {0, 1}, {23, 108}, {-976, 135}, {311, 54}, {-19, 60}, {17, 6},
+    {-1, 12},
+    {2383, 4100}, {0, 1}, {0, 1}, {-341, 164}, {4496, 1025}, {-301, 82}, {2133, 4100},
+    {45, 82}, {45, 164}, {18, 41},
+    {3, 205}, {0, 1}, {0, 1}, {0, 1}, {0, 1}, {-6, 41}, {-3, 205}, {-3, 41}, {3, 41},
+    {6, 41}, {0, 1},
+    {-1777, 4100}, {0, 1}, {0, 1}, {-341, 164}, {4496, 1025}, {-289, 82}, {2193, 4100},
+    {51, 82}, {33, 164}, {19, 41}, {0, 1}, {1, 1}};
+static const OrcQ rkf78_b[] = {{41, 840}, {0, 1}, {0, 1}, {0, 1}, {0, 1}, {34, 105}, {9, 35},
+                               {9, 35}, {9, 280}, {9, 280}, {41, 840}, {0, 1}, {0, 1}};
+static const OrcQ rkf78_bt[] = {{0, 1}, {0, 1}, {0, 1}, {0, 1}, {0, 1}, {34, 105}, {9, 35},
+                                {9, 35}, {9, 280}, {9, 280}, {0, 1}, {41, 840}, {41, 840}};
+
+/* integrator codes 5..8 (src/integrator_rk_embedded.c:36-58) */
+static const OrcTableau *orc_tableau(int integrator)
+{
+    static const OrcTableau t[4] = {
+        {6, 4, 5, rkf45_a, rkf45_b, rkf45_bt},
+        {7, 5, 4, dopri_a, dopri_b, dopri_bt},
+        {8, 6, 7, dverk_a, dverk_b, dverk_bt},
+        {13, 7, 8, rkf78_a, rkf78_b, rkf78_bt}};
+    return (integrator >= 5 && integrator <= 8) ? &t[integrator - 5] : NULL;
+}
+
+static double qv(OrcQ r) { return (double)r.p / (double)r.q; }
+
+/* :346-520, including the long double intermediates and the branch whose
+ * result is always overwritten (:496-501). */
+static int rk_initial_dt(int method, int n, const double *x, const double *v, const double *m,
+                         double G, double eps, double rel_tol, double abs_tol, int power,
+                         double *dt_out)
+{
+    const int L = 3 * n;
+    double *buf = (double *)malloc(sizeof(double) * (size_t)L * 6);
+    if (!buf) return 4;
+    double *sx = buf, *sv = buf + L, *x1 = buf + 2 * L, *v1 = buf + 3 * L, *a1 = buf + 4 * L,
+           *a = buf + 5 * L;
+    int rc = accel_of(method, n, x, m, G, eps, a);
+    if (rc) { free(buf); return rc; }
+    for (int k = 0; k < L; ++k) {
+        sx[k] = abs_tol + rel_tol * fabs(x[k]);
+        sv[k] = abs_tol + rel_tol * fabs(v[k]);
+    }
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int k = 0; k < L; ++k) {
+        s0 += (x[k] / sx[k]) * (x[k] / sx[k]);
+        s0 += (v[k] / sv[k]) * (v[k] / sv[k]);
+        s1 += (v[k] / sx[k]) * (v[k] / sx[k]);
+        s1 += (a[k] / sv[k]) * (a[k] / sv[k]);
+    }
+    const double d0 = sqrt(s0 / (n * 6));
+    const double d1 = sqrt(s1 / (n * 6));
+    const double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-4 : d0 / d1;
+    for (int k = 0; k < L; ++k) {
+        x1[k] = x[k] + (dt0 / 100.0) * v[k];
+        v1[k] = v[k] + (dt0 / 100.0) * a[k];
+    }
+    rc = accel_of(method, n, x1, m, G, eps, a1);
+    if (rc) { free(buf); return rc; }
+    for (int k = 0; k < L; ++k) {
+        s2 += ((v1[k] - v[k]) / sx[k]) * ((v1[k] - v[k]) / sx[k]);
+        s2 += ((a1[k] - a[k]) / sv[k]) * ((a1[k] - a[k]) / sv[k]);
+    }
+    const double d2 = sqrt(s2 / (n * 6)) / dt0;
+    const double dt1 = pow((double)(0.01L / (long double)fmax(d1, d2)),
+                           (double)(1.0L / (long double)(1 + power)));
+    const double dt = fmin((double)(100.0L * (long double)dt0), dt1);
+    free(buf);
+    *dt_out = dt * 1e-2;
+    return *dt_out > 0.0 ? 0 : 2;
+}
+
+int orc_rk_embedded_run(int integrator, int method, int n, double *x, double *v,
+                        const double *m, double G, double eps, double tolerance,
+                        double initial_dt, double tf, int64_t *num_steps, double *t_out,
+                        double *dt_out)
+{
+    const OrcTableau *T = orc_tableau(integrator);
+    if (!T) return 2;
+    const int S = T->stages, L = 3 * n;
+    const int min_power = T->power < T->power_test ? T->power : T->power_test;
+    double a[13][12], w[13], dw[13];
+    int off = 0;
+    for (int s = 1; s < S; ++s)
+        for (int i = 0; i < s; ++i) a[s][i] = qv(T->a[off++]);
+    for (int s = 0; s < S; ++s) {
+        w[s] = qv(T->b[s]);
+        dw[s] = w[s] - qv(T->bt[s]);
+    }
+    const double abs_tol = tolerance, rel_tol = tolerance;
+    const double fac_max = 6.0, fac_min = 0.33;
+    const double fac = pow(0.38, 1.0 / (1.0 + (double)min_power));
+    double *buf = (double *)calloc((size_t)L * (2 * (size_t)S + 12), sizeof(double));
+    if (!buf) return 4;
+    double *vk = buf, *xk = buf + (size_t)S * L, *p = buf + 2 * (size_t)S * L;
+    double *x1 = p, *v1 = p + L, *tv = p + 2 * L, *tx = p + 3 * L, *dv = p + 4 * L,
+           *dx = p + 5 * L, *xe = p + 8 * L, *ve = p + 9 * L, *txe = p + 10 * L,
+           *tve = p + 11 * L;
+    int rc = 0;
+    double dt;
+    if (initial_dt > 0.0) {
+        dt = initial_dt;
+    } else {
+        if ((rc = rk_initial_dt(method, n, x, v, m, G, eps, rel_tol, abs_tol, T->power, &dt)))
+            goto done;
+        if (dt > tf) dt = tf;
+    }
+    double t = 0.0;
+    int64_t steps = 0;
+    while (t < tf) {
+        /* stages (:721-777) */
+        if ((rc = accel_of(method, n, x, m, G, eps, vk))) goto done;
+        memcpy(xk, v, sizeof(double) * L);
+        for (int s = 1; s < S; ++s) {
+            for (int k = 0; k < L; ++k) { tv[k] = 0.0; tx[k] = 0.0; }
+            for (int i = 0; i < s; ++i)
+                for (int k = 0; k < L; ++k) {
+                    tv[k] += a[s][i] * vk[(size_t)i * L + k];
+                    tx[k] += a[s][i] * xk[(size_t)i * L + k];
+                }
+            for (int k = 0; k < L; ++k) {
+                tv[k] = v[k] + dt * tv[k] + ve[k];
+                tx[k] = x[k] + dt * tx[k] + xe[k];
+            }
+            if ((rc = accel_of(method, n, tx, m, G, eps, vk + (size_t)s * L))) goto done;
+            memcpy(xk + (size_t)s * L, tv, sizeof(double) * L);
+        }
+        /* weights, error deltas, compensated x1 / v1 (:779-830) */
+        for (int k = 0; k < L; ++k) { tv[k] = tx[k] = dv[k] = dx[k] = 0.0; }
+        for (int s = 0; s < S; ++s)
+            for (int k = 0; k < L; ++k) {
+                tv[k] += w[s] * vk[(size_t)s * L + k];
+                tx[k] += w[s] * xk[(size_t)s * L + k];
+                dv[k] += dt * dw[s] * vk[(size_t)s * L + k];
+                dx[k] += dt * dw[s] * xk[(size_t)s * L + k];
+            }
+        memcpy(txe, xe, sizeof(double) * L);
+        memcpy(tve, ve, sizeof(double) * L);
+        for (int k = 0; k < L; ++k) {
+            tve[k] += dt * tv[k];
+            txe[k] += dt * tx[k];
+            v1[k] = v[k] + tve[k];
+            x1[k] = x[k] + txe[k];
+            tve[k] += v[k] - v1[k];
+            txe[k] += x[k] - x1[k];
+        }
+        /* RMS of the scaled error (:832-856) */
+        double sum = 0.0;
+        for (int k = 0; k < L; ++k) {
+            const double sv = abs_tol + fmax(fabs(v[k]), fabs(v1[k])) * rel_tol;
+            const double sx = abs_tol + fmax(fabs(x[k]), fabs(x1[k])) * rel_tol;
+            double q = dv[k] / sv;
+            sum += q * q;
+            q = dx[k] / sx;
+            sum += q * q;
+        }
+        double error = sqrt(sum / (n * 3 * 2));
+        /* accept (:859-888) and step-size control (:895-923) */
+        if (error <= 1 || dt <= tf * 1e-12) {
+            ++steps;
+            t += dt;
+            memcpy(x, x1, sizeof(double) * L);
+            memcpy(v, v1, sizeof(double) * L);
+            memcpy(xe, txe, sizeof(double) * L);
+            memcpy(ve, tve, sizeof(double) * L);
+        }
+        if (error < 1e-10) error = 1e-10;
+        const double dt_new = dt * fac / pow(error, 1.0 / (1.0 + (double)min_power));
+        if (dt_new > fac_max * dt) dt *= fac_max;
+        else if (dt_new < fac_min * dt) dt *= fac_min;
+        else dt = dt_new;
+        if (dt_new / tf < 1e-12) dt = tf * 1e-12;
+        if (t < tf && t + dt > tf) dt = tf - t;
+    }
+    if (num_steps) *num_steps = steps;
+    if (t_out) *t_out = t;
+    if (dt_out) *dt_out = dt;
+done:
+    free(buf);
+    return rc;
+}
+
+/* ------------------------------------------------------------------ */
 /* WHFast (src/integrator_whfast.c)                                     */
 /* ------------------------------------------------------------------ */
 

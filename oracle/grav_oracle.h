@@ -107,6 +107,15 @@ int orc_fixed_step_run(int integrator, int method, int n, double *x, double *v,
                        const double *m, double G, double eps, double dt,
                        double tf);
 
+/* src/integrator_rk_embedded.c:346-987: RKF45 (5), DOPRI (6), DVERK (7) and
+ * RKF78 (8) with the pairwise (method 1) or massless (method 2) sum;
+ * abs = rel = tolerance; initial_dt <= 0 selects the reference's initial
+ * step estimate.  Reports the accepted steps, final t and the next dt. */
+int orc_rk_embedded_run(int integrator, int method, int n, double *x, double *v,
+                        const double *m, double G, double eps, double tolerance,
+                        double initial_dt, double tf, int64_t *num_steps, double *t_out,
+                        double *dt_out);
+
 /* src/integrator_whfast.c:200-407 for one system: sort by distance, eta,
  * Jacobi transforms, universal-variable Kepler drift, the interaction
  * accelerations (pairwise=0: the massless variant :959-1264, 1: the

@@ -214,6 +214,24 @@ def fixed_step_run(integrator, method, x, v, m, G, eps, dt, tf):
     return x, v
 
 
+def rk_embedded_run(integrator, method, x, v, m, G, eps, tolerance, tf, initial_dt=-1.0):
+    """Embedded RK (integrators 5-8) for one system; returns (x, v, steps, t, dt)."""
+    lib = load()
+    lib.orc_rk_embedded_run.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double,
+                                        ctypes.POINTER(ctypes.c_int64),
+                                        ctypes.POINTER(ctypes.c_double),
+                                        ctypes.POINTER(ctypes.c_double)]
+    x, v, m = _c(x).copy(), _c(v).copy(), _c(m)
+    steps, t, dt = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double()
+    rc = lib.orc_rk_embedded_run(integrator, method, m.size, _d(x), _d(v), _d(m), G, eps,
+                                 tolerance, initial_dt, tf, ctypes.byref(steps), ctypes.byref(t),
+                                 ctypes.byref(dt))
+    assert rc == 0, rc
+    return x.reshape(-1, 3), v.reshape(-1, 3), steps.value, t.value, dt.value
+
+
 def whfast_run(x, v, m, G, eps, dt, tf, remove_invalid=True, pairwise=False, ids=None):
     """WHFast for one system; returns (ids, x, v, m) of the survivors."""
     lib = load()

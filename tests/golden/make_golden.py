@@ -17,6 +17,7 @@ Outputs (compressed .npz, a few hundred KB in total):
   energy.npz         compute_energy_python   (src/python_interface.c:195-243)
   whfast.npz         WHFast, massless / pairwise / softened / removal
                      (src/integrator_whfast.c:200-407)
+  rk_embedded.npz    RKF45 / DOPRI / DVERK / RKF78 (src/integrator_rk_embedded.c)
 """
 from __future__ import annotations
 
@@ -105,6 +106,28 @@ def whfast_cases():
     return out
 
 
+def rk_embedded_cases():
+    """RKF45 / DOPRI / DVERK / RKF78 (src/integrator_rk_embedded.c) run by the
+    reference: the initial-step estimate (tolerance 1e-8) and a given
+    initial dt (tolerance 1e-6), pairwise sum; one massless run."""
+    out = {}
+    x, v, m = wl.plummer(64, 31)
+    out["x"], out["v"], out["m"] = x, v, m
+    for integ in (5, 6, 7, 8):
+        for tag, tol, idt in (("auto", 1e-8, -1.0), ("given", 1e-6, 1e-3)):
+            _, xr, vr, _ = ref.launch(x, v, m, 1.0, integ, 1e-3, 0.5, 1, eps=0.01, tolerance=tol,
+                                      initial_dt=idt)
+            out[f"int{integ}_{tag}/x"], out[f"int{integ}_{tag}/v"] = xr, vr
+            out[f"int{integ}_{tag}/tol"], out[f"int{integ}_{tag}/initial_dt"] = (np.float64(tol),
+                                                                                 np.float64(idt))
+    (xs, vs, ms), = wl.planetary_ensemble(1, 11, max_test=30)
+    _, xr, vr, _ = ref.launch(xs, vs, ms, wl.G_AU_MSUN_DAY, 6, 1.0, 200.0, 2, tolerance=1e-9)
+    out["massless_x0"], out["massless_v0"], out["massless_m"] = xs, vs, ms
+    out["massless_G"] = np.float64(wl.G_AU_MSUN_DAY)
+    out["massless_x"], out["massless_v"] = xr, vr
+    return out
+
+
 def main():
     assert ref.build() or ref.available(), "reference sources not found"
     out = {}
@@ -177,6 +200,7 @@ def main():
                         e=ref.energy_python(x, v, m, 1.3))
 
     np.savez_compressed(OUT / "whfast.npz", **whfast_cases())
+    np.savez_compressed(OUT / "rk_embedded.npz", **rk_embedded_cases())
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -91,3 +91,49 @@ def test_energy_diagnostics(lib, g, orc):
                                         ctypes.c_int32(1), ctypes.c_int32(n))
     Lr = orc.angular_momentum(d["x"], d["v"], d["m"])
     assert abs(L[0] - Lr) <= 1e-12 * max(1.0, abs(Lr))
+
+
+@pytest.mark.parametrize("integ", [5, 6, 7, 8])
+def test_rk_embedded_bitexact_golden(lib, g, integ):
+    """RKF45 / DOPRI / DVERK / RKF78: the GPU stages and combine with the
+    host-side error sum and step control reproduce the reference's adaptive
+    run bit for bit, with the reference's initial-step estimate and with a
+    given initial dt."""
+    d = golden("rk_embedded")
+    for tag in ("auto", "given"):
+        c = f"int{integ}_{tag}"
+        x, v = d["x"].copy(), d["v"].copy()
+        _, xo, vo, _ = g.launch_simulation(lib, x, v, d["m"].copy(), 1.0, integrator=integ,
+                                           dt=1e-3, tf=0.5, method=g.METHOD_GPU_PAIRWISE_FP64,
+                                           softening_length=0.01, tolerance=float(d[f"{c}/tol"]),
+                                           initial_dt=float(d[f"{c}/initial_dt"]))
+        assert np.array_equal(xo, d[f"{c}/x"]), c
+        assert np.array_equal(vo, d[f"{c}/v"]), c
+
+
+def test_rk_embedded_massless_golden(lib, g):
+    d = golden("rk_embedded")
+    x, v = d["massless_x0"].copy(), d["massless_v0"].copy()
+    _, xo, vo, _ = g.launch_simulation(lib, x, v, d["massless_m"].copy(), float(d["massless_G"]),
+                                       integrator=6, dt=1.0, tf=200.0,
+                                       method=g.METHOD_GPU_MASSLESS, tolerance=1e-9)
+    assert np.array_equal(xo, d["massless_x"]) and np.array_equal(vo, d["massless_v"])
+
+
+def test_rk_embedded_oracle_random(lib, g, orc, wl):
+    """A fresh system against the oracle's restatement (DOPRI, tf not reached
+    by whole steps)."""
+    x, v, m = wl.plummer(200, 777)
+    xo_ref, vo_ref, *_ = orc.rk_embedded_run(6, 1, x, v, m, 1.0, 0.02, 1e-7, 0.3)
+    _, xo, vo, _ = g.launch_simulation(lib, x.copy(), v.copy(), m, 1.0, integrator=6, dt=1e-3,
+                                       tf=0.3, method=g.METHOD_GPU_PAIRWISE_FP64,
+                                       softening_length=0.02, tolerance=1e-7)
+    assert np.array_equal(xo, xo_ref) and np.array_equal(vo, vo_ref)
+
+
+def test_ias15_reports_not_implemented(lib, g):
+    x, v, m = np.zeros((2, 3)), np.zeros((2, 3)), np.ones(2)
+    x[1, 0] = 1.0
+    with pytest.raises(RuntimeError):
+        g.launch_simulation(lib, x, v, m, 1.0, integrator=9, dt=1e-3, tf=0.01,
+                            method=g.METHOD_GPU_PAIRWISE_FP64, tolerance=1e-6)

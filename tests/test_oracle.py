@@ -93,6 +93,22 @@ def test_whfast_golden(orc):
     assert cases(golden("whfast"))["escape"]["ids"].size == cases(golden("whfast"))["escape"]["m0"].size - 1
 
 
+def test_rk_embedded_golden(orc):
+    """Embedded RK restatement against the reference's runs, bit for bit."""
+    d = golden("rk_embedded")
+    for integ in (5, 6, 7, 8):
+        for tag in ("auto", "given"):
+            c = f"int{integ}_{tag}"
+            xo, vo, steps, t, dt = orc.rk_embedded_run(integ, 1, d["x"], d["v"], d["m"], 1.0, 0.01,
+                                                       float(d[f"{c}/tol"]), 0.5,
+                                                       float(d[f"{c}/initial_dt"]))
+            assert t >= 0.5 and steps > 0, c
+            assert np.array_equal(xo, d[f"{c}/x"]) and np.array_equal(vo, d[f"{c}/v"]), c
+    xo, vo, *_ = orc.rk_embedded_run(6, 2, d["massless_x0"], d["massless_v0"], d["massless_m"],
+                                     float(d["massless_G"]), 0.0, 1e-9, 200.0)
+    assert np.array_equal(xo, d["massless_x"]) and np.array_equal(vo, d["massless_v"])
+
+
 def test_energy_golden(orc):
     d = golden("energy")
     e = orc.energy(d["x"], d["v"], d["m"], float(d["G"]))
