@@ -9,7 +9,18 @@ workload (drift + force evaluation + kick) over the whole particle set.
 Workloads (seeded synthetic inputs -- grav_sim publishes no dataset):
   plummer262144  -- equal-mass Plummer sphere, N = 262,144, G = M = a = 1,
                     compensated-FP32 direct sum, eps = 0.01, leapfrog,
-                    dt = 1e-3 (the mixed-precision direct-sum workload).
+                    dt = 1e-3 (the mixed-precision direct-sum workload; the
+                    default and the headline line).
+  galaxy2097152 / galaxy1048576 -- two-galaxy collision (disk, bulge, halo;
+                    equal masses), Barnes-Hut with monopole + quadrupole
+                    cells, theta = 0.5, eps = 0.01, leapfrog dt = 1e-3.
+  galaxy1048576_plain -- the same at N = 1,048,576 with the monopole walk.
+  galaxy1048576_learned -- theta = 1.0 walk + learned residual, judged by a
+                    4,096-particle direct sum per step (training before the
+                    timed region).
+  ensemble8192 / ensemble8192_leapfrog -- 8,192 planetary systems (Sun, 8
+                    planets, 0-4,096 massless test particles each), WHFast or
+                    leapfrog with the massless accelerations, dt = 1 day.
 
 value      particle-steps/s over all ranks, state resident in HBM, device
            time of K steps from CUDA events on the simulation's stream
@@ -62,11 +73,28 @@ def _module(name):
 
 
 WORKLOADS = {
-    "plummer262144": dict(n=262144, seed=2, G=1.0, eps=0.01, dt=1e-3, integrator=4,
+    "plummer262144": dict(ic="plummer", n=262144, seed=2, G=1.0, eps=0.01, dt=1e-3, integrator=4,
                           method=101, flop_per_interaction=20),
     # small case of the same kernel, for profiler captures
-    "plummer65536": dict(n=65536, seed=2, G=1.0, eps=0.01, dt=1e-3, integrator=4,
+    "plummer65536": dict(ic="plummer", n=65536, seed=2, G=1.0, eps=0.01, dt=1e-3, integrator=4,
                          method=101, flop_per_interaction=20),
+    "galaxy2097152": dict(ic="galaxy", n=2097152, seed=4, G=1.0, eps=0.01, dt=1e-3, integrator=4,
+                          method=105, theta=0.5, leaf=1, flop_per_interaction=20),
+    "galaxy1048576": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01, dt=1e-3, integrator=4,
+                          method=105, theta=0.5, leaf=1, flop_per_interaction=20),
+    "galaxy1048576_plain": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01, dt=1e-3,
+                                integrator=4, method=103, theta=0.5, leaf=1,
+                                flop_per_interaction=20),
+    "galaxy1048576_learned": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01, dt=1e-3,
+                                  integrator=4, method=104, theta=1.0, leaf=1,
+                                  flop_per_interaction=20),
+    # small case of the walk, for profiler captures
+    "galaxy262144": dict(ic="galaxy", n=262144, seed=6, G=1.0, eps=0.01, dt=1e-3, integrator=4,
+                         method=105, theta=0.5, leaf=1, flop_per_interaction=20),
+    "ensemble8192": dict(ic="ensemble", systems=8192, seed=3, max_test=4096, dt=1.0,
+                         integrator=10, method=102),
+    "ensemble8192_leapfrog": dict(ic="ensemble", systems=8192, seed=3, max_test=4096, dt=1.0,
+                                  integrator=4, method=102),
 }
 
 
@@ -185,8 +213,11 @@ def run_ours(args, world, rank, local):
     wl = _module("workloads")
     lib = g.load_c_lib()
     wk = WORKLOADS[args.workload]
+    if wk["ic"] == "ensemble":
+        return run_ensemble(args, world, rank, local, wk, g, wl, lib)
     n = wk["n"]
-    x, v, m = wl.plummer(n, wk["seed"])
+    x, v, m = (wl.plummer if wk["ic"] == "plummer" else wl.galaxy_pair)(n, wk["seed"])
+    bh = wk["method"] in (103, 104, 105, 113)
 
     dp = ctypes.POINTER(ctypes.c_double)
     lib.gsgpu_sim_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
@@ -201,15 +232,26 @@ def run_ours(args, world, rank, local):
     lib.gsgpu_sim_destroy.argtypes = [ctypes.c_void_p]
     lib.gsgpu_sim_download_acceleration.argtypes = [ctypes.c_void_p, dp]
     lib.gsgpu_measure_fma_peak.argtypes = [ctypes.c_int, dp, dp]
+    lib.gsgpu_sim_interaction_counts.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]
+    lib.gsgpu_sim_warmup_until_ready.argtypes = [ctypes.c_void_p, ctypes.c_int64,
+                                                 ctypes.POINTER(ctypes.c_int64)]
+    lib.gsgpu_sim_report.argtypes = [ctypes.c_void_p, dp, ctypes.c_int]
 
     stream = torch.cuda.Stream()
     sim = ctypes.c_void_p()
-    p = g.AccelerationParam(wk["method"], 1.0, wk["eps"], -1)
+    p = g.AccelerationParam(wk["method"], wk.get("theta", 1.0), wk["eps"], wk.get("leaf", -1))
     rc = lib.gsgpu_sim_create(ctypes.byref(sim), n, wk["G"], ctypes.byref(p), wk["integrator"],
                               wk["dt"], ctypes.c_void_p(stream.cuda_stream))
     assert rc == 0, rc
     assert lib.gsgpu_sim_upload(sim, x.ctypes.data_as(dp), v.ctypes.data_as(dp),
                                 m.ctypes.data_as(dp)) == 0
+    training_s = None
+    if wk["method"] == 104:
+        # collection snapshots and GPU training happen before the timed region
+        t0 = time.perf_counter()
+        spent = ctypes.c_int64()
+        assert lib.gsgpu_sim_warmup_until_ready(sim, 1000, ctypes.byref(spent)) == 0
+        training_s = time.perf_counter() - t0
     # warm-up (includes the leapfrog half kick and graph capture)
     assert lib.gsgpu_sim_run(sim, args.warmup) == 0
     torch.cuda.synchronize()
@@ -250,6 +292,15 @@ def run_ours(args, world, rank, local):
 
     value = world * n * args.steps / (total_ms / 1e3)
     interactions = float(n) * (n - 1)
+    if bh:
+        cnt = (ctypes.c_longlong * 2)()
+        lib.gsgpu_sim_interaction_counts(sim, cnt)
+        interactions = float(cnt[0] + cnt[1])
+    report = None
+    if wk["method"] == 104:
+        rep = np.zeros(13)
+        k = lib.gsgpu_sim_report(sim, rep.ctypes.data_as(dp), 13)
+        report = rep[:max(k, 0)].tolist()
     mean_force_ms = force_ms.value / max(force_n.value, 1)
     achieved_tflops = wk["flop_per_interaction"] * interactions / (mean_force_ms / 1e3) / 1e12
 
@@ -277,11 +328,22 @@ def run_ours(args, world, rank, local):
     e2e_val = world * n * args.steps / e2e_s
 
     traffic = None
-    prof = ROOT / "profiles" / "k_direct_sum_plummer262144.md"
+    kernel = "k_bh_walk" if bh else "k_direct_sum"
+    prof = ROOT / "profiles" / f"{kernel}_{args.workload}.md"
     if prof.exists():
         for ln in prof.read_text().splitlines():
             if ln.startswith("traffic_bytes_per_launch:"):
                 traffic = float(ln.split(":", 1)[1])
+    if bh:
+        desc = (f"{args.workload}: galaxy pair N={n}, Barnes-Hut method {wk['method']} "
+                f"theta={wk['theta']} leaf={wk['leaf']}, eps={wk['eps']}, leapfrog dt={wk['dt']}")
+        data = "synthetic (seeded two-galaxy model: exponential disk, Hernquist bulge and halo)"
+        dtype = "f32 walk terms (Kahan), f64 tree multipoles and state"
+    else:
+        desc = (f"{args.workload}: Plummer N={n}, compensated-FP32 direct sum, "
+                f"eps={wk['eps']}, leapfrog dt={wk['dt']}")
+        data = "synthetic (seeded Plummer sphere)"
+        dtype = "f32 pair terms (Kahan), f64 state"
 
     out = {
         "metric": METRIC,
@@ -294,10 +356,9 @@ def run_ours(args, world, rank, local):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32 pair terms (Kahan), f64 state",
-        "data": "synthetic (seeded Plummer sphere)",
-        "config": {"workload": f"{args.workload}: Plummer N={n}, compensated-FP32 direct sum, "
-                               f"eps={wk['eps']}, leapfrog dt={wk['dt']}",
+        "dtype": dtype,
+        "data": data,
+        "config": {"workload": desc,
                    "parallelism": f"replicas x{world}", "l2": "flushed between steps (256 MiB write)",
                    "interactions_per_s": value / n * interactions,
                    "accuracy": {"median_rel_err": med, "p99_rel_err": p99,
@@ -305,7 +366,7 @@ def run_ours(args, world, rank, local):
         "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak.value,
                      "unit": "TFLOP/s", "frac": achieved_tflops / peak.value if peak.value else None,
                      "traffic": traffic,
-                     "kernel": "k_direct_sum", "mean_launch_ms": mean_force_ms,
+                     "kernel": kernel, "mean_launch_ms": mean_force_ms,
                      "peak_source": "FP32 FMA probe on this GPU (gsgpu_measure_fma_peak), "
                                     "not in MEASURED_PEAKS.json",
                      "flop_per_interaction": wk["flop_per_interaction"]},
@@ -318,8 +379,80 @@ def run_ours(args, world, rank, local):
         "clocks": clk,
         "wall_s": wall,
     }
+    if bh:
+        out["config"]["interactions"] = "accepted cells + leaf pair terms of the last step "\
+                                        "(device counters), 20 FLOP each"
+    if training_s is not None:
+        out["config"]["training_s"] = training_s
+        out["config"]["learned_report"] = report
     if rank == 0:
-        out["cpu_baseline"] = cpu_baseline_pairwise(wk, x, m)
+        if wk["ic"] == "plummer":
+            out["cpu_baseline"] = cpu_baseline_pairwise(wk, x, m)
+        print(json.dumps(out), flush=True)
+
+
+def run_ensemble(args, world, rank, local, wk, g, wl, lib):
+    """Batched planetary ensembles: every phase of a step is one launch over
+    all systems; a step is captured in a CUDA graph and replayed."""
+    import torch
+    systems = wl.planetary_ensemble(wk["systems"], wk["seed"], max_test=wk["max_test"])
+    counts = np.array([s_[2].size for s_ in systems], dtype=np.int32)
+    ids = np.concatenate([np.arange(c, dtype=np.int32) for c in counts])
+    x = np.concatenate([s_[0] for s_ in systems])
+    v = np.concatenate([s_[1] for s_ in systems])
+    m = np.concatenate([s_[2] for s_ in systems])
+    P = int(counts.sum())
+    G = wl.G_AU_MSUN_DAY
+    ens = g.Ensemble(lib, counts, G, integrator=wk["integrator"], method=wk["method"], dt=wk["dt"])
+    ens.upload(ids, x, v, m)
+    ens.run(args.warmup)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    t0 = time.perf_counter()
+    ens.run(args.steps)
+    torch.cuda.synchronize()
+    total_s = time.perf_counter() - t0
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([total_s], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t.item())
+    kps = ens.kernels_per_step()
+    ens.close()
+    value = world * P * args.steps / total_s
+    # end to end: launch, upload, K steps, download through the ensemble API
+    t0 = time.perf_counter()
+    e2 = g.Ensemble(lib, counts, G, integrator=wk["integrator"], method=wk["method"], dt=wk["dt"])
+    e2.upload(ids, x, v, m)
+    e2.run(args.steps)
+    e2.download()
+    e2e_s = time.perf_counter() - t0
+    e2.close()
+    name = "WHFast" if wk["integrator"] == 10 else "leapfrog"
+    out = {
+        "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded planetary systems)",
+        "config": {"workload": f"{args.workload}: {wk['systems']} systems, {P} particles, "
+                               f"{name} + massless accelerations, dt={wk['dt']} day",
+                   "parallelism": f"replicas x{world}",
+                   "l2": f"working set {P * 250 / 2**20:.0f} MiB > L2",
+                   "accuracy": "bit-exact to the reference per system (tests/test_gpu_ensemble.py)",
+                   "timing": "host clock around K graph replays with device synchronisation"},
+        "e2e": {"value": world * P * args.steps / e2e_s, "unit": "particle-steps/s",
+                "h2d_bytes_per_step": (P * 60) / args.steps,
+                "d2h_bytes_per_step": (P * 60) / args.steps,
+                "note": "create + upload + K steps + download through gsgpu_ensemble_*"},
+        "gpu_launches": args.steps * kps,
+        "clocks": clk,
+    }
+    if rank == 0:
         print(json.dumps(out), flush=True)
 
 

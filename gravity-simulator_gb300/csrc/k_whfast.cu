@@ -38,6 +38,11 @@ enum { WH_MASSLESS = 0, WH_PAIRWISE = 1 };
 // slot of the next power of two in shared memory (192 KiB at 16384).
 constexpr int kEnsembleMaxSystem = 16384;
 
+// Shared pair sums of the interaction acceleration (k_wh_pairs): used when a
+// system has at most kPairMax massive bodies.
+constexpr int kPairMax = 32;
+constexpr int kPairSlots = kPairMax + 1;
+
 struct EnsDev {
     int S;
     const int *off;      // [S+1]
@@ -49,6 +54,7 @@ struct EnsDev {
     int *nh;             // [S]
     int *rm;             // [P] removal marks
     int *nrm;            // [S]
+    double *pairs;       // [S][2 * kPairSlots][3] shared pair sums
     // scratch for the permutation
     int *t_ids;
     double *t_x, *t_v, *t_m;
@@ -66,6 +72,15 @@ __device__ __forceinline__ double dot3(const double *a, const double *b)
 __device__ __forceinline__ double norm3d(const double *a) { return __dsqrt_rn(dot3(a, a)); }
 
 // ---- sort by distance ----------------------------------------------------
+// Sort key of a distance: its bit pattern (distances are >= 0, so the
+// patterns order like the values), NaN after +inf, padding after all.
+// This keeps the comparison a total order whatever the input, so every
+// live slot receives a live index.
+__device__ __forceinline__ unsigned long long dist_key(double d)
+{
+    return isnan(d) ? 0x7ff8000000000000ull : (unsigned long long)__double_as_longlong(fabs(d));
+}
+
 // Sorts slots of one system by |vec_i - vec_prim| and permutes vec, vel, m,
 // ids; then eta.  Dynamic shared memory: pow2 * (8 + 4) bytes.
 __global__ void k_wh_sort(EnsDev E, double *vec, double *vel, int pow2_max)
@@ -81,7 +96,7 @@ __global__ void k_wh_sort(EnsDev E, double *vec, double *vel, int pow2_max)
         if (threadIdx.x == 0) atomicOr(E.status, ST_CAPACITY);
         return;
     }
-    double *key = reinterpret_cast<double *>(wh_smem);
+    unsigned long long *key = reinterpret_cast<unsigned long long *>(wh_smem);
     int *idx = reinterpret_cast<int *>(wh_smem + (size_t)pow2_max * 8);
     __shared__ int prim_s;
     if (threadIdx.x == 0) {
@@ -110,10 +125,10 @@ __global__ void k_wh_sort(EnsDev E, double *vec, double *vel, int pow2_max)
             const double d[3] = {__dsub_rn(vec[3 * (base + i)], p0),
                                  __dsub_rn(vec[3 * (base + i) + 1], p1),
                                  __dsub_rn(vec[3 * (base + i) + 2], p2)};
-            key[i] = (i == prim) ? 0.0 : norm3d(d);
+            key[i] = (i == prim) ? 0ull : dist_key(norm3d(d));
             idx[i] = i;
         } else {
-            key[i] = __longlong_as_double(0x7ff0000000000000ll);   // +inf pads last
+            key[i] = ~0ull;   // padding sorts last
             idx[i] = 0x7fffffff;
         }
     }
@@ -125,7 +140,7 @@ __global__ void k_wh_sort(EnsDev E, double *vec, double *vel, int pow2_max)
                 const int l = i ^ j;
                 if (l > i) {
                     const bool up = (i & k) == 0;
-                    const double ki = key[i], kl = key[l];
+                    const unsigned long long ki = key[i], kl = key[l];
                     const int ii = idx[i], il = idx[l];
                     const bool gt = (ki > kl) || (ki == kl && ii > il);
                     if (gt == up) {
@@ -141,7 +156,12 @@ __global__ void k_wh_sort(EnsDev E, double *vec, double *vel, int pow2_max)
     }
     // permute through the scratch arrays
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int src = base + idx[i], dst = base + i;
+        const int j = idx[i];
+        if (j < 0 || j >= n) {   // unreachable with a total order; never read outside
+            atomicOr(E.status, ST_NONFINITE);
+            continue;
+        }
+        const int src = base + j, dst = base + i;
         E.t_ids[dst] = E.ids[src];
         E.t_m[dst] = E.m[src];
         for (int c = 0; c < 3; ++c) {
@@ -171,50 +191,116 @@ __global__ void k_wh_sort(EnsDev E, double *vec, double *vel, int pow2_max)
 }
 
 // ---- per-system sequential work ---------------------------------------------
-__device__ void wh_massive_list(const EnsDev &E, int base, int n, int s)
+// One warp per system.  The Jacobi recurrences are a chain through the
+// interior centre of mass, so lane 0 runs the chain while the warp stages
+// chunks of the system through shared memory with coalesced loads and
+// stores; the massive-body list is built by ballots.
+constexpr int SEQ_WARPS = 4;     // systems per CTA
+constexpr int SEQ_CHUNK = 96;    // particles staged per chunk (42 KiB per CTA)
+
+struct SeqStage {
+    double jx[3 * SEQ_CHUNK], jv[3 * SEQ_CHUNK], x[3 * SEQ_CHUNK], v[3 * SEQ_CHUNK];
+    double m[SEQ_CHUNK], eta[SEQ_CHUNK + 1];
+};
+
+// Massless runs of the Jacobi -> Cartesian chain.  For a particle with
+// m_i = 0 (finite Jacobi coordinates, eta_i = eta_{i-1} = e) a chain step is
+//     y = RN(xc / e),  x_i = jx_i + y,  xc <- RN(e y),
+// and after a step or two xc is a fixed point of that map (checked bit for
+// bit).  From there on every particle of the run adds the same y, so only
+// the first steps of a run and the massive particles are sequential; the
+// rest of the run is one add per coordinate, done by the whole warp.
+constexpr int kSeqMassMax = 64;   // massive particles handled by the run path
+
+struct SeqRuns {
+    int mass_idx[kSeqMassMax];
+    int lo[kSeqMassMax + 1], hi[kSeqMassMax + 1];
+    double y[kSeqMassMax + 1][6];
+    int nruns;
+};
+
+union SeqShared {
+    SeqStage st;
+    SeqRuns runs;
+};
+
+// One exact chain step of src/integrator_whfast.c:744-760 for particle i;
+// y[6] receives the offsets added to jx_i / jv_i.
+__device__ __forceinline__ void jac_step(double xc[3], double vc[3], double mi, double ei,
+                                         double ep, const double *jxi, const double *jvi,
+                                         double *xi, double *vi, double y[6])
+{
+    for (int k = 0; k < 3; ++k) {
+        xc[k] = __ddiv_rn(__dsub_rn(xc[k], __dmul_rn(mi, jxi[k])), ei);
+        vc[k] = __ddiv_rn(__dsub_rn(vc[k], __dmul_rn(mi, jvi[k])), ei);
+        y[k] = xc[k];
+        y[3 + k] = vc[k];
+        xi[k] = __dadd_rn(jxi[k], xc[k]);
+        vi[k] = __dadd_rn(jvi[k], vc[k]);
+        xc[k] = __dmul_rn(ep, xc[k]);
+        vc[k] = __dmul_rn(ep, vc[k]);
+    }
+}
+
+__device__ void wh_massive_list_warp(const EnsDev &E, int base, int n, int s, int lane)
 {
     int k = 0;
-    for (int i = 0; i < n; ++i)
-        if (E.variant == WH_PAIRWISE || E.m[base + i] != 0.0) E.hv[base + k++] = i;
-    E.nh[s] = k;
+    for (int c = 0; c < n; c += 32) {
+        const int i = c + lane;
+        const bool h = i < n && (E.variant == WH_PAIRWISE || E.m[base + i] != 0.0);
+        const unsigned b = __ballot_sync(0xffffffffu, h);
+        if (h) E.hv[base + k + __popc(b & ((1u << lane) - 1u))] = i;
+        k += __popc(b);
+    }
+    if (lane == 0) E.nh[s] = k;
 }
 
 // mode 0: Cartesian -> Jacobi (initialisation); mode 1: removals, eta,
 // Jacobi -> Cartesian.  Both rebuild the massive-body list.
-__global__ void k_wh_seq(EnsDev E, int mode)
+__global__ void __launch_bounds__(32 * SEQ_WARPS) k_wh_seq(EnsDev E, int mode)
 {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= E.S) return;
+    __shared__ SeqShared shared_all[SEQ_WARPS];
+    const int lane = threadIdx.x & 31;
+    const int s = blockIdx.x * SEQ_WARPS + (threadIdx.x >> 5);
+    if (s >= E.S) return;   // warp-uniform
+    SeqStage &st = shared_all[threadIdx.x >> 5].st;
+    SeqRuns &rs = shared_all[threadIdx.x >> 5].runs;
     const int base = E.off[s];
     int n = E.cnt[s];
     if (n <= 0) return;
     double *m = E.m + base, *eta = E.eta + base;
     double *x = E.x + 3 * base, *v = E.v + 3 * base, *jx = E.jx + 3 * base, *jv = E.jv + 3 * base;
     if (mode == 0) {
-        // src/integrator_whfast.c:682-724
-        double xc[3], vc[3];
-        for (int k = 0; k < 3; ++k) {
-            xc[k] = __dmul_rn(m[0], x[k]);
-            vc[k] = __dmul_rn(m[0], v[k]);
-        }
-        for (int i = 1; i < n; ++i) {
-            const double ie = eta[i - 1];
+        if (lane == 0) {
+            // src/integrator_whfast.c:682-724 (once per run)
+            double xc[3], vc[3];
             for (int k = 0; k < 3; ++k) {
-                jx[3 * i + k] = __dsub_rn(x[3 * i + k], __ddiv_rn(xc[k], ie));
-                jv[3 * i + k] = __dsub_rn(v[3 * i + k], __ddiv_rn(vc[k], ie));
-                const double f = __dadd_rn(1.0, __ddiv_rn(m[i], ie));
-                xc[k] = __dadd_rn(__dmul_rn(xc[k], f), __dmul_rn(m[i], jx[3 * i + k]));
-                vc[k] = __dadd_rn(__dmul_rn(vc[k], f), __dmul_rn(m[i], jv[3 * i + k]));
+                xc[k] = __dmul_rn(m[0], x[k]);
+                vc[k] = __dmul_rn(m[0], v[k]);
+            }
+            for (int i = 1; i < n; ++i) {
+                const double ie = eta[i - 1];
+                for (int k = 0; k < 3; ++k) {
+                    jx[3 * i + k] = __dsub_rn(x[3 * i + k], __ddiv_rn(xc[k], ie));
+                    jv[3 * i + k] = __dsub_rn(v[3 * i + k], __ddiv_rn(vc[k], ie));
+                    const double f = __dadd_rn(1.0, __ddiv_rn(m[i], ie));
+                    xc[k] = __dadd_rn(__dmul_rn(xc[k], f), __dmul_rn(m[i], jx[3 * i + k]));
+                    vc[k] = __dadd_rn(__dmul_rn(vc[k], f), __dmul_rn(m[i], jv[3 * i + k]));
+                }
+            }
+            for (int k = 0; k < 3; ++k) {
+                jx[k] = __ddiv_rn(xc[k], eta[n - 1]);
+                jv[k] = __ddiv_rn(vc[k], eta[n - 1]);
             }
         }
-        for (int k = 0; k < 3; ++k) {
-            jx[k] = __ddiv_rn(xc[k], eta[n - 1]);
-            jv[k] = __ddiv_rn(vc[k], eta[n - 1]);
-        }
-    } else {
-        if (E.nrm[s] > 0) {
-            // src/system.c:444-528 and :530-577: stable compaction of the
-            // surviving slots (Cartesian x, v, m, ids, Jacobi x, v), then eta
+        __syncwarp();
+        wh_massive_list_warp(E, base, n, s, lane);
+        return;
+    }
+    if (E.nrm[s] > 0) {
+        // src/system.c:444-528 and :530-577: stable compaction of the
+        // surviving slots (Cartesian x, v, m, ids, Jacobi x, v), then eta
+        if (lane == 0) {
             int w = 0;
             for (int i = 0; i < n; ++i) {
                 if (E.rm[base + i]) {
@@ -233,38 +319,211 @@ __global__ void k_wh_seq(EnsDev E, int mode)
                 }
                 ++w;
             }
-            n = w;
-            E.cnt[s] = n;
+            E.cnt[s] = w;
             E.nrm[s] = 0;
             double e = m[0];
             eta[0] = e;
-            for (int i = 1; i < n; ++i) {
+            for (int i = 1; i < w; ++i) {
                 e = __dadd_rn(e, m[i]);
                 eta[i] = e;
             }
         }
-        // src/integrator_whfast.c:726-772
-        double xc[3], vc[3];
+        __syncwarp();
+        n = E.cnt[s];
+    }
+    // src/integrator_whfast.c:726-772
+    double xc[3], vc[3];
+    if (lane == 0) {
         for (int k = 0; k < 3; ++k) {
             xc[k] = __dmul_rn(eta[n - 1], jx[k]);
             vc[k] = __dmul_rn(eta[n - 1], jv[k]);
         }
-        for (int i = n - 1; i > 0; --i) {
+    }
+    // run path: needs finite Jacobi coordinates and few massive particles
+    bool finite = true;
+    int nmass = 0;
+    for (int c = 0; c < n; c += 32) {
+        const int i = c + lane;
+        bool f = true, h = false;
+        if (i < n) {
+            for (int k = 0; k < 3; ++k) f = f && isfinite(jx[3 * i + k]) && isfinite(jv[3 * i + k]);
+            h = m[i] != 0.0;
+        }
+        finite = __all_sync(0xffffffffu, f) && finite;
+        const unsigned b = __ballot_sync(0xffffffffu, h);
+        const int at = nmass + __popc(b & ((1u << lane) - 1u));
+        if (h && at < kSeqMassMax) rs.mass_idx[at] = i;
+        nmass += __popc(b);
+    }
+    if (finite && nmass <= kSeqMassMax) {
+        __syncwarp();
+        if (lane == 0) {
+            int nr = 0;
+            int q = nmass - 1;   // highest massive particle not yet passed
+            int i = n - 1;
+            double y[6];
+            while (i >= 1) {
+                while (q >= 0 && rs.mass_idx[q] > i) --q;
+                const int mtop = q >= 0 ? rs.mass_idx[q] : -1;
+                if (mtop == i) {
+                    jac_step(xc, vc, m[i], eta[i], eta[i - 1], jx + 3 * i, jv + 3 * i, x + 3 * i,
+                             v + 3 * i, y);
+                    --i;
+                    continue;
+                }
+                const int lo = mtop + 1 > 1 ? mtop + 1 : 1;
+                int j = i;
+                bool fixed = false;
+                while (j >= lo && !fixed) {
+                    const double ox[3] = {xc[0], xc[1], xc[2]}, ov[3] = {vc[0], vc[1], vc[2]};
+                    jac_step(xc, vc, m[j], eta[j], eta[j - 1], jx + 3 * j, jv + 3 * j, x + 3 * j,
+                             v + 3 * j, y);
+                    fixed = true;
+                    for (int k = 0; k < 3; ++k)
+                        fixed = fixed && __double_as_longlong(xc[k]) == __double_as_longlong(ox[k]) &&
+                                __double_as_longlong(vc[k]) == __double_as_longlong(ov[k]) &&
+                                isfinite(xc[k]) && isfinite(vc[k]) && xc[k] != 0.0 && vc[k] != 0.0;
+                    --j;
+                }
+                if (j >= lo) {
+                    rs.lo[nr] = lo;
+                    rs.hi[nr] = j;
+                    for (int k = 0; k < 6; ++k) rs.y[nr][k] = y[k];
+                    ++nr;
+                }
+                i = lo - 1;
+            }
+            rs.nruns = nr;
             for (int k = 0; k < 3; ++k) {
-                xc[k] = __ddiv_rn(__dsub_rn(xc[k], __dmul_rn(m[i], jx[3 * i + k])), eta[i]);
-                vc[k] = __ddiv_rn(__dsub_rn(vc[k], __dmul_rn(m[i], jv[3 * i + k])), eta[i]);
-                x[3 * i + k] = __dadd_rn(jx[3 * i + k], xc[k]);
-                v[3 * i + k] = __dadd_rn(jv[3 * i + k], vc[k]);
-                xc[k] = __dmul_rn(eta[i - 1], xc[k]);
-                vc[k] = __dmul_rn(eta[i - 1], vc[k]);
+                x[k] = __ddiv_rn(xc[k], m[0]);
+                v[k] = __ddiv_rn(vc[k], m[0]);
             }
         }
+        __syncwarp();
+        const int nr = rs.nruns;
+        for (int r = 0; r < nr; ++r) {
+            const int lo = rs.lo[r], cnt = 3 * (rs.hi[r] - lo + 1);
+            for (int t = lane; t < cnt; t += 32) {
+                const int k = t % 3;
+                x[3 * lo + t] = __dadd_rn(jx[3 * lo + t], rs.y[r][k]);
+                v[3 * lo + t] = __dadd_rn(jv[3 * lo + t], rs.y[r][3 + k]);
+            }
+        }
+        __syncwarp();
+        wh_massive_list_warp(E, base, n, s, lane);
+        return;
+    }
+    __syncwarp();
+    // general path: the whole chain, chunk by chunk from the outside in
+    for (int hi = n; hi > 1; hi -= SEQ_CHUNK) {
+        const int lo = hi - SEQ_CHUNK > 1 ? hi - SEQ_CHUNK : 1;
+        const int c = hi - lo;
+        for (int t = lane; t < 3 * c; t += 32) {
+            st.jx[t] = jx[3 * lo + t];
+            st.jv[t] = jv[3 * lo + t];
+        }
+        for (int t = lane; t < c; t += 32) st.m[t] = m[lo + t];
+        for (int t = lane; t <= c; t += 32) st.eta[t] = eta[lo - 1 + t];
+        __syncwarp();
+        if (lane == 0) {
+            for (int q = c - 1; q >= 0; --q) {
+                const double mi = st.m[q], ei = st.eta[q + 1], ep = st.eta[q];
+                for (int k = 0; k < 3; ++k) {
+                    const double jxq = st.jx[3 * q + k], jvq = st.jv[3 * q + k];
+                    xc[k] = __ddiv_rn(__dsub_rn(xc[k], __dmul_rn(mi, jxq)), ei);
+                    vc[k] = __ddiv_rn(__dsub_rn(vc[k], __dmul_rn(mi, jvq)), ei);
+                    st.x[3 * q + k] = __dadd_rn(jxq, xc[k]);
+                    st.v[3 * q + k] = __dadd_rn(jvq, vc[k]);
+                    xc[k] = __dmul_rn(ep, xc[k]);
+                    vc[k] = __dmul_rn(ep, vc[k]);
+                }
+            }
+        }
+        __syncwarp();
+        for (int t = lane; t < 3 * c; t += 32) {
+            x[3 * lo + t] = st.x[t];
+            v[3 * lo + t] = st.v[t];
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
         for (int k = 0; k < 3; ++k) {
             x[k] = __ddiv_rn(xc[k], m[0]);
             v[k] = __ddiv_rn(vc[k], m[0]);
         }
     }
-    wh_massive_list(E, base, n, s);
+    wh_massive_list_warp(E, base, n, s, lane);
+}
+
+// ---- shared interaction pair sums ---------------------------------------------
+// The pair term of the interaction acceleration (src/integrator_whfast.c
+// :1125-1190 / :920-950) sums over interior massive bodies j and exterior
+// massive bodies k of particle i; it depends on i only through which massive
+// bodies are interior.  So it is formed once per system and partition, in
+// the reference's (j, k) order, and every particle with that partition reads
+// the same bits:
+//   slot g (1 <= g <= nh)         a particle with g interior massive bodies
+//                                  that is not itself massive;
+//   slot kPairSlots + r (r >= 1)  the massive body of list rank r.
+
+constexpr int PAIR_WARPS = 2;   // systems per CTA
+constexpr int kPairTerms = kPairMax * (kPairMax - 1) / 2;
+
+// One warp per system: every massive pair term G m_j m_k (x_k - x_j) /
+// (|x_k - x_j|^3 + eps^3) once into shared memory (pair (p, q), p < q in
+// list order, at q (q - 1) / 2 + p), then one lane per slot adds its terms
+// in the reference's order.
+__global__ void __launch_bounds__(32 * PAIR_WARPS) k_wh_pairs(EnsDev E)
+{
+    __shared__ double terms_all[PAIR_WARPS][kPairTerms][3];
+    const int lane = threadIdx.x & 31;
+    const int s = blockIdx.x * PAIR_WARPS + (threadIdx.x >> 5);
+    if (s >= E.S) return;   // warp-uniform
+    const int nh = E.nh[s];
+    if (nh > kPairMax) return;
+    double(*terms)[3] = terms_all[threadIdx.x >> 5];
+    const int base = E.off[s];
+    const double *x = E.x + 3 * (size_t)base;
+    const double *m = E.m + base;
+    const int *hv = E.hv + base;
+    const double e3 = __dmul_rn(__dmul_rn(E.eps, E.eps), E.eps);
+    const int npairs = nh * (nh - 1) / 2;
+    for (int t = lane; t < npairs; t += 32) {
+        int q = 1;
+        while ((q + 1) * q / 2 <= t) ++q;
+        const int p = t - q * (q - 1) / 2;
+        const int j = hv[p], kk = hv[q];
+        const double d[3] = {__dsub_rn(x[3 * kk], x[3 * j]), __dsub_rn(x[3 * kk + 1], x[3 * j + 1]),
+                             __dsub_rn(x[3 * kk + 2], x[3 * j + 2])};
+        const double dn = norm3d(d);
+        const double dc = __dadd_rn(__dmul_rn(__dmul_rn(dn, dn), dn), e3);
+        const double Gmm = __dmul_rn(__dmul_rn(E.G, m[j]), m[kk]);
+        for (int k = 0; k < 3; ++k) terms[t][k] = __ddiv_rn(__dmul_rn(Gmm, d[k]), dc);
+    }
+    __syncwarp();
+    for (int slot = lane; slot < 2 * kPairSlots; slot += 32) {
+        int p_end, q_begin;
+        if (slot < kPairSlots) {
+            if (slot > nh) continue;
+            p_end = slot;
+            q_begin = slot;
+        } else {
+            const int r = slot - kPairSlots;
+            if (r >= nh) continue;
+            p_end = r;
+            q_begin = r + 1;
+        }
+        double aux[3] = {0.0, 0.0, 0.0};
+        for (int p = 0; p < p_end; ++p)
+            for (int q = q_begin; q < nh; ++q) {
+                const double *tr = terms[q * (q - 1) / 2 + p];
+                for (int k = 0; k < 3; ++k) aux[k] = __dadd_rn(aux[k], tr[k]);
+            }
+        double *out = E.pairs + ((size_t)s * 2 * kPairSlots + slot) * 3;
+        out[0] = aux[0];
+        out[1] = aux[1];
+        out[2] = aux[2];
+    }
 }
 
 // ---- Kepler drift -------------------------------------------------------------
@@ -444,6 +703,18 @@ __global__ void k_wh_accel(EnsDev E, int P)
     }
     for (int k = 0; k < 3; ++k) acc[k] = __dadd_rn(acc[k], aux[k]);
     aux[0] = aux[1] = aux[2] = 0.0;
+    if (nh <= kPairMax) {
+        int g = 0, rank = -1;
+        for (int q = 0; q < nh; ++q) {
+            const int j = hv[q];
+            if (j == i) rank = q;
+            if (j < i) ++g;
+        }
+        const int slot = rank >= 0 ? kPairSlots + rank : g;
+        const double *pr = E.pairs + ((size_t)s * 2 * kPairSlots + slot) * 3;
+        for (int k = 0; k < 3; ++k) a[k] = __dsub_rn(acc[k], __ddiv_rn(pr[k], eta[i - 1]));
+        return;
+    }
     for (int q0 = 0; q0 < nh; ++q0) {
         const int j = hv[q0];
         if (j >= i) break;
@@ -525,11 +796,11 @@ __global__ void k_ens_massless_accel(EnsDev E, int P)
     E.a[3 * (size_t)p + 2] = a2;
 }
 
-__global__ void k_ens_massive_list(EnsDev E)
+__global__ void __launch_bounds__(32 * SEQ_WARPS) k_ens_massive_list(EnsDev E)
 {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= E.S) return;
-    wh_massive_list(E, E.off[s], E.cnt[s], s);
+    const int s = blockIdx.x * SEQ_WARPS + (threadIdx.x >> 5);
+    if (s >= E.S) return;   // warp-uniform
+    wh_massive_list_warp(E, E.off[s], E.cnt[s], s, threadIdx.x & 31);
 }
 
 }  // namespace gs
@@ -547,7 +818,7 @@ struct gsgpu_ensemble {
     bool own_stream = false;
     std::vector<int> h_off;
     DBuf off, cnt, sys_of, ids, x, v, m, jx, jv, a, eta, hv, nh, rm, nrm, t_ids, t_x, t_v, t_m,
-        status, xe, ve;
+        status, xe, ve, pairs;
     EnsDev E{};
     bool primed = false;
     double last_dt = 0.0;
@@ -571,10 +842,14 @@ struct gsgpu_ensemble {
         return ok();
     }
 
+    int seq_grid() const { return (S + SEQ_WARPS - 1) / SEQ_WARPS; }
+
     ErrorStatus accel()
     {
-        if (integrator == INTEGRATOR_WHFAST)
+        if (integrator == INTEGRATOR_WHFAST) {
+            k_wh_pairs<<<(S + PAIR_WARPS - 1) / PAIR_WARPS, 32 * PAIR_WARPS, 0, stream>>>(E);
             k_wh_accel<<<pgrid(), 128, 0, stream>>>(E, P);
+        }
         else
             k_ens_massless_accel<<<pgrid(), 128, 0, stream>>>(E, P);
         GS_CUDA(cudaGetLastError());
@@ -587,11 +862,11 @@ struct gsgpu_ensemble {
         if (integrator == INTEGRATOR_WHFAST) {
             // src/integrator_whfast.c:241-273
             GS_TRY(sort(E.x, E.v));
-            k_wh_seq<<<(S + 127) / 128, 128, 0, stream>>>(E, 0);
+            k_wh_seq<<<seq_grid(), 32 * SEQ_WARPS, 0, stream>>>(E, 0);
             GS_TRY(accel());
             k_wh_kick<<<pgrid(), 128, 0, stream>>>(E, P, 0.5 * dt);
         } else {
-            k_ens_massive_list<<<(S + 127) / 128, 128, 0, stream>>>(E);
+            k_ens_massive_list<<<seq_grid(), 32 * SEQ_WARPS, 0, stream>>>(E);
             GS_TRY(accel());
             launch_comp_update(E.v, ve.as<double>(), E.a, dt, 0.5, 3 * P, stream);
         }
@@ -606,7 +881,7 @@ struct gsgpu_ensemble {
             // src/integrator_whfast.c:290-343
             GS_TRY(sort(E.jx, E.jv));
             k_wh_drift<<<pgrid(), 128, 0, stream>>>(E, P, h);
-            k_wh_seq<<<(S + 127) / 128, 128, 0, stream>>>(E, 1);
+            k_wh_seq<<<seq_grid(), 32 * SEQ_WARPS, 0, stream>>>(E, 1);
             GS_TRY(accel());
             k_wh_kick<<<pgrid(), 128, 0, stream>>>(E, P, h);
         } else {
@@ -619,7 +894,7 @@ struct gsgpu_ensemble {
         return ok();
     }
 
-    int kernels_per_step() const { return integrator == INTEGRATOR_WHFAST ? 5 : 3; }
+    int kernels_per_step() const { return integrator == INTEGRATOR_WHFAST ? 6 : 3; }
 
     ErrorStatus step_graph(double h)
     {
@@ -661,6 +936,8 @@ struct gsgpu_ensemble {
         GS_CUDA(cudaStreamSynchronize(stream));
         if (h & ST_CAPACITY)
             return GS_RAISE(GRAV_VALUE_ERROR, "a system exceeds the ensemble's sort capacity");
+        if (h & ST_NONFINITE)
+            return GS_RAISE(GRAV_VALUE_ERROR, "an ensemble sort saw an inconsistent order");
         if (h & ST_NO_PRIMARY)
             return GS_RAISE(GRAV_VALUE_ERROR, "Primary particle ID not found in system");
         return ok();
@@ -720,6 +997,7 @@ ErrorStatus ensemble_create(gsgpu_ensemble **out, int num_systems, const int *co
     GS_TRY(e->eta.reserve(P * sizeof(double)));
     GS_TRY(e->t_m.reserve(P * sizeof(double)));
     GS_TRY(e->status.reserve(sizeof(unsigned)));
+    GS_TRY(e->pairs.reserve(S * 2 * kPairSlots * 3 * sizeof(double)));
     std::vector<int> sys(P);
     for (int s = 0; s < num_systems; ++s)
         for (int p = e->h_off[s]; p < e->h_off[s + 1]; ++p) sys[p] = s;
@@ -754,6 +1032,7 @@ ErrorStatus ensemble_create(gsgpu_ensemble **out, int num_systems, const int *co
     E.t_v = e->t_v.as<double>();
     E.t_m = e->t_m.as<double>();
     E.status = e->status.as<unsigned>();
+    E.pairs = e->pairs.as<double>();
     E.G = G;
     E.eps = eps;
     E.variant = method == GRAV_GPU_MASSLESS ? WH_MASSLESS : WH_PAIRWISE;

@@ -129,7 +129,7 @@ def test_ensemble_graph_replay_equals_run_until(g, lib, wl):
         else:
             ens.run_until(100.0)
         out.append(ens.download())
-        assert ens.kernels_per_step() == 5
+        assert ens.kernels_per_step() == 6
         ens.close()
     for a, b in zip(*out):
         assert np.array_equal(a, b)
