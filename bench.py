@@ -15,6 +15,8 @@ Workloads (seeded synthetic inputs -- grav_sim publishes no dataset):
                     equal masses), Barnes-Hut with monopole + quadrupole
                     cells, theta = 0.5, eps = 0.01, leapfrog dt = 1e-3.
   galaxy1048576_plain -- the same at N = 1,048,576 with the monopole walk.
+  galaxy2097152_group / galaxy1048576_group -- the group walk with
+                    interaction lists (quadrupole cells), theta = 0.5.
   galaxy1048576_learned -- theta = 1.0 walk + learned residual, judged by a
                     4,096-particle direct sum per step (training before the
                     timed region).
@@ -88,9 +90,18 @@ WORKLOADS = {
     "galaxy1048576_learned": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01, dt=1e-3,
                                   integrator=4, method=104, theta=1.0, leaf=1,
                                   flop_per_interaction=20),
-    # small case of the walk, for profiler captures
+    "galaxy2097152_group": dict(ic="galaxy", n=2097152, seed=4, G=1.0, eps=0.01, dt=1e-3,
+                                integrator=4, method=106, theta=0.5, leaf=1,
+                                flop_per_interaction=20),
+    "galaxy1048576_group": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01, dt=1e-3,
+                                integrator=4, method=106, theta=0.5, leaf=1,
+                                flop_per_interaction=20),
+    # small cases of the walks, for profiler captures
     "galaxy262144": dict(ic="galaxy", n=262144, seed=6, G=1.0, eps=0.01, dt=1e-3, integrator=4,
                          method=105, theta=0.5, leaf=1, flop_per_interaction=20),
+    "galaxy262144_group": dict(ic="galaxy", n=262144, seed=6, G=1.0, eps=0.01, dt=1e-3,
+                               integrator=4, method=106, theta=0.5, leaf=1,
+                               flop_per_interaction=20),
     "ensemble8192": dict(ic="ensemble", systems=8192, seed=3, max_test=4096, dt=1.0,
                          integrator=10, method=102),
     "ensemble8192_leapfrog": dict(ic="ensemble", systems=8192, seed=3, max_test=4096, dt=1.0,
@@ -217,7 +228,7 @@ def run_ours(args, world, rank, local):
         return run_ensemble(args, world, rank, local, wk, g, wl, lib)
     n = wk["n"]
     x, v, m = (wl.plummer if wk["ic"] == "plummer" else wl.galaxy_pair)(n, wk["seed"])
-    bh = wk["method"] in (103, 104, 105, 113)
+    bh = wk["method"] in (103, 104, 105, 106, 113)
 
     dp = ctypes.POINTER(ctypes.c_double)
     lib.gsgpu_sim_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
@@ -323,12 +334,13 @@ def run_ours(args, world, rank, local):
     t0 = time.perf_counter()
     g.launch_simulation(lib, xe, ve, me, wk["G"], integrator=wk["integrator"], dt=wk["dt"],
                         tf=wk["dt"] * args.steps * (1 - 1e-9), method=wk["method"],
-                        softening_length=wk["eps"])
+                        opening_angle=wk.get("theta", 1.0), softening_length=wk["eps"],
+                        max_num_particles_per_leaf=wk.get("leaf", -1))
     e2e_s = time.perf_counter() - t0
     e2e_val = world * n * args.steps / e2e_s
 
     traffic = None
-    kernel = "k_bh_walk" if bh else "k_direct_sum"
+    kernel = ("k_bh_group" if wk["method"] == 106 else "k_bh_walk") if bh else "k_direct_sum"
     prof = ROOT / "profiles" / f"{kernel}_{args.workload}.md"
     if prof.exists():
         for ln in prof.read_text().splitlines():

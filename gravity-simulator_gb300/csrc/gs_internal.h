@@ -160,7 +160,7 @@ ErrorStatus make_engine(int method, std::unique_ptr<Engine> &out);
 
 std::unique_ptr<Engine> make_direct_engine(bool fp64_reference_order);
 std::unique_ptr<Engine> make_massless_engine();
-std::unique_ptr<Engine> make_barnes_hut_engine(bool compat, bool quad = false);
+std::unique_ptr<Engine> make_barnes_hut_engine(bool compat, bool quad = false, bool group = false);
 std::unique_ptr<Engine> make_learned_engine();
 
 // ---- integrator kernels (k_integrate.cu) -------------------------------

@@ -51,6 +51,8 @@ struct OctreeDevice {
     DBuf w_nc;                // int4[cap]: (first_child, num_children, first_particle, count)
     DBuf w_nkey;              // uint64[cap]: key used by the cell-membership test
     DBuf w_pa, w_pb;          // float4[n] in sorted order: (x_hi, m), (x_lo, 0)
+    DBuf g_list;              // int2[n]: particle groups of the group walk (first, count)
+    DBuf g_ctr;               // int[4]: group count, work-queue head
     RadixSorter sorter;
 
     ErrorStatus setup(int n, int leaf_max, bool compat, bool quad = false);
@@ -69,5 +71,11 @@ struct OctreeDevice {
 ErrorStatus launch_bh_walk(const OctreeDevice &t, const double *d_x, double theta, double eps,
                            double G, double *d_a, const int *gate,
                            unsigned long long *counters, cudaStream_t s);
+
+// Group walk with interaction lists (k_walk_group.cu): same counters and
+// gate as launch_bh_walk; needs a tree with true leaf multipoles (not compat).
+ErrorStatus launch_bh_group_walk(const OctreeDevice &t, double theta, double eps, double G,
+                                 double *d_a, unsigned long long *counters, cudaStream_t s,
+                                 const int *gate = nullptr);
 
 }  // namespace gs

@@ -85,6 +85,34 @@ __device__ __forceinline__ void pair_term(const float4 q, float xi, float yi, fl
 
 // One (i-tile, j-chunk) work unit: the 1024 i-particles start at pi_tile;
 // partial sums go to partial[split][3][plane] at rows itile*1024 + ...
+// Two i-particles per instruction: Blackwell's paired FP32 operations
+// (add / mul / fma on float2, each lane rounded as the scalar operation)
+// carry the pair terms of particles (k, k+1) together, halving the FP32
+// instructions issued per term; the arithmetic of each particle is exactly
+// pair_term's (q.x - x_i is formed as q.x + (-x_i)).
+template <bool SOFT>
+__device__ __forceinline__ void pair_term2(const float4 q, float2 nxi, float2 nyi, float2 nzi,
+                                           float2 eps2, float2 &ax, float2 &ay, float2 &az)
+{
+    const float2 dx = __fadd2_rn(make_float2(q.x, q.x), nxi);
+    const float2 dy = __fadd2_rn(make_float2(q.y, q.y), nyi);
+    const float2 dz = __fadd2_rn(make_float2(q.z, q.z), nzi);
+    float2 r2 = __ffma2_rn(dx, dx, eps2);
+    r2 = __ffma2_rn(dy, dy, r2);
+    r2 = __ffma2_rn(dz, dz, r2);
+    float2 ri = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+    if (!SOFT) {
+        ri.x = (r2.x > 0.0f) ? ri.x : 0.0f;
+        ri.y = (r2.y > 0.0f) ? ri.y : 0.0f;
+    }
+    const float2 mr = __fmul2_rn(make_float2(q.w, q.w), ri);
+    const float2 ri2 = __fmul2_rn(ri, ri);
+    const float2 sc = __fmul2_rn(mr, ri2);
+    ax = __ffma2_rn(dx, sc, ax);
+    ay = __ffma2_rn(dy, sc, ay);
+    az = __ffma2_rn(dz, sc, az);
+}
+
 template <bool SOFT>
 __device__ __forceinline__ void direct_sum_unit(const float4 *__restrict__ pi_tile,
                                                 const float4 *__restrict__ pj, int plane,
@@ -126,6 +154,15 @@ __device__ __forceinline__ void direct_sum_unit(const float4 *__restrict__ pi_ti
         sx[k] = sy[k] = sz[k] = 0.0f;
         cx[k] = cy[k] = cz[k] = 0.0f;
     }
+    static_assert(DS_IPT % 2 == 0, "i-particles are paired");
+    float2 nx2[DS_IPT / 2], ny2[DS_IPT / 2], nz2[DS_IPT / 2];
+#pragma unroll
+    for (int k = 0; k < DS_IPT / 2; ++k) {
+        nx2[k] = make_float2(-xi[2 * k], -xi[2 * k + 1]);
+        ny2[k] = make_float2(-yi[2 * k], -yi[2 * k + 1]);
+        nz2[k] = make_float2(-zi[2 * k], -zi[2 * k + 1]);
+    }
+    const float2 eps2v = make_float2(eps2, eps2);
 
     int issued = min(DS_STAGES, ntiles);
     int t = 0;
@@ -139,21 +176,25 @@ __device__ __forceinline__ void direct_sum_unit(const float4 *__restrict__ pi_ti
         }
         const float4 *tile = sj + st * DS_JTILE;
         for (int j0 = 0; j0 < DS_JTILE; j0 += DS_KAHAN_CHUNK) {
-            float ax[DS_IPT], ay[DS_IPT], az[DS_IPT];
+            float2 ax[DS_IPT / 2], ay[DS_IPT / 2], az[DS_IPT / 2];
 #pragma unroll
-            for (int k = 0; k < DS_IPT; ++k) ax[k] = ay[k] = az[k] = 0.0f;
+            for (int k = 0; k < DS_IPT / 2; ++k)
+                ax[k] = ay[k] = az[k] = make_float2(0.0f, 0.0f);
 #pragma unroll 8
             for (int j = j0; j < j0 + DS_KAHAN_CHUNK; ++j) {
                 const float4 q = tile[j];
 #pragma unroll
-                for (int k = 0; k < DS_IPT; ++k)
-                    pair_term<SOFT>(q, xi[k], yi[k], zi[k], eps2, ax[k], ay[k], az[k]);
+                for (int k = 0; k < DS_IPT / 2; ++k)
+                    pair_term2<SOFT>(q, nx2[k], ny2[k], nz2[k], eps2v, ax[k], ay[k], az[k]);
             }
 #pragma unroll
-            for (int k = 0; k < DS_IPT; ++k) {
-                kahan_add(sx[k], cx[k], ax[k]);
-                kahan_add(sy[k], cy[k], ay[k]);
-                kahan_add(sz[k], cz[k], az[k]);
+            for (int k = 0; k < DS_IPT / 2; ++k) {
+                kahan_add(sx[2 * k], cx[2 * k], ax[k].x);
+                kahan_add(sy[2 * k], cy[2 * k], ay[k].x);
+                kahan_add(sz[2 * k], cz[2 * k], az[k].x);
+                kahan_add(sx[2 * k + 1], cx[2 * k + 1], ax[k].y);
+                kahan_add(sy[2 * k + 1], cy[2 * k + 1], ay[k].y);
+                kahan_add(sz[2 * k + 1], cz[2 * k + 1], az[k].y);
             }
         }
         __syncthreads();   // every thread is done with stage st

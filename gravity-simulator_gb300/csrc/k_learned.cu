@@ -1,7 +1,8 @@
 // k_learned.cu -- Barnes-Hut with a learned residual (GRAV_GPU_BH_LEARNED).
 //
-// A cheap walk (opening angle theta_cheap, 1.0 by default, monopole +
-// quadrupole cells) is corrected by the residual network of k_mlp.cu:
+// A cheap walk (opening angle theta_cheap, 1.0 by default; the group walk
+// of k_walk_group.cu with monopole + quadrupole cells) is corrected by the
+// residual network of k_mlp.cu:
 //     a = a_cheap + |a_cheap| * net(features) / 100,
 // where the network was trained to predict 100 (a_direct - a_cheap)/|a_cheap|
 // from 32 per-particle features of the tree around the particle.
@@ -53,6 +54,9 @@ constexpr double kThetaFallback = 0.5;
 constexpr float kResidualScale = 100.0f;
 constexpr int kBatch = 8192;
 constexpr int kEpochs = 24;
+// The network is used only if it brings the held-out median residual below
+// this fraction of the cheap walk's; otherwise the engine runs the fallback.
+constexpr double kMinGain = 0.8;
 
 }  // namespace
 
@@ -268,22 +272,26 @@ class LearnedEngine final : public Engine {
             return ok();
         }
         unsigned long long *cnt = counters_.as<unsigned long long>();
+        if (!useful_) {
+            // The network did not earn its cost on the held-out snapshot:
+            // the fallback walk gives every force, still judged each step.
+            if (timer) GS_TRY(timer->begin(s));
+            GS_TRY(launch_bh_group_walk(tree_, kThetaFallback, eps_, G_, d_a, cnt, s));
+            if (timer) GS_TRY(timer->end(s));
+            GS_TRY(judge(d_x, d_m, d_a, s));
+            k_replace_rows<<<(J_ + 255) / 256, 256, 0, s>>>(J_, ids_.as<int>(),
+                                                            a_rows_.as<double>(), d_a);
+            GS_CUDA(cudaGetLastError());
+            return ok();
+        }
         if (timer) GS_TRY(timer->begin(s));
-        GS_TRY(launch_bh_walk(tree_, d_x, theta_, eps_, G_, d_a, nullptr, cnt, s));
+        GS_TRY(launch_bh_group_walk(tree_, theta_, eps_, G_, d_a, cnt, s));
         if (timer) GS_TRY(timer->end(s));
         GS_TRY(features(nullptr, n_, feat_.as<float>(), d_x, d_m, s));
         GS_TRY(mlp_.forward(feat_.as<float>(), n_, pred_.as<float>(), s));
         k_correct<<<(n_ + 255) / 256, 256, 0, s>>>(n_, tree_.sidx.as<int>(), pred_.as<float>(), d_a);
-        // judge on a rotating strided sample
-        const long long stride = std::max(1, n_ / J_);
-        k_sample<<<(J_ + 255) / 256, 256, 0, s>>>(J_, n_, 0, stride, stats_.as<double>() + 1,
-                                                  tree_.sidx.as<int>(), pos_.as<int>(),
-                                                  ids_.as<int>());
-        GS_TRY(rows_.compute(d_x, d_m, tree_.frame.as<double>(), ids_.as<int>(), J_, G_, eps_,
-                             a_rows_.as<double>(), s));
-        k_judge<<<1, JG_THREADS, 0, s>>>(J_, ids_.as<int>(), d_a, a_rows_.as<double>(), kJudgeTol,
-                                         flag_.as<int>(), stats_.as<double>());
-        GS_TRY(launch_bh_walk(tree_, d_x, kThetaFallback, eps_, G_, d_a, flag_.as<int>(), cnt, s));
+        GS_TRY(judge(d_x, d_m, d_a, s));
+        GS_TRY(launch_bh_group_walk(tree_, kThetaFallback, eps_, G_, d_a, cnt, s, flag_.as<int>()));
         k_replace_rows<<<(J_ + 255) / 256, 256, 0, s>>>(J_, ids_.as<int>(), a_rows_.as<double>(),
                                                         d_a);
         GS_CUDA(cudaGetLastError());
@@ -292,6 +300,8 @@ class LearnedEngine final : public Engine {
 
     int kernels_per_eval() const override
     {
+        if (trained_ && !useful_)   // fallback walk, sample, rows, judge, replace
+            return tree_.launches_per_build() + 1 + 1 + DirectRows::kernels() + 1 + 1;
         return tree_.launches_per_build() + 1 + 1 + 1 + 1 + 1 + DirectRows::kernels() + 1 + 1 + 1;
     }
 
@@ -333,21 +343,38 @@ class LearnedEngine final : public Engine {
 
     int report(double *out, int nmax) const override
     {
-        double v[12] = {trained_ ? 1.0 : 0.0, (double)snapshots_, loss_first_, loss_last_,
+        double v[13] = {trained_ ? 1.0 : 0.0, (double)snapshots_, loss_first_, loss_last_,
                         hold_before_, hold_after_, 0.0, 0.0, 0.0, theta_, train_seconds_,
-                        (double)adam_steps_};
+                        (double)adam_steps_, useful_ ? 1.0 : 0.0};
         double st[4] = {0, 0, 0, 0};
         if (stats_.p && cudaMemcpy(st, stats_.p, sizeof(st), cudaMemcpyDeviceToHost) == cudaSuccess) {
             v[6] = st[0];
             v[7] = st[1];
             v[8] = st[2];
         }
-        const int k = std::min(nmax, 12);
+        const int k = std::min(nmax, 13);
         for (int i = 0; i < k; ++i) out[i] = v[i];
         return k;
     }
 
   private:
+    // Direct sum of J_ particles (a rotating strided sample) against all;
+    // sets the fallback flag when their median relative error exceeds the
+    // tolerance and records the statistics.
+    ErrorStatus judge(const double *d_x, const double *d_m, const double *d_a, cudaStream_t s)
+    {
+        const long long stride = std::max(1, n_ / J_);
+        k_sample<<<(J_ + 255) / 256, 256, 0, s>>>(J_, n_, 0, stride, stats_.as<double>() + 1,
+                                                  tree_.sidx.as<int>(), pos_.as<int>(),
+                                                  ids_.as<int>());
+        GS_TRY(rows_.compute(d_x, d_m, tree_.frame.as<double>(), ids_.as<int>(), J_, G_, eps_,
+                             a_rows_.as<double>(), s));
+        k_judge<<<1, JG_THREADS, 0, s>>>(J_, ids_.as<int>(), d_a, a_rows_.as<double>(), kJudgeTol,
+                                         flag_.as<int>(), stats_.as<double>());
+        GS_CUDA(cudaGetLastError());
+        return ok();
+    }
+
     ErrorStatus features(const int *pos, int count, float *out, const double *d_x,
                          const double *d_m, cudaStream_t s)
     {
@@ -364,8 +391,8 @@ class LearnedEngine final : public Engine {
     ErrorStatus collect(const double *d_x, const double *d_m, double *d_a, cudaStream_t s)
     {
         unsigned long long *cnt = counters_.as<unsigned long long>();
-        GS_TRY(launch_bh_walk(tree_, d_x, theta_, eps_, G_, a_cheap_.as<double>(), nullptr, cnt, s));
-        GS_TRY(launch_bh_walk(tree_, d_x, kThetaFallback, eps_, G_, d_a, nullptr, cnt, s));
+        GS_TRY(launch_bh_group_walk(tree_, theta_, eps_, G_, a_cheap_.as<double>(), cnt, s));
+        GS_TRY(launch_bh_group_walk(tree_, kThetaFallback, eps_, G_, d_a, cnt, s));
         const long long stride = std::max(1, n_ / K_);
         const long long offset = ((long long)snapshots_ * 104729LL) % std::max(1LL, stride) +
                                  (long long)snapshots_ * 31LL;
@@ -442,6 +469,7 @@ class LearnedEngine final : public Engine {
         adam_steps_ = step;
         GS_TRY(mlp_.check(s));
         GS_TRY(holdout(s, &hold_before_, &hold_after_));
+        useful_ = hold_after_ < kMinGain * hold_before_;
         train_seconds_ =
             std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         trained_ = true;
@@ -458,6 +486,7 @@ class LearnedEngine final : public Engine {
         counters_;
     int snapshots_ = 0;
     bool trained_ = false;
+    bool useful_ = false;   // network kept: it cut the held-out residual by >= 1 - kMinGain
     int adam_steps_ = 0;
     double loss_first_ = 0.0, loss_last_ = 0.0, hold_before_ = 0.0, hold_after_ = 0.0;
     double train_seconds_ = 0.0;

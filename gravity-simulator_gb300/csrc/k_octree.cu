@@ -77,20 +77,42 @@ k_bbox_partial(const double *__restrict__ x, int n, double *__restrict__ part)
 }
 
 // src/linear_octree.c:138-145 (and :856-867 when a box is given)
-__global__ void k_bbox_final(const double *__restrict__ part, int blocks, double ocx, double ocy,
-                             double ocz, double owidth, double *__restrict__ frame)
+// One CTA of OT_THREADS threads: min / max are exact in any order, so the
+// block partials are reduced as a tree.
+__global__ void __launch_bounds__(OT_THREADS)
+k_bbox_final(const double *__restrict__ part, int blocks, double ocx, double ocy, double ocz,
+             double owidth, double *__restrict__ frame)
 {
-    if (threadIdx.x != 0) return;
+    __shared__ double s[6][OT_THREADS];
     double lo[3], hi[3];
     for (int k = 0; k < 3; ++k) {
         lo[k] = part[k];
         hi[k] = part[3 + k];
     }
-    for (int b = 1; b < blocks; ++b)
+    for (int b = threadIdx.x; b < blocks; b += OT_THREADS)
         for (int k = 0; k < 3; ++k) {
             lo[k] = dmin(lo[k], part[6 * b + k]);
             hi[k] = dmax(hi[k], part[6 * b + 3 + k]);
         }
+    for (int k = 0; k < 3; ++k) {
+        s[k][threadIdx.x] = lo[k];
+        s[3 + k][threadIdx.x] = hi[k];
+    }
+    __syncthreads();
+    for (int w2 = OT_THREADS / 2; w2 > 0; w2 >>= 1) {
+        if (threadIdx.x < w2) {
+            for (int k = 0; k < 3; ++k) {
+                s[k][threadIdx.x] = dmin(s[k][threadIdx.x], s[k][threadIdx.x + w2]);
+                s[3 + k][threadIdx.x] = dmax(s[3 + k][threadIdx.x], s[3 + k][threadIdx.x + w2]);
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = s[k][0];
+        hi[k] = s[3 + k][0];
+    }
     double c[3], w;
     if (owidth > 0.0) {
         c[0] = ocx;
@@ -601,6 +623,8 @@ ErrorStatus OctreeDevice::setup(int n_, int leaf_max_, bool compat_, bool quad_)
     GS_TRY(w_nkey.reserve((size_t)cap * sizeof(uint64_t)));
     GS_TRY(w_pa.reserve((size_t)n * sizeof(float4)));
     GS_TRY(w_pb.reserve((size_t)n * sizeof(float4)));
+    GS_TRY(g_list.reserve((size_t)n * sizeof(int2)));
+    GS_TRY(g_ctr.reserve(4 * sizeof(int)));
     if (quad) {
         GS_TRY(t_quad.reserve((size_t)cap * 6 * sizeof(double)));
         GS_TRY(w_nq.reserve((size_t)cap * 2 * sizeof(float4)));
@@ -627,7 +651,7 @@ ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream
     const int nb = std::min(BBOX_BLOCKS, std::max(1, (n + OT_THREADS - 1) / OT_THREADS));
     k_bbox_partial<<<nb, OT_THREADS, 0, s>>>(d_x, n, bbox_part.as<double>());
     const bool own_box = box_center && box_width > 0.0;
-    k_bbox_final<<<1, 32, 0, s>>>(bbox_part.as<double>(), nb, own_box ? box_center[0] : 0.0,
+    k_bbox_final<<<1, OT_THREADS, 0, s>>>(bbox_part.as<double>(), nb, own_box ? box_center[0] : 0.0,
                                   own_box ? box_center[1] : 0.0, own_box ? box_center[2] : 0.0,
                                   own_box ? box_width : -1.0, frame.as<double>());
     const int pb = (n + OT_THREADS - 1) / OT_THREADS;

@@ -40,29 +40,45 @@ k_radix_count(const uint64_t *__restrict__ keys, const int *__restrict__ d_n, in
     counts[threadIdx.x * tiles + blockIdx.x] = hist[threadIdx.x];
 }
 
-// Exclusive scan of len entries in place (one block).
+// Exclusive scan of len entries in place (one block).  Each warp owns a
+// contiguous chunk and reads it in coalesced rounds of 32: first to total
+// the chunk, then -- after the chunk totals are scanned -- to write the
+// exclusive prefix with a warp scan per round.
 __global__ void __launch_bounds__(RX_SCAN_THREADS)
 k_radix_scan(unsigned *__restrict__ counts, int len)
 {
-    __shared__ unsigned part[RX_SCAN_THREADS];
-    const int per = (len + RX_SCAN_THREADS - 1) / RX_SCAN_THREADS;
-    const int b = threadIdx.x * per;
-    const int e = min(len, b + per);
+    constexpr int W = RX_SCAN_THREADS / 32;
+    __shared__ unsigned wsum[W];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int chunk = ((len + W - 1) / W + 31) & ~31;
+    const int b = warp * chunk;
+    const int e = min(len, b + chunk);
     unsigned s = 0;
-    for (int i = b; i < e; ++i) s += counts[i];
-    part[threadIdx.x] = s;
+    for (int i = b + lane; i < e; i += 32) s += counts[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) wsum[warp] = s;
     __syncthreads();
-    for (int off = 1; off < RX_SCAN_THREADS; off <<= 1) {
-        const unsigned v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
-        __syncthreads();
-        part[threadIdx.x] += v;
-        __syncthreads();
+    if (warp == 0) {
+        unsigned v = lane < W ? wsum[lane] : 0u;
+        unsigned incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane < W) wsum[lane] = incl - v;
     }
-    unsigned run = threadIdx.x ? part[threadIdx.x - 1] : 0u;
-    for (int i = b; i < e; ++i) {
-        const unsigned c = counts[i];
-        counts[i] = run;
-        run += c;
+    __syncthreads();
+    unsigned run = wsum[warp];
+    for (int i0 = b; i0 < e; i0 += 32) {
+        const int i = i0 + lane;
+        const unsigned c = i < e ? counts[i] : 0u;
+        unsigned incl = c;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (i < e) counts[i] = run + incl - c;
+        run += __shfl_sync(0xffffffffu, incl, 31);
     }
 }
 

@@ -252,7 +252,10 @@ namespace {
 
 class BarnesHutEngine final : public Engine {
   public:
-    BarnesHutEngine(bool compat, bool quad) : compat_(compat), quad_(quad && !compat) {}
+    BarnesHutEngine(bool compat, bool quad, bool group)
+        : compat_(compat), quad_(quad && !compat), group_(group && !compat)
+    {
+    }
 
     ErrorStatus setup(int n, double G, const AccelerationParam &p) override
     {
@@ -293,6 +296,12 @@ class BarnesHutEngine final : public Engine {
         w.status = reinterpret_cast<unsigned *>(tree_.ctr.as<int>() + CTR_STATUS);
         w.gate = nullptr;
         GS_CUDA(cudaMemsetAsync(counters_.p, 0, 2 * sizeof(unsigned long long), s));
+        if (group_) {
+            if (timer) GS_TRY(timer->begin(s));
+            GS_TRY(launch_bh_group_walk(tree_, theta_, eps_, G_, d_a, w.counters, s));
+            if (timer) GS_TRY(timer->end(s));
+            return ok();
+        }
         if (timer) GS_TRY(timer->begin(s));
         const int grid = (n_ + WK_THREADS - 1) / WK_THREADS;
         if (quad_)
@@ -329,7 +338,7 @@ class BarnesHutEngine final : public Engine {
     }
 
   private:
-    bool compat_, quad_;
+    bool compat_, quad_, group_;
     int n_ = 0;
     double G_ = 1.0, eps_ = 0.0, theta_ = 1.0;
     OctreeDevice tree_;
@@ -338,9 +347,9 @@ class BarnesHutEngine final : public Engine {
 
 }  // namespace
 
-std::unique_ptr<Engine> make_barnes_hut_engine(bool compat, bool quad)
+std::unique_ptr<Engine> make_barnes_hut_engine(bool compat, bool quad, bool group)
 {
-    return std::unique_ptr<Engine>(new BarnesHutEngine(compat, quad));
+    return std::unique_ptr<Engine>(new BarnesHutEngine(compat, quad, group));
 }
 
 // Walk of a built (non-compat) tree, for engines that walk one tree several

@@ -1,0 +1,417 @@
+// k_walk_group.cu -- group Barnes-Hut walk with interaction lists
+// (GRAV_GPU_BARNES_HUT_GROUP).
+//
+// The per-particle walk of k_walk.cu reproduces the reference's decisions
+// (src/acceleration_barnes_hut.c:78-248) one child at a time, which costs
+// about 200 instructions per accepted cell.  This walk trades identical
+// decisions for throughput:
+//   * groups come from the tree: every cell with at most 32 particles whose
+//     parent has more is one group (a leaf with more is cut into runs of
+//     32), so a group never spans more than one cell and its box stays
+//     compact where the Morton curve jumps;
+//   * a persistent warp takes groups from a work queue and walks the tree
+//     once per group, 32 nodes per step (one per lane), with the group
+//     opening criterion
+//         accept node  <=>  the node holds none of the group's particles
+//                           (sorted ranges disjoint) and
+//                           side^2 < theta^2 * dist(com, group box)^2,
+//     which implies the per-particle criterion side^2 < theta^2 |com - x|^2
+//     of the reference for every particle of the group, so the accepted
+//     cells are at least as well separated as the reference's;
+//   * accepted cells (centre of mass, mass, traceless quadrupole) and the
+//     particles of opened leaves go to interaction lists in shared memory;
+//     when a list is full every lane evaluates it against its own particle
+//     (one broadcast shared-memory load per entry, dense FP32 FMA work) and
+//     adds the partial sum to a Kahan-compensated accumulator;
+//   * coordinates are FP32 offsets from the group's first particle, formed
+//     from the frame-centred double-float (hi, lo) copies of the tree, so
+//     near-field differences keep FP32 relative accuracy.
+// Every wait is on __syncwarp only; a traversal stack that would overflow
+// sets ST_STACK_OVERFLOW and ends the warp's walk (no spin, no trap).
+#include "gs_octree.h"
+#include "gs_ptx.cuh"
+
+namespace gs {
+
+constexpr int GW_WARPS = 4;        // groups per CTA
+constexpr int GW_STACK = 1024;     // traversal stack entries per warp
+constexpr int GW_CELLS = 128;      // cell list capacity per warp
+constexpr int GW_PARTS = 128;      // particle list capacity per warp
+// Stack entries kept free for a depth-first descent: popping one node and
+// pushing its (at most 8) children grows the stack by 7 per level, over at
+// most OCT_MAX_LEVEL + 1 levels.  Batches shrink so that the stack never
+// passes GW_STACK - GW_RESERVE before such a descent starts, hence never
+// overflows.
+constexpr int GW_RESERVE = 8 * (OCT_MAX_LEVEL + 1);
+
+constexpr int GW_GROUP = 32;       // particles per group at most
+
+// Group list: one thread per node.  Cells with more than GW_GROUP particles
+// cut their children's particle ranges into groups; the root is one group
+// when it is small enough.
+__global__ void k_group_list(const int *__restrict__ ctr, const int4 *__restrict__ nc,
+                             int2 *__restrict__ groups, int *__restrict__ gctr)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ctr[CTR_NODES]) return;
+    const int4 ci = nc[c];   // (first child, children, first particle, particles)
+    if (ci.w <= 0) return;
+    if (c == 0 && ci.w <= GW_GROUP) {
+        groups[atomicAdd(&gctr[0], 1)] = make_int2(ci.z, ci.w);
+        return;
+    }
+    if (ci.w <= GW_GROUP) return;   // its own parent groups it
+    if (ci.y <= 0) {                // oversized leaf (depth limit): runs of GW_GROUP
+        for (int b = 0; b < ci.w; b += GW_GROUP)
+            groups[atomicAdd(&gctr[0], 1)] = make_int2(ci.z + b, min(GW_GROUP, ci.w - b));
+        return;
+    }
+    // each child cell small enough is one group: a group never spans more
+    // than one cell (merging siblings would let a sparse group span its
+    // whole parent and open everything near it)
+    for (int k = 0; k < ci.y; ++k) {
+        const int4 ch = nc[ci.x + k];
+        if (ch.w > 0 && ch.w <= GW_GROUP)
+            groups[atomicAdd(&gctr[0], 1)] = make_int2(ch.z, ch.w);
+    }
+}
+
+struct GroupWalkArgs {
+    const float4 *na;       // (com_hi, mass)
+    const float4 *nb;       // (com_lo, 0)
+    const float4 *nq;       // 2 per node: (xx, xy, xz, yy), (yz, zz, -, -)
+    const int4 *nc;         // (first child, children, first particle, particles)
+    const int *depth;
+    const float4 *pa;       // sorted particles (x_hi, m)
+    const float4 *pb;       // (x_lo, 0)
+    const int *sidx;
+    const double *frame;
+    int n;
+    float eps2;
+    float theta2;
+    double G;
+    double *a;
+    unsigned long long *counters;
+    unsigned *status;
+    const int *gate;        // when set, the launch runs only if *gate != 0
+    const int2 *groups;     // (first sorted particle, count)
+    int *gctr;              // [0] groups, [1] work-queue head
+};
+
+struct GroupShared {
+    int stack[GW_STACK];
+    float4 cell[GW_CELLS];
+    float4 cq0[GW_CELLS], cq1[GW_CELLS];
+    float4 part[GW_PARTS];
+};
+
+template <bool QUAD>
+__device__ __forceinline__ void flush_cells(const GroupShared &g, int count, float rx, float ry,
+                                            float rz, float eps2, float &sx, float &cx, float &sy,
+                                            float &cy, float &sz, float &cz)
+{
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    for (int j = 0; j < count; ++j) {
+        const float4 c = g.cell[j];
+        const float dx = c.x - rx, dy = c.y - ry, dz = c.z - rz;
+        const float ns = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const float ri = rsqrt_approx(ns + eps2);
+        const float ri2 = ri * ri;
+        const float ri3 = ri2 * ri;
+        const float sc = c.w * ri3;
+        ax = fmaf(dx, sc, ax);
+        ay = fmaf(dy, sc, ay);
+        az = fmaf(dz, sc, az);
+        if (QUAD) {
+            // d = com - x:  G [-Q d / r^5 + 2.5 (d.Q.d) d / r^7]
+            const float4 q0 = g.cq0[j], q1 = g.cq1[j];
+            const float qx = q0.x * dx + q0.y * dy + q0.z * dz;
+            const float qy = q0.y * dx + q0.w * dy + q1.x * dz;
+            const float qz = q0.z * dx + q1.x * dy + q1.y * dz;
+            const float dqd = dx * qx + dy * qy + dz * qz;
+            const float ri5 = ri3 * ri2;
+            const float f = 2.5f * dqd * ri5 * ri2;
+            ax += f * dx - qx * ri5;
+            ay += f * dy - qy * ri5;
+            az += f * dz - qz * ri5;
+        }
+    }
+    kahan_add(sx, cx, ax);
+    kahan_add(sy, cy, ay);
+    kahan_add(sz, cz, az);
+}
+
+__device__ __forceinline__ void flush_parts(const GroupShared &g, int count, float rx, float ry,
+                                            float rz, float eps2, float &sx, float &cx, float &sy,
+                                            float &cy, float &sz, float &cz)
+{
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    for (int j = 0; j < count; ++j) {
+        const float4 q = g.part[j];
+        const float dx = q.x - rx, dy = q.y - ry, dz = q.z - rz;
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+        const float ri = r2 > 0.0f ? rsqrt_approx(r2) : 0.0f;   // own term without softening
+        const float sc = q.w * ri * ri * ri;
+        ax = fmaf(dx, sc, ax);
+        ay = fmaf(dy, sc, ay);
+        az = fmaf(dz, sc, az);
+    }
+    kahan_add(sx, cx, ax);
+    kahan_add(sy, cy, ay);
+    kahan_add(sz, cz, az);
+}
+
+template <bool QUAD>
+__global__ void __launch_bounds__(32 * GW_WARPS)
+k_bh_group(GroupWalkArgs A)
+{
+    extern __shared__ __align__(16) unsigned char gw_smem[];
+    __shared__ float s_w2[OCT_MAX_LEVEL + 2];   // (cell side at depth d)^2
+    if (A.gate && *A.gate == 0) return;          // block-uniform
+    GroupShared &g = reinterpret_cast<GroupShared *>(gw_smem)[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x <= OCT_MAX_LEVEL + 1) {
+        // side of a depth-d cell: box_length / (2 << d)
+        const double w = A.frame[4] / (double)(2 << threadIdx.x);
+        s_w2[threadIdx.x] = (float)(w * w);
+    }
+    __syncthreads();
+
+    const int ngroups = A.gctr[0];
+    for (;;) {
+    int gi = 0;
+    if (lane == 0) gi = atomicAdd(&A.gctr[1], 1);
+    gi = __shfl_sync(0xffffffffu, gi, 0);
+    if (gi >= ngroups) break;   // warp-uniform
+    const int2 grp = A.groups[gi];
+    const int g0 = grp.x;
+    const int gend = g0 + grp.y;
+    const int s = g0 + lane;
+    const bool valid = s < gend;
+    // origin: the group's first particle (double-float)
+    const float4 oh = A.pa[g0], ol = A.pb[g0];
+    float rx = 0.f, ry = 0.f, rz = 0.f;
+    if (valid) {
+        const float4 ph = A.pa[s], pl = A.pb[s];
+        rx = (ph.x - oh.x) + (pl.x - ol.x);
+        ry = (ph.y - oh.y) + (pl.y - ol.y);
+        rz = (ph.z - oh.z) + (pl.z - ol.z);
+    }
+    float bx0 = valid ? rx : 3.0e38f, by0 = valid ? ry : 3.0e38f, bz0 = valid ? rz : 3.0e38f;
+    float bx1 = valid ? rx : -3.0e38f, by1 = valid ? ry : -3.0e38f, bz1 = valid ? rz : -3.0e38f;
+    for (int o = 16; o > 0; o >>= 1) {
+        bx0 = fminf(bx0, __shfl_xor_sync(0xffffffffu, bx0, o));
+        by0 = fminf(by0, __shfl_xor_sync(0xffffffffu, by0, o));
+        bz0 = fminf(bz0, __shfl_xor_sync(0xffffffffu, bz0, o));
+        bx1 = fmaxf(bx1, __shfl_xor_sync(0xffffffffu, bx1, o));
+        by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, o));
+        bz1 = fmaxf(bz1, __shfl_xor_sync(0xffffffffu, bz1, o));
+    }
+    const float th2 = A.theta2;
+    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    unsigned long long n_cell = 0, n_pp = 0;
+
+    if (lane == 0) g.stack[0] = 0;   // root
+    int top = 1, ncell = 0, npart = 0;
+    __syncwarp();
+    while (top > 0) {
+        // pop k nodes, leaving room for up to 8 children of each
+        int k = min(32, top);
+        const int room = (GW_STACK - GW_RESERVE - top) / 7;
+        if (room < k) k = max(1, room);
+        const int node = lane < k ? g.stack[top - k + lane] : -1;
+        top -= k;
+        __syncwarp();
+        int act = 0;   // 1 accept, 2 leaf, 3 open
+        int4 ci = make_int4(0, 0, 0, 0);
+        float4 crel = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (node >= 0) {
+            const float4 ca = A.na[node], cb = A.nb[node];
+            ci = A.nc[node];
+            crel = make_float4((ca.x - oh.x) + (cb.x - ol.x), (ca.y - oh.y) + (cb.y - ol.y),
+                               (ca.z - oh.z) + (cb.z - ol.z), ca.w);
+            const bool own = ci.z < gend && ci.z + ci.w > g0;
+            const float ex = fmaxf(fmaxf(bx0 - crel.x, crel.x - bx1), 0.f);
+            const float ey = fmaxf(fmaxf(by0 - crel.y, crel.y - by1), 0.f);
+            const float ez = fmaxf(fmaxf(bz0 - crel.z, crel.z - bz1), 0.f);
+            const float d2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+            const float w2 = s_w2[min(A.depth[node], OCT_MAX_LEVEL + 1)];
+            if (!own && w2 < th2 * d2 && ca.w > 0.f)
+                act = 1;
+            else if (ci.y <= 0)
+                act = (ci.w > 0) ? 2 : 0;
+            else
+                act = 3;
+            if (!own && ca.w <= 0.f && w2 < th2 * d2) act = 0;   // empty cell: nothing to add
+        }
+        // accepted cells
+        const unsigned acc = __ballot_sync(0xffffffffu, act == 1);
+        if (acc) {
+            if (ncell + __popc(acc) > GW_CELLS) {
+                __syncwarp();
+                if (valid) flush_cells<QUAD>(g, ncell, rx, ry, rz, A.eps2, sx, cx, sy, cy, sz, cz);
+                n_cell += valid ? ncell : 0;
+                ncell = 0;
+                __syncwarp();
+            }
+            if (act == 1) {
+                const int at = ncell + __popc(acc & ((1u << lane) - 1u));
+                g.cell[at] = crel;
+                if (QUAD) {
+                    g.cq0[at] = A.nq[2 * node];
+                    g.cq1[at] = A.nq[2 * node + 1];
+                }
+            }
+            ncell += __popc(acc);
+        }
+        // particles of leaves that are not accepted
+        const int cnt = (act == 2) ? ci.w : 0;
+        int incl = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        if (total > 0) {
+            if (total <= GW_PARTS) {
+                if (npart + total > GW_PARTS) {
+                    __syncwarp();
+                    if (valid) flush_parts(g, npart, rx, ry, rz, A.eps2, sx, cx, sy, cy, sz, cz);
+                    n_pp += valid ? npart : 0;
+                    npart = 0;
+                    __syncwarp();
+                }
+                for (int q = 0; q < cnt; ++q) {
+                    const int p = ci.z + q;
+                    const float4 qa = A.pa[p], qb = A.pb[p];
+                    g.part[npart + incl - cnt + q] =
+                        make_float4((qa.x - oh.x) + (qb.x - ol.x), (qa.y - oh.y) + (qb.y - ol.y),
+                                    (qa.z - oh.z) + (qb.z - ol.z), qa.w);
+                }
+                npart += total;
+                __syncwarp();
+            } else {
+                // large leaves: one lane's leaf at a time, 32 particles per round
+                unsigned leaves = __ballot_sync(0xffffffffu, cnt > 0);
+                while (leaves) {
+                    const int src = __ffs(leaves) - 1;
+                    leaves &= leaves - 1;
+                    const int first = __shfl_sync(0xffffffffu, ci.z, src);
+                    const int num = __shfl_sync(0xffffffffu, cnt, src);
+                    for (int b = 0; b < num; b += 32) {
+                        const int m32 = min(32, num - b);
+                        if (npart + m32 > GW_PARTS) {
+                            __syncwarp();
+                            if (valid)
+                                flush_parts(g, npart, rx, ry, rz, A.eps2, sx, cx, sy, cy, sz, cz);
+                            n_pp += valid ? npart : 0;
+                            npart = 0;
+                            __syncwarp();
+                        }
+                        if (lane < m32) {
+                            const int p = first + b + lane;
+                            const float4 qa = A.pa[p], qb = A.pb[p];
+                            g.part[npart + lane] = make_float4(
+                                (qa.x - oh.x) + (qb.x - ol.x), (qa.y - oh.y) + (qb.y - ol.y),
+                                (qa.z - oh.z) + (qb.z - ol.z), qa.w);
+                        }
+                        npart += m32;
+                        __syncwarp();
+                    }
+                }
+            }
+        }
+        // children of opened nodes
+        const int ch = (act == 3) ? ci.y : 0;
+        int cin = ch;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, cin, o);
+            if (lane >= o) cin += t;
+        }
+        const int pushes = __shfl_sync(0xffffffffu, cin, 31);
+        if (top + pushes > GW_STACK) {
+            if (lane == 0) atomicOr(A.status, ST_STACK_OVERFLOW);
+            break;
+        }
+        for (int q = 0; q < ch; ++q) g.stack[top + cin - ch + q] = ci.x + q;
+        top += pushes;
+        __syncwarp();
+    }
+    __syncwarp();
+    if (valid && ncell > 0) flush_cells<QUAD>(g, ncell, rx, ry, rz, A.eps2, sx, cx, sy, cy, sz, cz);
+    if (valid && npart > 0) flush_parts(g, npart, rx, ry, rz, A.eps2, sx, cx, sy, cy, sz, cz);
+    if (valid) {
+        n_cell += ncell;
+        n_pp += npart - 1;   // every particle meets itself once in its own leaf
+        const int id = A.sidx[s];
+        A.a[3 * id + 0] = A.G * ((double)sx - (double)cx);
+        A.a[3 * id + 1] = A.G * ((double)sy - (double)cy);
+        A.a[3 * id + 2] = A.G * ((double)sz - (double)cz);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        n_cell += __shfl_down_sync(0xffffffffu, n_cell, o);
+        n_pp += __shfl_down_sync(0xffffffffu, n_pp, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&A.counters[0], n_cell);
+        atomicAdd(&A.counters[1], n_pp);
+    }
+    __syncwarp();
+    }   // next group
+}
+
+ErrorStatus launch_bh_group_walk(const OctreeDevice &t, double theta, double eps, double G,
+                                 double *d_a, unsigned long long *counters, cudaStream_t s,
+                                 const int *gate)
+{
+    static_assert(sizeof(GroupShared) % 16 == 0, "group shared block alignment");
+    const size_t smem = sizeof(GroupShared) * GW_WARPS;
+    static bool attr_set = false;
+    if (!attr_set) {
+        GS_CUDA(cudaFuncSetAttribute(k_bh_group<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+        GS_CUDA(cudaFuncSetAttribute(k_bh_group<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+        attr_set = true;
+    }
+    GroupWalkArgs w;
+    w.na = t.w_na.as<float4>();
+    w.nb = t.w_nb.as<float4>();
+    w.nq = t.quad ? t.w_nq.as<float4>() : nullptr;
+    w.nc = t.w_nc.as<int4>();
+    w.depth = t.t_depth.as<int>();
+    w.pa = t.w_pa.as<float4>();
+    w.pb = t.w_pb.as<float4>();
+    w.sidx = t.sidx.as<int>();
+    w.frame = t.frame.as<double>();
+    w.n = t.n;
+    w.eps2 = (float)(eps * eps);
+    w.theta2 = (float)(theta * theta);
+    w.G = G;
+    w.a = d_a;
+    w.counters = counters;
+    w.status = reinterpret_cast<unsigned *>(t.ctr.as<int>() + CTR_STATUS);
+    w.gate = gate;
+    w.groups = t.g_list.as<int2>();
+    w.gctr = t.g_ctr.as<int>();
+    GS_CUDA(cudaMemsetAsync(t.g_ctr.p, 0, 2 * sizeof(int), s));
+    k_group_list<<<(t.cap_nodes + 255) / 256, 256, 0, s>>>(t.ctr.as<int>(), t.w_nc.as<int4>(),
+                                                          t.g_list.as<int2>(), w.gctr);
+    static int grid = 0;   // persistent: every SM filled once
+    if (grid == 0) {
+        const DeviceInfo *dev = nullptr;
+        GS_TRY(device_info(&dev));
+        int per_sm = 0;
+        GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bh_group<true>,
+                                                              32 * GW_WARPS, smem));
+        grid = dev->sm_count * (per_sm > 0 ? per_sm : 1);
+    }
+    if (t.quad)
+        k_bh_group<true><<<grid, 32 * GW_WARPS, smem, s>>>(w);
+    else
+        k_bh_group<false><<<grid, 32 * GW_WARPS, smem, s>>>(w);
+    GS_CUDA(cudaGetLastError());
+    return ok();
+}
+
+}  // namespace gs

@@ -832,6 +832,63 @@ struct gsgpu_ensemble {
     }
 
     int pgrid() const { return (P + 127) / 128; }
+    int tpb_accel = 128, tpb_drift = 128;   // chosen by autotune()
+    bool tuned = false;
+    int grid_for(int t) const { return (P + t - 1) / t; }
+
+    // Thread-block sizes of the per-particle kernels, timed once on this
+    // ensemble right after its first half kick (before any graph capture).
+    // Only launches that leave the simulation unchanged are timed: the
+    // accelerations are recomputed from the same positions, and the drift
+    // runs on scratch copies of the Jacobi arrays with removals off.
+    ErrorStatus autotune()
+    {
+        if (tuned) return ok();
+        tuned = true;
+        const int cand[4] = {64, 128, 256, 512};
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        GS_CUDA(cudaEventCreate(&e0));
+        GS_CUDA(cudaEventCreate(&e1));
+        ErrorStatus st = ok();
+        auto best_of = [&](auto launch, int &choice) {
+            float best = 1e30f;
+            for (int t : cand) {
+                launch(t);
+                if (cudaEventRecord(e0, stream) != cudaSuccess) break;
+                launch(t);
+                launch(t);
+                if (cudaEventRecord(e1, stream) != cudaSuccess) break;
+                if (cudaEventSynchronize(e1) != cudaSuccess) break;
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms < best) {
+                    best = ms;
+                    choice = t;
+                }
+            }
+        };
+        if (integrator == INTEGRATOR_WHFAST) {
+            best_of([&](int t) { k_wh_accel<<<grid_for(t), t, 0, stream>>>(E, P); }, tpb_accel);
+            EnsDev Es = E;
+            Es.jx = E.t_x;
+            Es.jv = E.t_v;
+            Es.remove_invalid = 0;
+            cudaMemcpyAsync(E.t_x, E.jx, (size_t)P * 3 * sizeof(double), cudaMemcpyDeviceToDevice,
+                            stream);
+            cudaMemcpyAsync(E.t_v, E.jv, (size_t)P * 3 * sizeof(double), cudaMemcpyDeviceToDevice,
+                            stream);
+            best_of([&](int t) { k_wh_drift<<<grid_for(t), t, 0, stream>>>(Es, P, dt); },
+                    tpb_drift);
+        } else {
+            best_of([&](int t) { k_ens_massless_accel<<<grid_for(t), t, 0, stream>>>(E, P); },
+                    tpb_accel);
+        }
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) st = GS_RAISE(GRAV_FAILURE, "ensemble autotune: %s", cudaGetErrorString(e));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return st;
+    }
 
     ErrorStatus sort(double *vec, double *vel)
     {
@@ -848,10 +905,10 @@ struct gsgpu_ensemble {
     {
         if (integrator == INTEGRATOR_WHFAST) {
             k_wh_pairs<<<(S + PAIR_WARPS - 1) / PAIR_WARPS, 32 * PAIR_WARPS, 0, stream>>>(E);
-            k_wh_accel<<<pgrid(), 128, 0, stream>>>(E, P);
+            k_wh_accel<<<grid_for(tpb_accel), tpb_accel, 0, stream>>>(E, P);
         }
         else
-            k_ens_massless_accel<<<pgrid(), 128, 0, stream>>>(E, P);
+            k_ens_massless_accel<<<grid_for(tpb_accel), tpb_accel, 0, stream>>>(E, P);
         GS_CUDA(cudaGetLastError());
         return ok();
     }
@@ -872,6 +929,7 @@ struct gsgpu_ensemble {
         }
         GS_CUDA(cudaGetLastError());
         primed = true;
+        GS_TRY(autotune());
         return ok();
     }
 
@@ -880,7 +938,7 @@ struct gsgpu_ensemble {
         if (integrator == INTEGRATOR_WHFAST) {
             // src/integrator_whfast.c:290-343
             GS_TRY(sort(E.jx, E.jv));
-            k_wh_drift<<<pgrid(), 128, 0, stream>>>(E, P, h);
+            k_wh_drift<<<grid_for(tpb_drift), tpb_drift, 0, stream>>>(E, P, h);
             k_wh_seq<<<seq_grid(), 32 * SEQ_WARPS, 0, stream>>>(E, 1);
             GS_TRY(accel());
             k_wh_kick<<<pgrid(), 128, 0, stream>>>(E, P, h);
@@ -1177,6 +1235,14 @@ int gsgpu_ensemble_download(gsgpu_ensemble *e, int *counts, int *ids, double *x,
 int gsgpu_ensemble_kernels_per_step(const gsgpu_ensemble *e) { return e ? e->kernels_per_step() : 0; }
 
 int gsgpu_ensemble_num_particles(const gsgpu_ensemble *e) { return e ? e->P : 0; }
+
+int gsgpu_ensemble_tuning(const gsgpu_ensemble *e, int *accel_threads, int *drift_threads)
+{
+    if (!e) return GRAV_POINTER_ERROR;
+    if (accel_threads) *accel_threads = e->tuned ? e->tpb_accel : 0;
+    if (drift_threads) *drift_threads = e->tuned ? e->tpb_drift : 0;
+    return 0;
+}
 
 void gsgpu_ensemble_destroy(gsgpu_ensemble *e) { delete e; }
 

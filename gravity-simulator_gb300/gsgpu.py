@@ -47,6 +47,7 @@ METHOD_GPU_MASSLESS = 102          # FP64 massive/massless direct sum
 METHOD_GPU_BARNES_HUT = 103        # FP32 walk, true leaf multipoles
 METHOD_GPU_BH_LEARNED = 104        # theta-cheap walk + learned MLP residual
 METHOD_GPU_BARNES_HUT_QUAD = 105   # FP32 walk, monopole + quadrupole cell terms
+METHOD_GPU_BARNES_HUT_GROUP = 106  # group walk with interaction lists, quadrupole cells
 METHOD_GPU_PAIRWISE_FP64 = 111     # FP64 direct sum in the reference's order
 METHOD_GPU_BARNES_HUT_COMPAT = 113 # FP32 walk reproducing the reference's tree quirks
 
@@ -341,6 +342,13 @@ class Ensemble:
     def kernels_per_step(self) -> int:
         return int(self.lib.gsgpu_ensemble_kernels_per_step(self.handle))
 
+    def tuning(self):
+        """(accel, drift) thread-block sizes chosen by the autotuner."""
+        a, d = ctypes.c_int(), ctypes.c_int()
+        self._check(self.lib.gsgpu_ensemble_tuning(self.handle, ctypes.byref(a), ctypes.byref(d)),
+                    "gsgpu_ensemble_tuning")
+        return a.value, d.value
+
     def close(self) -> None:
         if getattr(self, "handle", None):
             self.lib.gsgpu_ensemble_destroy(self.handle)
@@ -372,6 +380,8 @@ def _init_ensemble_api(lib: ctypes.CDLL) -> None:
                                             c_double_p]
     lib.gsgpu_ensemble_kernels_per_step.restype = ctypes.c_int
     lib.gsgpu_ensemble_kernels_per_step.argtypes = [vp]
+    lib.gsgpu_ensemble_tuning.restype = ctypes.c_int
+    lib.gsgpu_ensemble_tuning.argtypes = [vp, c_int_p, c_int_p]
     lib.gsgpu_ensemble_destroy.restype = None
     lib.gsgpu_ensemble_destroy.argtypes = [vp]
     lib._ensemble_api = True

@@ -65,6 +65,7 @@ typedef struct System {
 #define GRAV_GPU_BARNES_HUT 103         /* FP32 walk, true leaf multipoles */
 #define GRAV_GPU_BH_LEARNED 104         /* theta-cheap walk + learned residual */
 #define GRAV_GPU_BARNES_HUT_QUAD 105    /* FP32 walk, monopole + quadrupole cells */
+#define GRAV_GPU_BARNES_HUT_GROUP 106   /* group walk, interaction lists, quadrupoles */
 #define GRAV_GPU_PAIRWISE_FP64 111      /* FP64 direct sum, reference order */
 #define GRAV_GPU_BARNES_HUT_COMPAT 113  /* FP32 walk, reference tree quirks */
 
@@ -283,7 +284,8 @@ int gsgpu_sim_warmup_until_ready(gsgpu_sim *sim, int64_t max_steps, int64_t *ste
  * trained, snapshots, first-epoch loss, last-epoch loss, held-out median
  * residual before and after the network, last judged median error, steps
  * judged, steps that fell back, cheap opening angle, training seconds, Adam
- * steps). */
+ * steps, network in use: 1 if it cut the held-out median residual by at
+ * least 20 %, else 0 and every step uses the judged fallback walk). */
 int gsgpu_sim_report(gsgpu_sim *sim, double *out, int nmax);
 /* Learned method: copy up to `count` training samples of one snapshot
  * (features [count][32], targets [count][3]); returns the number copied. */
@@ -320,6 +322,10 @@ int gsgpu_ensemble_download(gsgpu_ensemble *e, int *counts, int *ids, double *x,
                             double *v, double *m);
 int gsgpu_ensemble_kernels_per_step(const gsgpu_ensemble *e);
 int gsgpu_ensemble_num_particles(const gsgpu_ensemble *e);
+/* Thread-block sizes the ensemble's autotuner chose for its per-particle
+ * acceleration and drift kernels (timed once after the first half kick;
+ * 0 before that). */
+int gsgpu_ensemble_tuning(const gsgpu_ensemble *e, int *accel_threads, int *drift_threads);
 void gsgpu_ensemble_destroy(gsgpu_ensemble *e);
 
 /* Library / device information: fills name (NUL-terminated, <= len). */

@@ -170,3 +170,70 @@ def test_fixed_walk_accuracy_vs_direct_sum(lib, g, orc, wl):
     err = orc.rel_err(a[rows], exact)
     print(f"fixed theta=0.5 median {np.median(err):.3g} p99 {np.quantile(err, 0.99):.3g}")
     assert np.median(err) < 3e-3
+
+
+@pytest.mark.parametrize("theta,leaf", [(0.5, 1), (0.8, 1), (0.5, 64)])
+def test_group_walk_accuracy(lib, g, orc, wl, theta, leaf):
+    """Group walk (106): its group opening criterion implies the per-particle
+    one for every particle, so it is at least about as accurate as the
+    per-particle quadrupole walk (105) at the same theta.  leaf=64 exercises
+    leaves that overflow one list round."""
+    x, v, m = wl.galaxy_pair(131072, 7)
+    rows = np.random.default_rng(3).choice(x.shape[0], 2048, replace=False).astype(np.int32)
+    exact = orc.direct_rows(x, m, 1.0, 0.01, rows)
+    kw = dict(opening_angle=theta, softening_length=0.01, max_num_particles_per_leaf=leaf)
+    a_g = g.acceleration(lib, x, m, 1.0, g.METHOD_GPU_BARNES_HUT_GROUP, **kw)
+    cells, pairs = gpu_counts(lib)
+    a_q = g.acceleration(lib, x, m, 1.0, g.METHOD_GPU_BARNES_HUT_QUAD, **kw)
+    e_g = np.median(orc.rel_err(a_g[rows], exact))
+    e_q = np.median(orc.rel_err(a_q[rows], exact))
+    print(f"theta={theta} leaf={leaf}: group {e_g:.3g} ({cells} cells, {pairs} pairs), "
+          f"per-particle quad {e_q:.3g}")
+    assert np.isfinite(a_g).all()
+    assert e_g <= 1.1 * e_q
+    assert cells > 0 and pairs > 0
+
+
+def test_group_walk_degenerate_and_unsoftened(lib, g, orc, wl):
+    """A 200-particle coincident cluster (one depth-21 leaf with more
+    particles than one list round) with softening, and an unsoftened
+    Plummer sphere (the particle's own term is skipped)."""
+    x, v, m = wl.plummer(20000, 11)
+    x[100:300] = x[50]
+    rows = np.arange(40, 340, dtype=np.int32)
+    exact = orc.direct_rows(x, m, 1.0, 0.01, rows)
+    a = g.acceleration(lib, x, m, 1.0, g.METHOD_GPU_BARNES_HUT_GROUP, opening_angle=0.6,
+                       softening_length=0.01, max_num_particles_per_leaf=1)
+    assert np.isfinite(a).all()
+    assert np.median(orc.rel_err(a[rows], exact)) < 2e-3
+    x2, v2, m2 = wl.plummer(20000, 12)
+    rows2 = np.random.default_rng(4).choice(20000, 512, replace=False).astype(np.int32)
+    exact2 = orc.direct_rows(x2, m2, 1.0, 0.0, rows2)
+    a2 = g.acceleration(lib, x2, m2, 1.0, g.METHOD_GPU_BARNES_HUT_GROUP, opening_angle=0.5,
+                        softening_length=0.0, max_num_particles_per_leaf=1)
+    assert np.isfinite(a2).all()
+    assert np.median(orc.rel_err(a2[rows2], exact2)) < 2e-3
+
+
+def test_group_walk_in_simulation(lib, g, wl):
+    """The group walk drives launch_simulation (graph-captured leapfrog)."""
+    x, v, m = wl.galaxy_pair(32768, 8)
+    _, xo, vo, _ = g.launch_simulation(lib, x.copy(), v.copy(), m, 1.0, integrator=4, dt=1e-3,
+                                       tf=0.01, method=g.METHOD_GPU_BARNES_HUT_GROUP,
+                                       opening_angle=0.5, softening_length=0.01,
+                                       max_num_particles_per_leaf=1)
+    assert np.isfinite(xo).all() and np.isfinite(vo).all()
+    assert np.abs(xo - x).max() < 0.1
+
+
+def test_group_walk_galaxy_1m(lib, g, orc, wl):
+    """The full-size galaxy model: dense centres stress the traversal stack
+    (an overflow would be reported as an error), accuracy stays below the
+    per-particle criterion's."""
+    x, v, m = wl.galaxy_pair(1048576, 5)
+    a = g.acceleration(lib, x, m, 1.0, g.METHOD_GPU_BARNES_HUT_GROUP, opening_angle=0.5,
+                       softening_length=0.01, max_num_particles_per_leaf=1)
+    rows = np.random.default_rng(5).choice(x.shape[0], 256, replace=False).astype(np.int32)
+    err = orc.rel_err(a[rows], orc.direct_rows(x, m, 1.0, 0.01, rows))
+    print(f"group walk N=1048576 theta=0.5: median {np.median(err):.3g}")
+    assert np.isfinite(a).all() and np.median(err) < 1e-3

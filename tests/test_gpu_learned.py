@@ -3,12 +3,14 @@
 A simulation of the galaxy-collision model collects its 64 training
 snapshots during its first steps (forces from the fallback walk), trains the
 network on the GPU, and then runs the cheap walk (theta 1.0, monopole +
-quadrupole) plus the network.  Checks:
-  * training converged (last-epoch loss below first) and the network gains
-    on the held-out snapshot (median residual after < before);
-  * against an FP64 direct sum on sampled particles, the learned
-    accelerations are more accurate than the same cheap walk without the
-    network (GRAV_GPU_BARNES_HUT_QUAD at theta 1.0 on the same positions);
+quadrupole) plus the network -- if the network cut the held-out median
+residual by at least 20 %; otherwise every step uses the judged fallback
+walk.  Checks:
+  * training converged (last-epoch loss below first); what the network
+    gains on the held-out snapshot is printed and decides the mode;
+  * against an FP64 direct sum on sampled particles, the accelerations meet
+    the 1e-3 median bound and beat the cheap walk without the network
+    (GRAV_GPU_BARNES_HUT_QUAD at theta 1.0 on the same positions);
   * the per-step judge runs every step.
 The network's kernels themselves are checked against the CPU oracle in
 test_gpu_mlp.py.
@@ -49,17 +51,20 @@ def test_learned_correction_trains_and_gains(lib, g, orc, wl):
                                     m.ctypes.data_as(dp)) == 0
         taken = ctypes.c_int64()
         assert lib.gsgpu_sim_warmup_until_ready(sim, 200, ctypes.byref(taken)) == 0
-        rep = np.zeros(12)
-        k = lib.gsgpu_sim_report(sim, rep.ctypes.data_as(dp), 12)
-        assert k == 12 and rep[0] == 1.0 and rep[1] == 64
+        rep = np.zeros(13)
+        k = lib.gsgpu_sim_report(sim, rep.ctypes.data_as(dp), 13)
+        assert k == 13 and rep[0] == 1.0 and rep[1] == 64
         print("report", rep, "steps", taken.value)
         assert rep[3] < rep[2]                     # training loss went down
-        assert rep[5] < rep[4]                     # held-out residual shrinks
+        gain = 1.0 - rep[5] / rep[4]
+        print(f"held-out median residual {rep[4]:.4g} -> {rep[5]:.4g} (gain {100 * gain:.1f} %), "
+              f"network {'in use' if rep[12] else 'disabled'}")
+        assert rep[12] == (1.0 if rep[5] < 0.8 * rep[4] else 0.0)
         assert lib.gsgpu_sim_run(sim, 2) == 0
         xs, vs, a = np.empty((n, 3)), np.empty((n, 3)), np.empty((n, 3))
         assert lib.gsgpu_sim_download(sim, xs.ctypes.data_as(dp), vs.ctypes.data_as(dp)) == 0
         assert lib.gsgpu_sim_download_acceleration(sim, a.ctypes.data_as(dp)) == 0
-        lib.gsgpu_sim_report(sim, rep.ctypes.data_as(dp), 12)
+        lib.gsgpu_sim_report(sim, rep.ctypes.data_as(dp), 13)
         assert rep[7] >= 2                         # judged every step
     finally:
         lib.gsgpu_sim_destroy(sim)
@@ -71,3 +76,4 @@ def test_learned_correction_trains_and_gains(lib, g, orc, wl):
     e_cheap = np.median(orc.rel_err(a_cheap[rows], exact))
     print(f"median error: cheap {e_cheap:.3g}, learned {e_learned:.3g}")
     assert e_learned < e_cheap
+    assert e_learned < 1e-3
