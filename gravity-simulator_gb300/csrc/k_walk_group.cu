@@ -5,10 +5,12 @@
 // (src/acceleration_barnes_hut.c:78-248) one child at a time, which costs
 // about 200 instructions per accepted cell.  This walk trades identical
 // decisions for throughput:
-//   * groups come from the tree: every cell with at most 32 particles whose
-//     parent has more is one group (a leaf with more is cut into runs of
-//     32), so a group never spans more than one cell and its box stays
-//     compact where the Morton curve jumps;
+//   * groups come from the tree: the children of a cell with more than 32
+//     particles are merged in octant order into runs of at most 32
+//     particles (a leaf with more is cut into runs of 32), so a group lies
+//     in one cell and its box stays compact where the Morton curve jumps;
+//     the one group that does not fit its cell (the particles whose Morton
+//     coordinate wraps at the box maximum) is walked particle by particle;
 //   * a persistent warp takes groups from a work queue and walks the tree
 //     once per group, 32 nodes per step (one per lane), with the group
 //     opening criterion
@@ -46,34 +48,46 @@ constexpr int GW_RESERVE = 8 * (OCT_MAX_LEVEL + 1);
 
 constexpr int GW_GROUP = 32;       // particles per group at most
 
-// Group list: one thread per node.  Cells with more than GW_GROUP particles
-// cut their children's particle ranges into groups; the root is one group
-// when it is small enough.
+// Group list: one thread per node.  A cell with more than GW_GROUP
+// particles merges its children, in octant order, into runs of at most
+// GW_GROUP particles (a leaf with more is cut into runs); the root is one
+// group when it is small enough.  Entry: (first sorted particle,
+// count | depth << 8) with depth that of the cell the group lies in.
+__device__ __forceinline__ void put_group(int2 *groups, int *gctr, int first, int count, int depth)
+{
+    groups[atomicAdd(&gctr[0], 1)] = make_int2(first, count | (depth << 8));
+}
+
 __global__ void k_group_list(const int *__restrict__ ctr, const int4 *__restrict__ nc,
-                             int2 *__restrict__ groups, int *__restrict__ gctr)
+                             const int *__restrict__ depth, int2 *__restrict__ groups,
+                             int *__restrict__ gctr)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ctr[CTR_NODES]) return;
     const int4 ci = nc[c];   // (first child, children, first particle, particles)
     if (ci.w <= 0) return;
+    const int d = depth[c];
     if (c == 0 && ci.w <= GW_GROUP) {
-        groups[atomicAdd(&gctr[0], 1)] = make_int2(ci.z, ci.w);
+        put_group(groups, gctr, ci.z, ci.w, d);
         return;
     }
     if (ci.w <= GW_GROUP) return;   // its own parent groups it
     if (ci.y <= 0) {                // oversized leaf (depth limit): runs of GW_GROUP
-        for (int b = 0; b < ci.w; b += GW_GROUP)
-            groups[atomicAdd(&gctr[0], 1)] = make_int2(ci.z + b, min(GW_GROUP, ci.w - b));
+        for (int b = 0; b < ci.w; b += GW_GROUP) put_group(groups, gctr, ci.z + b, min(GW_GROUP, ci.w - b), d);
         return;
     }
-    // each child cell small enough is one group: a group never spans more
-    // than one cell (merging siblings would let a sparse group span its
-    // whole parent and open everything near it)
+    int first = 0, count = 0;
     for (int k = 0; k < ci.y; ++k) {
         const int4 ch = nc[ci.x + k];
-        if (ch.w > 0 && ch.w <= GW_GROUP)
-            groups[atomicAdd(&gctr[0], 1)] = make_int2(ch.z, ch.w);
+        if (ch.w > GW_GROUP || count + ch.w > GW_GROUP) {
+            if (count > 0) put_group(groups, gctr, first, count, d);
+            count = 0;
+        }
+        if (ch.w > GW_GROUP || ch.w <= 0) continue;
+        if (count == 0) first = ch.z;
+        count += ch.w;
     }
+    if (count > 0) put_group(groups, gctr, first, count, d);
 }
 
 struct GroupWalkArgs {
@@ -161,31 +175,11 @@ __device__ __forceinline__ void flush_parts(const GroupShared &g, int count, flo
     kahan_add(sz, cz, az);
 }
 
+// Walk of one group: sorted particles [g0, gend) on lanes 0..gend-g0-1.
 template <bool QUAD>
-__global__ void __launch_bounds__(32 * GW_WARPS)
-k_bh_group(GroupWalkArgs A)
+__device__ void walk_group(const GroupWalkArgs &A, GroupShared &g, const float *s_w2, int lane,
+                           int g0, int gend)
 {
-    extern __shared__ __align__(16) unsigned char gw_smem[];
-    __shared__ float s_w2[OCT_MAX_LEVEL + 2];   // (cell side at depth d)^2
-    if (A.gate && *A.gate == 0) return;          // block-uniform
-    GroupShared &g = reinterpret_cast<GroupShared *>(gw_smem)[threadIdx.x >> 5];
-    const int lane = threadIdx.x & 31;
-    if (threadIdx.x <= OCT_MAX_LEVEL + 1) {
-        // side of a depth-d cell: box_length / (2 << d)
-        const double w = A.frame[4] / (double)(2 << threadIdx.x);
-        s_w2[threadIdx.x] = (float)(w * w);
-    }
-    __syncthreads();
-
-    const int ngroups = A.gctr[0];
-    for (;;) {
-    int gi = 0;
-    if (lane == 0) gi = atomicAdd(&A.gctr[1], 1);
-    gi = __shfl_sync(0xffffffffu, gi, 0);
-    if (gi >= ngroups) break;   // warp-uniform
-    const int2 grp = A.groups[gi];
-    const int g0 = grp.x;
-    const int gend = g0 + grp.y;
     const int s = g0 + lane;
     const bool valid = s < gend;
     // origin: the group's first particle (double-float)
@@ -356,8 +350,65 @@ k_bh_group(GroupWalkArgs A)
         atomicAdd(&A.counters[0], n_cell);
         atomicAdd(&A.counters[1], n_pp);
     }
-    __syncwarp();
-    }   // next group
+    __syncwarp();   // every lane is done with the lists before the next group
+}
+
+// Whether the particles of a group lie within the side of the cell holding
+// it.  A particle at the bounding-box maximum has its Morton coordinate
+// wrapped to 0 (as in the reference) and sits in a cell on the far side; the
+// group holding it spans the whole box and is walked one particle at a time.
+__device__ bool group_fits(const GroupWalkArgs &A, const float *s_w2, int lane, int g0, int cnt,
+                           int depth)
+{
+    const bool valid = lane < cnt;
+    float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+    if (valid) {
+        const float4 oh = A.pa[g0], ol = A.pb[g0];
+        const float4 ph = A.pa[g0 + lane], pl = A.pb[g0 + lane];
+        const float r[3] = {(ph.x - oh.x) + (pl.x - ol.x), (ph.y - oh.y) + (pl.y - ol.y),
+                            (ph.z - oh.z) + (pl.z - ol.z)};
+        for (int k = 0; k < 3; ++k) lo[k] = hi[k] = r[k];
+    }
+    float ext = 0.f;
+    for (int k = 0; k < 3; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+            hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+        }
+        ext = fmaxf(ext, hi[k] - lo[k]);
+    }
+    return ext * ext <= 1.0001f * s_w2[min(depth, OCT_MAX_LEVEL + 1)];
+}
+
+template <bool QUAD>
+__global__ void __launch_bounds__(32 * GW_WARPS)
+k_bh_group(GroupWalkArgs A)
+{
+    extern __shared__ __align__(16) unsigned char gw_smem[];
+    __shared__ float s_w2[OCT_MAX_LEVEL + 2];   // (cell side at depth d)^2
+    if (A.gate && *A.gate == 0) return;          // block-uniform
+    GroupShared &g = reinterpret_cast<GroupShared *>(gw_smem)[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x <= OCT_MAX_LEVEL + 1) {
+        // side of a depth-d cell: box_length / (2 << d)
+        const double w = A.frame[4] / (double)(2 << threadIdx.x);
+        s_w2[threadIdx.x] = (float)(w * w);
+    }
+    __syncthreads();
+    const int ngroups = A.gctr[0];
+    for (;;) {
+        int gi = 0;
+        if (lane == 0) gi = atomicAdd(&A.gctr[1], 1);
+        gi = __shfl_sync(0xffffffffu, gi, 0);
+        if (gi >= ngroups) break;   // warp-uniform
+        const int2 grp = A.groups[gi];
+        const int cnt = grp.y & 255, depth = grp.y >> 8;
+        if (group_fits(A, s_w2, lane, grp.x, cnt, depth)) {
+            walk_group<QUAD>(A, g, s_w2, lane, grp.x, grp.x + cnt);
+        } else {
+            for (int q = 0; q < cnt; ++q) walk_group<QUAD>(A, g, s_w2, lane, grp.x + q, grp.x + q + 1);
+        }
+    }
 }
 
 ErrorStatus launch_bh_group_walk(const OctreeDevice &t, double theta, double eps, double G,
@@ -396,6 +447,7 @@ ErrorStatus launch_bh_group_walk(const OctreeDevice &t, double theta, double eps
     w.gctr = t.g_ctr.as<int>();
     GS_CUDA(cudaMemsetAsync(t.g_ctr.p, 0, 2 * sizeof(int), s));
     k_group_list<<<(t.cap_nodes + 255) / 256, 256, 0, s>>>(t.ctr.as<int>(), t.w_nc.as<int4>(),
+                                                          t.t_depth.as<int>(),
                                                           t.g_list.as<int2>(), w.gctr);
     static int grid = 0;   // persistent: every SM filled once
     if (grid == 0) {

@@ -237,3 +237,20 @@ def test_group_walk_galaxy_1m(lib, g, orc, wl):
     err = orc.rel_err(a[rows], orc.direct_rows(x, m, 1.0, 0.01, rows))
     print(f"group walk N=1048576 theta=0.5: median {np.median(err):.3g}")
     assert np.isfinite(a).all() and np.median(err) < 1e-3
+
+
+def test_group_walk_particles_on_box_maximum(lib, g, orc, wl):
+    """Particles exactly on the bounding-box maximum get Morton coordinate 0
+    (the reference's wrap) and sit in a cell on the far side: their group
+    does not fit its cell and is walked particle by particle, with the same
+    accuracy as everyone else."""
+    x, v, m = wl.plummer(50000, 13)
+    hi = x.max(axis=0)
+    x[7] = hi
+    x[8] = hi - 1e-9
+    x[9, 0] = hi[0]
+    rows = np.array([7, 8, 9, 10, 11], dtype=np.int32)
+    a = g.acceleration(lib, x, m, 1.0, g.METHOD_GPU_BARNES_HUT_GROUP, opening_angle=0.5,
+                       softening_length=0.01, max_num_particles_per_leaf=1)
+    err = orc.rel_err(a[rows], orc.direct_rows(x, m, 1.0, 0.01, rows))
+    assert np.isfinite(a).all() and err.max() < 5e-3
