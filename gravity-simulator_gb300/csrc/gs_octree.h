@@ -61,6 +61,13 @@ struct OctreeDevice {
     ErrorStatus build(const double *d_x, const double *d_m, cudaStream_t s,
                       const double *box_center = nullptr, double box_width = -1.0);
     int launches_per_build() const;
+    // Bits of the internal-node sort key (first particle << 5 | depth).
+    int internal_key_bits() const
+    {
+        int b = 1;
+        while (b < 31 && (1 << b) <= n) ++b;
+        return b + 5;
+    }
     // Host copies: number of nodes, status word.
     ErrorStatus read_counts(cudaStream_t s, int *nodes, unsigned *status);
 };

@@ -21,7 +21,7 @@ class RadixSorter {
 
   private:
     int capacity_ = 0, tiles_ = 0;
-    DBuf counts_, tmp_keys_, tmp_vals_;
+    DBuf counts_, totals_, tmp_keys_, tmp_vals_;
 };
 
 }  // namespace gs

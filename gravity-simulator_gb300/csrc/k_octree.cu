@@ -196,6 +196,15 @@ __device__ __forceinline__ int octant_end(const uint64_t *__restrict__ keys, int
 }
 
 // src/linear_octree.c:342-576 for all internal nodes of depth d at once.
+// Levels with few nodes (the top of the tree, where a node's binary
+// searches are long) use eight lanes per node, one per octant: each finds
+// where its octant ends by its own binary search over the node's sorted
+// keys (the searches are independent: the keys of a node are sorted by
+// their octant digit), the eight ends are combined by shuffles within the
+// 8-lane group, and each lane writes its own child.  Levels with many nodes
+// use one thread per node.  Node ids come from an atomic counter; the
+// reference's numbering is recovered later by k_tree_number.
+constexpr int EXPAND_WIDE_NODES = 16384;
 __global__ void __launch_bounds__(OT_THREADS)
 k_tree_expand(int d, int leaf_max, int cap, const uint64_t *__restrict__ keys, int *__restrict__ ctr,
               int *__restrict__ nd_start, int *__restrict__ nd_count, int *__restrict__ nd_depth,
@@ -206,52 +215,109 @@ k_tree_expand(int d, int leaf_max, int cap, const uint64_t *__restrict__ keys, i
     const int hi = ctr[CTR_LVL + d + 1];
     const int cd = d + 1;
     const int shift = 3 * (OCT_MAX_LEVEL - cd);
-    for (int ii = lo + blockIdx.x * OT_THREADS + threadIdx.x; ii < hi;
-         ii += gridDim.x * OT_THREADS) {
-        const int q = in_node[ii];
-        const int s = nd_start[q];
-        const int e = s + nd_count[q];
-        int ends[8];
-        int nch = 0;
-        int prev = s;
-        for (int o = 0; o < 8; ++o) {
-            ends[o] = octant_end(keys, prev, e, shift, o);
-            if (ends[o] > prev) ++nch;
-            prev = ends[o];
+    if (hi - lo > EXPAND_WIDE_NODES) {
+        // many nodes (deep levels, few particles each): one thread per node,
+        // its eight searches over shrinking ranges
+        for (int ii = lo + blockIdx.x * OT_THREADS + threadIdx.x; ii < hi;
+             ii += gridDim.x * OT_THREADS) {
+            const int q = in_node[ii];
+            const int s = nd_start[q];
+            const int e = s + nd_count[q];
+            int ends[8];
+            int nch = 0;
+            int prev = s;
+            for (int o = 0; o < 8; ++o) {
+                ends[o] = octant_end(keys, prev, e, shift, o);
+                if (ends[o] > prev) ++nch;
+                prev = ends[o];
+            }
+            const int base = atomicAdd(&ctr[CTR_NODES], nch);
+            if (base + nch > cap) {
+                atomicOr((unsigned *)&ctr[CTR_STATUS], ST_TREE_OVERFLOW);
+                in_nchild[ii] = 0;
+                continue;
+            }
+            int r = 0;
+            prev = s;
+            for (int o = 0; o < 8; ++o) {
+                const int cnt = ends[o] - prev;
+                if (cnt > 0) {
+                    const int c = base + r;
+                    nd_start[c] = prev;
+                    nd_count[c] = cnt;
+                    nd_depth[c] = cd;
+                    nd_parent[c] = ii;
+                    nd_rank[c] = r;
+                    int slot = -1;
+                    if (cnt > leaf_max && cd < OCT_MAX_LEVEL) {
+                        slot = atomicAdd(&ctr[CTR_INTERNAL], 1);
+                        if (slot >= cap) {
+                            atomicOr((unsigned *)&ctr[CTR_STATUS], ST_TREE_OVERFLOW);
+                            slot = -1;
+                        } else {
+                            in_node[slot] = c;
+                        }
+                    }
+                    nd_int[c] = slot;
+                    ++r;
+                }
+                prev = ends[o];
+            }
+            in_nchild[ii] = nch;
         }
-        const int base = atomicAdd(&ctr[CTR_NODES], nch);
+        return;
+    }
+    const int lane = threadIdx.x & 31;
+    const int o = lane & 7;
+    const int g0 = lane & ~7;   // first lane of this node's group
+    for (int wt = blockIdx.x * OT_THREADS + (threadIdx.x & ~31);; wt += gridDim.x * OT_THREADS) {
+        if (lo + (wt >> 3) >= hi) break;   // warp-uniform
+        const int ii = lo + ((wt + lane) >> 3);
+        const bool act = ii < hi;
+        int s = 0, e = 0;
+        if (act) {
+            const int q = in_node[ii];
+            s = nd_start[q];
+            e = s + nd_count[q];
+        }
+        const int endo = act ? octant_end(keys, s, e, shift, o) : 0;
+        const int up = __shfl_up_sync(0xffffffffu, endo, 1, 8);
+        const int prev = (o == 0) ? s : up;
+        const int cnt = act ? endo - prev : 0;
+        const unsigned m8 = (__ballot_sync(0xffffffffu, cnt > 0) >> g0) & 0xffu;
+        const int nch = __popc(m8);
+        const int rank = __popc(m8 & ((1u << o) - 1u));
+        int base = 0;
+        if (act && o == 0) base = atomicAdd(&ctr[CTR_NODES], nch);
+        base = __shfl_sync(0xffffffffu, base, g0);
+        if (!act) continue;
         if (base + nch > cap) {
-            atomicOr((unsigned *)&ctr[CTR_STATUS], ST_TREE_OVERFLOW);
-            in_nchild[ii] = 0;
+            if (o == 0) {
+                atomicOr((unsigned *)&ctr[CTR_STATUS], ST_TREE_OVERFLOW);
+                in_nchild[ii] = 0;
+            }
             continue;
         }
-        int r = 0;
-        prev = s;
-        for (int o = 0; o < 8; ++o) {
-            const int cnt = ends[o] - prev;
-            if (cnt > 0) {
-                const int c = base + r;
-                nd_start[c] = prev;
-                nd_count[c] = cnt;
-                nd_depth[c] = cd;
-                nd_parent[c] = ii;
-                nd_rank[c] = r;
-                int slot = -1;
-                if (cnt > leaf_max && cd < OCT_MAX_LEVEL) {
-                    slot = atomicAdd(&ctr[CTR_INTERNAL], 1);
-                    if (slot >= cap) {
-                        atomicOr((unsigned *)&ctr[CTR_STATUS], ST_TREE_OVERFLOW);
-                        slot = -1;
-                    } else {
-                        in_node[slot] = c;
-                    }
+        if (cnt > 0) {
+            const int c = base + rank;
+            nd_start[c] = prev;
+            nd_count[c] = cnt;
+            nd_depth[c] = cd;
+            nd_parent[c] = ii;
+            nd_rank[c] = rank;
+            int slot = -1;
+            if (cnt > leaf_max && cd < OCT_MAX_LEVEL) {
+                slot = atomicAdd(&ctr[CTR_INTERNAL], 1);
+                if (slot >= cap) {
+                    atomicOr((unsigned *)&ctr[CTR_STATUS], ST_TREE_OVERFLOW);
+                    slot = -1;
+                } else {
+                    in_node[slot] = c;
                 }
-                nd_int[c] = slot;
-                ++r;
             }
-            prev = ends[o];
+            nd_int[c] = slot;
         }
-        in_nchild[ii] = nch;
+        if (o == 0) in_nchild[ii] = nch;
     }
 }
 
@@ -641,7 +707,8 @@ int OctreeDevice::launches_per_build() const
 {
     // bbox 2, morton 1, sort, init 1, levels 2*21, keys 1, sort, fc 3,
     // number 1, multipoles 21 (+1 leaves), walk arrays 2 (+ quadrupoles 21 + 1)
-    return 2 + 1 + RadixSorter::launches(63) + 1 + 42 + 1 + RadixSorter::launches(36) + 3 + 1 +
+    return 2 + 1 + RadixSorter::launches(63) + 1 + 42 + 1 +
+           RadixSorter::launches(internal_key_bits()) + 3 + 1 +
            21 + (compat ? 0 : 1) + 2 + (quad ? 22 : 0) + (links ? 1 : 0);
 }
 
@@ -677,8 +744,8 @@ ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream
     k_internal_keys<<<grid, OT_THREADS, 0, s>>>(ctr.as<int>(), in_node.as<int>(), nd_start.as<int>(),
                                                 nd_depth.as<int>(), in_key.as<uint64_t>(),
                                                 in_order.as<int>());
-    GS_TRY(sorter.sort(in_key.as<uint64_t>(), in_order.as<int>(), ctr.as<int>() + CTR_INTERNAL, 36,
-                       s));
+    GS_TRY(sorter.sort(in_key.as<uint64_t>(), in_order.as<int>(), ctr.as<int>() + CTR_INTERNAL,
+                       internal_key_bits(), s));
     const int tiles = (cap_nodes + SCAN_TILE - 1) / SCAN_TILE;
     k_fc_tile_sums<<<tiles, OT_THREADS, 0, s>>>(ctr.as<int>(), in_order.as<int>(),
                                                 in_nchild.as<int>(), scan_tiles.as<unsigned>());

@@ -4,7 +4,9 @@
 // Any stable sort by the full key gives the same order as the reference's
 // 9-bit LSD passes, so this sort uses 8-bit digits: per pass
 //   1. k_radix_count  -- per-tile digit histograms (4096 elements per tile);
-//   2. k_radix_scan   -- one exclusive scan over [digit][tile] counts;
+//   2. k_radix_scan_rows -- one CTA per digit: digit base (per-digit totals
+//      gathered by the count kernel) plus the scan of that digit's tile
+//      counts over the tiles that hold elements;
 //   3. k_radix_scatter -- stable in-tile ranks from warp match (each warp
 //      owns 512 consecutive elements, 16 rounds of 32, ranked in index
 //      order) and scatter to the scanned offsets.
@@ -20,65 +22,65 @@ constexpr int RX_THREADS = 256;
 constexpr int RX_ITEMS = 16;
 constexpr int RX_TILE = RX_THREADS * RX_ITEMS;   // 4096
 constexpr int RX_WARPS = RX_THREADS / 32;
-constexpr int RX_SCAN_THREADS = 1024;
 
 __global__ void __launch_bounds__(RX_THREADS)
 k_radix_count(const uint64_t *__restrict__ keys, const int *__restrict__ d_n, int shift, int tiles,
-              unsigned *__restrict__ counts)
+              unsigned *__restrict__ counts, unsigned *__restrict__ totals)
 {
     __shared__ unsigned hist[256];
     const int n = *d_n;
+    const int base = blockIdx.x * RX_TILE;
+    if (base >= n) return;   // block-uniform: tiles past the elements are never read
     hist[threadIdx.x] = 0;
     __syncthreads();
-    const int base = blockIdx.x * RX_TILE;
 #pragma unroll 4
     for (int k = 0; k < RX_ITEMS; ++k) {
         const int e = base + k * RX_THREADS + threadIdx.x;
         if (e < n) atomicAdd(&hist[(unsigned)(keys[e] >> shift) & 255u], 1u);
     }
     __syncthreads();
-    counts[threadIdx.x * tiles + blockIdx.x] = hist[threadIdx.x];
+    const unsigned h = hist[threadIdx.x];
+    counts[threadIdx.x * tiles + blockIdx.x] = h;
+    if (h) atomicAdd(&totals[threadIdx.x], h);
 }
 
-// Exclusive scan of len entries in place (one block).  Each warp owns a
-// contiguous chunk and reads it in coalesced rounds of 32: first to total
-// the chunk, then -- after the chunk totals are scanned -- to write the
-// exclusive prefix with a warp scan per round.
-__global__ void __launch_bounds__(RX_SCAN_THREADS)
-k_radix_scan(unsigned *__restrict__ counts, int len)
+// Output offset of every (digit, tile): the elements of all smaller digits
+// (from the per-digit totals) plus those of the same digit in earlier
+// tiles.  One CTA per digit scans its row over the tiles holding elements.
+__global__ void __launch_bounds__(256)
+k_radix_scan_rows(unsigned *__restrict__ counts, const unsigned *__restrict__ totals,
+                  const int *__restrict__ d_n, int tiles)
 {
-    constexpr int W = RX_SCAN_THREADS / 32;
-    __shared__ unsigned wsum[W];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int chunk = ((len + W - 1) / W + 31) & ~31;
-    const int b = warp * chunk;
-    const int e = min(len, b + chunk);
-    unsigned s = 0;
-    for (int i = b + lane; i < e; i += 32) s += counts[i];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) wsum[warp] = s;
+    __shared__ unsigned wsum[8];
+    const int d = blockIdx.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    unsigned v = t < d ? totals[t] : 0u;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) wsum[warp] = v;
     __syncthreads();
-    if (warp == 0) {
-        unsigned v = lane < W ? wsum[lane] : 0u;
-        unsigned incl = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
-        }
-        if (lane < W) wsum[lane] = incl - v;
-    }
+    unsigned run = 0;
+    for (int w = 0; w < 8; ++w) run += wsum[w];
     __syncthreads();
-    unsigned run = wsum[warp];
-    for (int i0 = b; i0 < e; i0 += 32) {
-        const int i = i0 + lane;
-        const unsigned c = i < e ? counts[i] : 0u;
+    const int used = (*d_n + RX_TILE - 1) / RX_TILE;
+    unsigned *row = counts + (size_t)d * tiles;
+    for (int c0 = 0; c0 < used; c0 += 256) {
+        const int i = c0 + t;
+        const unsigned c = i < used ? row[i] : 0u;
         unsigned incl = c;
         for (int o = 1; o < 32; o <<= 1) {
-            const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += t;
+            const unsigned u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += u;
         }
-        if (i < e) counts[i] = run + incl - c;
-        run += __shfl_sync(0xffffffffu, incl, 31);
+        if (lane == 31) wsum[warp] = incl;
+        __syncthreads();
+        unsigned before = 0, chunk = 0;
+        for (int w = 0; w < 8; ++w) {
+            const unsigned ws = wsum[w];
+            if (w < warp) before += ws;
+            chunk += ws;
+        }
+        if (i < used) row[i] = run + before + incl - c;
+        run += chunk;
+        __syncthreads();
     }
 }
 
@@ -91,6 +93,7 @@ k_radix_scatter(const uint64_t *__restrict__ keys_in, const int *__restrict__ va
     __shared__ unsigned whist[RX_WARPS][256];
     __shared__ unsigned tile_off[256];
     const int n = *d_n;
+    if ((int)blockIdx.x * RX_TILE >= n) return;   // block-uniform
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     for (int d = threadIdx.x; d < RX_WARPS * 256; d += RX_THREADS) (&whist[0][0])[d] = 0u;
@@ -150,6 +153,7 @@ ErrorStatus RadixSorter::reserve(int cap)
     capacity_ = cap;
     tiles_ = (cap + RX_TILE - 1) / RX_TILE;
     GS_TRY(counts_.reserve((size_t)256 * tiles_ * sizeof(unsigned)));
+    GS_TRY(totals_.reserve((size_t)8 * 256 * sizeof(unsigned)));
     GS_TRY(tmp_keys_.reserve((size_t)cap * sizeof(uint64_t)));
     GS_TRY(tmp_vals_.reserve((size_t)cap * sizeof(int)));
     return ok();
@@ -162,10 +166,14 @@ ErrorStatus RadixSorter::sort(uint64_t *keys, int *vals, const int *d_n, int key
     if (passes & 1) ++passes;   // even: the result lands back in keys / vals
     uint64_t *kin = keys, *kout = tmp_keys_.as<uint64_t>();
     int *vin = vals, *vout = tmp_vals_.as<int>();
+    if (passes > 8) return GS_RAISE(GRAV_VALUE_ERROR, "radix sort keys wider than 64 bits");
+    GS_CUDA(cudaMemsetAsync(totals_.p, 0, (size_t)passes * 256 * sizeof(unsigned), s));
     for (int p = 0; p < passes; ++p) {
         const int shift = 8 * p;
-        k_radix_count<<<tiles_, RX_THREADS, 0, s>>>(kin, d_n, shift, tiles_, counts_.as<unsigned>());
-        k_radix_scan<<<1, RX_SCAN_THREADS, 0, s>>>(counts_.as<unsigned>(), 256 * tiles_);
+        unsigned *tot = totals_.as<unsigned>() + 256 * p;
+        k_radix_count<<<tiles_, RX_THREADS, 0, s>>>(kin, d_n, shift, tiles_, counts_.as<unsigned>(),
+                                                    tot);
+        k_radix_scan_rows<<<256, 256, 0, s>>>(counts_.as<unsigned>(), tot, d_n, tiles_);
         k_radix_scatter<<<tiles_, RX_THREADS, 0, s>>>(kin, vin, kout, vout, d_n, shift, tiles_,
                                                       counts_.as<unsigned>());
         GS_CUDA(cudaGetLastError());
