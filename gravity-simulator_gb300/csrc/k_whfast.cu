@@ -83,7 +83,9 @@ __device__ __forceinline__ unsigned long long dist_key(double d)
 
 // Sorts slots of one system by |vec_i - vec_prim| and permutes vec, vel, m,
 // ids; then eta.  Dynamic shared memory: pow2 * (8 + 4) bytes.
-__global__ void k_wh_sort(EnsDev E, double *vec, double *vel, int pow2_max)
+constexpr int SORT_OET_PASSES = 32;   // odd-even passes tried before the bitonic network
+
+__global__ void k_wh_sort(EnsDev E, double *vec, double *vel, int pow2_max, int need_eta)
 {
     extern __shared__ __align__(16) unsigned char wh_smem[];
     const int s = blockIdx.x;
@@ -133,8 +135,42 @@ __global__ void k_wh_sort(EnsDev E, double *vec, double *vel, int pow2_max)
         }
     }
     __syncthreads();
+    // Already in order (the usual case from one step to the next): a stable
+    // sort is the identity; eta is kept unless it was never formed.
+    bool unsorted = false;
+    for (int i = threadIdx.x; i + 1 < n; i += blockDim.x)
+        unsorted = unsorted || key[i] > key[i + 1];
+    if (!__syncthreads_or(unsorted)) {
+        if (need_eta && threadIdx.x == 0) {
+            double e = E.m[base];
+            E.eta[base] = e;
+            for (int i = 1; i < n; ++i) {
+                e = __dadd_rn(e, E.m[base + i]);
+                E.eta[base + i] = e;
+            }
+        }
+        return;
+    }
+    // Nearly in order: odd-even transposition by (key, idx) until two
+    // passes in a row swap nothing; the bitonic network finishes otherwise.
+    int clean = 0;
+    for (int pass = 0; pass < SORT_OET_PASSES && clean < 2; ++pass) {
+        bool swapped = false;
+        for (int i = (pass & 1) + 2 * threadIdx.x; i + 1 < n; i += 2 * blockDim.x) {
+            const unsigned long long ka = key[i], kb = key[i + 1];
+            const int ia = idx[i], ib = idx[i + 1];
+            if (ka > kb || (ka == kb && ia > ib)) {
+                key[i] = kb;
+                key[i + 1] = ka;
+                idx[i] = ib;
+                idx[i + 1] = ia;
+                swapped = true;
+            }
+        }
+        clean = __syncthreads_or(swapped) ? 0 : clean + 1;
+    }
     // bitonic sort ascending by (key, idx)
-    for (int k = 2; k <= P2; k <<= 1) {
+    for (int k = 2; clean < 2 && k <= P2; k <<= 1) {
         for (int j = k >> 1; j > 0; j >>= 1) {
             for (int i = threadIdx.x; i < P2; i += blockDim.x) {
                 const int l = i ^ j;
@@ -204,7 +240,8 @@ struct SeqStage {
 };
 
 // Massless runs of the Jacobi -> Cartesian chain.  For a particle with
-// m_i = 0 (finite Jacobi coordinates, eta_i = eta_{i-1} = e) a chain step is
+// m_i = 0 (finite Jacobi coordinates, eta_i = eta_{i-1} = e, and a centre
+// that is not -0, which subtracting +-0 would turn into +0) a chain step is
 //     y = RN(xc / e),  x_i = jx_i + y,  xc <- RN(e y),
 // and after a step or two xc is a fixed point of that map (checked bit for
 // bit).  From there on every particle of the run adds the same y, so only
@@ -223,6 +260,11 @@ union SeqShared {
     SeqStage st;
     SeqRuns runs;
 };
+
+__device__ __forceinline__ bool neg_zero(double v)
+{
+    return __double_as_longlong(v) == (long long)0x8000000000000000ull;
+}
 
 // One exact chain step of src/integrator_whfast.c:744-760 for particle i;
 // y[6] receives the offsets added to jx_i / jv_i.
@@ -271,8 +313,87 @@ __global__ void __launch_bounds__(32 * SEQ_WARPS) k_wh_seq(EnsDev E, int mode)
     double *m = E.m + base, *eta = E.eta + base;
     double *x = E.x + 3 * base, *v = E.v + 3 * base, *jx = E.jx + 3 * base, *jv = E.jv + 3 * base;
     if (mode == 0) {
+        // src/integrator_whfast.c:682-724 (once per run).  For a massless
+        // particle the interior centre of mass is left exactly as it is
+        // (factor 1 + 0/eta = 1, added term +-0), so with finite
+        // coordinates and a non-zero centre every particle of a massless run
+        // subtracts the same y = xc / eta and the run is filled by the warp.
+        bool finite0 = true;
+        int nmass0 = 0;
+        for (int c = 0; c < n; c += 32) {
+            const int i = c + lane;
+            bool f = true, h = false;
+            if (i < n) {
+                for (int k = 0; k < 3; ++k) f = f && isfinite(x[3 * i + k]) && isfinite(v[3 * i + k]);
+                h = m[i] != 0.0;
+            }
+            finite0 = __all_sync(0xffffffffu, f) && finite0;
+            const unsigned b = __ballot_sync(0xffffffffu, h);
+            const int at = nmass0 + __popc(b & ((1u << lane) - 1u));
+            if (h && at < kSeqMassMax) rs.mass_idx[at] = i;
+            nmass0 += __popc(b);
+        }
+        if (finite0 && nmass0 <= kSeqMassMax) {
+            __syncwarp();
+            if (lane == 0) {
+                double xc[3], vc[3];
+                for (int k = 0; k < 3; ++k) {
+                    xc[k] = __dmul_rn(m[0], x[k]);
+                    vc[k] = __dmul_rn(m[0], v[k]);
+                }
+                int nr = 0, q = 0;
+                int i = 1;
+                while (i < n) {
+                    while (q < nmass0 && rs.mass_idx[q] < i) ++q;
+                    const int next_mass = q < nmass0 ? rs.mass_idx[q] : n;
+                    // only a centre of -0 is changed by adding +-0 (to +0)
+                    bool nz = true;
+                    for (int k = 0; k < 3; ++k) nz = nz && !neg_zero(xc[k]) && !neg_zero(vc[k]);
+                    if (next_mass > i && nz) {
+                        // massless run [i, next_mass): one offset for all
+                        const double ie = eta[i - 1];
+                        rs.lo[nr] = i;
+                        rs.hi[nr] = next_mass - 1;
+                        for (int k = 0; k < 3; ++k) {
+                            rs.y[nr][k] = __ddiv_rn(xc[k], ie);
+                            rs.y[nr][3 + k] = __ddiv_rn(vc[k], ie);
+                        }
+                        ++nr;
+                        i = next_mass;
+                        continue;
+                    }
+                    const double ie = eta[i - 1];
+                    for (int k = 0; k < 3; ++k) {
+                        jx[3 * i + k] = __dsub_rn(x[3 * i + k], __ddiv_rn(xc[k], ie));
+                        jv[3 * i + k] = __dsub_rn(v[3 * i + k], __ddiv_rn(vc[k], ie));
+                        const double f = __dadd_rn(1.0, __ddiv_rn(m[i], ie));
+                        xc[k] = __dadd_rn(__dmul_rn(xc[k], f), __dmul_rn(m[i], jx[3 * i + k]));
+                        vc[k] = __dadd_rn(__dmul_rn(vc[k], f), __dmul_rn(m[i], jv[3 * i + k]));
+                    }
+                    ++i;
+                }
+                for (int k = 0; k < 3; ++k) {
+                    jx[k] = __ddiv_rn(xc[k], eta[n - 1]);
+                    jv[k] = __ddiv_rn(vc[k], eta[n - 1]);
+                }
+                rs.nruns = nr;
+            }
+            __syncwarp();
+            const int nr = rs.nruns;
+            for (int r = 0; r < nr; ++r) {
+                const int lo = rs.lo[r], cnt = 3 * (rs.hi[r] - lo + 1);
+                for (int t = lane; t < cnt; t += 32) {
+                    const int k = t % 3;
+                    jx[3 * lo + t] = __dsub_rn(x[3 * lo + t], rs.y[r][k]);
+                    jv[3 * lo + t] = __dsub_rn(v[3 * lo + t], rs.y[r][3 + k]);
+                }
+            }
+            __syncwarp();
+            wh_massive_list_warp(E, base, n, s, lane);
+            return;
+        }
+        __syncwarp();
         if (lane == 0) {
-            // src/integrator_whfast.c:682-724 (once per run)
             double xc[3], vc[3];
             for (int k = 0; k < 3; ++k) {
                 xc[k] = __dmul_rn(m[0], x[k]);
@@ -382,7 +503,8 @@ __global__ void __launch_bounds__(32 * SEQ_WARPS) k_wh_seq(EnsDev E, int mode)
                     for (int k = 0; k < 3; ++k)
                         fixed = fixed && __double_as_longlong(xc[k]) == __double_as_longlong(ox[k]) &&
                                 __double_as_longlong(vc[k]) == __double_as_longlong(ov[k]) &&
-                                isfinite(xc[k]) && isfinite(vc[k]) && xc[k] != 0.0 && vc[k] != 0.0;
+                                isfinite(xc[k]) && isfinite(vc[k]) && !neg_zero(xc[k]) &&
+                                !neg_zero(vc[k]);
                     --j;
                 }
                 if (j >= lo) {
@@ -894,7 +1016,7 @@ struct gsgpu_ensemble {
     {
         const size_t smem = (size_t)pow2 * 12;
         const int threads = pow2 >= 256 ? 256 : (pow2 < 32 ? 32 : pow2);
-        k_wh_sort<<<S, threads, smem, stream>>>(E, vec, vel, pow2);
+        k_wh_sort<<<S, threads, smem, stream>>>(E, vec, vel, pow2, vec == E.x ? 1 : 0);
         GS_CUDA(cudaGetLastError());
         return ok();
     }

@@ -157,3 +157,31 @@ def test_ensemble_rejects_bad_input(g, lib, wl):
     with pytest.raises(g.GravError):
         ens.download()
     ens.close()
+
+
+@pytest.mark.parametrize("negzero", [False, True])
+def test_whfast_planar_systems_match_oracle(g, lib, wl, orc, negzero):
+    """Planar systems (z = 0): the interior centres of mass have +0 (or, with
+    -0.0 coordinates, -0) components, the case where the massless-run
+    shortcuts must keep the reference's zero signs."""
+    G = wl.G_AU_MSUN_DAY
+    systems = []
+    for x, v, m in wl.planetary_ensemble(10, 31, max_test=120):
+        x, v = x.copy(), v.copy()
+        x[:, 2] = 0.0
+        v[:, 2] = 0.0
+        if negzero:
+            x[::2, 2] = -0.0
+            v[1::3, 2] = -0.0
+        systems.append((x, v, m))
+    counts0, ids, x, v, m = _concat(systems)
+    ens = g.Ensemble(lib, counts0, G, integrator=WHFAST, method=GPU_MASSLESS, dt=6.0)
+    ens.upload(ids, x, v, m)
+    ens.run_until(90.0)
+    counts, ido, xo, vo, mo = ens.download()
+    for s, (i_s, x_s, v_s) in enumerate(_blocks(counts0, counts, ido, xo, vo)):
+        xs, vs, ms = systems[s]
+        ri, rx, rv, rm = orc.whfast_run(xs, vs, ms, G, 0.0, 6.0, 90.0)
+        assert np.array_equal(i_s, ri), s
+        assert x_s.tobytes() == rx.tobytes() and v_s.tobytes() == rv.tobytes(), s
+    ens.close()
