@@ -327,6 +327,24 @@ def run_ours(args, world, rank, local):
     lib.gsgpu_sim_download(sim, xs.ctypes.data_as(dp), vs.ctypes.data_as(dp))
     med, p99 = accuracy_sample(a_host, xs, m, wk["G"], wk["eps"], rows=512)
     lib.gsgpu_sim_destroy(sim)
+    energy = None
+    if wk["ic"] == "plummer":
+        # FP64 energies (unsoftened potential, src/utils.c:27-59) of the initial
+        # state and of the state after the warm-up and timed steps, on the GPU
+        state = np.zeros((2, n, 7))
+        state[:, :, 0] = m
+        state[0, :, 1:4], state[0, :, 4:7] = x, v
+        state[1, :, 1:4], state[1, :, 4:7] = xs, vs
+        e = np.zeros(2)
+        lib.compute_energy_python.argtypes = [dp, ctypes.c_double, dp, ctypes.c_int32,
+                                              ctypes.c_int32]
+        lib.compute_energy_python(e.ctypes.data_as(dp), ctypes.c_double(wk["G"]),
+                                  np.ascontiguousarray(state).ctypes.data_as(dp), 2, n)
+        energy = {"e0": float(e[0]), "e1": float(e[1]),
+                  "rel_drift": float(abs(e[1] - e[0]) / abs(e[0])),
+                  "steps": args.warmup + args.steps,
+                  "note": "unsoftened potential while the force is softened (eps=0.01), "
+                          "as the reference's compute_energy"}
 
     # end to end through the reference-facing entry point
     xe, ve, me = x.copy(), v.copy(), m.copy()
@@ -374,7 +392,8 @@ def run_ours(args, world, rank, local):
                    "parallelism": f"replicas x{world}", "l2": "flushed between steps (256 MiB write)",
                    "interactions_per_s": value / n * interactions,
                    "accuracy": {"median_rel_err": med, "p99_rel_err": p99,
-                                "sample": "512 particles vs FP64 direct sum"}},
+                                "sample": "512 particles vs FP64 direct sum"},
+                   "energy": energy},
         "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak.value,
                      "unit": "TFLOP/s", "frac": achieved_tflops / peak.value if peak.value else None,
                      "traffic": traffic,

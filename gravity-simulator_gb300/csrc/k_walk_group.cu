@@ -21,10 +21,11 @@
 //     of the reference for every particle of the group, so the accepted
 //     cells are at least as well separated as the reference's;
 //   * accepted cells (centre of mass, mass, traceless quadrupole) and the
-//     particles of opened leaves go to interaction lists in shared memory;
-//     when a list is full every lane evaluates it against its own particle
-//     (one broadcast shared-memory load per entry, dense FP32 FMA work) and
-//     adds the partial sum to a Kahan-compensated accumulator;
+//     particles of opened leaves go to interaction lists in shared memory
+//     (structure of arrays); when a list is full every lane evaluates it
+//     against its own particle, two entries at a time through paired FP32
+//     operations on float2 (broadcast shared-memory loads, dense FMA work),
+//     and adds the partial sum to a Kahan-compensated accumulator;
 //   * coordinates are FP32 offsets from the group's first particle, formed
 //     from the frame-centred double-float (hi, lo) copies of the tree, so
 //     near-field differences keep FP32 relative accuracy.
@@ -112,67 +113,125 @@ struct GroupWalkArgs {
     int *gctr;              // [0] groups, [1] work-queue head
 };
 
+// Lists as structure of arrays, so that entries (j, j+1) load as float2
+// pairs and are evaluated together by paired FP32 operations.
 struct GroupShared {
     int stack[GW_STACK];
-    float4 cell[GW_CELLS];
-    float4 cq0[GW_CELLS], cq1[GW_CELLS];
-    float4 part[GW_PARTS];
+    float cx[GW_CELLS], cy[GW_CELLS], cz[GW_CELLS], cm[GW_CELLS];
+    float qxx[GW_CELLS], qxy[GW_CELLS], qxz[GW_CELLS], qyy[GW_CELLS], qyz[GW_CELLS], qzz[GW_CELLS];
+    float px[GW_PARTS], py[GW_PARTS], pz[GW_PARTS], pm[GW_PARTS];
 };
+
+__device__ __forceinline__ float2 ld2(const float *a, int j)
+{
+    return *reinterpret_cast<const float2 *>(a + j);
+}
+
+__device__ __forceinline__ float2 splat(float v) { return make_float2(v, v); }
+
+// One cell term (monopole + optional quadrupole) for a lane's particle.
+template <bool QUAD>
+__device__ __forceinline__ void cell_term1(const GroupShared &g, int j, float rx, float ry, float rz,
+                                           float eps2, float &ax, float &ay, float &az)
+{
+    const float dx = g.cx[j] - rx, dy = g.cy[j] - ry, dz = g.cz[j] - rz;
+    const float ns = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float ri = rsqrt_approx(ns + eps2);
+    const float ri2 = ri * ri;
+    const float ri3 = ri2 * ri;
+    const float sc = g.cm[j] * ri3;
+    ax = fmaf(dx, sc, ax);
+    ay = fmaf(dy, sc, ay);
+    az = fmaf(dz, sc, az);
+    if (QUAD) {
+        // d = com - x:  G [-Q d / r^5 + 2.5 (d.Q.d) d / r^7]
+        const float qx = fmaf(g.qxx[j], dx, fmaf(g.qxy[j], dy, g.qxz[j] * dz));
+        const float qy = fmaf(g.qxy[j], dx, fmaf(g.qyy[j], dy, g.qyz[j] * dz));
+        const float qz = fmaf(g.qxz[j], dx, fmaf(g.qyz[j], dy, g.qzz[j] * dz));
+        const float dqd = fmaf(dx, qx, fmaf(dy, qy, dz * qz));
+        const float ri5 = ri3 * ri2;
+        const float f = 2.5f * dqd * (ri5 * ri2);
+        ax = fmaf(f, dx, fmaf(-qx, ri5, ax));
+        ay = fmaf(f, dy, fmaf(-qy, ri5, ay));
+        az = fmaf(f, dz, fmaf(-qz, ri5, az));
+    }
+}
 
 template <bool QUAD>
 __device__ __forceinline__ void flush_cells(const GroupShared &g, int count, float rx, float ry,
                                             float rz, float eps2, float &sx, float &cx, float &sy,
                                             float &cy, float &sz, float &cz)
 {
-    float ax = 0.f, ay = 0.f, az = 0.f;
-    for (int j = 0; j < count; ++j) {
-        const float4 c = g.cell[j];
-        const float dx = c.x - rx, dy = c.y - ry, dz = c.z - rz;
-        const float ns = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const float ri = rsqrt_approx(ns + eps2);
-        const float ri2 = ri * ri;
-        const float ri3 = ri2 * ri;
-        const float sc = c.w * ri3;
-        ax = fmaf(dx, sc, ax);
-        ay = fmaf(dy, sc, ay);
-        az = fmaf(dz, sc, az);
+    const float2 nrx = splat(-rx), nry = splat(-ry), nrz = splat(-rz), e2 = splat(eps2);
+    float2 ax = splat(0.f), ay = splat(0.f), az = splat(0.f);
+    int j = 0;
+    for (; j + 1 < count; j += 2) {
+        const float2 dx = __fadd2_rn(ld2(g.cx, j), nrx);
+        const float2 dy = __fadd2_rn(ld2(g.cy, j), nry);
+        const float2 dz = __fadd2_rn(ld2(g.cz, j), nrz);
+        const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
+        const float2 ri = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+        const float2 ri2 = __fmul2_rn(ri, ri);
+        const float2 ri3 = __fmul2_rn(ri2, ri);
+        const float2 sc = __fmul2_rn(ld2(g.cm, j), ri3);
+        ax = __ffma2_rn(dx, sc, ax);
+        ay = __ffma2_rn(dy, sc, ay);
+        az = __ffma2_rn(dz, sc, az);
         if (QUAD) {
-            // d = com - x:  G [-Q d / r^5 + 2.5 (d.Q.d) d / r^7]
-            const float4 q0 = g.cq0[j], q1 = g.cq1[j];
-            const float qx = q0.x * dx + q0.y * dy + q0.z * dz;
-            const float qy = q0.y * dx + q0.w * dy + q1.x * dz;
-            const float qz = q0.z * dx + q1.x * dy + q1.y * dz;
-            const float dqd = dx * qx + dy * qy + dz * qz;
-            const float ri5 = ri3 * ri2;
-            const float f = 2.5f * dqd * ri5 * ri2;
-            ax += f * dx - qx * ri5;
-            ay += f * dy - qy * ri5;
-            az += f * dz - qz * ri5;
+            const float2 xx = ld2(g.qxx, j), xy = ld2(g.qxy, j), xz = ld2(g.qxz, j);
+            const float2 yy = ld2(g.qyy, j), yz = ld2(g.qyz, j), zz = ld2(g.qzz, j);
+            const float2 qx = __ffma2_rn(xx, dx, __ffma2_rn(xy, dy, __fmul2_rn(xz, dz)));
+            const float2 qy = __ffma2_rn(xy, dx, __ffma2_rn(yy, dy, __fmul2_rn(yz, dz)));
+            const float2 qz = __ffma2_rn(xz, dx, __ffma2_rn(yz, dy, __fmul2_rn(zz, dz)));
+            const float2 dqd = __ffma2_rn(dx, qx, __ffma2_rn(dy, qy, __fmul2_rn(dz, qz)));
+            const float2 ri5 = __fmul2_rn(ri3, ri2);
+            const float2 nri5 = __fmul2_rn(ri5, splat(-1.0f));
+            const float2 f = __fmul2_rn(__fmul2_rn(splat(2.5f), dqd), __fmul2_rn(ri5, ri2));
+            ax = __ffma2_rn(f, dx, __ffma2_rn(qx, nri5, ax));
+            ay = __ffma2_rn(f, dy, __ffma2_rn(qy, nri5, ay));
+            az = __ffma2_rn(f, dz, __ffma2_rn(qz, nri5, az));
         }
     }
-    kahan_add(sx, cx, ax);
-    kahan_add(sy, cy, ay);
-    kahan_add(sz, cz, az);
+    float tx = ax.x + ax.y, ty = ay.x + ay.y, tz = az.x + az.y;
+    if (j < count) cell_term1<QUAD>(g, j, rx, ry, rz, eps2, tx, ty, tz);
+    kahan_add(sx, cx, tx);
+    kahan_add(sy, cy, ty);
+    kahan_add(sz, cz, tz);
 }
 
 __device__ __forceinline__ void flush_parts(const GroupShared &g, int count, float rx, float ry,
                                             float rz, float eps2, float &sx, float &cx, float &sy,
                                             float &cy, float &sz, float &cz)
 {
-    float ax = 0.f, ay = 0.f, az = 0.f;
-    for (int j = 0; j < count; ++j) {
-        const float4 q = g.part[j];
-        const float dx = q.x - rx, dy = q.y - ry, dz = q.z - rz;
-        const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-        const float ri = r2 > 0.0f ? rsqrt_approx(r2) : 0.0f;   // own term without softening
-        const float sc = q.w * ri * ri * ri;
-        ax = fmaf(dx, sc, ax);
-        ay = fmaf(dy, sc, ay);
-        az = fmaf(dz, sc, az);
+    const float2 nrx = splat(-rx), nry = splat(-ry), nrz = splat(-rz), e2 = splat(eps2);
+    float2 ax = splat(0.f), ay = splat(0.f), az = splat(0.f);
+    int j = 0;
+    for (; j + 1 < count; j += 2) {
+        const float2 dx = __fadd2_rn(ld2(g.px, j), nrx);
+        const float2 dy = __fadd2_rn(ld2(g.py, j), nry);
+        const float2 dz = __fadd2_rn(ld2(g.pz, j), nrz);
+        const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
+        // own term without softening: r2 = 0 contributes nothing
+        const float2 ri = make_float2(r2.x > 0.0f ? rsqrt_approx(r2.x) : 0.0f,
+                                      r2.y > 0.0f ? rsqrt_approx(r2.y) : 0.0f);
+        const float2 sc = __fmul2_rn(ld2(g.pm, j), __fmul2_rn(__fmul2_rn(ri, ri), ri));
+        ax = __ffma2_rn(dx, sc, ax);
+        ay = __ffma2_rn(dy, sc, ay);
+        az = __ffma2_rn(dz, sc, az);
     }
-    kahan_add(sx, cx, ax);
-    kahan_add(sy, cy, ay);
-    kahan_add(sz, cz, az);
+    float tx = ax.x + ax.y, ty = ay.x + ay.y, tz = az.x + az.y;
+    if (j < count) {
+        const float dx = g.px[j] - rx, dy = g.py[j] - ry, dz = g.pz[j] - rz;
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+        const float ri = r2 > 0.0f ? rsqrt_approx(r2) : 0.0f;
+        const float sc = g.pm[j] * ri * ri * ri;
+        tx = fmaf(dx, sc, tx);
+        ty = fmaf(dy, sc, ty);
+        tz = fmaf(dz, sc, tz);
+    }
+    kahan_add(sx, cx, tx);
+    kahan_add(sy, cy, ty);
+    kahan_add(sz, cz, tz);
 }
 
 // Walk of one group: sorted particles [g0, gend) on lanes 0..gend-g0-1.
@@ -250,10 +309,18 @@ __device__ void walk_group(const GroupWalkArgs &A, GroupShared &g, const float *
             }
             if (act == 1) {
                 const int at = ncell + __popc(acc & ((1u << lane) - 1u));
-                g.cell[at] = crel;
+                g.cx[at] = crel.x;
+                g.cy[at] = crel.y;
+                g.cz[at] = crel.z;
+                g.cm[at] = crel.w;
                 if (QUAD) {
-                    g.cq0[at] = A.nq[2 * node];
-                    g.cq1[at] = A.nq[2 * node + 1];
+                    const float4 q0 = A.nq[2 * node], q1 = A.nq[2 * node + 1];
+                    g.qxx[at] = q0.x;
+                    g.qxy[at] = q0.y;
+                    g.qxz[at] = q0.z;
+                    g.qyy[at] = q0.w;
+                    g.qyz[at] = q1.x;
+                    g.qzz[at] = q1.y;
                 }
             }
             ncell += __popc(acc);
@@ -278,9 +345,11 @@ __device__ void walk_group(const GroupWalkArgs &A, GroupShared &g, const float *
                 for (int q = 0; q < cnt; ++q) {
                     const int p = ci.z + q;
                     const float4 qa = A.pa[p], qb = A.pb[p];
-                    g.part[npart + incl - cnt + q] =
-                        make_float4((qa.x - oh.x) + (qb.x - ol.x), (qa.y - oh.y) + (qb.y - ol.y),
-                                    (qa.z - oh.z) + (qb.z - ol.z), qa.w);
+                    const int at = npart + incl - cnt + q;
+                    g.px[at] = (qa.x - oh.x) + (qb.x - ol.x);
+                    g.py[at] = (qa.y - oh.y) + (qb.y - ol.y);
+                    g.pz[at] = (qa.z - oh.z) + (qb.z - ol.z);
+                    g.pm[at] = qa.w;
                 }
                 npart += total;
                 __syncwarp();
@@ -305,9 +374,10 @@ __device__ void walk_group(const GroupWalkArgs &A, GroupShared &g, const float *
                         if (lane < m32) {
                             const int p = first + b + lane;
                             const float4 qa = A.pa[p], qb = A.pb[p];
-                            g.part[npart + lane] = make_float4(
-                                (qa.x - oh.x) + (qb.x - ol.x), (qa.y - oh.y) + (qb.y - ol.y),
-                                (qa.z - oh.z) + (qb.z - ol.z), qa.w);
+                            g.px[npart + lane] = (qa.x - oh.x) + (qb.x - ol.x);
+                            g.py[npart + lane] = (qa.y - oh.y) + (qb.y - ol.y);
+                            g.pz[npart + lane] = (qa.z - oh.z) + (qb.z - ol.z);
+                            g.pm[npart + lane] = qa.w;
                         }
                         npart += m32;
                         __syncwarp();
