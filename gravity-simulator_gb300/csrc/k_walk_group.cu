@@ -54,41 +54,68 @@ constexpr int GW_GROUP = 32;       // particles per group at most
 // GW_GROUP particles (a leaf with more is cut into runs); the root is one
 // group when it is small enough.  Entry: (first sorted particle,
 // count | depth << 8) with depth that of the cell the group lies in.
-__device__ __forceinline__ void put_group(int2 *groups, int *gctr, int first, int count, int depth)
+// A group whose particles do not fit within the side of its cell (the
+// particles whose Morton coordinate wraps at the box maximum sit in a cell
+// on the far side) goes to the queue as single particles, so that no warp
+// walks a box-wide group and its walks spread over the warps.
+__device__ void put_group(int2 *groups, int *gctr, int first, int count, int depth,
+                          const float4 *__restrict__ pa, const float4 *__restrict__ pb,
+                          double box_length)
 {
-    groups[atomicAdd(&gctr[0], 1)] = make_int2(first, count | (depth << 8));
+    const float4 oh = pa[first], ol = pb[first];
+    float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f};
+    for (int p = first + 1; p < first + count; ++p) {
+        const float4 ph = pa[p], pl = pb[p];
+        const float r[3] = {(ph.x - oh.x) + (pl.x - ol.x), (ph.y - oh.y) + (pl.y - ol.y),
+                            (ph.z - oh.z) + (pl.z - ol.z)};
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fminf(lo[k], r[k]);
+            hi[k] = fmaxf(hi[k], r[k]);
+        }
+    }
+    const float ext = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+    const double side = box_length / (double)(2 << min(depth, OCT_MAX_LEVEL + 1));
+    if ((double)ext * (double)ext <= 1.0001 * side * side) {
+        groups[atomicAdd(&gctr[0], 1)] = make_int2(first, count | (depth << 8));
+    } else {
+        const int at = atomicAdd(&gctr[0], count);
+        for (int q = 0; q < count; ++q) groups[at + q] = make_int2(first + q, 1 | (depth << 8));
+    }
 }
 
 __global__ void k_group_list(const int *__restrict__ ctr, const int4 *__restrict__ nc,
-                             const int *__restrict__ depth, int2 *__restrict__ groups,
-                             int *__restrict__ gctr)
+                             const int *__restrict__ depth, const float4 *__restrict__ pa,
+                             const float4 *__restrict__ pb, const double *__restrict__ frame,
+                             int2 *__restrict__ groups, int *__restrict__ gctr)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ctr[CTR_NODES]) return;
+    const double bl = frame[4];
     const int4 ci = nc[c];   // (first child, children, first particle, particles)
     if (ci.w <= 0) return;
     const int d = depth[c];
     if (c == 0 && ci.w <= GW_GROUP) {
-        put_group(groups, gctr, ci.z, ci.w, d);
+        put_group(groups, gctr, ci.z, ci.w, d, pa, pb, bl);
         return;
     }
     if (ci.w <= GW_GROUP) return;   // its own parent groups it
     if (ci.y <= 0) {                // oversized leaf (depth limit): runs of GW_GROUP
-        for (int b = 0; b < ci.w; b += GW_GROUP) put_group(groups, gctr, ci.z + b, min(GW_GROUP, ci.w - b), d);
+        for (int b = 0; b < ci.w; b += GW_GROUP)
+            put_group(groups, gctr, ci.z + b, min(GW_GROUP, ci.w - b), d, pa, pb, bl);
         return;
     }
     int first = 0, count = 0;
     for (int k = 0; k < ci.y; ++k) {
         const int4 ch = nc[ci.x + k];
         if (ch.w > GW_GROUP || count + ch.w > GW_GROUP) {
-            if (count > 0) put_group(groups, gctr, first, count, d);
+            if (count > 0) put_group(groups, gctr, first, count, d, pa, pb, bl);
             count = 0;
         }
         if (ch.w > GW_GROUP || ch.w <= 0) continue;
         if (count == 0) first = ch.z;
         count += ch.w;
     }
-    if (count > 0) put_group(groups, gctr, first, count, d);
+    if (count > 0) put_group(groups, gctr, first, count, d, pa, pb, bl);
 }
 
 struct GroupWalkArgs {
@@ -516,9 +543,9 @@ ErrorStatus launch_bh_group_walk(const OctreeDevice &t, double theta, double eps
     w.groups = t.g_list.as<int2>();
     w.gctr = t.g_ctr.as<int>();
     GS_CUDA(cudaMemsetAsync(t.g_ctr.p, 0, 2 * sizeof(int), s));
-    k_group_list<<<(t.cap_nodes + 255) / 256, 256, 0, s>>>(t.ctr.as<int>(), t.w_nc.as<int4>(),
-                                                          t.t_depth.as<int>(),
-                                                          t.g_list.as<int2>(), w.gctr);
+    k_group_list<<<(t.cap_nodes + 255) / 256, 256, 0, s>>>(
+        t.ctr.as<int>(), t.w_nc.as<int4>(), t.t_depth.as<int>(), t.w_pa.as<float4>(),
+        t.w_pb.as<float4>(), t.frame.as<double>(), t.g_list.as<int2>(), w.gctr);
     static int grid = 0;   // persistent: every SM filled once
     if (grid == 0) {
         const DeviceInfo *dev = nullptr;
