@@ -17,6 +17,8 @@ Workloads (seeded synthetic inputs -- grav_sim publishes no dataset):
   galaxy1048576_plain -- the same at N = 1,048,576 with the monopole walk.
   galaxy2097152_group / galaxy1048576_group -- the group walk with
                     interaction lists (quadrupole cells), theta = 0.5.
+  galaxy1048576_group_mono[_t035] -- the group walk with monopole cells
+                    only, theta = 0.5 (0.35).
   galaxy1048576_learned -- theta = 1.0 walk + learned residual, judged by a
                     4,096-particle direct sum per step (training before the
                     timed region).
@@ -96,6 +98,12 @@ WORKLOADS = {
     "galaxy1048576_group": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01, dt=1e-3,
                                 integrator=4, method=106, theta=0.5, leaf=1,
                                 flop_per_interaction=20),
+    "galaxy1048576_group_mono": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01, dt=1e-3,
+                                     integrator=4, method=107, theta=0.5, leaf=1,
+                                     flop_per_interaction=20),
+    "galaxy1048576_group_mono_t035": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01,
+                                          dt=1e-3, integrator=4, method=107, theta=0.35,
+                                          leaf=1, flop_per_interaction=20),
     # small cases of the walks, for profiler captures
     "galaxy262144": dict(ic="galaxy", n=262144, seed=6, G=1.0, eps=0.01, dt=1e-3, integrator=4,
                          method=105, theta=0.5, leaf=1, flop_per_interaction=20),
@@ -228,7 +236,7 @@ def run_ours(args, world, rank, local):
         return run_ensemble(args, world, rank, local, wk, g, wl, lib)
     n = wk["n"]
     x, v, m = (wl.plummer if wk["ic"] == "plummer" else wl.galaxy_pair)(n, wk["seed"])
-    bh = wk["method"] in (103, 104, 105, 106, 113)
+    bh = wk["method"] in (103, 104, 105, 106, 107, 113)
 
     dp = ctypes.POINTER(ctypes.c_double)
     lib.gsgpu_sim_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
@@ -358,7 +366,7 @@ def run_ours(args, world, rank, local):
     e2e_val = world * n * args.steps / e2e_s
 
     traffic = None
-    kernel = ("k_bh_group" if wk["method"] == 106 else "k_bh_walk") if bh else "k_direct_sum"
+    kernel = ("k_bh_group" if wk["method"] in (106, 107) else "k_bh_walk") if bh else "k_direct_sum"
     prof = ROOT / "profiles" / f"{kernel}_{args.workload}.md"
     if prof.exists():
         for ln in prof.read_text().splitlines():

@@ -185,6 +185,23 @@ void launch_rk_emb_combine(const double *x, const double *v, const double *xe, c
                            const double *dtdw, int stages, double dt, double abs_tol,
                            double rel_tol, int len, cudaStream_t s);
 
+// ---- IAS15 (k_ias15.cu) ------------------------------------------------
+extern const double kIas15H[8];   // Gauss-Radau spacings
+void launch_ias_predict(int L, double *x1, double *v1, const double *x0, const double *v0,
+                        const double *a0, double h, const double *b, double dt, const double *xe,
+                        const double *ve, cudaStream_t s);
+void launch_ias_update_gb(int L, double *g, double *b, const double *F, int i, cudaStream_t s);
+void launch_ias_absmax2(int L, const double *u, const double *w, unsigned long long *out,
+                        cudaStream_t s);
+void launch_ias_delta(int L, const double *b, double *b0, double *d7, cudaStream_t s);
+void launch_ias_advance(int L, double *x1, double *v1, double *txe, double *tve, const double *x0,
+                        const double *v0, const double *a0, const double *b, double dt,
+                        cudaStream_t s);
+void launch_ias_refine(int L, double *b, double *e, const double q[7], int refine, cudaStream_t s);
+void launch_ias_axpy(int L, double *out, const double *x, double c, const double *v,
+                     cudaStream_t s);
+void launch_ias_sub(int L, double *out, const double *u, const double *w, cudaStream_t s);
+
 // ---- embedded Runge-Kutta tableaus (host_rk.cpp) -------------------------
 struct RkTableau {
     int stages, power, power_test;
@@ -204,6 +221,52 @@ ErrorStatus octree_to_host(const AccelerationParam &p, const System *system,
                            const double *box_center, double box_width,
                            LinearOctree *out);
 
+// ---- particle mesh and cosmology (k_pm.cu) ------------------------------
+ErrorStatus pm_acceleration_host(double *a, int n, const double *x, const double *m,
+                                 const double *box_center, double box_width, double H0,
+                                 double omega_m, double mean_bkg_density, int pm_grid_size,
+                                 double scale_factor);
+ErrorStatus pm_leapfrog_cosmology(CosmologicalSystem *system, SimulationStatus *status,
+                                  const bool *is_exit, double dt, double a_begin, double a_final,
+                                  int pm_grid_size);
+
+// ---- snapshots (host_output.cpp) ----------------------------------------
+ErrorStatus output_prepare(OutputParam *op, const Settings *settings);
+// Write snapshot number op->output_count_ from host arrays and count it.
+ErrorStatus output_snapshot_csv(OutputParam *op, int n, const int *ids, const double *x,
+                                const double *v, const double *m, double G, double t, double dt);
+
+class SnapshotWriter;
+
+// Snapshots during a launch_simulation run.  A snapshot taken inside the
+// step loop is copied device->host on the run's stream into pinned memory
+// and written to its file by a writer thread, so the loop does not wait for
+// the file system; the file number is fixed when the snapshot is taken.
+struct OutputContext {
+    OutputParam *op = nullptr;
+    const System *system = nullptr;   // host ids and masses, G
+    double next_time = 0.0;           // the reference's next_output_time
+    std::unique_ptr<SnapshotWriter> writer;
+
+    OutputContext();
+    ~OutputContext();   // waits for the writer
+    bool active() const { return op && op->method == OUTPUT_METHOD_CSV; }
+    // Start of a run: the first snapshot after the initial one is due at
+    // one output interval (src/integrator.c:300-303).
+    void begin() { next_time = op->output_interval; }
+    bool initial() const { return op->output_initial; }
+    bool due(double t) const { return t >= next_time; }
+    // Take a snapshot of n particles at time t after a step of dt: x and v
+    // from the device; ids and masses from the device when d_ids / d_m are
+    // given (n then counts the slots copied and *d_cnt the particles
+    // written), else the host system's.  Moves the next output time to
+    // output_count * interval as the reference does after each snapshot.
+    ErrorStatus take(int n, const double *d_x, const double *d_v, const int *d_ids,
+                     const double *d_m, const int *d_cnt, cudaStream_t s, double t, double dt);
+    // Wait until every snapshot taken is on disk; the first write error.
+    ErrorStatus finish();
+};
+
 }  // namespace gs
 
 // ---- batched ensembles (k_whfast.cu) -----------------------------------
@@ -215,7 +278,7 @@ ErrorStatus ensemble_create(gsgpu_ensemble **out, int num_systems, const int *co
 ErrorStatus ensemble_upload(gsgpu_ensemble *e, const int *ids, const double *x, const double *v,
                             const double *m);
 ErrorStatus ensemble_run_until(gsgpu_ensemble *e, double tf, SimulationStatus *status,
-                               const bool *is_exit);
+                               const bool *is_exit, OutputContext *out = nullptr);
 ErrorStatus ensemble_download(gsgpu_ensemble *e, int *counts, int *ids, double *x, double *v,
                               double *m);
 void ensemble_destroy(gsgpu_ensemble *e);

@@ -192,6 +192,7 @@ bool is_gpu_method(int method)
     case GRAV_GPU_BARNES_HUT_COMPAT:
     case GRAV_GPU_BARNES_HUT_QUAD:
     case GRAV_GPU_BARNES_HUT_GROUP:
+    case GRAV_GPU_BARNES_HUT_GROUP_MONO:
     case GRAV_GPU_BH_LEARNED:
         return true;
     default:
@@ -209,12 +210,14 @@ ErrorStatus make_engine(int method, std::unique_ptr<Engine> &out)
     case GRAV_GPU_BARNES_HUT_COMPAT: out = make_barnes_hut_engine(true); break;
     case GRAV_GPU_BARNES_HUT_QUAD: out = make_barnes_hut_engine(false, true); break;
     case GRAV_GPU_BARNES_HUT_GROUP: out = make_barnes_hut_engine(false, true, true); break;
+    case GRAV_GPU_BARNES_HUT_GROUP_MONO: out = make_barnes_hut_engine(false, false, true); break;
     case GRAV_GPU_BH_LEARNED: out = make_learned_engine(); break;
     default:
         return GS_RAISE(GRAV_VALUE_ERROR,
                         "Unknown acceleration method. Got: %d (this library computes on the GPU "
                         "only: use 101 pairwise, 102 massless, 103 Barnes-Hut, 104 learned "
-                        "Barnes-Hut, 105 quadrupole Barnes-Hut, 106 group Barnes-Hut, 111 FP64 "
+                        "Barnes-Hut, 105 quadrupole Barnes-Hut, 106 / 107 group Barnes-Hut, 111 "
+                        "FP64 "
                         "pairwise, 113 "
                         "reference-compatible Barnes-Hut)",
                         method);
@@ -282,7 +285,8 @@ ErrorStatus finalize_acceleration_param(AccelerationParam *p)
                         p->softening_length);
     const bool bh = p->method == GRAV_GPU_BARNES_HUT || p->method == GRAV_GPU_BARNES_HUT_COMPAT ||
                     p->method == GRAV_GPU_BARNES_HUT_QUAD || p->method == GRAV_GPU_BH_LEARNED ||
-                    p->method == GRAV_GPU_BARNES_HUT_GROUP;
+                    p->method == GRAV_GPU_BARNES_HUT_GROUP ||
+                    p->method == GRAV_GPU_BARNES_HUT_GROUP_MONO;
     if (bh && p->opening_angle < 0.0)
         return GS_RAISE(GRAV_VALUE_ERROR, "Opening angle is negative. Got: %.3g",
                         p->opening_angle);

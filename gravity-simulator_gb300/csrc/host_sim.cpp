@@ -152,15 +152,18 @@ struct gsgpu_sim {
     bool graph_failed = false;
     ForceTimer timer;
     int kernels_last = 0;
-    // embedded Runge-Kutta (integrators 5-8)
+    // embedded Runge-Kutta (integrators 5-8) and IAS15 (9)
     double tolerance = -1.0, initial_dt = -1.0;
     DBuf e_vk, e_xk, e_x1, e_v1, e_txe, e_tve, e_xs, e_terms;
     double *h_terms = nullptr;   // pinned host copy of the 6N error terms
+    DBuf i_b0, i_b, i_g, i_e, i_F, i_a1, i_d7, i_max;
+    unsigned long long *h_max = nullptr;   // pinned: two maxima
 
     ~gsgpu_sim()
     {
         if (graph) cudaGraphExecDestroy(graph);
         if (h_terms) cudaFreeHost(h_terms);
+        if (h_max) cudaFreeHost(h_max);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
 
@@ -214,12 +217,150 @@ struct gsgpu_sim {
         return ok();
     }
 
+    // Exact maxima of |u| and |w| over 3N elements (one synchronisation).
+    ErrorStatus absmax2(const double *u, const double *w, double *mu, double *mw)
+    {
+        GS_CUDA(cudaMemsetAsync(i_max.p, 0, 2 * sizeof(unsigned long long), stream));
+        launch_ias_absmax2(len(), u, w, i_max.as<unsigned long long>(), stream);
+        GS_CUDA(cudaGetLastError());
+        GS_CUDA(cudaMemcpyAsync(h_max, i_max.p, 2 * sizeof(unsigned long long),
+                                cudaMemcpyDeviceToHost, stream));
+        GS_CUDA(cudaStreamSynchronize(stream));
+        GS_TRY(engine->check_status(stream));
+        std::memcpy(mu, &h_max[0], sizeof(double));
+        std::memcpy(mw, &h_max[1], sizeof(double));
+        return ok();
+    }
+
+    // src/integrator_ias15.c:229-616.  The element-wise predictor, g / b
+    // updates, step end and b prediction run on the GPU (k_ias15.cu); the
+    // predictor-corrector iterations, the convergence test, the error
+    // estimate (glibc pow) and the step-size control run here on exact
+    // maxima, so the step sequence is the reference's.
+    ErrorStatus ias15_run(double tf, SimulationStatus *status, const bool *is_exit,
+                          OutputContext *oc)
+    {
+        if (!(tolerance > 0.0))
+            return GS_RAISE(GRAV_VALUE_ERROR, "tolerance must be positive. Got: %g", tolerance);
+        const int L = len();
+        const size_t SL = (size_t)L;
+        double *b0 = i_b0.as<double>(), *b = i_b.as<double>(), *g = i_g.as<double>(),
+               *e = i_e.as<double>(), *F = i_F.as<double>(), *a1 = i_a1.as<double>(),
+               *d7 = i_d7.as<double>();
+        double *x1 = e_x1.as<double>(), *v1 = e_v1.as<double>(), *txe = e_txe.as<double>(),
+               *tve = e_tve.as<double>();
+        GS_CUDA(cudaMemsetAsync(b0, 0, 7 * SL * sizeof(double), stream));
+        GS_CUDA(cudaMemsetAsync(b, 0, 7 * SL * sizeof(double), stream));
+        GS_CUDA(cudaMemsetAsync(g, 0, 7 * SL * sizeof(double), stream));
+        GS_CUDA(cudaMemsetAsync(e, 0, 7 * SL * sizeof(double), stream));
+        GS_CUDA(cudaMemsetAsync(F, 0, 8 * SL * sizeof(double), stream));
+        GS_TRY(force(a.as<double>()));
+        double h;
+        if (initial_dt > 0.0) {
+            h = initial_dt;
+        } else {
+            // src/integrator_ias15.c:702-806 (power 15)
+            double d0 = 0.0, d1 = 0.0, d2 = 0.0, dummy = 0.0;
+            GS_TRY(absmax2(x.as<double>(), a.as<double>(), &d0, &d1));
+            const double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
+            launch_ias_axpy(L, x1, x.as<double>(), dt0, v.as<double>(), stream);
+            GS_CUDA(cudaGetLastError());
+            GS_TRY(engine->compute(x1, m.as<double>(), a1, stream, nullptr));
+            launch_ias_sub(L, d7, a1, a.as<double>(), stream);
+            GS_CUDA(cudaGetLastError());
+            GS_TRY(absmax2(d7, d7, &d2, &dummy));
+            d2 = d2 / dt0;
+            double dt1;
+            if (std::fmax(d1, d2) <= 1e-15)
+                dt1 = std::fmax(1e-6, dt0 * 1e-3);
+            else
+                dt1 = std::pow((0.01 / std::fmax(d1, d2)), 1.0 / (1.0 + (double)15));
+            h = std::fmin(100.0 * dt0, dt1);
+            if (h <= 0.0) return GS_RAISE(GRAV_VALUE_ERROR, "Initial dt is less than or equal to zero");
+            if (h > tf) h = tf;
+        }
+        GS_TRY(initial_snapshot(oc, status));
+        double t = 0.0;
+        int64_t steps = 0;
+        bool refine = false;
+        if (status) {
+            status->t = 0.0;
+            status->dt = h;
+            status->num_steps = 0;
+        }
+        while (t < tf) {
+            for (int it = 0; it < 12; ++it) {
+                for (int i = 0; i < 8; ++i) {
+                    launch_ias_predict(L, x1, v1, x.as<double>(), v.as<double>(), a.as<double>(),
+                                       kIas15H[i], b, h, xe.as<double>(), ve.as<double>(), stream);
+                    GS_CUDA(cudaGetLastError());
+                    GS_TRY(engine->compute(x1, m.as<double>(), F + (size_t)i * SL, stream,
+                                           timer.enabled ? &timer : nullptr));
+                    launch_ias_update_gb(L, g, b, F, i, stream);
+                    GS_CUDA(cudaGetLastError());
+                }
+                launch_ias_delta(L, b, b0, d7, stream);
+                GS_CUDA(cudaGetLastError());
+                double md = 0.0, mf = 0.0;
+                GS_TRY(absmax2(d7, F + 7 * SL, &md, &mf));
+                if ((md / mf) < 1e-16) break;
+            }
+            GS_CUDA(cudaMemcpyAsync(txe, xe.p, bytes3(), cudaMemcpyDeviceToDevice, stream));
+            GS_CUDA(cudaMemcpyAsync(tve, ve.p, bytes3(), cudaMemcpyDeviceToDevice, stream));
+            launch_ias_advance(L, x1, v1, txe, tve, x.as<double>(), v.as<double>(), a.as<double>(),
+                               b, h, stream);
+            GS_CUDA(cudaGetLastError());
+            GS_TRY(engine->compute(x1, m.as<double>(), a1, stream, nullptr));
+            double mb = 0.0, ma = 0.0;
+            GS_TRY(absmax2(b + 6 * SL, a1, &mb, &ma));
+            const double eb7 = mb / ma;
+            double error = std::pow((eb7 / tolerance), 1.0 / 7.0);
+            if (error < 1e-10) error = 1e-10;
+            const double dt_new = h / error;
+            if (error <= 1.0 || h == tf * 1e-12) {
+                ++steps;
+                t += h;
+                const double q = dt_new / h;
+                double qs[7];
+                qs[0] = q;
+                for (int r = 1; r < 7; ++r) qs[r] = qs[r - 1] * q;
+                launch_ias_refine(L, b, e, qs, refine ? 1 : 0, stream);
+                GS_CUDA(cudaGetLastError());
+                refine = true;
+                GS_CUDA(cudaMemcpyAsync(xe.p, txe, bytes3(), cudaMemcpyDeviceToDevice, stream));
+                GS_CUDA(cudaMemcpyAsync(ve.p, tve, bytes3(), cudaMemcpyDeviceToDevice, stream));
+                GS_CUDA(cudaMemcpyAsync(x.p, x1, bytes3(), cudaMemcpyDeviceToDevice, stream));
+                GS_CUDA(cudaMemcpyAsync(v.p, v1, bytes3(), cudaMemcpyDeviceToDevice, stream));
+                GS_CUDA(cudaMemcpyAsync(a.p, a1, bytes3(), cudaMemcpyDeviceToDevice, stream));
+                if (oc && oc->due(t)) GS_TRY(snapshot(oc, v.as<double>(), t, h));
+            }
+            if (dt_new > (h / 0.25))
+                h /= 0.25;
+            else if (dt_new < h * 0.25)
+                h *= 0.25;
+            else
+                h = dt_new;
+            if (dt_new < tf * 1e-12) h = tf * 1e-12;
+            if (t < tf && t + h > tf) h = tf - t;
+            if (status) {
+                status->t = t;
+                status->dt = h;
+                status->num_steps = steps;
+            }
+            if (is_exit && *is_exit) break;
+        }
+        GS_CUDA(cudaStreamSynchronize(stream));
+        if (oc) GS_TRY(oc->finish());
+        return ok();
+    }
+
     // src/integrator_rk_embedded.c:522-987: stages and the weighted combine
     // on the GPU; the RMS error is summed on the host in the reference's
     // element order from the per-element terms, and the step-size control
     // (glibc pow) runs on the host, so accept / reject decisions and dt
     // follow the reference's exactly.
-    ErrorStatus rk_emb_run(double tf, SimulationStatus *status, const bool *is_exit)
+    ErrorStatus rk_emb_run(double tf, SimulationStatus *status, const bool *is_exit,
+                           OutputContext *oc)
     {
         const RkTableau *T = rk_tableau(integrator);
         if (!T) return GS_RAISE(GRAV_VALUE_ERROR, "Invalid integrator method");
@@ -238,6 +379,7 @@ struct gsgpu_sim {
             GS_TRY(rk_emb_initial_dt(T->power, &h));
             if (h > tf) h = tf;
         }
+        GS_TRY(initial_snapshot(oc, status));
         double t = 0.0;
         int64_t steps = 0;
         if (status) {
@@ -278,6 +420,7 @@ struct gsgpu_sim {
                 GS_CUDA(cudaMemcpyAsync(v.p, e_v1.p, bytes3(), cudaMemcpyDeviceToDevice, stream));
                 GS_CUDA(cudaMemcpyAsync(xe.p, e_txe.p, bytes3(), cudaMemcpyDeviceToDevice, stream));
                 GS_CUDA(cudaMemcpyAsync(ve.p, e_tve.p, bytes3(), cudaMemcpyDeviceToDevice, stream));
+                if (oc && oc->due(t)) GS_TRY(snapshot(oc, v.as<double>(), t, h));
             }
             if (error < 1e-10) error = 1e-10;
             const double dt_new = h * fac / std::pow(error, 1.0 / (1.0 + (double)min_power));
@@ -297,7 +440,27 @@ struct gsgpu_sim {
             if (is_exit && *is_exit) break;
         }
         GS_CUDA(cudaStreamSynchronize(stream));
+        if (oc) GS_TRY(oc->finish());
         return ok();
+    }
+
+    // The initial snapshot (output_initial): the caller's host state, with
+    // the time and dt the status holds on entry, as the reference writes it.
+    ErrorStatus initial_snapshot(OutputContext *oc, const SimulationStatus *status)
+    {
+        if (!oc) return ok();
+        oc->begin();
+        if (!oc->initial()) return ok();
+        const System *sys = oc->system;
+        return output_snapshot_csv(oc->op, n, sys->particle_ids, sys->x, sys->v, sys->m, G,
+                                   status ? status->t : 0.0, status ? status->dt : 0.0);
+    }
+
+    // A snapshot of x and the velocity array dv at time t after a step of h
+    // (asynchronous: dv must stay unchanged until the next step's kernels).
+    ErrorStatus snapshot(OutputContext *oc, const double *dv, double t, double h)
+    {
+        return oc->take(n, x.as<double>(), dv, nullptr, nullptr, nullptr, stream, t, h);
     }
 
     size_t bytes3() const { return (size_t)n * 3 * sizeof(double); }
@@ -461,6 +624,15 @@ ErrorStatus sim_create(gsgpu_sim **out, int n, double G, const AccelerationParam
         GS_TRY(s->x0.reserve(b3));
         GS_TRY(s->v0.reserve(b3));
         for (int k = 0; k < 8; ++k) GS_TRY(s->rk[k].reserve(b3));
+    } else if (integrator == INTEGRATOR_IAS15) {
+        DBuf *b7[] = {&s->i_b0, &s->i_b, &s->i_g, &s->i_e};
+        for (DBuf *b : b7) GS_TRY(b->reserve(7 * b3));
+        GS_TRY(s->i_F.reserve(8 * b3));
+        DBuf *b1[] = {&s->i_a1, &s->i_d7, &s->e_x1, &s->e_v1, &s->e_txe, &s->e_tve};
+        for (DBuf *b : b1) GS_TRY(b->reserve(b3));
+        GS_TRY(s->i_max.reserve(2 * sizeof(unsigned long long)));
+        GS_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&s->h_max), 2 * sizeof(unsigned long long),
+                              cudaHostAllocDefault));
     } else if (const RkTableau *T = rk_tableau(integrator)) {
         GS_TRY(s->e_vk.reserve(b3 * T->stages));
         GS_TRY(s->e_xk.reserve(b3 * T->stages));
@@ -525,14 +697,23 @@ ErrorStatus sim_download(gsgpu_sim *s, double *x, double *v)
 }
 
 // Run the reference's step loop for time tf with an is_exit check per step.
-ErrorStatus sim_run_until(gsgpu_sim *s, double tf, SimulationStatus *status, const bool *is_exit)
+ErrorStatus sim_run_until(gsgpu_sim *s, double tf, SimulationStatus *status, const bool *is_exit,
+                          OutputContext *out)
 {
-    if (rk_tableau(s->integrator)) return s->rk_emb_run(tf, status, is_exit);
+    OutputContext *oc = out && out->active() ? out : nullptr;
+    if (rk_tableau(s->integrator)) return s->rk_emb_run(tf, status, is_exit, oc);
+    if (s->integrator == INTEGRATOR_IAS15) return s->ias15_run(tf, status, is_exit, oc);
     double dt = s->dt;
     const int64_t total = (int64_t)std::ceil(tf / dt);
+    GS_TRY(s->initial_snapshot(oc, status));
     GS_TRY(s->prime());
     double t = 0.0;
     int64_t steps = 0;
+    if (status) {
+        status->t = 0.0;
+        status->dt = dt;
+        status->num_steps = 0;
+    }
     const bool clamp = s->integrator != INTEGRATOR_RK4;
     while (steps < total) {
         if (clamp && t + dt > tf) dt = tf - t;
@@ -540,6 +721,19 @@ ErrorStatus sim_run_until(gsgpu_sim *s, double tf, SimulationStatus *status, con
         GS_TRY(s->step_graph(dt));
         ++steps;
         t = (double)steps * dt;
+        if (oc && oc->due(t)) {
+            // leapfrog writes v at integer time, v - 0.5 a dt (src/integrator.c:1043-1071)
+            const double *dv = s->v.as<double>();
+            if (s->integrator == INTEGRATOR_LEAPFROG) {
+                GS_CUDA(cudaMemcpyAsync(s->tmp.p, s->v.p, s->bytes3(), cudaMemcpyDeviceToDevice,
+                                        s->stream));
+                launch_plain_kick(s->tmp.as<double>(), s->a.as<double>(), 0.5, dt, s->len(),
+                                  s->stream);
+                GS_CUDA(cudaGetLastError());
+                dv = s->tmp.as<double>();
+            }
+            GS_TRY(s->snapshot(oc, dv, t, dt));
+        }
         if ((steps & 31) == 0) {
             GS_CUDA(cudaStreamSynchronize(s->stream));
             GS_TRY(s->engine->check_status(s->stream));
@@ -551,6 +745,7 @@ ErrorStatus sim_run_until(gsgpu_sim *s, double tf, SimulationStatus *status, con
         status->num_steps = steps;
     }
     GS_CUDA(cudaStreamSynchronize(s->stream));
+    if (oc) GS_TRY(oc->finish());
     return ok();
 }
 
@@ -620,7 +815,7 @@ int gsgpu_sim_run_until(gsgpu_sim *sim, double tf)
 {
     if (!sim) return GRAV_POINTER_ERROR;
     SimulationStatus ss{};
-    ErrorStatus st = gs::sim_run_until(sim, tf, &ss, nullptr);
+    ErrorStatus st = gs::sim_run_until(sim, tf, &ss, nullptr, nullptr);
     if (st.return_code != GRAV_SUCCESS) {
         print_and_free_traceback(&st);
         return st.return_code;
@@ -780,23 +975,15 @@ ErrorStatus launch_simulation(System *system, IntegratorParam *integrator_param,
     if (!fixed && integrator_param->tolerance <= 0.0)
         return GS_RAISE(GRAV_VALUE_ERROR, "tolerance must be positive. Got: %g",
                         integrator_param->tolerance);
-    // finalize_output_param (src/output.c:126-239): snapshots are not written
-    // by the GPU library.
-    if (!output_param) return GS_RAISE(GRAV_POINTER_ERROR, "output_param is NULL");
-    if (output_param->method != OUTPUT_METHOD_DISABLED) {
-        if (output_param->method == OUTPUT_METHOD_CSV || output_param->method == OUTPUT_METHOD_HDF5)
-            return GS_RAISE(GRAV_NOT_IMPLEMENTED_ERROR,
-                            "snapshot output (method %d) is not part of the GPU library; "
-                            "use output method 1 (disabled)", output_param->method);
-        return GS_RAISE(GRAV_VALUE_ERROR, "Unknown output method. Got: %d", output_param->method);
-    }
-    if (tf < 0.0) return GS_RAISE(GRAV_VALUE_ERROR, "tf must be non-negative. Got: %g", tf);
+    // finalize_output_param (src/output.c:126-239)
     if (!settings) return GS_RAISE(GRAV_POINTER_ERROR, "settings is NULL");
+    GS_TRY(output_prepare(output_param, settings));
+    if (tf < 0.0) return GS_RAISE(GRAV_VALUE_ERROR, "tf must be non-negative. Got: %g", tf);
     if (!simulation_status) return GS_RAISE(GRAV_POINTER_ERROR, "simulation_status is NULL");
+    OutputContext oc;
+    oc.op = output_param;
+    oc.system = system;
 
-    if (integ == INTEGRATOR_IAS15)
-        return GS_RAISE(GRAV_NOT_IMPLEMENTED_ERROR,
-                        "integrator %d has no GPU implementation in this library", integ);
 
     if (integ == INTEGRATOR_WHFAST) {
         // src/integrator_whfast.c:200-407 as a one-system ensemble; the
@@ -811,11 +998,9 @@ ErrorStatus launch_simulation(System *system, IntegratorParam *integrator_param,
         std::unique_ptr<gsgpu_ensemble, void (*)(gsgpu_ensemble *)> ens(raw, gs::ensemble_destroy);
         GS_TRY(gs::ensemble_upload(ens.get(), system->particle_ids, system->x, system->v,
                                    system->m));
-        simulation_status->t = 0.0;
-        simulation_status->dt = integrator_param->dt;
-        simulation_status->num_steps = 0;
         if (settings->verbose >= 1) std::fputs("Launching simulation...\n", stdout);
-        GS_TRY(gs::ensemble_run_until(ens.get(), tf, simulation_status, settings->is_exit_ptr));
+        GS_TRY(gs::ensemble_run_until(ens.get(), tf, simulation_status, settings->is_exit_ptr,
+                                      &oc));
         int n1 = n0;
         GS_TRY(gs::ensemble_download(ens.get(), &n1, system->particle_ids, system->x, system->v,
                                      system->m));
@@ -840,10 +1025,7 @@ ErrorStatus launch_simulation(System *system, IntegratorParam *integrator_param,
     sim->tolerance = integrator_param->tolerance;
     sim->initial_dt = integrator_param->initial_dt;
     GS_TRY(gs::sim_upload(sim.get(), system->x, system->v, system->m));
-    simulation_status->t = 0.0;
-    simulation_status->dt = integrator_param->dt;
-    simulation_status->num_steps = 0;
-    GS_TRY(gs::sim_run_until(sim.get(), tf, simulation_status, settings->is_exit_ptr));
+    GS_TRY(gs::sim_run_until(sim.get(), tf, simulation_status, settings->is_exit_ptr, &oc));
     GS_TRY(gs::sim_download(sim.get(), system->x, system->v));
     return ok();
 }

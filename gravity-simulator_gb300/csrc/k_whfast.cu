@@ -1035,12 +1035,16 @@ struct gsgpu_ensemble {
         return ok();
     }
 
-    ErrorStatus prime()
+    ErrorStatus prime(OutputContext *oc = nullptr, const SimulationStatus *status = nullptr)
     {
         if (primed) return ok();
         if (integrator == INTEGRATOR_WHFAST) {
             // src/integrator_whfast.c:241-273
             GS_TRY(sort(E.x, E.v));
+            if (oc && oc->initial()) {
+                // the initial snapshot is of the system sorted by distance
+                GS_TRY(snapshot(oc, E.v, status ? status->t : 0.0, status ? status->dt : 0.0));
+            }
             k_wh_seq<<<seq_grid(), 32 * SEQ_WARPS, 0, stream>>>(E, 0);
             GS_TRY(accel());
             k_wh_kick<<<pgrid(), 128, 0, stream>>>(E, P, 0.5 * dt);
@@ -1075,6 +1079,28 @@ struct gsgpu_ensemble {
     }
 
     int kernels_per_step() const { return integrator == INTEGRATOR_WHFAST ? 6 : 3; }
+
+    // Snapshot of system 0 (a launch_simulation run holds one system): E.x
+    // and the velocity array dv with the ids and masses of its live slots.
+    ErrorStatus snapshot(OutputContext *oc, const double *dv, double t, double h)
+    {
+        return oc->take(P, E.x, dv, E.ids, E.m, E.cnt, stream, t, h);
+    }
+
+    // src/integrator_whfast.c:345-364: the Cartesian state at integer time
+    // from the Jacobi velocities kicked back by half a step (in scratch),
+    // written into the Cartesian arrays, which the next step recomputes.
+    ErrorStatus whfast_snapshot(OutputContext *oc, double t, double h)
+    {
+        GS_CUDA(cudaMemcpyAsync(E.t_v, E.jv, (size_t)P * 3 * sizeof(double),
+                                cudaMemcpyDeviceToDevice, stream));
+        EnsDev T = E;
+        T.jv = E.t_v;
+        k_wh_kick<<<pgrid(), 128, 0, stream>>>(T, P, -0.5 * h);
+        k_wh_seq<<<seq_grid(), 32 * SEQ_WARPS, 0, stream>>>(T, 1);
+        GS_CUDA(cudaGetLastError());
+        return snapshot(oc, E.v, t, h);
+    }
 
     ErrorStatus step_graph(double h)
     {
@@ -1238,19 +1264,29 @@ ErrorStatus ensemble_upload(gsgpu_ensemble *e, const int *ids, const double *x, 
 
 // The reference's step loop over time tf (same step count and dt clamp).
 ErrorStatus ensemble_run_until(gsgpu_ensemble *e, double tf, SimulationStatus *status,
-                               const bool *is_exit)
+                               const bool *is_exit, OutputContext *out)
 {
+    OutputContext *oc = out && out->active() ? out : nullptr;
+    if (oc && (e->S != 1 || e->integrator != INTEGRATOR_WHFAST))
+        return GS_RAISE(GRAV_VALUE_ERROR, "snapshots are written for one-system WHFast runs only");
     double dt = e->dt;
     const int64_t total = (int64_t)std::ceil(tf / dt);
-    GS_TRY(e->prime());
+    GS_TRY(e->prime(oc, status));
+    if (oc) oc->begin();   // the initial snapshot leaves the next output time alone
     double t = 0.0;
     int64_t steps = 0;
+    if (status) {
+        status->t = 0.0;
+        status->dt = dt;
+        status->num_steps = 0;
+    }
     while (steps < total) {
         if (t + dt > tf) dt = tf - t;
         if (status) status->dt = dt;
         GS_TRY(e->step_graph(dt));
         ++steps;
         t = (double)steps * dt;
+        if (oc && oc->due(t)) GS_TRY(e->whfast_snapshot(oc, t, dt));
         if ((steps & 31) == 0) GS_TRY(e->check());
         if (is_exit && *is_exit) break;
     }
@@ -1259,6 +1295,7 @@ ErrorStatus ensemble_run_until(gsgpu_ensemble *e, double tf, SimulationStatus *s
         status->num_steps = steps;
     }
     GS_TRY(e->check());
+    if (oc) GS_TRY(oc->finish());
     return ok();
 }
 

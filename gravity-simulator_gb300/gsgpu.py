@@ -48,6 +48,7 @@ METHOD_GPU_BARNES_HUT = 103        # FP32 walk, true leaf multipoles
 METHOD_GPU_BH_LEARNED = 104        # theta-cheap walk + learned MLP residual
 METHOD_GPU_BARNES_HUT_QUAD = 105   # FP32 walk, monopole + quadrupole cell terms
 METHOD_GPU_BARNES_HUT_GROUP = 106  # group walk with interaction lists, quadrupole cells
+METHOD_GPU_BARNES_HUT_GROUP_MONO = 107  # group walk with interaction lists, monopole cells
 METHOD_GPU_PAIRWISE_FP64 = 111     # FP64 direct sum in the reference's order
 METHOD_GPU_BARNES_HUT_COMPAT = 113 # FP32 walk reproducing the reference's tree quirks
 
@@ -124,6 +125,51 @@ class LinearOctree(ctypes.Structure):
     ]
 
 
+class CosmologicalSystem(ctypes.Structure):
+    """src/system.h:22-38"""
+    _fields_ = [
+        ("num_particles", ctypes.c_int),
+        ("particle_ids", c_int_p),
+        ("x", c_double_p),
+        ("v", c_double_p),
+        ("m", c_double_p),
+        ("h", ctypes.c_double),
+        ("omega_m", ctypes.c_double),
+        ("omega_lambda", ctypes.c_double),
+        ("omega_k", ctypes.c_double),
+        ("box_center", ctypes.c_double * 3),
+        ("box_width", ctypes.c_double),
+        ("unit_mass", ctypes.c_double),
+        ("unit_length", ctypes.c_double),
+        ("unit_time", ctypes.c_double),
+    ]
+
+
+class OutputParam(ctypes.Structure):
+    """src/common.h:38-49"""
+    _fields_ = [
+        ("method", ctypes.c_int),
+        ("output_dir", ctypes.c_char_p),
+        ("output_initial", ctypes.c_bool),
+        ("output_interval", ctypes.c_double),
+        ("coordinate_output_dtype", ctypes.c_int),
+        ("velocity_output_dtype", ctypes.c_int),
+        ("mass_output_dtype", ctypes.c_int),
+        ("output_count_", ctypes.c_int),
+    ]
+
+
+class SimulationStatus(ctypes.Structure):
+    """src/common.h:51-56"""
+    _fields_ = [("t", ctypes.c_double), ("dt", ctypes.c_double), ("num_steps", ctypes.c_int64)]
+
+
+class Settings(ctypes.Structure):
+    """src/settings.h:11-16"""
+    _fields_ = [("verbose", ctypes.c_int), ("enable_progress_bar", ctypes.c_bool),
+                ("is_exit_ptr", ctypes.POINTER(ctypes.c_bool))]
+
+
 def library_path() -> Path:
     return HERE / LIB_NAME
 
@@ -186,6 +232,61 @@ def make_system(x: np.ndarray, m: np.ndarray, G: float,
     return s, (x, v, m, ids)
 
 
+def acceleration_pm(lib: ctypes.CDLL, x: np.ndarray, m: np.ndarray, box_center, box_width: float,
+                    H0: float, omega_m: float, mean_bkg_density: float, pm_grid_size: int,
+                    scale_factor: float) -> np.ndarray:
+    """acceleration_PM (src/acceleration_PM.c:274-391) on host arrays."""
+    lib.acceleration_PM.restype = ErrorStatus
+    lib.acceleration_PM.argtypes = [c_double_p, ctypes.c_int, c_double_p, c_double_p, c_double_p,
+                                    ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_double, ctypes.c_int, ctypes.c_double]
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    m = np.ascontiguousarray(m, dtype=np.float64)
+    c = np.ascontiguousarray(box_center, dtype=np.float64)
+    a = np.empty((m.shape[0], 3))
+    st = lib.acceleration_PM(_dp(a), int(m.shape[0]), _dp(x), _dp(m), _dp(c), float(box_width),
+                             float(H0), float(omega_m), float(mean_bkg_density), int(pm_grid_size),
+                             float(scale_factor))
+    if st.return_code != 0:
+        raise GravError(st.return_code, take_traceback(lib, st))
+    return a
+
+
+def launch_cosmological_simulation(lib: ctypes.CDLL, x: np.ndarray, v: np.ndarray, m: np.ndarray,
+                                   *, h: float, omega_m: float, omega_lambda: float, box_center,
+                                   box_width: float, dt: float, a_begin: float, a_final: float,
+                                   pm_grid_size: int, output_method: int = OUTPUT_METHOD_DISABLED,
+                                   ids: Optional[np.ndarray] = None):
+    """launch_cosmological_simulation (src/grav_sim.c:140-255).  x is advanced
+    in place (v is left as the reference leaves it); returns the status
+    (t = final scale factor, dt, num_steps)."""
+    lib.launch_cosmological_simulation.restype = ErrorStatus
+    lib.launch_cosmological_simulation.argtypes = [
+        ctypes.POINTER(CosmologicalSystem), ctypes.POINTER(OutputParam),
+        ctypes.POINTER(SimulationStatus), ctypes.POINTER(Settings), ctypes.c_double,
+        ctypes.c_double, ctypes.c_double, ctypes.c_int]
+    n = int(m.shape[0])
+    assert x.flags.c_contiguous and x.dtype == np.float64 and v.flags.c_contiguous
+    ids = np.arange(n, dtype=np.int32) if ids is None else np.ascontiguousarray(ids, np.int32)
+    m = np.ascontiguousarray(m, dtype=np.float64)
+    sysc = CosmologicalSystem(n, _ip(ids), _dp(x), _dp(v), _dp(m), float(h), float(omega_m),
+                              float(omega_lambda), 1.0 - omega_m - omega_lambda,
+                              (ctypes.c_double * 3)(*[float(q) for q in box_center]),
+                              float(box_width), 1.0, 1.0, 1.0)
+    op = OutputParam(int(output_method), None, False, 1.0, OUTPUT_DTYPE_DOUBLE,
+                     OUTPUT_DTYPE_DOUBLE, OUTPUT_DTYPE_DOUBLE, 0)
+    status = SimulationStatus(0.0, 0.0, 0)
+    flag = ctypes.c_bool(False)
+    settings = Settings(0, False, ctypes.pointer(flag))
+    st = lib.launch_cosmological_simulation(ctypes.byref(sysc), ctypes.byref(op),
+                                            ctypes.byref(status), ctypes.byref(settings),
+                                            float(dt), float(a_begin), float(a_final),
+                                            int(pm_grid_size))
+    if st.return_code != 0:
+        raise GravError(st.return_code, take_traceback(lib, st))
+    return status
+
+
 def take_traceback(lib: ctypes.CDLL, st: ErrorStatus) -> str:
     text = ""
     if st.traceback:
@@ -226,11 +327,19 @@ def launch_simulation(lib: ctypes.CDLL, x: np.ndarray, v: np.ndarray,
                       tolerance: float = -1.0, initial_dt: float = -1.0,
                       whfast_remove_invalid_particles: bool = True,
                       ids: Optional[np.ndarray] = None, verbose: int = 0,
-                      is_exit: Optional[ctypes.c_bool] = None):
+                      is_exit: Optional[ctypes.c_bool] = None,
+                      output_method: int = OUTPUT_METHOD_DISABLED,
+                      output_dir: Optional[str] = None, output_initial: bool = False,
+                      output_interval: float = 0.0,
+                      coordinate_output_dtype: int = OUTPUT_DTYPE_DOUBLE,
+                      velocity_output_dtype: int = OUTPUT_DTYPE_DOUBLE,
+                      mass_output_dtype: int = OUTPUT_DTYPE_DOUBLE):
     """Mirror of Simulator.launch_simulation (grav_sim/simulator.py:22-143):
     runs ``launch_simulation_python`` on a worker thread, raises
     RuntimeError when it returns non-zero, and returns the (possibly
-    shrunk) (ids, x, v, m) arrays.  x and v are updated in place."""
+    shrunk) (ids, x, v, m) arrays.  x and v are updated in place.  The
+    output arguments are those of grav_sim/parameters.py's OutputParam
+    (``output_dir`` None lets the library name a snapshots_<date>/ folder)."""
     n = int(m.shape[0])
     num = ctypes.c_int32(n)
     ids = np.arange(n, dtype=np.int32) if ids is None else ids
@@ -252,9 +361,11 @@ def launch_simulation(lib: ctypes.CDLL, x: np.ndarray, v: np.ndarray,
         ctypes.c_double(initial_dt), ctypes.c_bool(whfast_remove_invalid_particles),
         ctypes.c_int32(method), ctypes.c_double(opening_angle),
         ctypes.c_double(softening_length), ctypes.c_int32(max_num_particles_per_leaf),
-        ctypes.c_int32(OUTPUT_METHOD_DISABLED), b"", ctypes.c_bool(False),
-        ctypes.c_double(0.0), ctypes.c_int32(OUTPUT_DTYPE_DOUBLE),
-        ctypes.c_int32(OUTPUT_DTYPE_DOUBLE), ctypes.c_int32(OUTPUT_DTYPE_DOUBLE),
+        ctypes.c_int32(output_method),
+        None if output_dir is None else ctypes.c_char_p(str(output_dir).encode()),
+        ctypes.c_bool(output_initial), ctypes.c_double(output_interval),
+        ctypes.c_int32(coordinate_output_dtype), ctypes.c_int32(velocity_output_dtype),
+        ctypes.c_int32(mass_output_dtype),
         ctypes.c_int32(verbose), ctypes.c_bool(False), ctypes.byref(flag),
         ctypes.c_double(tf),
     )

@@ -66,6 +66,7 @@ typedef struct System {
 #define GRAV_GPU_BH_LEARNED 104         /* theta-cheap walk + learned residual */
 #define GRAV_GPU_BARNES_HUT_QUAD 105    /* FP32 walk, monopole + quadrupole cells */
 #define GRAV_GPU_BARNES_HUT_GROUP 106   /* group walk, interaction lists, quadrupoles */
+#define GRAV_GPU_BARNES_HUT_GROUP_MONO 107  /* group walk, monopole cells only */
 #define GRAV_GPU_PAIRWISE_FP64 111      /* FP64 direct sum, reference order */
 #define GRAV_GPU_BARNES_HUT_COMPAT 113  /* FP32 walk, reference tree quirks */
 
@@ -109,6 +110,9 @@ typedef struct OutputParam {
 #define OUTPUT_METHOD_DISABLED 1
 #define OUTPUT_METHOD_CSV 2
 #define OUTPUT_METHOD_HDF5 3
+/* src/output.h:18-19 */
+#define OUTPUT_DTYPE_FLOAT 1
+#define OUTPUT_DTYPE_DOUBLE 2
 
 typedef struct SimulationStatus {
     double t;
@@ -190,6 +194,58 @@ ErrorStatus launch_simulation(System *system, IntegratorParam *integrator_param,
                               SimulationStatus *simulation_status,
                               Settings *settings, double tf);
 
+/* ---- particle mesh and cosmology (src/acceleration_PM.c,
+ *      src/integrator_cosmology_leapfrog.c, src/cosmology.c) ----------- */
+
+/* src/system.h:22-38 */
+typedef struct CosmologicalSystem {
+    int num_particles;
+    int *particle_ids;
+    double *x;
+    double *v;
+    double *m;
+    double h;
+    double omega_m;
+    double omega_lambda;
+    double omega_k;
+    double box_center[3];
+    double box_width;
+    double unit_mass;
+    double unit_length;
+    double unit_time;
+} CosmologicalSystem;
+
+/* src/system.h:78 */
+CosmologicalSystem get_new_cosmological_system(void);
+/* src/system.h:111 */
+ErrorStatus finalize_cosmological_system(CosmologicalSystem *system);
+/* src/system.h:287 (host arrays) */
+void set_periodic_boundary_conditions(CosmologicalSystem *system);
+/* src/cosmology.h:5-15 */
+double compute_omega_k(double omega_m, double omega_lambda);
+double compute_da(double a, double H0, double omega_m, double omega_lambda);
+
+/* src/acceleration.h:73-85.  Host arrays in and out; the cloud-in-cell
+ * deposit and interpolation, the Green's function and the gradient run on the
+ * GPU, the 3-D r2c / c2r transforms through cuFFT (FFTW's layout). */
+ErrorStatus acceleration_PM(double *a, int num_particles, const double *x, const double *m,
+                            const double *box_center, double box_width, double H0,
+                            double omega_m, double mean_bkg_density, int pm_grid_size,
+                            double scale_factor);
+
+/* src/integrator.h:155-164.  Output must be disabled: cosmological
+ * snapshots are HDF5, which is not available (as in the reference built
+ * without libhdf5).  x advances in place; v is left as given. */
+ErrorStatus leapfrog_cosmology(CosmologicalSystem *system, OutputParam *output_param,
+                               SimulationStatus *simulation_status, Settings *settings, double dt,
+                               double a_begin, double a_final, int pm_grid_size);
+
+/* src/grav_sim.h:71-80 */
+ErrorStatus launch_cosmological_simulation(CosmologicalSystem *system, OutputParam *output_param,
+                                           SimulationStatus *simulation_status,
+                                           Settings *settings, double dt, double a_begin,
+                                           double a_final, int pm_grid_size);
+
 /* src/python_interface.c:94-125 */
 int launch_simulation_python(
     int32_t *num_particles, int32_t *particle_ids, double *x, double *v,
@@ -252,10 +308,12 @@ int gsgpu_sim_upload(gsgpu_sim *sim, const double *x, const double *v,
 int gsgpu_sim_run(gsgpu_sim *sim, int64_t num_steps);
 /* The reference's loop to time tf (src/integrator.c, fixed-step: ceil(tf/dt)
  * steps with the last one clamped; src/integrator_rk_embedded.c:680-930,
- * integrators 5-8: adaptive steps from the initial dt to tf).  Synchronous. */
+ * integrators 5-8, and src/integrator_ias15.c:229-616, integrator 9:
+ * adaptive steps from the initial dt to tf).  Synchronous. */
 int gsgpu_sim_run_until(gsgpu_sim *sim, double tf);
-/* Embedded Runge-Kutta (integrators 5-8): abs = rel tolerance and the initial
- * dt (<= 0: the reference's estimate, src/integrator_rk_embedded.c:346-520). */
+/* Adaptive integrators (5-9): the tolerance and the initial dt (<= 0: the
+ * reference's estimate, src/integrator_rk_embedded.c:346-520 and
+ * src/integrator_ias15.c:702-806). */
 int gsgpu_sim_set_tolerance(gsgpu_sim *sim, double tolerance, double initial_dt);
 /* Device -> host copy of x, v (v synchronised to integer time for leapfrog). */
 int gsgpu_sim_download(gsgpu_sim *sim, double *x, double *v);

@@ -905,6 +905,212 @@ done:
 }
 
 /* ------------------------------------------------------------------ */
+/* IAS15 (src/integrator_ias15.c)                                       */
+/* ------------------------------------------------------------------ */
+
+/* The method's constants (Gauss-Radau spacings and the c / r coefficient
+ * tables of src/integrator_ias15.c:617-700) as exact doubles; each rounds the
+ * same from its decimal form in double or long double. */
+/* Gauss-Radau spacings h_0..h_7 */
+static const double kRadauH[8] = {0.0, 0x1.cce7242fd9812p-5, 0x1.7122082358d27p-3, 0x1.6916742f0c9c5p-2, 0x1.18248525f4802p-1, 0x1.77ea65770fa49p-1, 0x1.c548c982467cdp-1, 0x1.f47d94f4d2bb2p-1};
+/* c[i][j] (j <= i): b from g */
+static const double kRadauC[7][7] = {
+    {0x1.0000000000000p+0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {-0x1.cce7242fd9812p-5, 0x1.0000000000000p+0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {0x1.4c4b384151c1ep-7, -0x1.e45bd12f4f32cp-3, 0x1.0000000000000p+0, 0.0, 0.0, 0.0, 0.0},
+    {-0x1.d4b3379a1992dp-9, 0x1.7f2161e152586p-4, -0x1.2da22e635a1aep-1, 0x1.0000000000000p+0, 0.0, 0.0, 0.0},
+    {0x1.007370e57b89dp-9, -0x1.c08e5e7efcf23p-5, 0x1.a9dcc2e57fbbfp-2, -0x1.22e359c4a74d8p+0, 0x1.0000000000000p+0, 0.0, 0.0},
+    {-0x1.7893e98a2a997p-10, 0x1.595cd739ee74fp-5, -0x1.70bdf2d91dd44p-2, 0x1.4009e0866d488p+0, -0x1.ded88c802f1fcp+0, 0x1.0000000000000p+0, 0.0},
+    {0x1.4d64672378b3dp-10, -0x1.3d865cb429919p-5, 0x1.71a0161ae20fep-2, -0x1.7785b93619434p+0, 0x1.73fc45dfb9889p+1, -0x1.60be78a0a92f1p+1, 0x1.0000000000000p+0}};
+/* r[i][j] = 1 / (h_i - h_j) (j < i): g from the accelerations */
+static const double kRadauR[8][8] = {
+    {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {0x1.1c618574b517bp+4, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {0x1.6314ac07f6a9ap+2, 0x1.021c2b5e4af6fp+3, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {0x1.6afdfcc2a4aefp+1, 0x1.afe76c59caa8ap+1, 0x1.73439c0b4562bp+2, 0.0, 0.0, 0.0, 0.0, 0.0},
+    {0x1.d3e03b89d73cfp+0, 0x1.04c014a3946fbp+1, 0x1.5cdb4a576d57ap+1, 0x1.48fffc3fdf2e6p+2, 0.0, 0.0, 0.0, 0.0},
+    {0x1.5cac8b52e27b1p+0, 0x1.799c3c56b4e9dp+0, 0x1.ce1e8b86f5ae8p+0, 0x1.4f714afea15ccp+1, 0x1.56247c4b878b4p+2, 0.0, 0.0, 0.0},
+    {0x1.212921ce4baffp+0, 0x1.34c8b7028f418p+0, 0x1.6b1448c75e4d5p+0, 0x1.e092f6d7c8a42p+0, 0x1.7a82c7145ec17p+1, 0x1.a787c6413556bp+2, 0.0, 0.0},
+    {0x1.05e3166485188p+0, 0x1.15e18175af101p+0, 0x1.41177c7d3aff5p+0, 0x1.99ab118ef2216p+0, 0x1.296bab4a3e0d2p+1, 0x1.0709d7d8d5e3cp+2, 0x1.5b12a584540e2p+3, 0.0}};
+
+
+static double absmax(const double *v, int len)
+{
+    double mx = fabs(v[0]);
+    for (int i = 1; i < len; ++i) mx = fmax(mx, fabs(v[i]));
+    return mx;
+}
+
+/* :808-919, predictor at spacing h */
+static void ias_predict(int L, double *x1, double *v1, const double *x0, const double *v0,
+                        const double *a0, double h, const double *b, double dt,
+                        const double *xe, const double *ve)
+{
+    for (int k = 0; k < L; ++k) {
+        const double *bk = b + k;
+        const double dth = dt * h;
+        double p = bk[5 * L] / 28.0 + h * bk[6 * L] / 36.0;
+        p = bk[4 * L] / 21.0 + h * p;
+        p = bk[3 * L] / 15.0 + h * p;
+        p = bk[2 * L] / 10.0 + h * p;
+        p = bk[1 * L] / 6.0 + h * p;
+        p = bk[0] / 3.0 + h * p;
+        x1[k] = x0[k];
+        x1[k] += xe[k] + dth * (v0[k] + dth * (a0[k] + h * p) / 2.0);
+        double q = bk[5 * L] / 7.0 + h * bk[6 * L] / 8.0;
+        q = bk[4 * L] / 6.0 + h * q;
+        q = bk[3 * L] / 5.0 + h * q;
+        q = bk[2 * L] / 4.0 + h * q;
+        q = bk[1 * L] / 3.0 + h * q;
+        q = bk[0] / 2.0 + h * q;
+        v1[k] = v0[k];
+        v1[k] += ve[k] + dth * (a0[k] + h * q);
+    }
+}
+
+/* :921-983, end of the step with compensated sums */
+static void ias_advance(int L, double *x1, double *v1, double *txe, double *tve, const double *x0,
+                        const double *v0, const double *a0, const double *b, double dt)
+{
+    for (int k = 0; k < L; ++k) {
+        const double *bk = b + k;
+        const double sx = a0[k] + bk[0] / 3.0 + bk[1 * L] / 6.0 + bk[2 * L] / 10.0 +
+                          bk[3 * L] / 15.0 + bk[4 * L] / 21.0 + bk[5 * L] / 28.0 + bk[6 * L] / 36.0;
+        txe[k] += dt * (v0[k] + dt * sx / 2.0);
+        x1[k] = x0[k] + txe[k];
+        txe[k] += x0[k] - x1[k];
+        const double sv = a0[k] + bk[0] / 2.0 + bk[1 * L] / 3.0 + bk[2 * L] / 4.0 + bk[3 * L] / 5.0 +
+                          bk[4 * L] / 6.0 + bk[5 * L] / 7.0 + bk[6 * L] / 8.0;
+        tve[k] += dt * sv;
+        v1[k] = v0[k] + tve[k];
+        tve[k] += v0[k] - v1[k];
+    }
+}
+
+/* :1117-1274 (g from the accelerations F at spacings 0..i) and :985-1115
+ * (b from g), element by element */
+static void ias_update_gb(int L, double *g, double *b, const double *F, int i)
+{
+    for (int k = 0; k < L; ++k) {
+        double *gk = g + k, *bk = b + k;
+        const double f0 = F[k];
+        for (int m = 1; m <= i && m <= 7; ++m) {
+            double t = (F[(size_t)m * L + k] - f0) * kRadauR[m][0];
+            for (int j = 1; j < m; ++j) t = (t - gk[(size_t)(j - 1) * L]) * kRadauR[m][j];
+            gk[(size_t)(m - 1) * L] = t;
+        }
+        for (int r = 0; r < i && r < 7; ++r) {
+            double t = kRadauC[r][r] * gk[(size_t)r * L];
+            for (int j = r + 1; j < 7; ++j) t += kRadauC[j][r] * gk[(size_t)j * L];
+            bk[(size_t)r * L] = t;
+        }
+    }
+}
+
+/* :1276-1382 */
+static void ias_refine(int L, double *b, double *e, double *db, double q, int refine)
+{
+    const double q2 = q * q, q3 = q2 * q, q4 = q3 * q, q5 = q4 * q, q6 = q5 * q, q7 = q6 * q;
+    for (size_t k = 0; k < (size_t)7 * L; ++k) db[k] = refine ? b[k] - e[k] : 0.0;
+    for (int k = 0; k < L; ++k) {
+        const double b0 = b[k], b1 = b[L + k], b2 = b[2 * L + k], b3 = b[3 * L + k],
+                     b4 = b[4 * L + k], b5 = b[5 * L + k], b6 = b[6 * L + k];
+        e[k] = q * (b6 * 7.0 + b5 * 6.0 + b4 * 5.0 + b3 * 4.0 + b2 * 3.0 + b1 * 2.0 + b0);
+        e[L + k] = q2 * (b6 * 21.0 + b5 * 15.0 + b4 * 10.0 + b3 * 6.0 + b2 * 3.0 + b1);
+        e[2 * L + k] = q3 * (b6 * 35.0 + b5 * 20.0 + b4 * 10.0 + b3 * 4.0 + b2);
+        e[3 * L + k] = q4 * (b6 * 35.0 + b5 * 15.0 + b4 * 5.0 + b3);
+        e[4 * L + k] = q5 * (b6 * 21.0 + b5 * 6.0 + b4);
+        e[5 * L + k] = q6 * (b6 * 7.0 + b5);
+        e[6 * L + k] = q7 * b6;
+    }
+    for (size_t k = 0; k < (size_t)7 * L; ++k) b[k] = e[k] + db[k];
+}
+
+int orc_ias15_run(int method, int n, double *x, double *v, const double *m, double G, double eps,
+                  double tolerance, double initial_dt, double tf, int64_t *num_steps,
+                  double *t_out, double *dt_out)
+{
+    const int L = 3 * n;
+    const size_t SL = (size_t)L;
+    double *buf = (double *)calloc(SL * (7 * 5 + 8 + 10), sizeof(double));
+    if (!buf) return 4;
+    double *b0 = buf, *b = b0 + 7 * SL, *g = b + 7 * SL, *e = g + 7 * SL, *db = e + 7 * SL;
+    double *F = db + 7 * SL;   /* 8 * L */
+    double *a = F + 8 * SL, *x1 = a + SL, *v1 = x1 + SL, *a1 = v1 + SL, *d7 = a1 + SL,
+           *xe = d7 + SL, *ve = xe + SL, *txe = ve + SL, *tve = txe + SL;
+    double *tmp = tve + SL;
+    int rc = accel_of(method, n, x, m, G, eps, a);
+    if (rc) goto done;
+    double dt;
+    if (initial_dt > 0.0) {
+        dt = initial_dt;
+    } else {
+        /* :702-806, power 15 */
+        const double d0 = absmax(x, L), d1 = absmax(a, L);
+        const double dt0 = (d0 < 1e-5 || d1 < 1e-5) ? 1e-6 : 0.01 * (d0 / d1);
+        for (int k = 0; k < L; ++k) tmp[k] = x[k] + dt0 * v[k];
+        if ((rc = accel_of(method, n, tmp, m, G, eps, a1))) goto done;
+        for (int k = 0; k < L; ++k) a1[k] = a1[k] - a[k];
+        const double d2 = absmax(a1, L) / dt0;
+        double dt1;
+        if (fmax(d1, d2) <= 1e-15)
+            dt1 = fmax(1e-6, dt0 * 1e-3);
+        else
+            dt1 = pow((0.01 / fmax(d1, d2)), 1.0 / (1.0 + (double)15));
+        dt = fmin(100.0 * dt0, dt1);
+        if (dt <= 0.0) { rc = 2; goto done; }
+        if (dt > tf) dt = tf;
+    }
+    {
+        double t = 0.0, dt_new;
+        int64_t steps = 0;
+        int refine = 0;
+        while (t < tf) {
+            for (int it = 0; it < 12; ++it) {
+                for (int i = 0; i < 8; ++i) {
+                    ias_predict(L, x1, v1, x, v, a, kRadauH[i], b, dt, xe, ve);
+                    if ((rc = accel_of(method, n, x1, m, G, eps, F + (size_t)i * SL))) goto done;
+                    ias_update_gb(L, g, b, F, i);
+                }
+                for (int k = 0; k < L; ++k) d7[k] = b[6 * SL + k] - b0[6 * SL + k];
+                memcpy(b0, b, sizeof(double) * 7 * SL);
+                if ((absmax(d7, L) / absmax(F + 7 * SL, L)) < 1e-16) break;
+            }
+            memcpy(txe, xe, sizeof(double) * SL);
+            memcpy(tve, ve, sizeof(double) * SL);
+            ias_advance(L, x1, v1, txe, tve, x, v, a, b, dt);
+            if ((rc = accel_of(method, n, x1, m, G, eps, a1))) goto done;
+            const double eb7 = absmax(b + 6 * SL, L) / absmax(a1, L);
+            double err = pow((eb7 / tolerance), 1.0 / 7.0);
+            if (err < 1e-10) err = 1e-10;
+            dt_new = dt / err;
+            if (err <= 1.0 || dt == tf * 1e-12) {
+                ++steps;
+                t += dt;
+                ias_refine(L, b, e, db, dt_new / dt, refine);
+                refine = 1;
+                memcpy(xe, txe, sizeof(double) * SL);
+                memcpy(ve, tve, sizeof(double) * SL);
+                memcpy(x, x1, sizeof(double) * SL);
+                memcpy(v, v1, sizeof(double) * SL);
+                memcpy(a, a1, sizeof(double) * SL);
+            }
+            if (dt_new > (dt / 0.25)) dt /= 0.25;
+            else if (dt_new < dt * 0.25) dt *= 0.25;
+            else dt = dt_new;
+            if (dt_new < tf * 1e-12) dt = tf * 1e-12;
+            if (t < tf && t + dt > tf) dt = tf - t;
+        }
+        if (num_steps) *num_steps = steps;
+        if (t_out) *t_out = t;
+        if (dt_out) *dt_out = dt;
+    }
+done:
+    free(buf);
+    return rc;
+}
+
+/* ------------------------------------------------------------------ */
 /* WHFast (src/integrator_whfast.c)                                     */
 /* ------------------------------------------------------------------ */
 

@@ -116,6 +116,13 @@ int orc_rk_embedded_run(int integrator, int method, int n, double *x, double *v,
                         double initial_dt, double tf, int64_t *num_steps, double *t_out,
                         double *dt_out);
 
+/* src/integrator_ias15.c:229-616 (IAS15, integrator 9) with the pairwise
+ * (method 1) or massless (method 2) sum; initial_dt <= 0 selects the
+ * reference's estimate.  Reports the accepted steps, final t and next dt. */
+int orc_ias15_run(int method, int n, double *x, double *v, const double *m, double G, double eps,
+                  double tolerance, double initial_dt, double tf, int64_t *num_steps,
+                  double *t_out, double *dt_out);
+
 /* src/integrator_whfast.c:200-407 for one system: sort by distance, eta,
  * Jacobi transforms, universal-variable Kepler drift, the interaction
  * accelerations (pairwise=0: the massless variant :959-1264, 1: the
@@ -124,6 +131,27 @@ int orc_rk_embedded_run(int integrator, int method, int n, double *x, double *v,
  * particles whose Kepler solve failed. */
 int orc_whfast_run(int *n, int *ids, double *x, double *v, double *m, double G,
                    double eps, double dt, double tf, int remove_invalid, int pairwise);
+
+/* FFTW 3's r2c / c2r 3-D transforms (unnormalised) by direct DFT
+ * (pm_dft.c); out of r2c and in of c2r are n0 x n1 x (n2/2+1) complex
+ * values, interleaved. */
+void orc_dft3_r2c(int n0, int n1, int n2, const double *in, double *out);
+void orc_dft3_c2r(int n0, int n1, int n2, const double *in, double *out);
+
+/* src/acceleration_PM.c:15-391: cloud-in-cell deposit, Poisson solve in
+ * Fourier space, fourth-order gradient, cloud-in-cell interpolation. */
+void orc_acceleration_pm(double *a, int n, const double *x, const double *m,
+                         const double *box_center, double box_width, double H0, double omega_m,
+                         double mean_bkg_density, int pm_grid_size, double scale_factor);
+/* src/cosmology.c:15-26 */
+double orc_compute_da(double a, double H0, double omega_m, double omega_lambda);
+/* src/system.c:1337-1375 */
+void orc_periodic_boundary(int n, double *x, const double *box_center, double box_width);
+/* src/integrator_cosmology_leapfrog.c:24-255, output disabled. */
+void orc_leapfrog_cosmology(int n, double *x, const double *v, const double *m, double h,
+                            double omega_m, double omega_lambda, const double *box_center,
+                            double box_width, double dt, double a_begin, double a_final,
+                            int pm_grid_size, int64_t *num_steps, double *t_out);
 
 /* src/utils.c:27-59 (kinetic + unsoftened pairwise potential energy). */
 double orc_energy(int n, const double *x, const double *v, const double *m,

@@ -20,6 +20,9 @@ HERE = Path(__file__).resolve().parent
 REF_DIR = Path(os.environ.get("GRAV_SIM_REFERENCE_DIR", "/root/reference"))
 SERIAL = HERE / "_ref" / "libgrav_sim_ref.so"
 OPENMP = HERE / "_ref" / "libgrav_sim_ref_omp.so"
+# the reference with its particle-mesh sources, FFTW calls served by the
+# oracle's direct DFT (oracle/fftw_compat)
+PM = HERE / "_ref" / "libgrav_sim_ref_pm.so"
 
 _PKG = HERE.parent / "gravity-simulator_gb300"
 
@@ -123,7 +126,7 @@ def octree(x, m, leaf_max):
 
 
 def launch(x, v, m, G, integrator, dt, tf, method, theta=1.0, eps=0.0, leaf=-1,
-           tolerance=-1.0, initial_dt=-1.0, openmp=False):
+           tolerance=-1.0, initial_dt=-1.0, openmp=False, **output):
     g = _gsgpu()
     x = np.ascontiguousarray(x, dtype=np.float64).copy()
     v = np.ascontiguousarray(v, dtype=np.float64).copy()
@@ -131,8 +134,35 @@ def launch(x, v, m, G, integrator, dt, tf, method, theta=1.0, eps=0.0, leaf=-1,
     ids, xo, vo, mo = g.launch_simulation(
         load(openmp), x, v, m, G, integrator=integrator, dt=dt, tf=tf, method=method,
         opening_angle=theta, softening_length=eps, max_num_particles_per_leaf=leaf,
-        tolerance=tolerance, initial_dt=initial_dt)
+        tolerance=tolerance, initial_dt=initial_dt, **output)
     return ids.copy(), xo.copy(), vo.copy(), mo.copy()
+
+
+def load_pm() -> ctypes.CDLL:
+    if "pm" not in _cache:
+        g = _gsgpu()
+        lib = ctypes.CDLL(str(PM))
+        lib.free_traceback.restype = None
+        lib.free_traceback.argtypes = [ctypes.POINTER(g.ErrorStatus)]
+        _cache["pm"] = lib
+    return _cache["pm"]
+
+
+def acceleration_pm(x, m, box_center, box_width, H0, omega_m, mean_bkg_density, grid,
+                    scale_factor):
+    """acceleration_PM (src/acceleration_PM.c:274-391) of the reference."""
+    g = _gsgpu()
+    return g.acceleration_pm(load_pm(), x, m, box_center, box_width, H0, omega_m,
+                             mean_bkg_density, grid, scale_factor)
+
+
+def cosmological_run(x, v, m, **kw):
+    """launch_cosmological_simulation of the reference; returns (x, status)."""
+    g = _gsgpu()
+    x = np.ascontiguousarray(x, dtype=np.float64).copy()
+    v = np.ascontiguousarray(v, dtype=np.float64).copy()
+    st = g.launch_cosmological_simulation(load_pm(), x, v, m, **kw)
+    return x, (st.t, st.dt, st.num_steps)
 
 
 def energy_python(x, v, m, G):

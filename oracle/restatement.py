@@ -48,8 +48,8 @@ def load():
     global _lib
     if _lib is not None:
         return _lib
-    src = HERE / "grav_oracle.c"
-    if not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
+    srcs = [HERE / f for f in ("grav_oracle.c", "grav_oracle.h", "pm_oracle.c", "pm_dft.c")]
+    if not LIB.exists() or LIB.stat().st_mtime < max(f.stat().st_mtime for f in srcs):
         build()
     lib = ctypes.CDLL(str(LIB))
     lib.orc_pairwise.argtypes = [ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double, dp]
@@ -232,6 +232,22 @@ def rk_embedded_run(integrator, method, x, v, m, G, eps, tolerance, tf, initial_
     return x.reshape(-1, 3), v.reshape(-1, 3), steps.value, t.value, dt.value
 
 
+def ias15_run(method, x, v, m, G, eps, tolerance, tf, initial_dt=-1.0):
+    """IAS15 (integrator 9) for one system; returns (x, v, steps, t, dt)."""
+    lib = load()
+    lib.orc_ias15_run.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, dp, ctypes.c_double,
+                                  ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                  ctypes.c_double, ctypes.POINTER(ctypes.c_int64),
+                                  ctypes.POINTER(ctypes.c_double),
+                                  ctypes.POINTER(ctypes.c_double)]
+    x, v, m = _c(x).copy(), _c(v).copy(), _c(m)
+    steps, t, dt = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double()
+    rc = lib.orc_ias15_run(method, m.size, _d(x), _d(v), _d(m), G, eps, tolerance, initial_dt, tf,
+                           ctypes.byref(steps), ctypes.byref(t), ctypes.byref(dt))
+    assert rc == 0, rc
+    return x.reshape(-1, 3), v.reshape(-1, 3), steps.value, t.value, dt.value
+
+
 def whfast_run(x, v, m, G, eps, dt, tf, remove_invalid=True, pairwise=False, ids=None):
     """WHFast for one system; returns (ids, x, v, m) of the survivors."""
     lib = load()
@@ -246,6 +262,61 @@ def whfast_run(x, v, m, G, eps, dt, tf, remove_invalid=True, pairwise=False, ids
     assert rc == 0, rc
     k = n.value
     return ids[:k], x.reshape(-1, 3)[:k], v.reshape(-1, 3)[:k], m[:k]
+
+
+def dft3_r2c(a):
+    """FFTW-style r2c of a real (n0, n1, n2) array: complex (n0, n1, n2//2+1)."""
+    a = _c(a)
+    n0, n1, n2 = a.shape
+    out = np.empty((n0, n1, n2 // 2 + 1, 2))
+    lib = load()
+    lib.orc_dft3_r2c.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp]
+    lib.orc_dft3_r2c(n0, n1, n2, _d(a), _d(out))
+    return out[..., 0] + 1j * out[..., 1]
+
+
+def dft3_c2r(y, n2):
+    """FFTW-style unnormalised c2r of a half spectrum (n0, n1, n2//2+1)."""
+    n0, n1, h = y.shape
+    assert h == n2 // 2 + 1
+    yy = _c(np.stack([y.real, y.imag], axis=-1))
+    out = np.empty((n0, n1, n2))
+    lib = load()
+    lib.orc_dft3_c2r.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp]
+    lib.orc_dft3_c2r(n0, n1, n2, _d(yy), _d(out))
+    return out
+
+
+def acceleration_pm(x, m, box_center, box_width, H0, omega_m, mean_bkg_density, grid,
+                    scale_factor):
+    """src/acceleration_PM.c:274-391 with the direct DFT."""
+    lib = load()
+    lib.orc_acceleration_pm.argtypes = [dp, ctypes.c_int, dp, dp, dp, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_int, ctypes.c_double]
+    x, m, c = _c(x), _c(m), _c(box_center)
+    a = np.empty((m.size, 3))
+    lib.orc_acceleration_pm(_d(a), m.size, _d(x), _d(m), _d(c), box_width, H0, omega_m,
+                            mean_bkg_density, grid, scale_factor)
+    return a
+
+
+def leapfrog_cosmology(x, v, m, h, omega_m, omega_lambda, box_center, box_width, dt, a_begin,
+                       a_final, grid):
+    """src/integrator_cosmology_leapfrog.c with output disabled; returns
+    (x, steps, t): v is left unchanged, as by the reference."""
+    lib = load()
+    lib.orc_leapfrog_cosmology.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_double, dp, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
+                                           ctypes.POINTER(ctypes.c_double)]
+    x, v, m, c = _c(x).copy(), _c(v), _c(m), _c(box_center)
+    steps, t = ctypes.c_int64(), ctypes.c_double()
+    lib.orc_leapfrog_cosmology(m.size, _d(x), _d(v), _d(m), h, omega_m, omega_lambda, _d(c),
+                               box_width, dt, a_begin, a_final, grid, ctypes.byref(steps),
+                               ctypes.byref(t))
+    return x.reshape(-1, 3), steps.value, t.value
 
 
 def energy(x, v, m, G):

@@ -18,11 +18,21 @@ Outputs (compressed .npz, a few hundred KB in total):
   whfast.npz         WHFast, massless / pairwise / softened / removal
                      (src/integrator_whfast.c:200-407)
   rk_embedded.npz    RKF45 / DOPRI / DVERK / RKF78 (src/integrator_rk_embedded.c)
+  ias15.npz          IAS15 (src/integrator_ias15.c)
+  output.npz         CSV snapshots written during launch_simulation
+                     (src/output.c:340-470), one case per loop family
+  pm.npz             acceleration_PM and launch_cosmological_simulation
+                     (src/acceleration_PM.c, src/integrator_cosmology_leapfrog.c)
+
+``python tests/golden/make_golden.py whfast output`` remakes only the named
+files of the last group (whfast, rk_embedded, ias15, output, pm).
 """
 from __future__ import annotations
 
 import importlib.util
+import json
 import sys
+import tempfile
 from pathlib import Path
 
 import numpy as np
@@ -128,8 +138,138 @@ def rk_embedded_cases():
     return out
 
 
+def ias15_cases():
+    """IAS15 (src/integrator_ias15.c) run by the reference: the initial-step
+    estimate (tolerance 1e-9) and a given initial dt (1e-6), pairwise sum;
+    one massless planetary run."""
+    out = {}
+    x, v, m = wl.plummer(64, 31)
+    out["x"], out["v"], out["m"] = x, v, m
+    for tag, tol, idt in (("auto", 1e-9, -1.0), ("given", 1e-6, 1e-3)):
+        _, xr, vr, _ = ref.launch(x, v, m, 1.0, 9, 1e-3, 0.5, 1, eps=0.01, tolerance=tol,
+                                  initial_dt=idt)
+        out[f"{tag}/x"], out[f"{tag}/v"] = xr, vr
+        out[f"{tag}/tol"], out[f"{tag}/initial_dt"] = np.float64(tol), np.float64(idt)
+    (xs, vs, ms), = wl.planetary_ensemble(1, 11, max_test=30)
+    _, xr, vr, _ = ref.launch(xs, vs, ms, wl.G_AU_MSUN_DAY, 9, 1.0, 200.0, 2, tolerance=1e-9)
+    out["massless_x0"], out["massless_v0"], out["massless_m"] = xs, vs, ms
+    out["massless_G"] = np.float64(wl.G_AU_MSUN_DAY)
+    out["massless_x"], out["massless_v"] = xr, vr
+    return out
+
+
+OUTPUT_CASES = {
+    # name: (system, integrator, method, dt, tf, extra launch arguments, output arguments)
+    "leapfrog": ("plummer", 4, 1, 1e-3, 0.0105, {"eps": 0.01},
+                 dict(output_initial=True, output_interval=3e-3)),
+    "euler_float": ("plummer", 1, 1, 1e-3, 0.006, {"eps": 0.01},
+                    dict(output_initial=False, output_interval=2e-3, coordinate_output_dtype=1,
+                         mass_output_dtype=1)),
+    "rk4": ("plummer", 3, 1, 1e-3, 0.009, {"eps": 0.01},
+            dict(output_initial=True, output_interval=4e-3, velocity_output_dtype=1)),
+    "rkf45": ("plummer", 5, 1, 1e-3, 0.05, {"eps": 0.01, "tolerance": 1e-8},
+              dict(output_initial=True, output_interval=1e-2)),
+    "ias15": ("plummer", 9, 1, 1e-3, 0.05, {"eps": 0.01, "tolerance": 1e-9},
+              dict(output_initial=True, output_interval=1e-2)),
+    "whfast": ("planetary", 10, 2, 1.0, 50.5, {},
+               dict(output_initial=True, output_interval=10.0)),
+}
+
+
+def output_system(kind):
+    if kind == "plummer":
+        x, v, m = wl.plummer(24, 51)
+        return x, v, m, 1.0
+    (x, v, m), = wl.planetary_ensemble(1, 10, max_test=12)
+    return x, v, m, wl.G_AU_MSUN_DAY
+
+
+def output_cases():
+    """Snapshot files the reference writes (CSV output method) for one case of
+    each loop family, stored byte for byte as uint8 arrays under
+    "<case>/<file name>".  The reference's Python entry point leaves the
+    status of the initial snapshot (output_initial) uninitialised, so the
+    time and dt lines of snapshot_00000.csv in those cases carry no meaning."""
+    out = {}
+    for name, (kind, integ, method, dt, tf, extra, oargs) in OUTPUT_CASES.items():
+        x, v, m, G = output_system(kind)
+        with tempfile.TemporaryDirectory() as tmp:
+            d = Path(tmp) / "snaps"
+            ref.launch(x, v, m, G, integ, dt, tf, method, output_method=2,
+                       output_dir=str(d) + "/", **extra, **oargs)
+            files = sorted(d.iterdir())
+            assert files, name
+            for f in files:
+                out[f"{name}/{f.name}"] = np.frombuffer(f.read_bytes(), dtype=np.uint8)
+        args = dict(kind=kind, integrator=integ, method=method, dt=dt, tf=tf, extra=extra,
+                    output=oargs)
+        out[f"{name}/args.json"] = np.frombuffer(json.dumps(args).encode(), dtype=np.uint8)
+        out[f"{name}/x0"], out[f"{name}/v0"], out[f"{name}/m0"] = x, v, m
+        out[f"{name}/G"] = np.float64(G)
+    return out
+
+
+def pm_cases():
+    """Particle-mesh force and cosmological leapfrog of the reference
+    (src/acceleration_PM.c, src/integrator_cosmology_leapfrog.c), built from
+    its own sources with FFTW's calls served by the oracle's direct DFT
+    (oracle/fftw_compat): uniform and clustered particles, an off-centre
+    box, particles on the box faces; and a five-step cosmological run with
+    particles leaving the box."""
+    out = {}
+    rng = np.random.default_rng(61)
+    c = np.array([1.5, -2.0, 0.25])
+    bw = 4.0
+    cases = {
+        "uniform_g16": (c + rng.uniform(-bw, bw, (2000, 3)), np.full(2000, 1.0 / 2000), 16),
+        "clustered_g32": (c + np.clip(wl.plummer(2500, 62)[0] * 0.8, -bw, bw),
+                          rng.uniform(0.5, 1.5, 2500) / 2500, 32),
+    }
+    xf = c + rng.uniform(-bw, bw, (200, 3))
+    xf[:20, 0] = c[0] + bw            # on the upper face: cell index g wraps to 0
+    xf[20:40, 1] = c[1] - bw          # on the lower face
+    cases["faces_g8"] = (xf, np.full(200, 0.005), 8)
+    H0, om = 70.0, 0.3
+    for name, (x, m, grid) in cases.items():
+        rho = m.sum() / ((bw * 2) ** 3)
+        a = ref.acceleration_pm(x, m, c, bw, H0, om, rho, grid, 0.5)
+        out[f"{name}/x"], out[f"{name}/m"], out[f"{name}/grid"] = x, m, np.int64(grid)
+        out[f"{name}/a"] = a
+    out["box_center"], out["box_width"] = c, np.float64(bw)
+    out["H0"], out["omega_m"], out["scale_factor"] = np.float64(H0), np.float64(om), np.float64(0.5)
+    # cosmological run: 1000 particles, 16^3 mesh, a = 0.1 -> 0.2 in steps of 0.02
+    n = 1000
+    x = c + rng.uniform(-bw, bw, (n, 3))
+    v = rng.normal(0.0, 40.0, (n, 3))
+    m = np.full(n, 1.0)
+    x[0] = c + np.array([bw + 0.5, -bw - 9.0, 0.0])   # starts outside: wrapped first
+    kw = dict(h=0.7, omega_m=0.3, omega_lambda=0.7, box_center=c, box_width=bw, dt=0.02,
+              a_begin=0.1, a_final=0.2, pm_grid_size=16)
+    xr, (t, dt, steps) = ref.cosmological_run(x, v, m, **kw)
+    out["cosmo/x0"], out["cosmo/v0"], out["cosmo/m"] = x, v, m
+    out["cosmo/x"], out["cosmo/t"], out["cosmo/steps"] = xr, np.float64(t), np.int64(steps)
+    out["cosmo/args.json"] = np.frombuffer(json.dumps({k: (list(map(float, v)) if k == "box_center"
+                                                           else v) for k, v in kw.items()}).encode(),
+                                           dtype=np.uint8)
+    return out
+
+
+LATE = {
+    "whfast": lambda: whfast_cases(),
+    "rk_embedded": lambda: rk_embedded_cases(),
+    "ias15": lambda: ias15_cases(),
+    "output": lambda: output_cases(),
+    "pm": lambda: pm_cases(),
+}
+
+
 def main():
     assert ref.build() or ref.available(), "reference sources not found"
+    if len(sys.argv) > 1:
+        for name in sys.argv[1:]:
+            np.savez_compressed(OUT / f"{name}.npz", **LATE[name]())
+            print(name, (OUT / f"{name}.npz").stat().st_size)
+        return
     out = {}
     for name, (x, m, G, eps) in pairwise_cases().items():
         a = ref.acceleration(x, m, G, 1, eps=eps)
@@ -199,8 +339,8 @@ def main():
     np.savez_compressed(OUT / "energy.npz", x=x, v=v, m=m, G=np.float64(1.3),
                         e=ref.energy_python(x, v, m, 1.3))
 
-    np.savez_compressed(OUT / "whfast.npz", **whfast_cases())
-    np.savez_compressed(OUT / "rk_embedded.npz", **rk_embedded_cases())
+    for name, make in LATE.items():
+        np.savez_compressed(OUT / f"{name}.npz", **make())
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -44,6 +44,10 @@ LAYOUT_C = textwrap.dedent("""
       printf("SimulationStatus %zu\\n", sizeof(SimulationStatus));
       printf("Settings %zu\\n", sizeof(Settings));
       P(Settings, is_exit_ptr)
+      printf("CosmologicalSystem %zu\\n", sizeof(CosmologicalSystem));
+      P(CosmologicalSystem, m) P(CosmologicalSystem, h) P(CosmologicalSystem, omega_k)
+      P(CosmologicalSystem, box_center) P(CosmologicalSystem, box_width)
+      P(CosmologicalSystem, unit_time)
       printf("LinearOctree %zu\\n", sizeof(LinearOctree));
       P(LinearOctree, num_internal_nodes) P(LinearOctree, sorted_indices)
       P(LinearOctree, tree_center_of_mass_z)
@@ -79,6 +83,8 @@ def test_ctypes_mirror_sizes(g):
     assert ctypes.sizeof(g.AccelerationParam) == 32
     assert ctypes.sizeof(g.ErrorStatus) == 24
     assert ctypes.sizeof(g.LinearOctree) == 96
+    assert ctypes.sizeof(g.CosmologicalSystem) == 128
+    assert ctypes.sizeof(g.OutputParam) == 48
 
 
 def test_finalize_acceleration_param_host_logic(lib, g):
@@ -121,9 +127,65 @@ def test_launch_validation_order_on_host(lib, g):
                             method=g.METHOD_GPU_PAIRWISE)
 
 
+def test_output_param_checks_on_host(lib, g, tmp_path, capfd):
+    """finalize_output_param (src/output.c:126-239) runs before any device
+    work: each bad output argument fails with the reference's message, and
+    a valid snapshot folder is created (the run itself then needs a GPU)."""
+    import numpy as np
+    x, v, m = np.zeros((4, 3)), np.zeros((4, 3)), np.ones(4)
+    bad = [
+        (dict(output_method=2, output_dir=str(tmp_path / "a"), output_interval=1.0),
+         "must end with a trailing slash"),
+        (dict(output_method=2, output_dir=str(tmp_path / "b") + "/", output_interval=0.0),
+         "Output interval must be positive"),
+        (dict(output_method=3, output_dir=str(tmp_path / "b") + "/", output_interval=1.0),
+         "HDF5 output method is not available"),
+        (dict(output_method=7, output_dir=str(tmp_path / "b") + "/", output_interval=1.0),
+         "Unknown output method"),
+    ]
+    capfd.readouterr()
+    for kw, msg in bad:
+        with pytest.raises(RuntimeError):
+            g.launch_simulation(lib, x.copy(), v.copy(), m, 1.0, integrator=4, dt=1e-3, tf=0.01,
+                                method=g.METHOD_GPU_PAIRWISE, **kw)
+        assert msg in capfd.readouterr().err
+    assert not (tmp_path / "a").exists() and not (tmp_path / "b").exists()
+    try:
+        g.launch_simulation(lib, x.copy(), v.copy(), m, 1.0, integrator=4, dt=1e-3, tf=0.0,
+                            method=g.METHOD_GPU_PAIRWISE, output_method=2,
+                            output_dir=str(tmp_path / "c") + "/", output_interval=1.0)
+    except RuntimeError:
+        pass
+    assert (tmp_path / "c").is_dir()
+
+
 def test_check_if_included(lib):
     f = lib.linear_octree_check_if_included
     f.restype = ctypes.c_bool
     f.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int]
     assert f(0b111000, 0b111111, 20)
     assert not f(0b111000, 0b111111, 21)
+
+
+def test_cosmological_checks_on_host(lib, g, capfd):
+    """launch_cosmological_simulation's checks (src/grav_sim.c:166-229) run
+    before any device work, in the reference's order and words."""
+    import numpy as np
+    x, v, m = np.zeros((4, 3)), np.zeros((4, 3)), np.ones(4)
+    good = dict(h=0.7, omega_m=0.3, omega_lambda=0.7, box_center=[0, 0, 0], box_width=1.0,
+                dt=0.01, a_begin=0.1, a_final=0.2, pm_grid_size=8)
+    bad = [
+        (dict(h=-1.0), "Hubble parameter"),
+        (dict(box_width=0.0), "Box width must be positive"),
+        (dict(output_method=2), "CSV output is not supported"),
+        (dict(output_method=3), "HDF5 output method is not available"),
+        (dict(dt=-1.0), "dt must be non=negative"),
+        (dict(a_begin=0.0), "a_begin must be positive"),
+        (dict(a_final=0.05), "a_final must be greater or equal"),
+        (dict(pm_grid_size=0), "pm_grid_size must be positive"),
+    ]
+    for over, msg in bad:
+        kw = dict(good, **over)
+        with pytest.raises(g.GravError) as e:
+            g.launch_cosmological_simulation(lib, x.copy(), v.copy(), m, **kw)
+        assert msg in str(e.value), (msg, str(e.value))

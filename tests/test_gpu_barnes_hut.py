@@ -254,3 +254,18 @@ def test_group_walk_particles_on_box_maximum(lib, g, orc, wl):
                        softening_length=0.01, max_num_particles_per_leaf=1)
     err = orc.rel_err(a[rows], orc.direct_rows(x, m, 1.0, 0.01, rows))
     assert np.isfinite(a).all() and err.max() < 5e-3
+
+
+def test_group_walk_monopole_vs_per_particle(lib, g, orc, wl):
+    """Monopole group walk (107): at least about as accurate as the
+    per-particle monopole walk (103) at the same theta."""
+    x, v, m = wl.galaxy_pair(131072, 9)
+    rows = np.random.default_rng(6).choice(x.shape[0], 2048, replace=False).astype(np.int32)
+    exact = orc.direct_rows(x, m, 1.0, 0.01, rows)
+    kw = dict(opening_angle=0.5, softening_length=0.01, max_num_particles_per_leaf=1)
+    e_g = np.median(orc.rel_err(g.acceleration(lib, x, m, 1.0, g.METHOD_GPU_BARNES_HUT_GROUP_MONO,
+                                               **kw)[rows], exact))
+    e_p = np.median(orc.rel_err(g.acceleration(lib, x, m, 1.0, g.METHOD_GPU_BARNES_HUT, **kw)[rows],
+                                exact))
+    print(f"monopole: group {e_g:.3g}, per-particle {e_p:.3g}")
+    assert e_g <= 1.1 * e_p

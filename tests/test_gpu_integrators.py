@@ -131,9 +131,34 @@ def test_rk_embedded_oracle_random(lib, g, orc, wl):
     assert np.array_equal(xo, xo_ref) and np.array_equal(vo, vo_ref)
 
 
-def test_ias15_reports_not_implemented(lib, g):
-    x, v, m = np.zeros((2, 3)), np.zeros((2, 3)), np.ones(2)
-    x[1, 0] = 1.0
-    with pytest.raises(RuntimeError):
-        g.launch_simulation(lib, x, v, m, 1.0, integrator=9, dt=1e-3, tf=0.01,
-                            method=g.METHOD_GPU_PAIRWISE_FP64, tolerance=1e-6)
+def test_ias15_bitexact_golden(lib, g):
+    """IAS15: the GPU predictor / corrector kernels with the host-side
+    convergence test and step control reproduce the reference's run bit for
+    bit, with its initial-step estimate and with a given initial dt."""
+    d = golden("ias15")
+    for tag in ("auto", "given"):
+        x, v = d["x"].copy(), d["v"].copy()
+        _, xo, vo, _ = g.launch_simulation(lib, x, v, d["m"].copy(), 1.0, integrator=9, dt=1e-3,
+                                           tf=0.5, method=g.METHOD_GPU_PAIRWISE_FP64,
+                                           softening_length=0.01, tolerance=float(d[f"{tag}/tol"]),
+                                           initial_dt=float(d[f"{tag}/initial_dt"]))
+        assert np.array_equal(xo, d[f"{tag}/x"]), tag
+        assert np.array_equal(vo, d[f"{tag}/v"]), tag
+
+
+def test_ias15_massless_golden(lib, g):
+    d = golden("ias15")
+    x, v = d["massless_x0"].copy(), d["massless_v0"].copy()
+    _, xo, vo, _ = g.launch_simulation(lib, x, v, d["massless_m"].copy(), float(d["massless_G"]),
+                                       integrator=9, dt=1.0, tf=200.0,
+                                       method=g.METHOD_GPU_MASSLESS, tolerance=1e-9)
+    assert np.array_equal(xo, d["massless_x"]) and np.array_equal(vo, d["massless_v"])
+
+
+def test_ias15_oracle_random(lib, g, orc, wl):
+    x, v, m = wl.plummer(300, 778)
+    xo_ref, vo_ref, *_ = orc.ias15_run(1, x, v, m, 1.0, 0.02, 1e-8, 0.2)
+    _, xo, vo, _ = g.launch_simulation(lib, x.copy(), v.copy(), m, 1.0, integrator=9, dt=1e-3,
+                                       tf=0.2, method=g.METHOD_GPU_PAIRWISE_FP64,
+                                       softening_length=0.02, tolerance=1e-8)
+    assert np.array_equal(xo, xo_ref) and np.array_equal(vo, vo_ref)

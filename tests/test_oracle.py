@@ -109,6 +109,20 @@ def test_rk_embedded_golden(orc):
     assert np.array_equal(xo, d["massless_x"]) and np.array_equal(vo, d["massless_v"])
 
 
+def test_ias15_golden(orc):
+    """IAS15 restatement against the reference's runs, bit for bit."""
+    d = golden("ias15")
+    for tag in ("auto", "given"):
+        xo, vo, steps, t, dt = orc.ias15_run(1, d["x"], d["v"], d["m"], 1.0, 0.01,
+                                             float(d[f"{tag}/tol"]), 0.5,
+                                             float(d[f"{tag}/initial_dt"]))
+        assert t >= 0.5 and steps > 0, tag
+        assert np.array_equal(xo, d[f"{tag}/x"]) and np.array_equal(vo, d[f"{tag}/v"]), tag
+    xo, vo, *_ = orc.ias15_run(2, d["massless_x0"], d["massless_v0"], d["massless_m"],
+                               float(d["massless_G"]), 0.0, 1e-9, 200.0)
+    assert np.array_equal(xo, d["massless_x"]) and np.array_equal(vo, d["massless_v"])
+
+
 def test_energy_golden(orc):
     d = golden("energy")
     e = orc.energy(d["x"], d["v"], d["m"], float(d["G"]))
@@ -141,3 +155,93 @@ def test_fixed_mode_tree_is_more_accurate(orc, wl):
     e_ref = np.median(orc.rel_err(orc.barnes_hut(x, m, 1.0, 0.01, 0.5, 1, True), exact))
     e_fix = np.median(orc.rel_err(orc.barnes_hut(x, m, 1.0, 0.01, 0.5, 1, False), exact))
     assert e_fix < 5e-3 < e_ref
+
+
+def _snapshot_rows(ids, m, x, v, fm, fx, fv):
+    rows = []
+    for i in range(len(m)):
+        rows.append(f"{ids[i]}," + (fm % m[i]) + "," + ",".join(fx % q for q in x[i]) + ","
+                    + ",".join(fv % q for q in v[i]))
+    return rows
+
+
+@pytest.mark.parametrize("name", ["leapfrog", "euler_float"])
+def test_output_golden_rows_follow_oracle(orc, name):
+    """The reference's snapshot files (output.npz) hold the oracle's state at
+    each snapshot time -- t = steps * dt, and for leapfrog v synchronised to
+    integer time -- printed as src/output.c:425-462 prints it ("%.17g", or
+    "%.8g" for a float output dtype)."""
+    import json
+    c = cases(golden("output"))[name]
+    args = json.loads(bytes(c["args.json"]).decode())
+    o = args["output"]
+    f = {1: "%.8g", 2: "%.17g"}
+    fm = f[o.get("mass_output_dtype", 2)]
+    fx = f[o.get("coordinate_output_dtype", 2)]
+    fv = f[o.get("velocity_output_dtype", 2)]
+    x0, v0, m0, G = c["x0"], c["v0"], c["m0"], float(c["G"])
+    dt, eps = args["dt"], args["extra"]["eps"]
+    files = sorted(k for k in c if k.startswith("snapshot_"))
+    assert len(files) >= 3
+    for k, fname in enumerate(files):
+        lines = bytes(c[fname]).decode().split("\n")
+        assert lines[0] == f"# num_particles: {m0.size}" and lines[1] == "# G: %.17g" % G
+        assert lines[4] == "particle_id,m,x,y,z,vx,vy,vz" and lines[-1] == ""
+        if k == 0 and o["output_initial"]:
+            x, v = x0, v0
+        else:
+            t = float(lines[2].split(": ")[1])
+            steps = round(t / dt)
+            assert steps * dt == t and float(lines[3].split(": ")[1]) == dt
+            x, v = orc.fixed_step_run(args["integrator"], 1, x0, v0, m0, G, eps, dt, steps * dt)
+        assert lines[5:-1] == _snapshot_rows(np.arange(m0.size), m0, x, v, fm, fx, fv), fname
+
+
+def test_dft_matches_numpy_fft(orc):
+    """The oracle's direct DFT has FFTW's r2c / c2r semantics (checked
+    against numpy's FFT, an independent implementation)."""
+    rng = np.random.default_rng(3)
+    for shape in [(4, 6, 8), (5, 3, 7), (8, 8, 8), (1, 1, 2)]:
+        a = rng.standard_normal(shape)
+        y = orc.dft3_r2c(a)
+        scale = np.abs(a).sum()
+        assert np.abs(y - np.fft.rfftn(a)).max() <= 1e-14 * scale
+        back = orc.dft3_c2r(y, shape[2])
+        assert np.abs(back - a * a.size).max() <= 1e-13 * scale * a.size
+
+
+def test_pm_golden(orc):
+    """acceleration_PM and the cosmological leapfrog: the restatement equals
+    the reference (built from its sources with the same DFT standing in for
+    FFTW) bit for bit."""
+    import json
+    d = golden("pm")
+    c, bw = d["box_center"], float(d["box_width"])
+    H0, om, sf = float(d["H0"]), float(d["omega_m"]), float(d["scale_factor"])
+    for name, cs in cases(d).items():
+        if name == "cosmo":
+            continue
+        rho = cs["m"].sum() / ((bw * 2) ** 3)
+        a = orc.acceleration_pm(cs["x"], cs["m"], c, bw, H0, om, rho, int(cs["grid"]), sf)
+        assert np.array_equal(a, cs["a"]), name
+    cs = cases(d)["cosmo"]
+    kw = json.loads(bytes(cs["args.json"]).decode())
+    x, steps, t = orc.leapfrog_cosmology(cs["x0"], cs["v0"], cs["m"], kw["h"], kw["omega_m"],
+                                         kw["omega_lambda"], np.array(kw["box_center"]),
+                                         kw["box_width"], kw["dt"], kw["a_begin"], kw["a_final"],
+                                         kw["pm_grid_size"])
+    assert steps == int(cs["steps"]) and t == float(cs["t"])
+    assert np.array_equal(x, cs["x"])
+
+
+@pytest.mark.skipif(not reference._loadable(reference.PM), reason="reference not built here")
+def test_pm_against_fresh_reference_run(orc):
+    """A fresh case through the reference's own particle-mesh code."""
+    rng = np.random.default_rng(77)
+    c, bw = np.array([0.0, 1.0, -1.0]), 2.0
+    x = c + rng.uniform(-bw, bw, (700, 3))
+    m = rng.uniform(0.1, 1.0, 700)
+    rho = m.sum() / ((bw * 2) ** 3)
+    a_ref = reference.acceleration_pm(x, m, c, bw, 67.0, 0.31, rho, 12, 0.7)
+    a = orc.acceleration_pm(x, m, c, bw, 67.0, 0.31, rho, 12, 0.7)
+    assert np.array_equal(a, a_ref)
