@@ -25,6 +25,11 @@ Workloads (seeded synthetic inputs -- grav_sim publishes no dataset):
   ensemble8192 / ensemble8192_leapfrog -- 8,192 planetary systems (Sun, 8
                     planets, 0-4,096 massless test particles each), WHFast or
                     leapfrog with the massless accelerations, dt = 1 day.
+  cosmo_pm256    -- cosmological particle-mesh run: 256^3 particles on a
+                    perturbed lattice in a periodic box, 256^3 mesh, h = 0.7,
+                    Omega_m = 0.3, Omega_Lambda = 0.7, a = 1/8 in steps of
+                    1/256 (exact in binary, so K steps are ceil(K da / da) = K;
+                    launch_cosmological_simulation).
 
 value      particle-steps/s over all ranks, state resident in HBM, device
            time of K steps from CUDA events on the simulation's stream
@@ -112,6 +117,8 @@ WORKLOADS = {
                                flop_per_interaction=20),
     "ensemble8192": dict(ic="ensemble", systems=8192, seed=3, max_test=4096, dt=1.0,
                          integrator=10, method=102),
+    "cosmo_pm256": dict(ic="cosmo", n=256 ** 3, grid=256, seed=7, box_width=50.0, h=0.7,
+                        omega_m=0.3, omega_lambda=0.7, a_begin=0.125, da=1.0 / 256),
     "ensemble8192_leapfrog": dict(ic="ensemble", systems=8192, seed=3, max_test=4096, dt=1.0,
                                   integrator=4, method=102),
 }
@@ -234,6 +241,8 @@ def run_ours(args, world, rank, local):
     wk = WORKLOADS[args.workload]
     if wk["ic"] == "ensemble":
         return run_ensemble(args, world, rank, local, wk, g, wl, lib)
+    if wk["ic"] == "cosmo":
+        return run_cosmo(args, world, rank, local, wk, g, lib)
     n = wk["n"]
     x, v, m = (wl.plummer if wk["ic"] == "plummer" else wl.galaxy_pair)(n, wk["seed"])
     bh = wk["method"] in (103, 104, 105, 106, 107, 113)
@@ -489,6 +498,94 @@ def run_ensemble(args, world, rank, local, wk, g, wl, lib):
                 "d2h_bytes_per_step": (P * 60) / args.steps,
                 "note": "create + upload + K steps + download through gsgpu_ensemble_*"},
         "gpu_launches": args.steps * kps,
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def run_cosmo(args, world, rank, local, wk, g, lib):
+    """Cosmological particle-mesh run through launch_cosmological_simulation:
+    value from the device time of the step loop (CUDA events on the
+    library's stream), e2e from the wall time of the whole call (host->device
+    copies, allocation, K steps, device->host copy of x)."""
+    import torch
+    n, grid, bw = wk["n"], wk["grid"], wk["box_width"]
+    rng = np.random.default_rng(wk["seed"])
+    side = round(n ** (1.0 / 3.0))
+    spacing = 2.0 * bw / side
+    centre = np.zeros(3)
+    lattice = np.indices((side, side, side)).reshape(3, -1).T.astype(np.float64)
+    x = np.ascontiguousarray(centre - bw + (lattice + 0.5 + rng.uniform(-0.3, 0.3, (n, 3)))
+                             * spacing)
+    v = np.ascontiguousarray(rng.normal(0.0, 5.0, (n, 3)))
+    m = np.ones(n)
+    del lattice
+    kw = dict(h=wk["h"], omega_m=wk["omega_m"], omega_lambda=wk["omega_lambda"],
+              box_center=centre, box_width=bw, dt=wk["da"], a_begin=wk["a_begin"],
+              pm_grid_size=grid)
+    lib.gsgpu_cosmology_last_timing.argtypes = [ctypes.POINTER(ctypes.c_double),
+                                                ctypes.POINTER(ctypes.c_int64),
+                                                ctypes.POINTER(ctypes.c_int)]
+    xw = x.copy()
+    g.launch_cosmological_simulation(lib, xw, v.copy(), m,
+                                     a_final=wk["a_begin"] + args.warmup * wk["da"], **kw)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    clocks.start()
+    time.sleep(0.3)
+    xt = x.copy()
+    t0 = time.perf_counter()
+    st = g.launch_cosmological_simulation(lib, xt, v.copy(), m,
+                                          a_final=wk["a_begin"] + args.steps * wk["da"], **kw)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    loop_ms, steps, kps = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int()
+    assert lib.gsgpu_cosmology_last_timing(ctypes.byref(loop_ms), ctypes.byref(steps),
+                                           ctypes.byref(kps)) == 0
+    assert steps.value == args.steps == st.num_steps, (steps.value, st.num_steps)
+    dev_s = loop_ms.value / 1e3
+    if world > 1:
+        t = torch.tensor([dev_s, wall], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_s, wall = float(t[0]), float(t[1])
+    # The step is bound by the FP64 pipe (1/64 of the FP32 rate on this GPU).
+    # Algorithmic FP64 work per step (an FMA counts 2): per particle the two
+    # cloud-in-cell weight sets (2 x 15), the deposit products (14), the
+    # interpolation (8 products + 24 FMA = 56), two kicks and the drift
+    # (3 x 6) = 118; per mesh cell the contrast (2), the gradient (15) and the
+    # Green's function (~3) = 20; the r2c and c2r transforms 2.5 N log2 N each.
+    cells = grid ** 3
+    flop_step = 118.0 * n + 20.0 * cells + 2 * 2.5 * cells * math.log2(cells)
+    lib.gsgpu_measure_fma_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_double)]
+    peak64 = ctypes.c_double()
+    lib.gsgpu_measure_fma_peak(1, ctypes.byref(peak64), None)
+    achieved = flop_step / (dev_s / args.steps) / 1e12
+    out = {
+        "metric": METRIC, "value": world * n * args.steps / dev_s, "unit": "particle-steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded perturbed lattice)",
+        "config": {"workload": f"{args.workload}: {n} particles, {grid}^3 mesh, periodic box "
+                               f"width {2 * bw}, a from {wk['a_begin']} in steps of {wk['da']}",
+                   "parallelism": f"replicas x{world}",
+                   "l2": f"inputs larger than L2 ({n * 24 / 2**20:.0f} MiB of positions, "
+                         f"{grid ** 3 * 56 / 2**20:.0f} MiB of meshes)",
+                   "accuracy": "within 1e-10 of the largest acceleration of the reference's "
+                               "particle-mesh code (tests/test_gpu_pm.py)"},
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64.value,
+                     "unit": "TFLOP/s", "frac": achieved / peak64.value, "traffic": None,
+                     "kernel": "whole step (8 kernels + 2 cuFFT transforms)",
+                     "algorithmic_flop_per_step": flop_step,
+                     "peak_source": "FP64 FMA probe on this GPU (gsgpu_measure_fma_peak), "
+                                    "not in MEASURED_PEAKS.json"},
+        "e2e": {"value": world * n * args.steps / wall, "unit": "particle-steps/s",
+                "h2d_bytes_per_step": n * 56 / args.steps, "d2h_bytes_per_step": n * 24 / args.steps,
+                "note": "one launch_cosmological_simulation call of K steps"},
+        "gpu_launches": args.steps * kps.value,
         "clocks": clk,
     }
     if rank == 0:

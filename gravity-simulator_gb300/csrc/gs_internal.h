@@ -229,6 +229,8 @@ ErrorStatus pm_acceleration_host(double *a, int n, const double *x, const double
 ErrorStatus pm_leapfrog_cosmology(CosmologicalSystem *system, SimulationStatus *status,
                                   const bool *is_exit, double dt, double a_begin, double a_final,
                                   int pm_grid_size);
+// Device time of the step loop of this thread's last cosmological run.
+ErrorStatus pm_last_timing(double *loop_ms, int64_t *steps);
 
 // ---- snapshots (host_output.cpp) ----------------------------------------
 ErrorStatus output_prepare(OutputParam *op, const Settings *settings);

@@ -146,4 +146,19 @@ ErrorStatus launch_cosmological_simulation(CosmologicalSystem *system, OutputPar
     return gs::ok();
 }
 
+// Device time (CUDA events on the run's stream) of the step loop of the
+// calling thread's last leapfrog_cosmology / launch_cosmological_simulation,
+// and its step count.  Kernels of this library per step: two kicks, the
+// drift with the periodic wrap, and five particle-mesh kernels.
+int gsgpu_cosmology_last_timing(double *loop_ms, int64_t *steps, int *kernels_per_step)
+{
+    ErrorStatus st = gs::pm_last_timing(loop_ms, steps);
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    if (kernels_per_step) *kernels_per_step = 8;
+    return 0;
+}
+
 }  // extern "C"

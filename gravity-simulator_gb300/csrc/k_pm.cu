@@ -13,11 +13,16 @@
 //                  acceleration mesh (the reference scales phi in place
 //                  first; the product is formed on load here, same bits);
 //   k_pm_interp    cloud-in-cell interpolation back to the particles.
-// The device expressions are the reference's C expressions in its order and
-// the file is compiled with --fmad=false, so given the same transform
-// output every kernel rounds as the reference does; the transform (cuFFT
-// against FFTW) and the atomic deposit order are the only sources of
-// difference.
+// Every kernel computes the reference's quantity in FP64.  The FP64 pipe of
+// this GPU runs at 1/64 of the FP32 rate and bounds the particle kernels, so
+// they use algebraically equal forms with fewer FP64 operations than the
+// reference's expressions: weight products shared between the eight
+// corners, fused multiply-adds, the constant divisions of the kicks, the
+// drift and the gradient folded into one multiplier each.  These round
+// differently from the reference's order by a few ulps, far below the
+// differences of the transforms (cuFFT against FFTW) and of the atomic
+// deposit order.  The file is compiled with --fmad=false; the fused
+// operations are the explicit fma() calls.
 //
 // Memory: delta / phi g^3 doubles, the spectrum g^2 (g/2+1) complex, the
 // acceleration mesh 3 g^3 doubles: 56 g^3 bytes, 940 MB at g = 256.
@@ -91,8 +96,12 @@ __device__ __forceinline__ void cic_cell(const double *xi, const PmGeom &G, int 
     }
 }
 
-// Corner order of the reference's eight terms: bit 0 x, bit 1 y, bit 2 z.
-__constant__ unsigned char kCorner[8] = {0, 1, 2, 4, 3, 5, 6, 7};
+// Corner order of the reference's eight terms: bit 0 x, bit 1 y, bit 2 z
+// (a constant in unrolled loops, so the per-corner arrays stay in registers).
+__host__ __device__ constexpr int corner_bits(int c)
+{
+    return c == 3 ? 4 : (c == 4 ? 3 : c);
+}
 
 __global__ void k_pm_deposit(const double *__restrict__ x, const double *__restrict__ m, int n,
                              PmGeom G, double *__restrict__ delta)
@@ -104,19 +113,28 @@ __global__ void k_pm_deposit(const double *__restrict__ x, const double *__restr
     cic_cell(x + 3 * (size_t)i, G, idx, w);
     const long long g = G.g, g2 = g * g;
     const double mi = m[i];
+    double mx[2], mxy[2][2];
+#pragma unroll
+    for (int bx = 0; bx < 2; ++bx) {
+        mx[bx] = mi * w[bx][0];
+#pragma unroll
+        for (int by = 0; by < 2; ++by) mxy[bx][by] = mx[bx] * w[by][1];
+    }
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
-        const int bx = kCorner[c] & 1, by = (kCorner[c] >> 1) & 1, bz = (kCorner[c] >> 2) & 1;
+        const int bx = corner_bits(c) & 1, by = (corner_bits(c) >> 1) & 1,
+                  bz = (corner_bits(c) >> 2) & 1;
         const long long cell = idx[bx][0] * g2 + idx[by][1] * g + idx[bz][2];
-        atomicAdd(delta + cell, mi * w[bx][0] * w[by][1] * w[bz][2]);
+        atomicAdd(delta + cell, mxy[bx][by] * w[bz][2]);
     }
 }
 
-__global__ void k_pm_contrast(double *__restrict__ delta, long long cells, double denom)
+// delta = rho / (V_cell rho_mean) - 1 with inv = 1 / (V_cell rho_mean)
+__global__ void k_pm_contrast(double *__restrict__ delta, long long cells, double inv)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cells) return;
-    delta[i] = (delta[i] / denom) - 1.0;
+    delta[i] = fma(delta[i], inv, -1.0);
 }
 
 // src/acceleration_PM.c:321-345
@@ -140,8 +158,10 @@ __global__ void k_pm_green(double2 *__restrict__ spec, int g, double two_pi_over
     spec[e] = v;
 }
 
-// src/acceleration_PM.c:212-272 on phi * factor.
-__global__ void k_pm_gradient(const double *__restrict__ phi, int g, double factor, double denom,
+// src/acceleration_PM.c:212-272: (phi[-2] - 8 phi[-1] + 8 phi[+1] - phi[+2])
+// * factor / (12 cell_length), as ((phi[-2] - phi[+2]) + 8 (phi[+1] - phi[-1]))
+// * scale with scale = factor / (12 cell_length).
+__global__ void k_pm_gradient(const double *__restrict__ phi, int g, double scale,
                               double *__restrict__ acc)
 {
     const long long g2 = (long long)g * g, cells = g2 * g;
@@ -155,11 +175,11 @@ __global__ void k_pm_gradient(const double *__restrict__ phi, int g, double fact
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const long long b = index - c[d] * st[d];
-        const double pm2 = phi[b + (long long)((c[d] - 2 + g) % g) * st[d]] * factor;
-        const double pm1 = phi[b + (long long)((c[d] - 1 + g) % g) * st[d]] * factor;
-        const double pp1 = phi[b + (long long)((c[d] + 1) % g) * st[d]] * factor;
-        const double pp2 = phi[b + (long long)((c[d] + 2) % g) * st[d]] * factor;
-        acc[index * 3 + d] = (pm2 - 8.0 * pm1 + 8.0 * pp1 - pp2) / denom;
+        const double pm2 = phi[b + (long long)((c[d] - 2 + g) % g) * st[d]];
+        const double pm1 = phi[b + (long long)((c[d] - 1 + g) % g) * st[d]];
+        const double pp1 = phi[b + (long long)((c[d] + 1) % g) * st[d]];
+        const double pp2 = phi[b + (long long)((c[d] + 2) % g) * st[d]];
+        acc[index * 3 + d] = fma(8.0, pp1 - pm1, pm2 - pp2) * scale;
     }
 }
 
@@ -173,23 +193,26 @@ __global__ void k_pm_interp(const double *__restrict__ x, int n, PmGeom G,
     double w[2][3];
     cic_cell(x + 3 * (size_t)i, G, idx, w);
     const long long g = G.g, g2 = g * g;
-    long long cell[8];
-    double wt[8][3];
+    double wxy[2][2];
+#pragma unroll
+    for (int bx = 0; bx < 2; ++bx)
+#pragma unroll
+        for (int by = 0; by < 2; ++by) wxy[bx][by] = w[bx][0] * w[by][1];
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
-        const int bx = kCorner[c] & 1, by = (kCorner[c] >> 1) & 1, bz = (kCorner[c] >> 2) & 1;
-        cell[c] = idx[bx][0] * g2 + idx[by][1] * g + idx[bz][2];
-        wt[c][0] = w[bx][0];
-        wt[c][1] = w[by][1];
-        wt[c][2] = w[bz][2];
+        const int bx = corner_bits(c) & 1, by = (corner_bits(c) >> 1) & 1,
+                  bz = (corner_bits(c) >> 2) & 1;
+        const long long cell = idx[bx][0] * g2 + idx[by][1] * g + idx[bz][2];
+        const double wc = wxy[bx][by] * w[bz][2];
+        const double *ac = acc + cell * 3;
+        s0 = fma(ac[0], wc, s0);
+        s1 = fma(ac[1], wc, s1);
+        s2 = fma(ac[2], wc, s2);
     }
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        double s = acc[cell[0] * 3 + d] * wt[0][0] * wt[0][1] * wt[0][2];
-#pragma unroll
-        for (int c = 1; c < 8; ++c) s = s + acc[cell[c] * 3 + d] * wt[c][0] * wt[c][1] * wt[c][2];
-        a[3 * (size_t)i + d] = s;
-    }
+    a[3 * (size_t)i + 0] = s0;
+    a[3 * (size_t)i + 1] = s1;
+    a[3 * (size_t)i + 2] = s2;
 }
 
 // ---- cosmological leapfrog (src/integrator_cosmology_leapfrog.c) -----------
@@ -225,23 +248,23 @@ __global__ void k_cosmo_momentum(double *__restrict__ p, const double *__restric
     p[k] = t * t * v[k];
 }
 
-// momentum -= (0.5 dt) a / da (:142-149, :176-183); hdt = 0.5 * dt
+// momentum -= (0.5 dt) a / da (:142-149, :176-183); c = 0.5 dt / da
 __global__ void k_cosmo_kick(double *__restrict__ p, const double *__restrict__ a, int len,
-                             double hdt, double da)
+                             double c)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= len) return;
-    p[k] -= hdt * a[k] / da;
+    p[k] = fma(-c, a[k], p[k]);
 }
 
-// x += dt p / (a^2 da) (:152-160), then the periodic wrap (:163); a2da = t * t * da
+// x += dt p / (a^2 da) (:152-160), then the periodic wrap (:163); c = dt / (a^2 da)
 __global__ void k_cosmo_drift(double *__restrict__ x, const double *__restrict__ p, int len,
-                              double dt, double a2da, double cx, double cy, double cz, double bw)
+                              double c, double cx, double cy, double cz, double bw)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= len) return;
     const int d = k % 3;
-    const double xv = x[k] + dt * p[k] / a2da;
+    const double xv = fma(c, p[k], x[k]);
     x[k] = periodic(xv, d == 0 ? cx : (d == 1 ? cy : cz), bw);
 }
 
@@ -294,7 +317,8 @@ class PmSolver {
         GS_CUDA(cudaMemsetAsync(mesh, 0, (size_t)cells * sizeof(double), s));
         k_pm_deposit<<<blocks(n), TPB, 0, s>>>(d_x, d_m, n, G, mesh);
         const double cell_volume = cell_length * cell_length * cell_length;
-        k_pm_contrast<<<blocks(cells), TPB, 0, s>>>(mesh, cells, cell_volume * mean_bkg_density);
+        k_pm_contrast<<<blocks(cells), TPB, 0, s>>>(mesh, cells,
+                                                    1.0 / (cell_volume * mean_bkg_density));
         GS_CUDA(cudaGetLastError());
         GS_CUFFT(cufftSetStream(fwd_, s));
         GS_CUFFT(cufftExecD2Z(fwd_, mesh, spec_.as<cufftDoubleComplex>()));
@@ -305,7 +329,7 @@ class PmSolver {
         GS_CUFFT(cufftSetStream(inv_, s));
         GS_CUFFT(cufftExecZ2D(inv_, spec_.as<cufftDoubleComplex>(), mesh));
         const double factor = ((3.0 / 2.0) * omega_m * H0 * H0) / (scale_factor * (double)cells);
-        k_pm_gradient<<<blocks(cells), TPB, 0, s>>>(mesh, g, factor, 12.0 * cell_length,
+        k_pm_gradient<<<blocks(cells), TPB, 0, s>>>(mesh, g, factor / (12.0 * cell_length),
                                                     acc_.as<double>());
         k_pm_interp<<<blocks(n), TPB, 0, s>>>(d_x, n, G, acc_.as<double>(), d_a);
         GS_CUDA(cudaGetLastError());
@@ -324,8 +348,13 @@ struct PmCall {
     cudaStream_t stream = nullptr;
     PmSolver solver;
     DBuf x, m, a;
+    cudaEvent_t ev[2] = {nullptr, nullptr};   // around the step loop
+    double loop_ms = 0.0;
+    int64_t loop_steps = 0;
     ~PmCall()
     {
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -339,6 +368,8 @@ ErrorStatus pm_call(PmCall **out)
         GS_TRY(device_info(&d));
         std::unique_ptr<PmCall> c(new PmCall());
         GS_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        GS_CUDA(cudaEventCreate(&c->ev[0]));
+        GS_CUDA(cudaEventCreate(&c->ev[1]));
         tl_pm = std::move(c);
     }
     *out = tl_pm.get();
@@ -428,19 +459,20 @@ ErrorStatus pm_leapfrog_cosmology(CosmologicalSystem *system, SimulationStatus *
     const int64_t total = (std::isfinite(q) && q >= 0.0) ? (int64_t)std::ceil(q) : 0;
     if (status) status->dt = dt;
     int64_t steps = 0;
+    GS_CUDA(cudaEventRecord(pc->ev[0], s));
     while (steps < total) {
         if (t + dt > a_final) dt = a_final - t;
         if (status) status->dt = dt;
         double da = compute_da(t, H0, omega_m, omega_lambda);
-        k_cosmo_kick<<<blocks(L), TPB, 0, s>>>(p.as<double>(), a.as<double>(), L, 0.5 * dt, da);
+        k_cosmo_kick<<<blocks(L), TPB, 0, s>>>(p.as<double>(), a.as<double>(), L, 0.5 * dt / da);
         t += 0.5 * dt;
         da = compute_da(t, H0, omega_m, omega_lambda);
-        k_cosmo_drift<<<blocks(L), TPB, 0, s>>>(x.as<double>(), p.as<double>(), L, dt, t * t * da,
-                                                c[0], c[1], c[2], bw);
+        k_cosmo_drift<<<blocks(L), TPB, 0, s>>>(x.as<double>(), p.as<double>(), L,
+                                                dt / (t * t * da), c[0], c[1], c[2], bw);
         GS_CUDA(cudaGetLastError());
         GS_TRY(pc->solver.compute(a.as<double>(), n, x.as<double>(), m.as<double>(), c, bw, H0,
                                   omega_m, mean_bkg_density, g, t, s));
-        k_cosmo_kick<<<blocks(L), TPB, 0, s>>>(p.as<double>(), a.as<double>(), L, 0.5 * dt, da);
+        k_cosmo_kick<<<blocks(L), TPB, 0, s>>>(p.as<double>(), a.as<double>(), L, 0.5 * dt / da);
         GS_CUDA(cudaGetLastError());
         ++steps;
         t = a_begin + steps * dt;
@@ -450,8 +482,21 @@ ErrorStatus pm_leapfrog_cosmology(CosmologicalSystem *system, SimulationStatus *
         }
         if (is_exit && *is_exit) break;
     }
+    GS_CUDA(cudaEventRecord(pc->ev[1], s));
     GS_CUDA(cudaMemcpyAsync(system->x, x.p, b3, cudaMemcpyDeviceToHost, s));
     GS_CUDA(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    GS_CUDA(cudaEventElapsedTime(&ms, pc->ev[0], pc->ev[1]));
+    pc->loop_ms = ms;
+    pc->loop_steps = steps;
+    return ok();
+}
+
+ErrorStatus pm_last_timing(double *loop_ms, int64_t *steps)
+{
+    if (!tl_pm) return GS_RAISE(GRAV_VALUE_ERROR, "no cosmological run on this thread");
+    if (loop_ms) *loop_ms = tl_pm->loop_ms;
+    if (steps) *steps = tl_pm->loop_steps;
     return ok();
 }
 

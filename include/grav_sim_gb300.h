@@ -246,6 +246,11 @@ ErrorStatus launch_cosmological_simulation(CosmologicalSystem *system, OutputPar
                                            Settings *settings, double dt, double a_begin,
                                            double a_final, int pm_grid_size);
 
+/* No reference counterpart: device time (CUDA events on the run's stream) of
+ * the step loop of the calling thread's last cosmological run, its steps,
+ * and this library's kernels per step (cuFFT's own kernels not counted). */
+int gsgpu_cosmology_last_timing(double *loop_ms, int64_t *steps, int *kernels_per_step);
+
 /* src/python_interface.c:94-125 */
 int launch_simulation_python(
     int32_t *num_particles, int32_t *particle_ids, double *x, double *v,
