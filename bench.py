@@ -17,6 +17,11 @@ Workloads (seeded synthetic inputs -- grav_sim publishes no dataset):
   galaxy1048576_plain -- the same at N = 1,048,576 with the monopole walk.
   galaxy2097152_group / galaxy1048576_group -- the group walk with
                     interaction lists (quadrupole cells), theta = 0.5.
+  galaxy2097152_group_leaf1 / _t065, galaxy1048576_group_leaf1 -- with one
+                    particle per leaf (the reference's default tree), or at
+                    theta = 0.65 (median error 6.4e-4, inside the 1e-3 bound).
+                    The group workloads use up to 8 particles per leaf, the
+                    library's default for methods 106 and 107.
   galaxy1048576_group_mono[_t035] -- the group walk with monopole cells
                     only, theta = 0.5 (0.35).
   galaxy1048576_learned -- theta = 1.0 walk + learned residual, judged by a
@@ -98,22 +103,31 @@ WORKLOADS = {
                                   integrator=4, method=104, theta=1.0, leaf=1,
                                   flop_per_interaction=20),
     "galaxy2097152_group": dict(ic="galaxy", n=2097152, seed=4, G=1.0, eps=0.01, dt=1e-3,
-                                integrator=4, method=106, theta=0.5, leaf=1,
+                                integrator=4, method=106, theta=0.5, leaf=8,
                                 flop_per_interaction=20),
+    "galaxy2097152_group_leaf1": dict(ic="galaxy", n=2097152, seed=4, G=1.0, eps=0.01, dt=1e-3,
+                                      integrator=4, method=106, theta=0.5, leaf=1,
+                                      flop_per_interaction=20),
+    "galaxy2097152_group_t065": dict(ic="galaxy", n=2097152, seed=4, G=1.0, eps=0.01, dt=1e-3,
+                                     integrator=4, method=106, theta=0.65, leaf=8,
+                                     flop_per_interaction=20),
     "galaxy1048576_group": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01, dt=1e-3,
-                                integrator=4, method=106, theta=0.5, leaf=1,
+                                integrator=4, method=106, theta=0.5, leaf=8,
                                 flop_per_interaction=20),
+    "galaxy1048576_group_leaf1": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01, dt=1e-3,
+                                      integrator=4, method=106, theta=0.5, leaf=1,
+                                      flop_per_interaction=20),
     "galaxy1048576_group_mono": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01, dt=1e-3,
-                                     integrator=4, method=107, theta=0.5, leaf=1,
+                                     integrator=4, method=107, theta=0.5, leaf=8,
                                      flop_per_interaction=20),
     "galaxy1048576_group_mono_t035": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01,
                                           dt=1e-3, integrator=4, method=107, theta=0.35,
-                                          leaf=1, flop_per_interaction=20),
+                                          leaf=8, flop_per_interaction=20),
     # small cases of the walks, for profiler captures
     "galaxy262144": dict(ic="galaxy", n=262144, seed=6, G=1.0, eps=0.01, dt=1e-3, integrator=4,
                          method=105, theta=0.5, leaf=1, flop_per_interaction=20),
     "galaxy262144_group": dict(ic="galaxy", n=262144, seed=6, G=1.0, eps=0.01, dt=1e-3,
-                               integrator=4, method=106, theta=0.5, leaf=1,
+                               integrator=4, method=106, theta=0.5, leaf=8,
                                flop_per_interaction=20),
     "ensemble8192": dict(ic="ensemble", systems=8192, seed=3, max_test=4096, dt=1.0,
                          integrator=10, method=102),

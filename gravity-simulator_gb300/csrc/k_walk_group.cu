@@ -192,6 +192,7 @@ __device__ __forceinline__ void flush_cells(const GroupShared &g, int count, flo
     const float2 nrx = splat(-rx), nry = splat(-ry), nrz = splat(-rz), e2 = splat(eps2);
     float2 ax = splat(0.f), ay = splat(0.f), az = splat(0.f);
     int j = 0;
+#pragma unroll 4
     for (; j + 1 < count; j += 2) {
         const float2 dx = __fadd2_rn(ld2(g.cx, j), nrx);
         const float2 dy = __fadd2_rn(ld2(g.cy, j), nry);
@@ -233,6 +234,7 @@ __device__ __forceinline__ void flush_parts(const GroupShared &g, int count, flo
     const float2 nrx = splat(-rx), nry = splat(-ry), nrz = splat(-rz), e2 = splat(eps2);
     float2 ax = splat(0.f), ay = splat(0.f), az = splat(0.f);
     int j = 0;
+#pragma unroll 4
     for (; j + 1 < count; j += 2) {
         const float2 dx = __fadd2_rn(ld2(g.px, j), nrx);
         const float2 dy = __fadd2_rn(ld2(g.py, j), nry);
