@@ -493,14 +493,17 @@ __device__ __forceinline__ void add_particles(const double *__restrict__ x,
     }
 }
 
-// Internal nodes of depth d (reference :652-735).
+// Internal nodes of depth d (reference :652-735).  When q is not null, also
+// their quadrupoles from the children's by the parallel-axis shift:
+// Q = sum_c [Q_c + M_c (3 s s^T - |s|^2 I)], s = com_c - com.
 __global__ void k_multipole_level(int d, const int *__restrict__ ctr, const double *__restrict__ x,
                                   const double *__restrict__ m, const int *__restrict__ sidx,
                                   const int *__restrict__ in_id, const int *__restrict__ in_fc,
                                   const int *__restrict__ in_nchild, const int *__restrict__ t_np,
                                   const int *__restrict__ t_nc, const int *__restrict__ t_fp,
                                   const int *__restrict__ t_int, double *__restrict__ in_sum,
-                                  double *__restrict__ t_mass, double *__restrict__ t_com)
+                                  double *__restrict__ t_mass, double *__restrict__ t_com,
+                                  double *__restrict__ q)
 {
     const int lo = ctr[CTR_LVL + d];
     const int hi = ctr[CTR_LVL + d + 1];
@@ -526,10 +529,28 @@ __global__ void k_multipole_level(int d, const int *__restrict__ ctr, const doub
         ws[2] = S1;
         ws[3] = S2;
         const int id = in_id[ii];
+        const double c0 = __ddiv_rn(S0, M), c1 = __ddiv_rn(S1, M), c2 = __ddiv_rn(S2, M);
         t_mass[id] = M;
-        t_com[3 * id + 0] = __ddiv_rn(S0, M);
-        t_com[3 * id + 1] = __ddiv_rn(S1, M);
-        t_com[3 * id + 2] = __ddiv_rn(S2, M);
+        t_com[3 * id + 0] = c0;
+        t_com[3 * id + 1] = c1;
+        t_com[3 * id + 2] = c2;
+        if (q) {
+            double Q[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+            for (int c = fc; c < fc + nch; ++c) {
+                const double Mc = t_mass[c];
+                const double s0 = t_com[3 * c] - c0, s1 = t_com[3 * c + 1] - c1,
+                             s2 = t_com[3 * c + 2] - c2;
+                const double r2 = s0 * s0 + s1 * s1 + s2 * s2;
+                const double *qc = q + 6 * (size_t)c;
+                Q[0] += qc[0] + Mc * (3.0 * s0 * s0 - r2);
+                Q[1] += qc[1] + Mc * 3.0 * s0 * s1;
+                Q[2] += qc[2] + Mc * 3.0 * s0 * s2;
+                Q[3] += qc[3] + Mc * (3.0 * s1 * s1 - r2);
+                Q[4] += qc[4] + Mc * 3.0 * s1 * s2;
+                Q[5] += qc[5] + Mc * (3.0 * s2 * s2 - r2);
+            }
+            for (int k = 0; k < 6; ++k) q[6 * (size_t)id + k] = Q[k];
+        }
     }
 }
 
@@ -567,36 +588,6 @@ __global__ void k_leaf_multipoles(const int *__restrict__ ctr, const double *__r
             }
             for (int k = 0; k < 6; ++k) q[6 * (size_t)id + k] = Q[k];
         }
-    }
-}
-
-// Quadrupoles of the internal nodes of depth d from their children by the
-// parallel-axis shift: Q = sum_c [Q_c + M_c (3 s s^T - |s|^2 I)], s = com_c - com.
-__global__ void k_quadrupole_level(int d, const int *__restrict__ ctr, const int *__restrict__ in_id,
-                                   const int *__restrict__ in_fc, const int *__restrict__ in_nchild,
-                                   const double *__restrict__ t_mass,
-                                   const double *__restrict__ t_com, double *__restrict__ q)
-{
-    const int lo = ctr[CTR_LVL + d];
-    const int hi = ctr[CTR_LVL + d + 1];
-    for (int ii = lo + blockIdx.x * blockDim.x + threadIdx.x; ii < hi;
-         ii += gridDim.x * blockDim.x) {
-        const int id = in_id[ii];
-        const double c0 = t_com[3 * id], c1 = t_com[3 * id + 1], c2 = t_com[3 * id + 2];
-        double Q[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-        for (int c = in_fc[ii]; c < in_fc[ii] + in_nchild[ii]; ++c) {
-            const double Mc = t_mass[c];
-            const double s0 = t_com[3 * c] - c0, s1 = t_com[3 * c + 1] - c1, s2 = t_com[3 * c + 2] - c2;
-            const double r2 = s0 * s0 + s1 * s1 + s2 * s2;
-            const double *qc = q + 6 * (size_t)c;
-            Q[0] += qc[0] + Mc * (3.0 * s0 * s0 - r2);
-            Q[1] += qc[1] + Mc * 3.0 * s0 * s1;
-            Q[2] += qc[2] + Mc * 3.0 * s0 * s2;
-            Q[3] += qc[3] + Mc * (3.0 * s1 * s1 - r2);
-            Q[4] += qc[4] + Mc * 3.0 * s1 * s2;
-            Q[5] += qc[5] + Mc * (3.0 * s2 * s2 - r2);
-        }
-        for (int k = 0; k < 6; ++k) q[6 * (size_t)id + k] = Q[k];
     }
 }
 
@@ -706,10 +697,11 @@ ErrorStatus OctreeDevice::setup(int n_, int leaf_max_, bool compat_, bool quad_)
 int OctreeDevice::launches_per_build() const
 {
     // bbox 2, morton 1, sort, init 1, levels 2*21, keys 1, sort, fc 3,
-    // number 1, multipoles 21 (+1 leaves), walk arrays 2 (+ quadrupoles 21 + 1)
+    // number 1, multipoles 21 (+1 leaves; quadrupoles in the same launches),
+    // walk arrays 2 (+1 quadrupole copy)
     return 2 + 1 + RadixSorter::launches(63) + 1 + 42 + 1 +
            RadixSorter::launches(internal_key_bits()) + 3 + 1 +
-           21 + (compat ? 0 : 1) + 2 + (quad ? 22 : 0) + (links ? 1 : 0);
+           21 + (compat ? 0 : 1) + 2 + (quad ? 1 : 0) + (links ? 1 : 0);
 }
 
 ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream_t s,
@@ -774,11 +766,8 @@ ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream
         k_multipole_level<<<grid, OT_THREADS, 0, s>>>(
             d, ctr.as<int>(), d_x, d_m, sidx.as<int>(), in_id.as<int>(), in_fc.as<int>(),
             in_nchild.as<int>(), t_np.as<int>(), t_nc.as<int>(), t_fp.as<int>(), t_int.as<int>(),
-            in_sum.as<double>(), t_mass.as<double>(), t_com.as<double>());
-        if (quad)
-            k_quadrupole_level<<<grid, OT_THREADS, 0, s>>>(
-                d, ctr.as<int>(), in_id.as<int>(), in_fc.as<int>(), in_nchild.as<int>(),
-                t_mass.as<double>(), t_com.as<double>(), t_quad.as<double>());
+            in_sum.as<double>(), t_mass.as<double>(), t_com.as<double>(),
+            quad ? t_quad.as<double>() : nullptr);
     }
     if (quad)
         k_walk_quads<<<grid, OT_THREADS, 0, s>>>(ctr.as<int>(), t_quad.as<double>(),

@@ -128,3 +128,58 @@ extern "C" int gsgpu_tc_gemm_selftest(int N, int K, int a_mn_major, int b_mn_maj
     }
     return hs ? GRAV_FAILURE : GRAV_SUCCESS;
 }
+
+namespace gs {
+
+// A bounded wait that runs out: thread 0 waits on an mbarrier that no
+// thread arrives at, polling %globaltimer; after limit_ns it gives up and
+// records ST_WAIT_TIMEOUT, and the kernel ends normally.  This is the exit
+// every wait of the library's kernels takes (mbar_wait: 2 s), exercised
+// with a short limit.
+__global__ void k_wait_timeout_selftest(unsigned long long limit_ns, unsigned *status)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    bool done = mbar_try_wait(&bar, 0);
+    const unsigned long long t0 = global_ns();
+    while (!done && global_ns() - t0 <= limit_ns) done = mbar_try_wait(&bar, 0);
+    if (!done) atomicOr(status, ST_WAIT_TIMEOUT);
+}
+
+}  // namespace gs
+
+// Test entry point (no counterpart in the reference): runs the expiring
+// wait with a limit of limit_ms (1..2000) and returns the status word.
+extern "C" int gsgpu_wait_timeout_selftest(double limit_ms, unsigned *status_out)
+{
+    using namespace gs;
+    if (!status_out) return GRAV_POINTER_ERROR;
+    if (!(limit_ms >= 1.0 && limit_ms <= 2000.0)) return GRAV_VALUE_ERROR;
+    const DeviceInfo *dev = nullptr;
+    ErrorStatus st = device_info(&dev);
+    if (st.return_code == GRAV_SUCCESS) {
+        DBuf s;
+        st = s.reserve(sizeof(unsigned));
+        if (st.return_code == GRAV_SUCCESS) {
+            cudaError_t e = cudaMemset(s.p, 0, sizeof(unsigned));
+            if (e == cudaSuccess) {
+                k_wait_timeout_selftest<<<1, 32>>>((unsigned long long)(limit_ms * 1e6),
+                                                   s.as<unsigned>());
+                e = cudaGetLastError();
+            }
+            if (e == cudaSuccess)
+                e = cudaMemcpy(status_out, s.p, sizeof(unsigned), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) st = GS_RAISE(GRAV_FAILURE, "wait selftest: %s", cudaGetErrorString(e));
+        }
+    }
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    return GRAV_SUCCESS;
+}

@@ -453,6 +453,12 @@ int gsgpu_mlp_train_step(gsgpu_mlp *mlp, const float *features, const float *tar
  * reference; it supplies the FP32/FP64 pipe peaks of the rooflines. */
 int gsgpu_measure_fma_peak(int fp64, double *tflops, double *ms);
 
+/* No reference counterpart: a kernel whose bounded wait runs out (an
+ * mbarrier nobody arrives at, limit_ms in 1..2000) writes the device status
+ * word, which is returned in *status_out (ST_WAIT_TIMEOUT = 1).  Shows that
+ * an expired wait ends with an error status and leaves the context usable. */
+int gsgpu_wait_timeout_selftest(double limit_ms, unsigned *status_out);
+
 #ifdef __cplusplus
 }
 #endif
