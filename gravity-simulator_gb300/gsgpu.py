@@ -287,6 +287,32 @@ def launch_cosmological_simulation(lib: ctypes.CDLL, x: np.ndarray, v: np.ndarra
     return status
 
 
+def load_gadget2_ic(lib: ctypes.CDLL, path):
+    """Gadget-2 HDF5 initial conditions (load_gadget2_ic): returns
+    (x, v, m, (unit_length, unit_mass, unit_time)) as numpy copies."""
+    lib.load_gadget2_ic.restype = ErrorStatus
+    lib.load_gadget2_ic.argtypes = [ctypes.c_char_p, ctypes.POINTER(System), c_double_p,
+                                    c_double_p, c_double_p]
+    lib.free_system.restype = None
+    lib.free_system.argtypes = [ctypes.POINTER(System)]
+    s = System()
+    units = (ctypes.c_double * 3)()
+    st = lib.load_gadget2_ic(str(path).encode(), ctypes.byref(s),
+                             ctypes.cast(ctypes.byref(units, 0), c_double_p),
+                             ctypes.cast(ctypes.byref(units, 8), c_double_p),
+                             ctypes.cast(ctypes.byref(units, 16), c_double_p))
+    if st.return_code != 0:
+        raise GravError(st.return_code, take_traceback(lib, st))
+    n = s.num_particles
+    x = np.ctypeslib.as_array(s.x, (n, 3)).copy()
+    v = np.ctypeslib.as_array(s.v, (n, 3)).copy()
+    m = np.ctypeslib.as_array(s.m, (n,)).copy()
+    ids = np.ctypeslib.as_array(s.particle_ids, (n,)).copy()
+    lib.free_system(ctypes.byref(s))
+    assert (ids == np.arange(n)).all()
+    return x, v, m, tuple(units)
+
+
 def take_traceback(lib: ctypes.CDLL, st: ErrorStatus) -> str:
     text = ""
     if st.traceback:

@@ -128,6 +128,17 @@ typedef struct Settings {
 
 /* src/system.h:28 */
 System get_new_system(void);
+/* src/system.h:125 */
+void free_system(System *system);
+
+/* Gadget-2 initial conditions from an HDF5 file, as grav_sim's galaxy-collision
+ * example reads them through libhdf5 (examples/galaxy_collision/c/
+ * galaxy_collision.c:109-293): particles of PartType1 then PartType2 (Masses,
+ * Coordinates, Velocities), ids 0..n-1, and the three unit attributes of
+ * /Units.  The file is parsed directly (no libhdf5); the arrays are allocated
+ * with malloc and released by free_system.  G is left to the caller. */
+ErrorStatus load_gadget2_ic(const char *path, System *system, double *unit_length,
+                            double *unit_mass, double *unit_time);
 /* src/acceleration.h:33 */
 AccelerationParam get_new_acceleration_param(void);
 /* src/acceleration.h:40-42 */
