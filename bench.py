@@ -100,7 +100,7 @@ WORKLOADS = {
                                 integrator=4, method=103, theta=0.5, leaf=1,
                                 flop_per_interaction=20),
     "galaxy1048576_learned": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01, dt=1e-3,
-                                  integrator=4, method=104, theta=1.0, leaf=1,
+                                  integrator=4, method=104, theta=1.0, leaf=8,
                                   flop_per_interaction=20),
     "galaxy2097152_group": dict(ic="galaxy", n=2097152, seed=4, G=1.0, eps=0.01, dt=1e-3,
                                 integrator=4, method=106, theta=0.5, leaf=8,
