@@ -205,6 +205,20 @@ def dist_setup():
     return world, rank, local
 
 
+def max_over_ranks(values, world):
+    """Each value's maximum over the ranks (replicas: the slowest rank sets
+    the job's time).  Uses whichever torch.distributed backend is up: NCCL on
+    CUDA tensors, gloo on CPU tensors."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu().tolist()]
+
+
 def cpu_baseline_pairwise(wk, x, m, target_s=12.0):
     """Time the reference's pairwise loop (oracle restatement, 1 thread) on a
     bounded slice of outer rows and extrapolate to one full leapfrog step."""
@@ -322,10 +336,7 @@ def run_ours(args, world, rank, local):
         torch.distributed.barrier()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = float(sum(step_ms))
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms, = max_over_ranks([total_ms], world)
     force_ms = ctypes.c_double()
     force_n = ctypes.c_int64()
     lib.gsgpu_sim_force_timing(sim, ctypes.byref(force_ms), ctypes.byref(force_n))
@@ -385,7 +396,7 @@ def run_ours(args, world, rank, local):
                         tf=wk["dt"] * args.steps * (1 - 1e-9), method=wk["method"],
                         opening_angle=wk.get("theta", 1.0), softening_length=wk["eps"],
                         max_num_particles_per_leaf=wk.get("leaf", -1))
-    e2e_s = time.perf_counter() - t0
+    e2e_s, = max_over_ranks([time.perf_counter() - t0], world)
     e2e_val = world * n * args.steps / e2e_s
 
     traffic = None
@@ -480,10 +491,7 @@ def run_ensemble(args, world, rank, local, wk, g, wl, lib):
     torch.cuda.synchronize()
     total_s = time.perf_counter() - t0
     clk = clocks.stop()
-    if world > 1:
-        t = torch.tensor([total_s], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
+    total_s, = max_over_ranks([total_s], world)
     kps = ens.kernels_per_step()
     ens.close()
     value = world * P * args.steps / total_s
@@ -493,7 +501,7 @@ def run_ensemble(args, world, rank, local, wk, g, wl, lib):
     e2.upload(ids, x, v, m)
     e2.run(args.steps)
     e2.download()
-    e2e_s = time.perf_counter() - t0
+    e2e_s, = max_over_ranks([time.perf_counter() - t0], world)
     e2.close()
     name = "WHFast" if wk["integrator"] == 10 else "leapfrog"
     out = {
@@ -561,10 +569,7 @@ def run_cosmo(args, world, rank, local, wk, g, lib):
                                            ctypes.byref(kps)) == 0
     assert steps.value == args.steps == st.num_steps, (steps.value, st.num_steps)
     dev_s = loop_ms.value / 1e3
-    if world > 1:
-        t = torch.tensor([dev_s, wall], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_s, wall = float(t[0]), float(t[1])
+    dev_s, wall = max_over_ranks([dev_s, wall], world)
     # The step is bound by the FP64 pipe (1/64 of the FP32 rate on this GPU).
     # Algorithmic FP64 work per step (an FMA counts 2): per particle the two
     # cloud-in-cell weight sets (2 x 15), the deposit products (14), the
