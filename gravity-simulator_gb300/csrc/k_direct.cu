@@ -6,8 +6,9 @@
 //   * positions and masses are packed once per evaluation into a float4
 //     array (x, y, z, m) relative to a fixed frame centre, padded to a whole
 //     number of 1024-particle tiles with massless far-away particles;
-//   * a CTA of 256 threads owns 1024 i-particles (4 per thread, register
-//     blocked) and one contiguous j-chunk; j-tiles of 1024 particles (16 KiB)
+//   * a CTA of 128 threads owns 1024 i-particles (8 per thread, register
+//     blocked; two CTAs per SM) and one contiguous j-chunk; j-tiles of 1024
+//     particles (16 KiB)
 //     stream through a 3-stage shared-memory ring filled by TMA bulk copies
 //     (cp.async.bulk + mbarrier complete_tx), read back as broadcast float4;
 //   * each pair term is 3 FADD + 3 FFMA + rsqrt + 3 FMUL + 3 FFMA in FP32;
@@ -33,8 +34,8 @@
 
 namespace gs {
 
-constexpr int DS_THREADS = 256;
-constexpr int DS_IPT = 4;
+constexpr int DS_THREADS = 128;
+constexpr int DS_IPT = 8;
 constexpr int DS_ITILE = DS_THREADS * DS_IPT;  // 1024
 constexpr int DS_JTILE = 1024;                 // 16 KiB of float4
 constexpr int DS_STAGES = 3;
