@@ -307,7 +307,15 @@ __device__ void walk_group(const GroupWalkArgs &A, GroupShared &g, const float *
         int act = 0;   // 1 accept, 2 leaf, 3 open
         int4 ci = make_int4(0, 0, 0, 0);
         float4 crel = make_float4(0.f, 0.f, 0.f, 0.f);
+        // quadrupole of the node, loaded with the node (used if accepted), so
+        // that its latency overlaps the other loads instead of following the
+        // decision
+        float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
         if (node >= 0) {
+            if (QUAD) {
+                q0 = A.nq[2 * node];
+                q1 = A.nq[2 * node + 1];
+            }
             const float4 ca = A.na[node], cb = A.nb[node];
             ci = A.nc[node];
             crel = make_float4((ca.x - oh.x) + (cb.x - ol.x), (ca.y - oh.y) + (cb.y - ol.y),
@@ -343,7 +351,6 @@ __device__ void walk_group(const GroupWalkArgs &A, GroupShared &g, const float *
                 g.cz[at] = crel.z;
                 g.cm[at] = crel.w;
                 if (QUAD) {
-                    const float4 q0 = A.nq[2 * node], q1 = A.nq[2 * node + 1];
                     g.qxx[at] = q0.x;
                     g.qxy[at] = q0.y;
                     g.qxz[at] = q0.z;
@@ -480,7 +487,9 @@ __device__ bool group_fits(const GroupWalkArgs &A, const float *s_w2, int lane, 
 }
 
 template <bool QUAD>
-__global__ void __launch_bounds__(32 * GW_WARPS)
+// Five CTAs per SM (shared memory allows five; the register cap costs a few
+// spilled bytes but keeps the fifth CTA resident).
+__global__ void __launch_bounds__(32 * GW_WARPS, 5)
 k_bh_group(GroupWalkArgs A)
 {
     extern __shared__ __align__(16) unsigned char gw_smem[];
