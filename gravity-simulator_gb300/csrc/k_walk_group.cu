@@ -378,14 +378,30 @@ __device__ void walk_group(const GroupWalkArgs &A, GroupShared &g, const float *
                     npart = 0;
                     __syncwarp();
                 }
-                for (int q = 0; q < cnt; ++q) {
-                    const int p = ci.z + q;
-                    const float4 qa = A.pa[p], qb = A.pb[p];
-                    const int at = npart + incl - cnt + q;
-                    g.px[at] = (qa.x - oh.x) + (qb.x - ol.x);
-                    g.py[at] = (qa.y - oh.y) + (qb.y - ol.y);
-                    g.pz[at] = (qa.z - oh.z) + (qb.z - ol.z);
-                    g.pm[at] = qa.w;
+                // The warp copies the step's leaf particles together, one slot
+                // per lane per round: slot t belongs to the last lane whose
+                // exclusive prefix is <= t (found by a binary search over the
+                // lanes), so every lane issues its loads at once.
+                const int excl = incl - cnt;
+                for (int base = 0; base < total; base += 32) {
+                    const int t = base + lane;
+                    int lo = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1) {
+                        const int e = __shfl_sync(0xffffffffu, excl, lo + step);
+                        if (e <= t) lo += step;
+                    }
+                    const int first = __shfl_sync(0xffffffffu, ci.z, lo);
+                    const int off = t - __shfl_sync(0xffffffffu, excl, lo);
+                    if (t < total) {
+                        const int p = first + off;
+                        const float4 qa = A.pa[p], qb = A.pb[p];
+                        const int at = npart + t;
+                        g.px[at] = (qa.x - oh.x) + (qb.x - ol.x);
+                        g.py[at] = (qa.y - oh.y) + (qb.y - ol.y);
+                        g.pz[at] = (qa.z - oh.z) + (qb.z - ol.z);
+                        g.pm[at] = qa.w;
+                    }
                 }
                 npart += total;
                 __syncwarp();
