@@ -315,6 +315,13 @@ struct gsgpu_sim {
             GS_TRY(absmax2(b + 6 * SL, a1, &mb, &ma));
             const double eb7 = mb / ma;
             double error = std::pow((eb7 / tolerance), 1.0 / 7.0);
+            // With every acceleration zero (a single particle, or no mass) the
+            // estimate is 0/0; the reference's loop then never advances t and
+            // never ends.  Stop with an error instead.
+            if (std::isnan(error))
+                return GS_RAISE(GRAV_VALUE_ERROR,
+                                "IAS15 error estimate is not a number (all accelerations are "
+                                "zero); the step size cannot be controlled");
             if (error < 1e-10) error = 1e-10;
             const double dt_new = h / error;
             if (error <= 1.0 || h == tf * 1e-12) {

@@ -23,9 +23,11 @@ Outputs (compressed .npz, a few hundred KB in total):
                      (src/output.c:340-470), one case per loop family
   pm.npz             acceleration_PM and launch_cosmological_simulation
                      (src/acceleration_PM.c, src/integrator_cosmology_leapfrog.c)
+  edges.npz          one- and two-particle systems, tf = 0 and three steps, every
+                     integrator of launch_simulation
 
 ``python tests/golden/make_golden.py whfast output`` remakes only the named
-files of the last group (whfast, rk_embedded, ias15, output, pm).
+files of the last group (whfast, rk_embedded, ias15, output, pm, edges).
 """
 from __future__ import annotations
 
@@ -254,12 +256,39 @@ def pm_cases():
     return out
 
 
+def edge_cases():
+    """One- and two-particle systems through every integrator of
+    launch_simulation, for no time (tf = 0) and three steps, pairwise sum
+    (massless for WHFast).  IAS15 with a single particle is left out: its
+    error estimate is 0/0 and the reference's step loop never ends.  So is
+    WHFast with two particles over steps: the reference kicks the centre-of-
+    mass velocity with a[0], which it never writes (src/integrator_whfast.c
+    :409-422), and in this run that memory held a non-zero value."""
+    out = {}
+    x, v, m = wl.plummer(3, 5)
+    out["x"], out["v"], out["m"] = x, v, m
+    for n in (1, 2):
+        for integ in (1, 2, 3, 4, 5, 6, 7, 8, 9, 10):
+            if integ == 9 and n == 1:
+                continue
+            tfs = (0.0,) if (integ == 10 and n == 2) else (0.0, 3e-3)
+            for tf in tfs:
+                kw = dict(tolerance=1e-8) if 5 <= integ <= 9 else {}
+                method = 2 if integ == 10 else 1
+                ids, xr, vr, mr = ref.launch(x[:n], v[:n], m[:n], 1.0, integ, 1e-3, tf, method,
+                                             eps=0.01, **kw)
+                key = f"n{n}_int{integ}_tf{tf:g}"
+                out[f"{key}/ids"], out[f"{key}/x"], out[f"{key}/v"] = ids, xr, vr
+    return out
+
+
 LATE = {
     "whfast": lambda: whfast_cases(),
     "rk_embedded": lambda: rk_embedded_cases(),
     "ias15": lambda: ias15_cases(),
     "output": lambda: output_cases(),
     "pm": lambda: pm_cases(),
+    "edges": lambda: edge_cases(),
 }
 
 
