@@ -55,6 +55,10 @@ ErrorStatus cuda_error(cudaError_t e, const char *what, const char *file,
             return gs::cuda_error(e_, #call, __FILE__, __LINE__, __func__);   \
     } while (0)
 
+// Largest particle count: 3N components are indexed with int, as in the
+// reference's arrays.
+constexpr int kMaxParticles = 0x7fffffff / 3;
+
 // ---- device buffers ----------------------------------------------------
 // Grow-only device allocation owned by an engine or simulation.
 struct DBuf {

@@ -76,6 +76,9 @@ ErrorStatus check_system(const System *s, bool need_v)
     if (s->num_particles <= 0)
         return GS_RAISE(GRAV_VALUE_ERROR, "Number of particles must be positive. Got: %d",
                         s->num_particles);
+    if (s->num_particles > kMaxParticles)
+        return GS_RAISE(GRAV_VALUE_ERROR, "Number of particles exceeds %d. Got: %d", kMaxParticles,
+                        s->num_particles);
     if (!s->x) return GS_RAISE(GRAV_POINTER_ERROR, "System array x is NULL");
     if (need_v && !s->v) return GS_RAISE(GRAV_POINTER_ERROR, "System array v is NULL");
     if (!s->m) return GS_RAISE(GRAV_POINTER_ERROR, "System array m is NULL");
@@ -603,6 +606,8 @@ ErrorStatus sim_create(gsgpu_sim **out, int n, double G, const AccelerationParam
     if (!out) return GS_RAISE(GRAV_POINTER_ERROR, "output pointer is NULL");
     if (!param) return GS_RAISE(GRAV_POINTER_ERROR, "Acceleration parameter pointer is NULL");
     if (n <= 0) return GS_RAISE(GRAV_VALUE_ERROR, "Number of particles must be positive. Got: %d", n);
+    if (n > kMaxParticles)
+        return GS_RAISE(GRAV_VALUE_ERROR, "Number of particles exceeds %d. Got: %d", kMaxParticles, n);
     if (!(dt > 0.0)) return GS_RAISE(GRAV_VALUE_ERROR, "dt must be positive. Got: %g", dt);
     const DeviceInfo *d = nullptr;
     GS_TRY(device_info(&d));

@@ -1173,6 +1173,11 @@ ErrorStatus ensemble_create(gsgpu_ensemble **out, int num_systems, const int *co
     e->S = num_systems;
     e->integrator = integrator;
     e->dt = dt;
+    long long total = 0;
+    for (int s = 0; s < num_systems; ++s) total += counts[s] > 0 ? counts[s] : 0;
+    if (total > kMaxParticles)
+        return GS_RAISE(GRAV_VALUE_ERROR, "ensemble of %lld particles exceeds %d", total,
+                        kMaxParticles);
     e->h_off.assign(num_systems + 1, 0);
     for (int s = 0; s < num_systems; ++s) {
         if (counts[s] <= 0) return GS_RAISE(GRAV_VALUE_ERROR, "system %d is empty", s);
