@@ -2,6 +2,8 @@
 // small parameter helpers of grav_sim's C ABI.
 #include "gs_internal.h"
 
+#include <atomic>
+
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -94,12 +96,19 @@ void DBuf::release()
     bytes = 0;
 }
 
+// Host-side fault injection for tests: when set to k > 0, the k-th device
+// allocation from now on fails as an out-of-memory cudaMalloc would.
+static std::atomic<int> g_fail_alloc_in{0};
+
 ErrorStatus DBuf::reserve(size_t b)
 {
     if (b <= bytes && p) return ok();
     release();
     if (b == 0) b = 16;
-    cudaError_t e = cudaMalloc(&p, b);
+    int k = g_fail_alloc_in.load();
+    while (k > 0 && !g_fail_alloc_in.compare_exchange_weak(k, k - 1)) {
+    }
+    cudaError_t e = (k == 1) ? cudaErrorMemoryAllocation : cudaMalloc(&p, b);
     if (e != cudaSuccess) {
         p = nullptr;
         (void)cudaGetLastError();
@@ -235,6 +244,13 @@ using namespace gs;
 extern "C" {
 
 ErrorStatus make_success_error_status(void) { return ok(); }
+
+// Test hook (no reference counterpart): the k-th device allocation from now
+// on fails with an out-of-memory error; k = 0 switches the injection off.
+void gsgpu_test_fail_allocation(int k)
+{
+    g_fail_alloc_in.store(k > 0 ? k : 0);
+}
 
 void free_traceback(ErrorStatus *error_status)
 {

@@ -470,6 +470,11 @@ int gsgpu_measure_fma_peak(int fp64, double *tflops, double *ms);
  * an expired wait ends with an error status and leaves the context usable. */
 int gsgpu_wait_timeout_selftest(double limit_ms, unsigned *status_out);
 
+/* No reference counterpart: host-side fault injection for tests.  The k-th
+ * device allocation from now on fails as an out-of-memory cudaMalloc would
+ * (the call returns GRAV_MEMORY_ERROR); k = 0 switches it off. */
+void gsgpu_test_fail_allocation(int k);
+
 #ifdef __cplusplus
 }
 #endif
