@@ -127,7 +127,8 @@ __global__ void k_wh_sort(EnsDev E, double *vec, double *vel, int pow2_max, int 
             const double d[3] = {__dsub_rn(vec[3 * (base + i)], p0),
                                  __dsub_rn(vec[3 * (base + i) + 1], p1),
                                  __dsub_rn(vec[3 * (base + i) + 2], p2)};
-            key[i] = (i == prim) ? 0ull : dist_key(norm3d(d));
+            // first the squared distance, the radicand of the reference's key
+            key[i] = (i == prim) ? 0ull : dist_key(dot3(d, d));
             idx[i] = i;
         } else {
             key[i] = ~0ull;   // padding sorts last
@@ -136,10 +137,22 @@ __global__ void k_wh_sort(EnsDev E, double *vec, double *vel, int pow2_max, int 
     }
     __syncthreads();
     // Already in order (the usual case from one step to the next): a stable
-    // sort is the identity; eta is kept unless it was never formed.
+    // sort is the identity; eta is kept unless it was never formed.  The
+    // square root is monotone, so squared distances in order imply distances
+    // in order, and the check needs no square roots.  Otherwise the keys
+    // become the distances themselves (rounded square roots can tie where
+    // the squares did not) and are checked again.
     bool unsorted = false;
     for (int i = threadIdx.x; i + 1 < n; i += blockDim.x)
         unsorted = unsorted || key[i] > key[i + 1];
+    if (__syncthreads_or(unsorted)) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+            if (i != prim) key[i] = dist_key(__dsqrt_rn(__longlong_as_double((long long)key[i])));
+        __syncthreads();
+        unsorted = false;
+        for (int i = threadIdx.x; i + 1 < n; i += blockDim.x)
+            unsorted = unsorted || key[i] > key[i + 1];
+    }
     if (!__syncthreads_or(unsorted)) {
         if (need_eta && threadIdx.x == 0) {
             double e = E.m[base];
