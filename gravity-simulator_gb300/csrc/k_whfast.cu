@@ -8,7 +8,8 @@
 //
 // Layout: all systems concatenated; system s owns slots [off[s], off[s+1])
 // of every per-particle array and its first cnt[s] slots are live (WHFast
-// can remove particles).  Every kernel covers all systems in one launch:
+// can remove particles).  Every kernel covers all systems in one launch
+// (the sort: one launch per size class of systems):
 //   k_wh_sort       one CTA per system: sort by distance from the primary
 //                   (bitonic sort of (distance, index) in shared memory,
 //                   ties by index), permute, eta (sequential prefix);
@@ -85,10 +86,11 @@ __device__ __forceinline__ unsigned long long dist_key(double d)
 // ids; then eta.  Dynamic shared memory: pow2 * (8 + 4) bytes.
 constexpr int SORT_OET_PASSES = 32;   // odd-even passes tried before the bitonic network
 
-__global__ void k_wh_sort(EnsDev E, double *vec, double *vel, int pow2_max, int need_eta)
+__global__ void k_wh_sort(EnsDev E, double *vec, double *vel, int pow2_max, int need_eta,
+                          const int *__restrict__ systems)
 {
     extern __shared__ __align__(16) unsigned char wh_smem[];
-    const int s = blockIdx.x;
+    const int s = systems[blockIdx.x];
     const int base = E.off[s];
     const int n = E.cnt[s];
     if (n <= 0) return;
@@ -945,8 +947,17 @@ __global__ void __launch_bounds__(32 * SEQ_WARPS) k_ens_massive_list(EnsDev E)
 // ---------------------------------------------------------------------------
 using namespace gs;
 
+// The sort is launched once per size class of systems, with shared memory
+// and threads for the largest system of the class, so that the many small
+// systems do not each reserve the largest system's shared memory.
+constexpr int kSortClasses = 3;
+constexpr int kSortClassPow2[kSortClasses] = {256, 1024, kEnsembleMaxSystem};
+
 struct gsgpu_ensemble {
     int S = 0, P = 0, max_n = 0, pow2 = 1;
+    DBuf sort_list;                        // system ids grouped by class
+    int sort_first[kSortClasses + 1] = {};  // class c: sort_list[sort_first[c]..sort_first[c+1])
+    int sort_pow2[kSortClasses] = {};       // largest power of two of the class's systems
     int integrator = INTEGRATOR_WHFAST;
     double dt = 0.0;
     cudaStream_t stream = nullptr;
@@ -1027,9 +1038,16 @@ struct gsgpu_ensemble {
 
     ErrorStatus sort(double *vec, double *vel)
     {
-        const size_t smem = (size_t)pow2 * 12;
-        const int threads = pow2 >= 256 ? 256 : (pow2 < 32 ? 32 : pow2);
-        k_wh_sort<<<S, threads, smem, stream>>>(E, vec, vel, pow2, vec == E.x ? 1 : 0);
+        for (int c = 0; c < kSortClasses; ++c) {
+            const int count = sort_first[c + 1] - sort_first[c];
+            if (count == 0) continue;
+            const int p2 = sort_pow2[c];
+            const size_t smem = (size_t)p2 * 12;
+            // one thread per pair of slots for the odd-even passes, 32..1024
+            const int threads = std::min(1024, std::max(32, p2 / 2));
+            k_wh_sort<<<count, threads, smem, stream>>>(E, vec, vel, p2, vec == E.x ? 1 : 0,
+                                                        sort_list.as<int>() + sort_first[c]);
+        }
         GS_CUDA(cudaGetLastError());
         return ok();
     }
@@ -1091,7 +1109,13 @@ struct gsgpu_ensemble {
         return ok();
     }
 
-    int kernels_per_step() const { return integrator == INTEGRATOR_WHFAST ? 6 : 3; }
+    int sort_launches() const
+    {
+        int k = 0;
+        for (int c = 0; c < kSortClasses; ++c) k += sort_first[c + 1] > sort_first[c] ? 1 : 0;
+        return k;
+    }
+    int kernels_per_step() const { return integrator == INTEGRATOR_WHFAST ? 5 + sort_launches() : 3; }
 
     // Snapshot of system 0 (a launch_simulation run holds one system): E.x
     // and the velocity array dv with the ids and masses of its live slots.
@@ -1234,6 +1258,29 @@ ErrorStatus ensemble_create(gsgpu_ensemble **out, int num_systems, const int *co
     GS_CUDA(cudaMemset(e->a.p, 0, P * 3 * sizeof(double)));
     GS_CUDA(cudaFuncSetAttribute(k_wh_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)std::max<size_t>((size_t)e->pow2 * 12, 48 * 1024)));
+    {
+        // size classes of the sort (counts only shrink, by removals)
+        std::vector<int> list;
+        list.reserve(S);
+        for (int c = 0; c < kSortClasses; ++c) {
+            e->sort_first[c] = (int)list.size();
+            const int lo = c == 0 ? 0 : kSortClassPow2[c - 1];
+            int p2 = 1;
+            for (int s = 0; s < S; ++s) {
+                int q = 1;
+                while (q < counts[s]) q <<= 1;
+                if (q > lo && q <= kSortClassPow2[c]) {
+                    list.push_back(s);
+                    p2 = std::max(p2, q);
+                }
+            }
+            e->sort_pow2[c] = p2;
+        }
+        e->sort_first[kSortClasses] = (int)list.size();
+        GS_TRY(e->sort_list.reserve(list.size() * sizeof(int)));
+        GS_CUDA(cudaMemcpy(e->sort_list.p, list.data(), list.size() * sizeof(int),
+                           cudaMemcpyHostToDevice));
+    }
     EnsDev &E = e->E;
     E.S = e->S;
     E.off = e->off.as<int>();
