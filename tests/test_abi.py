@@ -2,6 +2,7 @@
 include/grav_sim_gb300.h declares, lays its structs out exactly like
 grav_sim, and applies grav_sim's parameter validation on the host."""
 import ctypes
+import os
 import subprocess
 import sys
 import textwrap
@@ -67,7 +68,7 @@ def _layout(tmp_path, include_line: str, extra_flags=()):
 def test_struct_layout_matches_reference(tmp_path):
     ours = _layout(tmp_path, f'"{HEADER}"')
     assert "System 48" in ours and "AccelerationParam 32" in ours and "ErrorStatus 24" in ours
-    refsrc = Path("/root/reference/src")
+    refsrc = Path(os.environ.get("GRAV_SIM_REFERENCE_DIR", "/root/reference")) / "src"
     if not (refsrc / "linear_octree.h").exists():
         pytest.skip("reference headers not present")
     shim = tmp_path / "ref_all.h"
