@@ -47,7 +47,7 @@ struct OctreeDevice {
     DBuf t_com;                                                      // double[3*cap]
     DBuf in_sum;                                                     // double[4*cap]
     // walk arrays (frame-centred double-float positions)
-    DBuf w_na, w_nb;          // float4[cap]: (com_hi, mass), (com_lo, 0)
+    DBuf w_na, w_nb;          // float4[cap]: (com_hi, mass), (com_lo, (cell side)^2)
     DBuf w_nc;                // int4[cap]: (first_child, num_children, first_particle, count)
     DBuf w_nkey;              // uint64[cap]: key used by the cell-membership test
     DBuf w_pa, w_pb;          // float4[n] in sorted order: (x_hi, m), (x_lo, 0)

@@ -613,6 +613,7 @@ __global__ void k_walk_nodes(const int *__restrict__ ctr, int compat, const doub
                              const uint64_t *__restrict__ keys, const int *__restrict__ sidx,
                              const int *__restrict__ t_np, const int *__restrict__ t_nc,
                              const int *__restrict__ t_fp, const int *__restrict__ t_fc,
+                             const int *__restrict__ t_depth,
                              const double *__restrict__ t_mass, const double *__restrict__ t_com,
                              float4 *__restrict__ na, float4 *__restrict__ nb, int4 *__restrict__ nc,
                              uint64_t *__restrict__ nkey)
@@ -625,7 +626,10 @@ __global__ void k_walk_nodes(const int *__restrict__ ctr, int compat, const doub
         split_df(__dsub_rn(t_com[3 * id + 1], c1), h1, l1);
         split_df(__dsub_rn(t_com[3 * id + 2], c2), h2, l2);
         na[id] = make_float4(h0, h1, h2, (float)t_mass[id]);
-        nb[id] = make_float4(l0, l1, l2, 0.0f);
+        // (cell side)^2 of the node's depth, box_length / (2 << d), for the
+        // opening test of the group walk
+        const double side = frame[4] / (double)(2 << min(t_depth[id], OCT_MAX_LEVEL + 1));
+        nb[id] = make_float4(l0, l1, l2, (float)(side * side));
         const int fp = t_fp[id];
         nc[id] = make_int4(t_fc[id], t_nc[id], fp, t_np[id]);
         // the reference's membership test reads keys[sorted_indices[first]]
@@ -774,9 +778,9 @@ ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream
                                                  w_nq.as<float4>());
     k_walk_nodes<<<grid, OT_THREADS, 0, s>>>(
         ctr.as<int>(), compat ? 1 : 0, frame.as<double>(), keys.as<uint64_t>(), sidx.as<int>(),
-        t_np.as<int>(), t_nc.as<int>(), t_fp.as<int>(), t_fc.as<int>(), t_mass.as<double>(),
-        t_com.as<double>(), w_na.as<float4>(), w_nb.as<float4>(), w_nc.as<int4>(),
-        w_nkey.as<uint64_t>());
+        t_np.as<int>(), t_nc.as<int>(), t_fp.as<int>(), t_fc.as<int>(), t_depth.as<int>(),
+        t_mass.as<double>(), t_com.as<double>(), w_na.as<float4>(), w_nb.as<float4>(),
+        w_nc.as<int4>(), w_nkey.as<uint64_t>());
     k_walk_particles<<<pb, OT_THREADS, 0, s>>>(n, frame.as<double>(), d_x, d_m, sidx.as<int>(),
                                                w_pa.as<float4>(), w_pb.as<float4>());
     GS_CUDA(cudaGetLastError());

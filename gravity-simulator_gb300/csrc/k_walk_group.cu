@@ -120,7 +120,7 @@ __global__ void k_group_list(const int *__restrict__ ctr, const int4 *__restrict
 
 struct GroupWalkArgs {
     const float4 *na;       // (com_hi, mass)
-    const float4 *nb;       // (com_lo, 0)
+    const float4 *nb;       // (com_lo, (cell side)^2)
     const float4 *nq;       // 2 per node: (xx, xy, xz, yy), (yz, zz, -, -)
     const int4 *nc;         // (first child, children, first particle, particles)
     const int *depth;
@@ -325,7 +325,7 @@ __device__ void walk_group(const GroupWalkArgs &A, GroupShared &g, const float *
             const float ey = fmaxf(fmaxf(by0 - crel.y, crel.y - by1), 0.f);
             const float ez = fmaxf(fmaxf(bz0 - crel.z, crel.z - bz1), 0.f);
             const float d2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-            const float w2 = s_w2[min(A.depth[node], OCT_MAX_LEVEL + 1)];
+            const float w2 = cb.w;   // (cell side)^2 of the node's depth
             if (!own && w2 < th2 * d2 && ca.w > 0.f)
                 act = 1;
             else if (ci.y <= 0)
