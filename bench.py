@@ -7,6 +7,9 @@ Prints ONE JSON line (rank 0).  A step is one integrator step of the
 workload (drift + force evaluation + kick) over the whole particle set.
 
 Workloads (seeded synthetic inputs -- grav_sim publishes no dataset):
+  plummer1024_fp64 -- the reference's CPU-sized case: Plummer N = 1,024, the
+                    FP64 direct sum in the reference's order (bit-exact),
+                    leapfrog dt = 1e-3; every step is one CUDA-graph replay.
   plummer262144  -- equal-mass Plummer sphere, N = 262,144, G = M = a = 1,
                     compensated-FP32 direct sum, eps = 0.01, leapfrog,
                     dt = 1e-3 (the mixed-precision direct-sum workload; the
@@ -89,6 +92,10 @@ def _module(name):
 WORKLOADS = {
     "plummer262144": dict(ic="plummer", n=262144, seed=2, G=1.0, eps=0.01, dt=1e-3, integrator=4,
                           method=101, flop_per_interaction=20),
+    # the reference's own CPU-sized case (N = 1,024, leapfrog, 1,000 steps in the
+    # parity test), FP64 reference-order forces: launch- and graph-bound
+    "plummer1024_fp64": dict(ic="plummer", n=1024, seed=1, G=1.0, eps=0.01, dt=1e-3,
+                             integrator=4, method=111, flop_per_interaction=20),
     # small case of the same kernel, for profiler captures
     "plummer65536": dict(ic="plummer", n=65536, seed=2, G=1.0, eps=0.01, dt=1e-3, integrator=4,
                          method=101, flop_per_interaction=20),
@@ -315,7 +322,6 @@ def run_ours(args, world, rank, local):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    lib.gsgpu_sim_set_force_timing(sim, 1)
     clocks = ClockSampler(local)
     if world > 1:
         torch.distributed.barrier()
@@ -337,10 +343,19 @@ def run_ours(args, world, rank, local):
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = float(sum(step_ms))
     total_ms, = max_over_ranks([total_ms], world)
+    kernels_per_step = lib.gsgpu_sim_kernels_per_step(sim)
+    # The dominant kernel's duration, for the roofline: K more steps with CUDA
+    # events around each force evaluation (launched directly, not from the
+    # graph; outside the timed region).
+    lib.gsgpu_sim_set_force_timing(sim, 1)
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)
+            assert lib.gsgpu_sim_run(sim, 1) == 0
+    torch.cuda.synchronize()
     force_ms = ctypes.c_double()
     force_n = ctypes.c_int64()
     lib.gsgpu_sim_force_timing(sim, ctypes.byref(force_ms), ctypes.byref(force_n))
-    kernels_per_step = lib.gsgpu_sim_kernels_per_step(sim)
     lib.gsgpu_sim_set_force_timing(sim, 0)
 
     value = world * n * args.steps / (total_ms / 1e3)
@@ -357,8 +372,9 @@ def run_ours(args, world, rank, local):
     mean_force_ms = force_ms.value / max(force_n.value, 1)
     achieved_tflops = wk["flop_per_interaction"] * interactions / (mean_force_ms / 1e3) / 1e12
 
+    fp64 = wk["method"] == 111   # the FP64 reference-order direct sum
     peak = ctypes.c_double()
-    lib.gsgpu_measure_fma_peak(0, ctypes.byref(peak), None)
+    lib.gsgpu_measure_fma_peak(1 if fp64 else 0, ctypes.byref(peak), None)
 
     # accuracy of the forces of the last step
     a_host = np.empty((n, 3))
@@ -384,7 +400,7 @@ def run_ours(args, world, rank, local):
                                   np.ascontiguousarray(state).ctypes.data_as(dp), 2, n)
         energy = {"e0": float(e[0]), "e1": float(e[1]),
                   "rel_drift": float(abs(e[1] - e[0]) / abs(e[0])),
-                  "steps": args.warmup + args.steps,
+                  "steps": args.warmup + 2 * args.steps,
                   "note": "unsoftened potential while the force is softened (eps=0.01), "
                           "as the reference's compute_energy"}
 
@@ -400,7 +416,8 @@ def run_ours(args, world, rank, local):
     e2e_val = world * n * args.steps / e2e_s
 
     traffic = None
-    kernel = ("k_bh_group" if wk["method"] in (106, 107) else "k_bh_walk") if bh else "k_direct_sum"
+    kernel = ("k_bh_group" if wk["method"] in (106, 107) else "k_bh_walk") if bh else \
+        ("k_direct_fp64_reference_order" if fp64 else "k_direct_sum")
     prof = ROOT / "profiles" / f"{kernel}_{args.workload}.md"
     if prof.exists():
         for ln in prof.read_text().splitlines():
@@ -411,6 +428,11 @@ def run_ours(args, world, rank, local):
                 f"theta={wk['theta']} leaf={wk['leaf']}, eps={wk['eps']}, leapfrog dt={wk['dt']}")
         data = "synthetic (seeded two-galaxy model: exponential disk, Hernquist bulge and halo)"
         dtype = "f32 walk terms (Kahan), f64 tree multipoles and state"
+    elif fp64:
+        desc = (f"{args.workload}: Plummer N={n}, FP64 direct sum in the reference's order "
+                f"(bit-exact), eps={wk['eps']}, leapfrog dt={wk['dt']}")
+        data = "synthetic (seeded Plummer sphere)"
+        dtype = "f64"
     else:
         desc = (f"{args.workload}: Plummer N={n}, compensated-FP32 direct sum, "
                 f"eps={wk['eps']}, leapfrog dt={wk['dt']}")
@@ -436,12 +458,13 @@ def run_ours(args, world, rank, local):
                    "accuracy": {"median_rel_err": med, "p99_rel_err": p99,
                                 "sample": "512 particles vs FP64 direct sum"},
                    "energy": energy},
-        "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak.value,
+        "roofline": {"bound": "fp64" if fp64 else "fp32", "achieved": achieved_tflops,
+                     "peak": peak.value,
                      "unit": "TFLOP/s", "frac": achieved_tflops / peak.value if peak.value else None,
                      "traffic": traffic,
                      "kernel": kernel, "mean_launch_ms": mean_force_ms,
-                     "peak_source": "FP32 FMA probe on this GPU (gsgpu_measure_fma_peak), "
-                                    "not in MEASURED_PEAKS.json",
+                     "peak_source": ("FP64" if fp64 else "FP32") + " FMA probe on this GPU "
+                                    "(gsgpu_measure_fma_peak), not in MEASURED_PEAKS.json",
                      "flop_per_interaction": wk["flop_per_interaction"]},
         "e2e": {"value": e2e_val, "unit": "particle-steps/s",
                 "h2d_bytes_per_step": (7 * n * 8) / args.steps,

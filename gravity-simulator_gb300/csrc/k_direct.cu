@@ -19,11 +19,12 @@
 //     sums go to an FP64 scratch array [split][3][N] that a second kernel
 //     reduces in fixed order and scales by G.
 //
-// GRAV_GPU_PAIRWISE_FP64 (reference order): one thread per particle sums the
-// pair terms of all other particles in index order with every FP64 product,
-// sum, sqrt and quotient rounded separately -- the same operations as the
-// reference's symmetric loop applies to that particle, so the result equals
-// the reference's bit for bit where the reference is not FMA-contracted.
+// GRAV_GPU_PAIRWISE_FP64 (reference order): a warp per ten particles forms
+// the pair terms of all other particles, 32 at a time, and sums them in index
+// order with every FP64 product, sum, sqrt and quotient rounded separately --
+// the same operations as the reference's symmetric loop applies to that
+// particle, so the result equals the reference's bit for bit where the
+// reference is not FMA-contracted.
 #include "gs_internal.h"
 #include "gs_ptx.cuh"
 
@@ -278,56 +279,71 @@ __global__ void k_reduce_splits(const double *__restrict__ partial, int splits, 
     a[3 * i + 2] = G * s2;
 }
 
-// FP64, reference operation order (see file comment).
-constexpr int RF_THREADS = 128;
+// FP64, reference operation order (see file comment).  One warp per PER
+// particles: for 32 consecutive j the lanes form the pair terms of the PER
+// particles (each term is independent), then lane 3p + c subtracts the
+// component-c terms of particle p from its accumulator one by one in j
+// order, which is the order the reference's loop adds them to a_i.  With
+// PER = 10, ten particles share each in-order accumulation instruction (30
+// of 32 lanes); with PER = 1 there are ten times as many warps, which small
+// systems need to fill the GPU.
+constexpr int RF_WARPS = 4;
+constexpr int RF_PER_WARP_LARGE = 10;
+constexpr int RF_LARGE_N = 32768;   // from here on, ten particles per warp
 
-__global__ void __launch_bounds__(RF_THREADS)
+template <int RF_PER_WARP>
+__global__ void __launch_bounds__(32 * RF_WARPS)
 k_direct_fp64_reference_order(const double *__restrict__ x, const double *__restrict__ m,
                               int n, double G, double eps2, double *__restrict__ a)
 {
-    __shared__ double sx[RF_THREADS], sy[RF_THREADS], sz[RF_THREADS], sm[RF_THREADS];
-    const int i = blockIdx.x * RF_THREADS + threadIdx.x;
-    double x0 = 0.0, x1 = 0.0, x2 = 0.0;
-    if (i < n) {
-        x0 = x[3 * i + 0];
-        x1 = x[3 * i + 1];
-        x2 = x[3 * i + 2];
-    }
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-    for (int base = 0; base < n; base += RF_THREADS) {
-        const int j = base + threadIdx.x;
+    __shared__ double terms[RF_WARPS][RF_PER_WARP * 3][32];
+    __shared__ double xi_s[RF_WARPS][RF_PER_WARP * 3];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int i0 = (blockIdx.x * RF_WARPS + w) * RF_PER_WARP;
+    if (i0 >= n) return;   // warp-uniform
+    const int np = min(RF_PER_WARP, n - i0);
+    if (lane < 3 * np) xi_s[w][lane] = x[3 * i0 + lane];
+    __syncwarp();
+    double acc = 0.0;   // lane 3p + c < 3 np: component c of a_(i0 + p)
+    for (int base = 0; base < n; base += 32) {
+        const int j = base + lane;
+        double xj0 = 0.0, xj1 = 0.0, xj2 = 0.0, mj = 0.0;
         if (j < n) {
-            sx[threadIdx.x] = x[3 * j + 0];
-            sy[threadIdx.x] = x[3 * j + 1];
-            sz[threadIdx.x] = x[3 * j + 2];
-            sm[threadIdx.x] = m[j];
+            xj0 = x[3 * j + 0];
+            xj1 = x[3 * j + 1];
+            xj2 = x[3 * j + 2];
+            mj = m[j];
         }
-        __syncthreads();
-        const int cnt = min(RF_THREADS, n - base);
-        if (i < n) {
-            for (int jj = 0; jj < cnt; ++jj) {
-                if (base + jj == i) continue;
-                const double r0 = __dsub_rn(x0, sx[jj]);
-                const double r1 = __dsub_rn(x1, sy[jj]);
-                const double r2 = __dsub_rn(x2, sz[jj]);
+        for (int p = 0; p < np; ++p) {
+            double t0 = 0.0, t1 = 0.0, t2 = 0.0;
+            if (j < n && j != i0 + p) {
+                const double r0 = __dsub_rn(xi_s[w][3 * p + 0], xj0);
+                const double r1 = __dsub_rn(xi_s[w][3 * p + 1], xj1);
+                const double r2 = __dsub_rn(xi_s[w][3 * p + 2], xj2);
                 const double s = __dadd_rn(
                     __dadd_rn(__dadd_rn(__dmul_rn(r0, r0), __dmul_rn(r1, r1)), __dmul_rn(r2, r2)),
                     eps2);
                 const double rn = __dsqrt_rn(s);
                 const double t = __ddiv_rn(G, __dmul_rn(__dmul_rn(rn, rn), rn));
-                const double mj = sm[jj];
-                a0 = __dsub_rn(a0, __dmul_rn(__dmul_rn(t, r0), mj));
-                a1 = __dsub_rn(a1, __dmul_rn(__dmul_rn(t, r1), mj));
-                a2 = __dsub_rn(a2, __dmul_rn(__dmul_rn(t, r2), mj));
+                t0 = __dmul_rn(__dmul_rn(t, r0), mj);
+                t1 = __dmul_rn(__dmul_rn(t, r1), mj);
+                t2 = __dmul_rn(__dmul_rn(t, r2), mj);
             }
+            terms[w][3 * p + 0][lane] = t0;
+            terms[w][3 * p + 1][lane] = t1;
+            terms[w][3 * p + 2][lane] = t2;
         }
-        __syncthreads();
+        __syncwarp();
+        if (lane < 3 * np) {
+            const int cnt = min(32, n - base);
+            const int self = i0 + lane / 3 - base;   // this particle's own slot, if in the chunk
+            const double *tc = terms[w][lane];
+            for (int q = 0; q < cnt; ++q)
+                if (q != self) acc = __dsub_rn(acc, tc[q]);
+        }
+        __syncwarp();
     }
-    if (i < n) {
-        a[3 * i + 0] = a0;
-        a[3 * i + 1] = a1;
-        a[3 * i + 2] = a2;
-    }
+    if (lane < 3 * np) a[3 * i0 + lane] = acc;
 }
 
 // ------------------------------------------------------------------------
@@ -393,9 +409,13 @@ class DirectEngine final : public Engine {
                         ForceTimer *timer) override
     {
         if (fp64_) {
-            const int grid = (n_ + RF_THREADS - 1) / RF_THREADS;
+            const bool large = n_ >= RF_LARGE_N;
+            const int per_cta = RF_WARPS * (large ? RF_PER_WARP_LARGE : 1);
+            const int grid = (n_ + per_cta - 1) / per_cta;
             if (timer) GS_TRY(timer->begin(s));
-            k_direct_fp64_reference_order<<<grid, RF_THREADS, 0, s>>>(d_x, d_m, n_, G_, eps_ * eps_,
+            auto kernel = large ? k_direct_fp64_reference_order<RF_PER_WARP_LARGE>
+                                : k_direct_fp64_reference_order<1>;
+            kernel<<<grid, 32 * RF_WARPS, 0, s>>>(d_x, d_m, n_, G_, eps_ * eps_,
                                                                       d_a);
             GS_CUDA(cudaGetLastError());
             if (timer) GS_TRY(timer->end(s));

@@ -97,3 +97,11 @@ def test_cpu_method_code_rejected(lib, g, wl):
     with pytest.raises(g.GravError) as e:
         g.acceleration(lib, x, m, 1.0, 1)
     assert e.value.code == g.GRAV_VALUE_ERROR
+
+
+def test_fp64_reference_order_bitexact_large(lib, g, orc, wl):
+    """Above 32,768 particles the FP64 reference-order sum runs ten particles
+    per warp; still the reference's operations in the reference's order."""
+    x, v, m = wl.plummer(33000, 17)
+    a = g.acceleration(lib, x, m, 1.0, g.METHOD_GPU_PAIRWISE_FP64, 1.0, 0.01, -1)
+    assert np.array_equal(a, orc.pairwise(x, m, 1.0, 0.01))
