@@ -20,6 +20,8 @@ Workloads (seeded synthetic inputs -- grav_sim publishes no dataset):
   galaxy1048576_plain -- the same at N = 1,048,576 with the monopole walk.
   galaxy2097152_group / galaxy1048576_group -- the group walk with
                     interaction lists (quadrupole cells), theta = 0.5.
+  galaxy16777216_group -- the group walk at N = 16,777,216 (about 4 GB of
+                    state and tree in HBM).
   galaxy2097152_group_leaf1 / _t065, galaxy1048576_group_leaf1 -- with one
                     particle per leaf (the reference's default tree), or at
                     theta = 0.65 (median error 6.4e-4, inside the 1e-3 bound).
@@ -112,6 +114,9 @@ WORKLOADS = {
     "galaxy2097152_group": dict(ic="galaxy", n=2097152, seed=4, G=1.0, eps=0.01, dt=1e-3,
                                 integrator=4, method=106, theta=0.5, leaf=8,
                                 flop_per_interaction=20),
+    "galaxy16777216_group": dict(ic="galaxy", n=16777216, seed=8, G=1.0, eps=0.01, dt=1e-3,
+                                 integrator=4, method=106, theta=0.5, leaf=8,
+                                 flop_per_interaction=20),
     "galaxy2097152_group_leaf1": dict(ic="galaxy", n=2097152, seed=4, G=1.0, eps=0.01, dt=1e-3,
                                       integrator=4, method=106, theta=0.5, leaf=1,
                                       flop_per_interaction=20),
