@@ -456,8 +456,6 @@ class DirectEngine final : public Engine {
         return ok();
     }
 
-    int splits() const { return splits_; }
-
   private:
     bool fp64_;
     int n_ = 0, n_pad_ = 0, i_tiles_ = 0, jt_total_ = 0, jt_per_chunk_ = 1, splits_ = 1;

@@ -1266,7 +1266,7 @@ ErrorStatus ensemble_create(gsgpu_ensemble **out, int num_systems, const int *co
             e->sort_first[c] = (int)list.size();
             const int lo = c == 0 ? 0 : kSortClassPow2[c - 1];
             int p2 = 1;
-            for (int s = 0; s < S; ++s) {
+            for (int s = 0; s < (int)S; ++s) {
                 int q = 1;
                 while (q < counts[s]) q <<= 1;
                 if (q > lo && q <= kSortClassPow2[c]) {
