@@ -20,7 +20,7 @@ namespace gs {
 // Bits of the device status word written by kernels (never a trap).
 enum StatusBits : unsigned {
     ST_WAIT_TIMEOUT = 1u,     // an mbarrier / flag wait ran out of time
-    ST_TREE_OVERFLOW = 2u,    // node capacity exceeded (host retries larger)
+    ST_TREE_OVERFLOW = 2u,    // node capacity exceeded (GRAV_MEMORY_ERROR)
     ST_STACK_OVERFLOW = 4u,   // walk stack deeper than the octree limit
     ST_NONFINITE = 8u,        // NaN/Inf seen where the kernel checks
     ST_BAD_KEY = 16u,         // octant digit out of range while building

@@ -15,9 +15,27 @@ enum OctCtr {
     CTR_INTERNAL = 1,   // internal (expanded) nodes
     CTR_STATUS = 2,     // StatusBits
     CTR_N = 3,          // particle count (for device-count kernels)
+    CTR_SAFE_INTERNAL = 4,   // internal nodes for the kernels after the expansion:
+                             // CTR_INTERNAL, or 0 once the node capacity overflowed
     CTR_LVL = 8,        // CTR_LVL + d: first internal index of depth d (d = 0..22)
     CTR_SIZE = 40
 };
+
+#ifdef __CUDACC__
+// A build whose node capacity overflowed leaves its counters past the
+// capacity and its arrays partly written.  Every kernel after the expansion
+// reads its node counts through these, so it does no work on such a build and
+// stays inside the buffers; the status word keeps ST_TREE_OVERFLOW until the
+// host reports it.
+__device__ __forceinline__ bool tree_failed(const int *ctr)
+{
+    return (ctr[CTR_STATUS] & ST_TREE_OVERFLOW) != 0;
+}
+__device__ __forceinline__ int tree_nodes(const int *ctr)
+{
+    return tree_failed(ctr) ? 0 : ctr[CTR_NODES];
+}
+#endif
 
 struct OctreeDevice {
     int n = 0;
@@ -25,8 +43,7 @@ struct OctreeDevice {
     int leaf_max = 1;
     bool compat = true;
     bool quad = false;   // traceless quadrupoles about the centre of mass
-    DBuf t_quad;         // double[6*cap]: xx, xy, xz, yy, yz, zz
-    DBuf w_nq;           // float4[2*cap]: (xx, xy, xz, yy), (yz, zz, 0, 0)
+    DBuf w_nq;           // float4[2*cap]: (xx, xy, xz, yy), (yz, zz, 0, 0), FP32
     bool links = false;  // parent ids and particle -> leaf map
     DBuf t_parent;       // int[cap] (-1 for the root)
     DBuf leaf_of;        // int[n]: leaf id of sorted particle p
@@ -46,6 +63,7 @@ struct OctreeDevice {
     DBuf t_mass;                                                     // double[cap]
     DBuf t_com;                                                      // double[3*cap]
     DBuf in_sum;                                                     // double[4*cap]
+    DBuf in_arrive;   // int[cap]: children whose multipoles are done (bottom-up pass)
     // walk arrays (frame-centred double-float positions)
     DBuf w_na, w_nb;          // float4[cap]: (com_hi, mass), (com_lo, (cell side)^2)
     DBuf w_nc;                // int4[cap]: (first_child, num_children, first_particle, count)
@@ -70,6 +88,8 @@ struct OctreeDevice {
     }
     // Host copies: number of nodes, status word.
     ErrorStatus read_counts(cudaStream_t s, int *nodes, unsigned *status);
+    // Clears the status word once the host has reported it.
+    ErrorStatus clear_status(cudaStream_t s);
 };
 
 // Barnes-Hut walk of a built tree (k_walk.cu).  counters (2 x u64) receive

@@ -60,16 +60,17 @@ constexpr double kMinGain = 0.8;
 
 }  // namespace
 
-__global__ void k_features(int count, const int *__restrict__ pos, const int *__restrict__ sidx,
+__global__ void k_features(const int *__restrict__ ctr, int count, const int *__restrict__ pos,
+                           const int *__restrict__ sidx,
                            const int *__restrict__ leaf_of, const int *__restrict__ t_parent,
                            const int *__restrict__ t_nc, const int *__restrict__ t_fc,
                            const int *__restrict__ t_depth, const double *__restrict__ t_mass,
-                           const double *__restrict__ t_com, const double *__restrict__ t_quad,
+                           const double *__restrict__ t_com, const float4 *__restrict__ nq,
                            const double *__restrict__ frame, const double *__restrict__ x,
                            const double *__restrict__ m, float *__restrict__ feat)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= count) return;
+    if (k >= count || tree_failed(ctr)) return;
     const int s = pos ? pos[k] : k;
     const int id = sidx[s];
     const int L = leaf_of[s];
@@ -81,8 +82,10 @@ __global__ void k_features(int count, const int *__restrict__ pos, const int *__
     const double *cL = t_com + 3 * (size_t)L;
     const double *cP = t_com + 3 * (size_t)P;
     const double ML = fmax(t_mass[L], 1e-300), MP = fmax(t_mass[P], 1e-300);
-    const double *QL = t_quad + 6 * (size_t)L;
-    const double *QP = t_quad + 6 * (size_t)P;
+    const float4 qL0 = nq[2 * (size_t)L], qL1 = nq[2 * (size_t)L + 1];
+    const float4 qP0 = nq[2 * (size_t)P], qP1 = nq[2 * (size_t)P + 1];
+    const float QL[6] = {qL0.x, qL0.y, qL0.z, qL0.w, qL1.x, qL1.y};
+    const float QP[6] = {qP0.x, qP0.y, qP0.z, qP0.w, qP1.x, qP1.y};
     float f[MLP_IN];
     f[0] = (float)((x0 - cL[0]) / hL);
     f[1] = (float)((x1 - cL[1]) / hL);
@@ -310,6 +313,7 @@ class LearnedEngine final : public Engine {
         int nodes = 0;
         unsigned st = 0;
         GS_TRY(tree_.read_counts(s, &nodes, &st));
+        if (st) GS_TRY(tree_.clear_status(s));
         if (st & ST_TREE_OVERFLOW)
             return GS_RAISE(GRAV_MEMORY_ERROR, "octree node capacity (%d) exceeded", tree_.cap_nodes);
         if (st & ST_STACK_OVERFLOW)
@@ -379,9 +383,9 @@ class LearnedEngine final : public Engine {
                          const double *d_m, cudaStream_t s)
     {
         k_features<<<(count + 127) / 128, 128, 0, s>>>(
-            count, pos, tree_.sidx.as<int>(), tree_.leaf_of.as<int>(), tree_.t_parent.as<int>(),
+            tree_.ctr.as<int>(), count, pos, tree_.sidx.as<int>(), tree_.leaf_of.as<int>(), tree_.t_parent.as<int>(),
             tree_.t_nc.as<int>(), tree_.t_fc.as<int>(), tree_.t_depth.as<int>(),
-            tree_.t_mass.as<double>(), tree_.t_com.as<double>(), tree_.t_quad.as<double>(),
+            tree_.t_mass.as<double>(), tree_.t_com.as<double>(), tree_.w_nq.as<float4>(),
             tree_.frame.as<double>(), d_x, d_m, out);
         GS_CUDA(cudaGetLastError());
         return ok();

@@ -23,14 +23,16 @@
 //                  that key and an exclusive scan of their child counts gives
 //                  each one's first-child id; a node's id is then its
 //                  parent's first-child id plus its octant rank.
-//   multipoles     bottom-up, one launch per depth: an internal node adds,
-//                  child by child in octant order, the particles of leaf
-//                  children (sorted order) and the running sums of internal
-//                  children -- the reference's order (:652-735).  Leaves keep
+//   multipoles     bottom-up in one launch (arrival counters): an internal
+//                  node adds, child by child in octant order, the particles
+//                  of leaf children (sorted order) and the running sums of
+//                  internal children -- the reference's order (:652-735).  Leaves keep
 //                  mass 0 and centre of mass 0 in compat mode (the
 //                  reference's behaviour); otherwise they get their own sums.
 // Every count the kernels need is read from device memory, so a whole build
-// is graph-capturable.  Node-capacity overflow sets ST_TREE_OVERFLOW.
+// is graph-capturable.  Node-capacity overflow sets ST_TREE_OVERFLOW, which
+// stays set until the host reports it; the kernels after the expansion then do
+// no work (tree_failed / tree_nodes).
 #include "gs_octree.h"
 #include "gs_ptx.cuh"
 
@@ -167,7 +169,6 @@ __global__ void k_tree_init(int *__restrict__ ctr, int n, int *__restrict__ nd_s
     if (threadIdx.x != 0) return;
     ctr[CTR_NODES] = 1;
     ctr[CTR_INTERNAL] = 1;
-    ctr[CTR_STATUS] = 0;
     ctr[CTR_N] = n;
     ctr[CTR_LVL + 0] = 0;
     ctr[CTR_LVL + 1] = 1;
@@ -211,6 +212,7 @@ k_tree_expand(int d, int leaf_max, int cap, const uint64_t *__restrict__ keys, i
               int *__restrict__ nd_parent, int *__restrict__ nd_rank, int *__restrict__ nd_int,
               int *__restrict__ in_node, int *__restrict__ in_nchild)
 {
+    if (tree_failed(ctr)) return;   // an earlier level overflowed
     const int lo = ctr[CTR_LVL + d];
     const int hi = ctr[CTR_LVL + d + 1];
     const int cd = d + 1;
@@ -323,19 +325,24 @@ k_tree_expand(int d, int leaf_max, int cap, const uint64_t *__restrict__ keys, i
 
 __global__ void k_tree_mark(int d, int *__restrict__ ctr)
 {
-    if (threadIdx.x == 0) ctr[CTR_LVL + d + 2] = ctr[CTR_INTERNAL];
+    if (threadIdx.x == 0) {
+        ctr[CTR_LVL + d + 2] = ctr[CTR_INTERNAL];
+        ctr[CTR_SAFE_INTERNAL] = tree_failed(ctr) ? 0 : ctr[CTR_INTERNAL];
+    }
 }
 
 // Sort key of an internal node: pre-order = (first particle, depth).
 __global__ void k_internal_keys(const int *__restrict__ ctr, const int *__restrict__ in_node,
                                 const int *__restrict__ nd_start, const int *__restrict__ nd_depth,
-                                uint64_t *__restrict__ in_key, int *__restrict__ in_order)
+                                uint64_t *__restrict__ in_key, int *__restrict__ in_order,
+                                int *__restrict__ in_arrive)
 {
-    const int ni = ctr[CTR_INTERNAL];
+    const int ni = ctr[CTR_SAFE_INTERNAL];
     for (int ii = blockIdx.x * blockDim.x + threadIdx.x; ii < ni; ii += gridDim.x * blockDim.x) {
         const int q = in_node[ii];
         in_key[ii] = ((uint64_t)nd_start[q] << 5) | (uint64_t)nd_depth[q];
         in_order[ii] = ii;
+        in_arrive[ii] = 0;
     }
 }
 
@@ -345,7 +352,7 @@ k_fc_tile_sums(const int *__restrict__ ctr, const int *__restrict__ in_order,
                const int *__restrict__ in_nchild, unsigned *__restrict__ tile_sum)
 {
     __shared__ unsigned red[OT_THREADS];
-    const int ni = ctr[CTR_INTERNAL];
+    const int ni = ctr[CTR_SAFE_INTERNAL];
     const int base = blockIdx.x * SCAN_TILE;
     unsigned s = 0;
     for (int k = threadIdx.x; k < SCAN_TILE; k += OT_THREADS) {
@@ -393,7 +400,7 @@ k_fc_apply(const int *__restrict__ ctr, const int *__restrict__ in_order,
 {
     constexpr int PER = SCAN_TILE / OT_THREADS;   // 16 consecutive per thread
     __shared__ unsigned part[OT_THREADS];
-    const int ni = ctr[CTR_INTERNAL];
+    const int ni = ctr[CTR_SAFE_INTERNAL];
     const int base = blockIdx.x * SCAN_TILE + threadIdx.x * PER;
     unsigned v[PER];
     unsigned s = 0;
@@ -430,7 +437,7 @@ __global__ void k_tree_number(const int *__restrict__ ctr, int compat,
                               int *__restrict__ t_int, double *__restrict__ t_mass,
                               double *__restrict__ t_com)
 {
-    const int nn = min(ctr[CTR_NODES], 0x7fffffff);
+    const int nn = tree_nodes(ctr);
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nn; q += gridDim.x * blockDim.x) {
         const int id = (q == 0) ? 0 : in_fc[nd_parent[q]] + nd_rank[q];
         t_np[id] = nd_count[q];
@@ -463,7 +470,7 @@ __global__ void k_tree_links(const int *__restrict__ ctr, const int *__restrict_
                              const int *__restrict__ in_node, const int *__restrict__ in_fc,
                              int *__restrict__ t_parent, int *__restrict__ leaf_of)
 {
-    const int nn = ctr[CTR_NODES];
+    const int nn = tree_nodes(ctr);
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nn; q += gridDim.x * blockDim.x) {
         int id = 0, parent = -1;
         if (q != 0) {
@@ -493,122 +500,197 @@ __device__ __forceinline__ void add_particles(const double *__restrict__ x,
     }
 }
 
-// Internal nodes of depth d (reference :652-735).  When q is not null, also
-// their quadrupoles from the children's by the parallel-axis shift:
-// Q = sum_c [Q_c + M_c (3 s s^T - |s|^2 I)], s = com_c - com.
-__global__ void k_multipole_level(int d, const int *__restrict__ ctr, const double *__restrict__ x,
-                                  const double *__restrict__ m, const int *__restrict__ sidx,
-                                  const int *__restrict__ in_id, const int *__restrict__ in_fc,
-                                  const int *__restrict__ in_nchild, const int *__restrict__ t_np,
-                                  const int *__restrict__ t_nc, const int *__restrict__ t_fp,
-                                  const int *__restrict__ t_int, double *__restrict__ in_sum,
-                                  double *__restrict__ t_mass, double *__restrict__ t_com,
-                                  double *__restrict__ q)
-{
-    const int lo = ctr[CTR_LVL + d];
-    const int hi = ctr[CTR_LVL + d + 1];
-    for (int ii = lo + blockIdx.x * blockDim.x + threadIdx.x; ii < hi;
-         ii += gridDim.x * blockDim.x) {
-        double M = 0.0, S0 = 0.0, S1 = 0.0, S2 = 0.0;
-        const int fc = in_fc[ii];
-        const int nch = in_nchild[ii];
-        for (int c = fc; c < fc + nch; ++c) {
-            if (t_nc[c] > 0) {
-                const double *cs = in_sum + 4 * (size_t)t_int[c];
-                M = __dadd_rn(M, cs[0]);
-                S0 = __dadd_rn(S0, cs[1]);
-                S1 = __dadd_rn(S1, cs[2]);
-                S2 = __dadd_rn(S2, cs[3]);
-            } else {
-                add_particles(x, m, sidx, t_fp[c], t_np[c], M, S0, S1, S2);
-            }
-        }
-        double *ws = in_sum + 4 * (size_t)ii;
-        ws[0] = M;
-        ws[1] = S0;
-        ws[2] = S1;
-        ws[3] = S2;
-        const int id = in_id[ii];
-        const double c0 = __ddiv_rn(S0, M), c1 = __ddiv_rn(S1, M), c2 = __ddiv_rn(S2, M);
-        t_mass[id] = M;
-        t_com[3 * id + 0] = c0;
-        t_com[3 * id + 1] = c1;
-        t_com[3 * id + 2] = c2;
-        if (q) {
-            double Q[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-            for (int c = fc; c < fc + nch; ++c) {
-                const double Mc = t_mass[c];
-                const double s0 = t_com[3 * c] - c0, s1 = t_com[3 * c + 1] - c1,
-                             s2 = t_com[3 * c + 2] - c2;
-                const double r2 = s0 * s0 + s1 * s1 + s2 * s2;
-                const double *qc = q + 6 * (size_t)c;
-                Q[0] += qc[0] + Mc * (3.0 * s0 * s0 - r2);
-                Q[1] += qc[1] + Mc * 3.0 * s0 * s1;
-                Q[2] += qc[2] + Mc * 3.0 * s0 * s2;
-                Q[3] += qc[3] + Mc * (3.0 * s1 * s1 - r2);
-                Q[4] += qc[4] + Mc * 3.0 * s1 * s2;
-                Q[5] += qc[5] + Mc * (3.0 * s2 * s2 - r2);
-            }
-            for (int k = 0; k < 6; ++k) q[6 * (size_t)id + k] = Q[k];
-        }
-    }
-}
-
-// Leaves with their own mass and centre of mass (non-compat trees), and,
-// when q is not null, their quadrupole sum_p m (3 d d^T - |d|^2 I) about it.
-__global__ void k_leaf_multipoles(const int *__restrict__ ctr, const double *__restrict__ x,
-                                  const double *__restrict__ m, const int *__restrict__ sidx,
-                                  const int *__restrict__ t_np, const int *__restrict__ t_nc,
-                                  const int *__restrict__ t_fp, double *__restrict__ t_mass,
-                                  double *__restrict__ t_com, double *__restrict__ q)
-{
-    const int nn = ctr[CTR_NODES];
-    for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < nn; id += gridDim.x * blockDim.x) {
-        if (t_nc[id] > 0) continue;
-        double M = 0.0, S0 = 0.0, S1 = 0.0, S2 = 0.0;
-        add_particles(x, m, sidx, t_fp[id], t_np[id], M, S0, S1, S2);
-        const double c0 = __ddiv_rn(S0, M), c1 = __ddiv_rn(S1, M), c2 = __ddiv_rn(S2, M);
-        t_mass[id] = M;
-        t_com[3 * id + 0] = c0;
-        t_com[3 * id + 1] = c1;
-        t_com[3 * id + 2] = c2;
-        if (q) {
-            double Q[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-            for (int p = t_fp[id]; p < t_fp[id] + t_np[id]; ++p) {
-                const int pid = sidx[p];
-                const double mp = m[pid];
-                const double d0 = x[3 * pid] - c0, d1 = x[3 * pid + 1] - c1, d2 = x[3 * pid + 2] - c2;
-                const double r2 = d0 * d0 + d1 * d1 + d2 * d2;
-                Q[0] += mp * (3.0 * d0 * d0 - r2);
-                Q[1] += mp * 3.0 * d0 * d1;
-                Q[2] += mp * 3.0 * d0 * d2;
-                Q[3] += mp * (3.0 * d1 * d1 - r2);
-                Q[4] += mp * 3.0 * d1 * d2;
-                Q[5] += mp * (3.0 * d2 * d2 - r2);
-            }
-            for (int k = 0; k < 6; ++k) q[6 * (size_t)id + k] = Q[k];
-        }
-    }
-}
-
-__global__ void k_walk_quads(const int *__restrict__ ctr, const double *__restrict__ q,
-                             float4 *__restrict__ nq)
-{
-    const int nn = ctr[CTR_NODES];
-    for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < nn; id += gridDim.x * blockDim.x) {
-        const double *Q = q + 6 * (size_t)id;
-        nq[2 * (size_t)id] = make_float4((float)Q[0], (float)Q[1], (float)Q[2], (float)Q[3]);
-        nq[2 * (size_t)id + 1] = make_float4((float)Q[4], (float)Q[5], 0.0f, 0.0f);
-    }
-}
-
 __device__ __forceinline__ void split_df(double v, float &hi, float &lo)
 {
     hi = __double2float_rn(v);
     lo = __double2float_rn(__dsub_rn(v, (double)hi));
 }
 
-// Frame-centred double-float copies for the FP32 walk.
+// (cell side)^2 at depth d, box_length / (2 << d), for the group walk's
+// opening test.  The divisor is a power of two, so the product with its
+// exact reciprocal (built from the exponent bits) equals the quotient.
+__device__ __forceinline__ float cell_side2(const double *__restrict__ frame, int depth)
+{
+    const int e = min(depth, OCT_MAX_LEVEL + 1) + 1;
+    const double side = __dmul_rn(frame[4], __longlong_as_double((long long)(1023 - e) << 52));
+    return (float)(side * side);
+}
+
+// Walk record of a node: centre of mass relative to the frame centre as
+// (hi, lo) FP32 pairs, FP32 mass, (cell side)^2.  The same arithmetic for
+// every node, whichever kernel computes its multipoles.
+__device__ __forceinline__ void write_node_record(int id, double M, double c0, double c1, double c2,
+                                                  int depth, const double *__restrict__ frame,
+                                                  float4 *na, float4 *nb, float h[3], float l[3])
+{
+    split_df(__dsub_rn(c0, frame[0]), h[0], l[0]);
+    split_df(__dsub_rn(c1, frame[1]), h[1], l[1]);
+    split_df(__dsub_rn(c2, frame[2]), h[2], l[2]);
+    na[id] = make_float4(h[0], h[1], h[2], (float)M);
+    nb[id] = make_float4(l[0], l[1], l[2], cell_side2(frame, depth));
+}
+
+// m (3 d d^T - |d|^2 I) added to the packed quadrupole (xx, xy, xz, yy, yz, zz).
+__device__ __forceinline__ void add_quad(float Q[6], float mp, float d0, float d1, float d2)
+{
+    const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
+    const float m3 = 3.0f * mp;
+    Q[0] += mp * (3.0f * d0 * d0 - r2);
+    Q[1] += m3 * d0 * d1;
+    Q[2] += m3 * d0 * d2;
+    Q[3] += mp * (3.0f * d1 * d1 - r2);
+    Q[4] += m3 * d1 * d2;
+    Q[5] += mp * (3.0f * d2 * d2 - r2);
+}
+
+__device__ __forceinline__ void store_quad(float4 *nq, int id, const float Q[6])
+{
+    nq[2 * (size_t)id] = make_float4(Q[0], Q[1], Q[2], Q[3]);
+    nq[2 * (size_t)id + 1] = make_float4(Q[4], Q[5], 0.0f, 0.0f);
+}
+
+// Offset of a (hi, lo) FP32 pair point from a (hi, lo) centre, in FP32:
+// the hi parts of points in one cell are close, so their difference is
+// exact, and the lo parts carry the rest.
+__device__ __forceinline__ float df_offset(float ph, float pl, float ch, float cl)
+{
+    return (ph - ch) + (pl - cl);
+}
+
+struct MultipoleArgs {
+    const double *x, *m;
+    const int *sidx, *in_node, *nd_parent, *in_id, *in_fc, *in_nchild;
+    const int *t_np, *t_nc, *t_fp, *t_int, *t_depth;
+    const double *frame;
+    int *in_arrive;
+    double *in_sum, *t_mass, *t_com;
+    float4 *na, *nb, *nq;   // nq null: no quadrupoles
+};
+
+// Multipoles of internal node ii from its children (reference :652-735): mass
+// and the mass-weighted coordinate sums in child order, the centre of mass by
+// division, its walk record, and, when nq is not null, the quadrupole from the
+// children's by the parallel-axis shift Q = sum_c [Q_c + M_c (3 s s^T - |s|^2 I)],
+// s = com_c - com, in FP32 from the children's walk records (FP64 runs at 1/64
+// of the FP32 rate here, and the walk uses FP32 quadrupoles).  Children's
+// values written by other threads of the same launch are read through L2
+// (__ldcg), after the fence that follows the arrival counter.
+__device__ void multipole_node(int ii, const MultipoleArgs &A)
+{
+    double M = 0.0, S0 = 0.0, S1 = 0.0, S2 = 0.0;
+    const int fc = A.in_fc[ii];
+    const int nch = A.in_nchild[ii];
+    for (int c = fc; c < fc + nch; ++c) {
+        if (A.t_nc[c] > 0) {
+            const double *cs = A.in_sum + 4 * (size_t)A.t_int[c];
+            M = __dadd_rn(M, __ldcg(cs + 0));
+            S0 = __dadd_rn(S0, __ldcg(cs + 1));
+            S1 = __dadd_rn(S1, __ldcg(cs + 2));
+            S2 = __dadd_rn(S2, __ldcg(cs + 3));
+        } else {
+            add_particles(A.x, A.m, A.sidx, A.t_fp[c], A.t_np[c], M, S0, S1, S2);
+        }
+    }
+    double *ws = A.in_sum + 4 * (size_t)ii;
+    ws[0] = M;
+    ws[1] = S0;
+    ws[2] = S1;
+    ws[3] = S2;
+    const int id = A.in_id[ii];
+    const double c0 = __ddiv_rn(S0, M), c1 = __ddiv_rn(S1, M), c2 = __ddiv_rn(S2, M);
+    A.t_mass[id] = M;
+    A.t_com[3 * id + 0] = c0;
+    A.t_com[3 * id + 1] = c1;
+    A.t_com[3 * id + 2] = c2;
+    float h[3], l[3];
+    write_node_record(id, M, c0, c1, c2, A.t_depth[id], A.frame, A.na, A.nb, h, l);
+    if (A.nq) {
+        float Q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        for (int c = fc; c < fc + nch; ++c) {
+            const float4 ca = __ldcg(A.na + c), cb = __ldcg(A.nb + c);
+            const float4 qa = __ldcg(A.nq + 2 * (size_t)c), qb = __ldcg(A.nq + 2 * (size_t)c + 1);
+            add_quad(Q, ca.w, df_offset(ca.x, cb.x, h[0], l[0]), df_offset(ca.y, cb.y, h[1], l[1]),
+                     df_offset(ca.z, cb.z, h[2], l[2]));
+            Q[0] += qa.x;
+            Q[1] += qa.y;
+            Q[2] += qa.z;
+            Q[3] += qa.w;
+            Q[4] += qb.x;
+            Q[5] += qb.y;
+        }
+        store_quad(A.nq, id, Q);
+    }
+}
+
+// All internal nodes in one launch, bottom-up.  A thread starts at each
+// internal node none of whose children is internal, computes it, and climbs:
+// it counts itself in the parent's arrival counter, and the thread that
+// completes the count (the last of the parent's internal children to finish)
+// computes the parent.  Nothing waits: a thread that is not last stops.  Every
+// node is computed once, by the same arithmetic in the same child order as a
+// level-by-level pass, so the sums are identical to it.
+__global__ void __launch_bounds__(OT_THREADS) k_multipole_up(const int *__restrict__ ctr,
+                                                             MultipoleArgs A)
+{
+    const int ni = ctr[CTR_SAFE_INTERNAL];
+    for (int i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < ni; i0 += gridDim.x * blockDim.x) {
+        const int fc0 = A.in_fc[i0];
+        const int nch0 = A.in_nchild[i0];
+        bool bottom = true;
+        for (int c = fc0; c < fc0 + nch0; ++c) bottom = bottom && A.t_nc[c] == 0;
+        if (!bottom) continue;
+        int ii = i0;
+        for (;;) {
+            multipole_node(ii, A);
+            const int p = A.nd_parent[A.in_node[ii]];
+            if (p < 0) break;
+            const int fc = A.in_fc[p];
+            const int nch = A.in_nchild[p];
+            int internal = 0;
+            for (int c = fc; c < fc + nch; ++c) internal += A.t_nc[c] > 0 ? 1 : 0;
+            __threadfence();
+            if (atomicAdd(&A.in_arrive[p], 1) != internal - 1) break;
+            __threadfence();
+            ii = p;
+        }
+    }
+}
+
+// Leaves with their own mass and centre of mass (non-compat trees), their walk
+// records, and, when nq is not null, their quadrupole sum_p m (3 d d^T - |d|^2 I)
+// about the centre of mass, from the particles' (hi, lo) FP32 pairs.
+__global__ void k_leaf_multipoles(const int *__restrict__ ctr, MultipoleArgs A,
+                                  const float4 *__restrict__ pa, const float4 *__restrict__ pb)
+{
+    const int nn = tree_nodes(ctr);
+    for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < nn; id += gridDim.x * blockDim.x) {
+        if (A.t_nc[id] > 0) continue;
+        const int fp = A.t_fp[id], np = A.t_np[id];
+        double M = 0.0, S0 = 0.0, S1 = 0.0, S2 = 0.0;
+        add_particles(A.x, A.m, A.sidx, fp, np, M, S0, S1, S2);
+        const double c0 = __ddiv_rn(S0, M), c1 = __ddiv_rn(S1, M), c2 = __ddiv_rn(S2, M);
+        A.t_mass[id] = M;
+        A.t_com[3 * id + 0] = c0;
+        A.t_com[3 * id + 1] = c1;
+        A.t_com[3 * id + 2] = c2;
+        float h[3], l[3];
+        write_node_record(id, M, c0, c1, c2, A.t_depth[id], A.frame, A.na, A.nb, h, l);
+        if (A.nq) {
+            float Q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            for (int p = fp; p < fp + np; ++p) {
+                const float4 a = pa[p], b = pb[p];
+                add_quad(Q, a.w, df_offset(a.x, b.x, h[0], l[0]), df_offset(a.y, b.y, h[1], l[1]),
+                         df_offset(a.z, b.z, h[2], l[2]));
+            }
+            store_quad(A.nq, id, Q);
+        }
+    }
+}
+
+// Walk arrays of every node: (first child, children, first particle,
+// particles), the membership key, and the records of the nodes whose
+// multipoles the kernels above did not compute -- the zero-mass leaves of a
+// compat tree.
 __global__ void k_walk_nodes(const int *__restrict__ ctr, int compat, const double *__restrict__ frame,
                              const uint64_t *__restrict__ keys, const int *__restrict__ sidx,
                              const int *__restrict__ t_np, const int *__restrict__ t_nc,
@@ -618,18 +700,13 @@ __global__ void k_walk_nodes(const int *__restrict__ ctr, int compat, const doub
                              float4 *__restrict__ na, float4 *__restrict__ nb, int4 *__restrict__ nc,
                              uint64_t *__restrict__ nkey)
 {
-    const int nn = ctr[CTR_NODES];
-    const double c0 = frame[0], c1 = frame[1], c2 = frame[2];
+    const int nn = tree_nodes(ctr);
     for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < nn; id += gridDim.x * blockDim.x) {
-        float h0, l0, h1, l1, h2, l2;
-        split_df(__dsub_rn(t_com[3 * id + 0], c0), h0, l0);
-        split_df(__dsub_rn(t_com[3 * id + 1], c1), h1, l1);
-        split_df(__dsub_rn(t_com[3 * id + 2], c2), h2, l2);
-        na[id] = make_float4(h0, h1, h2, (float)t_mass[id]);
-        // (cell side)^2 of the node's depth, box_length / (2 << d), for the
-        // opening test of the group walk
-        const double side = frame[4] / (double)(2 << min(t_depth[id], OCT_MAX_LEVEL + 1));
-        nb[id] = make_float4(l0, l1, l2, (float)(side * side));
+        if (compat && t_nc[id] == 0) {
+            float h[3], l[3];
+            write_node_record(id, t_mass[id], t_com[3 * id], t_com[3 * id + 1], t_com[3 * id + 2],
+                              t_depth[id], frame, na, nb, h, l);
+        }
         const int fp = t_fp[id];
         nc[id] = make_int4(t_fc[id], t_nc[id], fp, t_np[id]);
         // the reference's membership test reads keys[sorted_indices[first]]
@@ -665,6 +742,7 @@ ErrorStatus OctreeDevice::setup(int n_, int leaf_max_, bool compat_, bool quad_)
     cap_nodes = cap;
     const size_t ci = (size_t)cap * sizeof(int);
     GS_TRY(ctr.reserve(CTR_SIZE * sizeof(int)));
+    GS_CUDA(cudaMemset(ctr.p, 0, CTR_SIZE * sizeof(int)));   // status word starts clear
     GS_TRY(frame.reserve(8 * sizeof(double)));
     GS_TRY(bbox_part.reserve((size_t)BBOX_BLOCKS * 6 * sizeof(double)));
     GS_TRY(keys.reserve((size_t)n * sizeof(uint64_t)));
@@ -678,6 +756,7 @@ ErrorStatus OctreeDevice::setup(int n_, int leaf_max_, bool compat_, bool quad_)
     GS_TRY(t_mass.reserve((size_t)cap * sizeof(double)));
     GS_TRY(t_com.reserve((size_t)cap * 3 * sizeof(double)));
     GS_TRY(in_sum.reserve((size_t)cap * 4 * sizeof(double)));
+    GS_TRY(in_arrive.reserve(ci));
     GS_TRY(w_na.reserve((size_t)cap * sizeof(float4)));
     GS_TRY(w_nb.reserve((size_t)cap * sizeof(float4)));
     GS_TRY(w_nc.reserve((size_t)cap * sizeof(int4)));
@@ -686,10 +765,7 @@ ErrorStatus OctreeDevice::setup(int n_, int leaf_max_, bool compat_, bool quad_)
     GS_TRY(w_pb.reserve((size_t)n * sizeof(float4)));
     GS_TRY(g_list.reserve((size_t)n * sizeof(int2)));
     GS_TRY(g_ctr.reserve(4 * sizeof(int)));
-    if (quad) {
-        GS_TRY(t_quad.reserve((size_t)cap * 6 * sizeof(double)));
-        GS_TRY(w_nq.reserve((size_t)cap * 2 * sizeof(float4)));
-    }
+    if (quad) GS_TRY(w_nq.reserve((size_t)cap * 2 * sizeof(float4)));
     if (links) {
         GS_TRY(t_parent.reserve((size_t)cap * sizeof(int)));
         GS_TRY(leaf_of.reserve((size_t)n * sizeof(int)));
@@ -701,11 +777,11 @@ ErrorStatus OctreeDevice::setup(int n_, int leaf_max_, bool compat_, bool quad_)
 int OctreeDevice::launches_per_build() const
 {
     // bbox 2, morton 1, sort, init 1, levels 2*21, keys 1, sort, fc 3,
-    // number 1, multipoles 21 (+1 leaves; quadrupoles in the same launches),
-    // walk arrays 2 (+1 quadrupole copy)
+    // number 1, multipoles 1 (+1 leaves; quadrupoles in the same launches),
+    // walk arrays 2
     return 2 + 1 + RadixSorter::launches(63) + 1 + 42 + 1 +
            RadixSorter::launches(internal_key_bits()) + 3 + 1 +
-           21 + (compat ? 0 : 1) + 2 + (quad ? 1 : 0) + (links ? 1 : 0);
+           1 + (compat ? 0 : 1) + 2 + (links ? 1 : 0);
 }
 
 ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream_t s,
@@ -739,8 +815,8 @@ ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream
     GS_CUDA(cudaGetLastError());
     k_internal_keys<<<grid, OT_THREADS, 0, s>>>(ctr.as<int>(), in_node.as<int>(), nd_start.as<int>(),
                                                 nd_depth.as<int>(), in_key.as<uint64_t>(),
-                                                in_order.as<int>());
-    GS_TRY(sorter.sort(in_key.as<uint64_t>(), in_order.as<int>(), ctr.as<int>() + CTR_INTERNAL,
+                                                in_order.as<int>(), in_arrive.as<int>());
+    GS_TRY(sorter.sort(in_key.as<uint64_t>(), in_order.as<int>(), ctr.as<int>() + CTR_SAFE_INTERNAL,
                        internal_key_bits(), s));
     const int tiles = (cap_nodes + SCAN_TILE - 1) / SCAN_TILE;
     k_fc_tile_sums<<<tiles, OT_THREADS, 0, s>>>(ctr.as<int>(), in_order.as<int>(),
@@ -761,28 +837,40 @@ ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream
                                                  nd_rank.as<int>(), nd_int.as<int>(),
                                                  in_node.as<int>(), in_fc.as<int>(),
                                                  t_parent.as<int>(), leaf_of.as<int>());
+    MultipoleArgs A;
+    A.x = d_x;
+    A.m = d_m;
+    A.sidx = sidx.as<int>();
+    A.in_node = in_node.as<int>();
+    A.nd_parent = nd_parent.as<int>();
+    A.in_id = in_id.as<int>();
+    A.in_fc = in_fc.as<int>();
+    A.in_nchild = in_nchild.as<int>();
+    A.t_np = t_np.as<int>();
+    A.t_nc = t_nc.as<int>();
+    A.t_fp = t_fp.as<int>();
+    A.t_int = t_int.as<int>();
+    A.t_depth = t_depth.as<int>();
+    A.frame = frame.as<double>();
+    A.in_arrive = in_arrive.as<int>();
+    A.in_sum = in_sum.as<double>();
+    A.t_mass = t_mass.as<double>();
+    A.t_com = t_com.as<double>();
+    A.na = w_na.as<float4>();
+    A.nb = w_nb.as<float4>();
+    A.nq = quad ? w_nq.as<float4>() : nullptr;
+    // particle records first: the leaves' quadrupoles are formed from them
+    k_walk_particles<<<pb, OT_THREADS, 0, s>>>(n, frame.as<double>(), d_x, d_m, sidx.as<int>(),
+                                               w_pa.as<float4>(), w_pb.as<float4>());
     if (!compat)
-        k_leaf_multipoles<<<grid, OT_THREADS, 0, s>>>(
-            ctr.as<int>(), d_x, d_m, sidx.as<int>(), t_np.as<int>(), t_nc.as<int>(),
-            t_fp.as<int>(), t_mass.as<double>(), t_com.as<double>(),
-            quad ? t_quad.as<double>() : nullptr);
-    for (int d = OCT_MAX_LEVEL - 1; d >= 0; --d) {
-        k_multipole_level<<<grid, OT_THREADS, 0, s>>>(
-            d, ctr.as<int>(), d_x, d_m, sidx.as<int>(), in_id.as<int>(), in_fc.as<int>(),
-            in_nchild.as<int>(), t_np.as<int>(), t_nc.as<int>(), t_fp.as<int>(), t_int.as<int>(),
-            in_sum.as<double>(), t_mass.as<double>(), t_com.as<double>(),
-            quad ? t_quad.as<double>() : nullptr);
-    }
-    if (quad)
-        k_walk_quads<<<grid, OT_THREADS, 0, s>>>(ctr.as<int>(), t_quad.as<double>(),
-                                                 w_nq.as<float4>());
+        k_leaf_multipoles<<<grid, OT_THREADS, 0, s>>>(ctr.as<int>(), A, w_pa.as<float4>(),
+                                                      w_pb.as<float4>());
+    k_multipole_up<<<grid, OT_THREADS, 0, s>>>(ctr.as<int>(), A);
     k_walk_nodes<<<grid, OT_THREADS, 0, s>>>(
         ctr.as<int>(), compat ? 1 : 0, frame.as<double>(), keys.as<uint64_t>(), sidx.as<int>(),
         t_np.as<int>(), t_nc.as<int>(), t_fp.as<int>(), t_fc.as<int>(), t_depth.as<int>(),
         t_mass.as<double>(), t_com.as<double>(), w_na.as<float4>(), w_nb.as<float4>(),
         w_nc.as<int4>(), w_nkey.as<uint64_t>());
-    k_walk_particles<<<pb, OT_THREADS, 0, s>>>(n, frame.as<double>(), d_x, d_m, sidx.as<int>(),
-                                               w_pa.as<float4>(), w_pb.as<float4>());
     GS_CUDA(cudaGetLastError());
     return ok();
 }
@@ -794,6 +882,13 @@ ErrorStatus OctreeDevice::read_counts(cudaStream_t s, int *nodes, unsigned *stat
     GS_CUDA(cudaStreamSynchronize(s));
     if (nodes) *nodes = h[CTR_NODES];
     if (status) *status = (unsigned)h[CTR_STATUS];
+    return ok();
+}
+
+ErrorStatus OctreeDevice::clear_status(cudaStream_t s)
+{
+    GS_CUDA(cudaMemsetAsync(ctr.as<int>() + CTR_STATUS, 0, sizeof(int), s));
+    GS_CUDA(cudaStreamSynchronize(s));
     return ok();
 }
 

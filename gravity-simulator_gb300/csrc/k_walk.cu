@@ -78,6 +78,7 @@ k_bh_walk(WalkArgs A)
     __shared__ double s_w[WK_STACK];     // cell width at depth, FP64 (reference formula)
 
     if (A.gate && *A.gate == 0) return;   // block-uniform
+    if (*A.status & ST_TREE_OVERFLOW) return;   // the build overflowed: no tree to walk
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     if (threadIdx.x < WK_STACK) {
@@ -320,6 +321,7 @@ class BarnesHutEngine final : public Engine {
         int nodes = 0;
         unsigned st = 0;
         GS_TRY(tree_.read_counts(s, &nodes, &st));
+        if (st) GS_TRY(tree_.clear_status(s));
         if (st & ST_TREE_OVERFLOW)
             return GS_RAISE(GRAV_MEMORY_ERROR, "octree node capacity (%d) exceeded", tree_.cap_nodes);
         if (st & ST_STACK_OVERFLOW)

@@ -89,7 +89,7 @@ __global__ void k_group_list(const int *__restrict__ ctr, const int4 *__restrict
                              int2 *__restrict__ groups, int *__restrict__ gctr)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ctr[CTR_NODES]) return;
+    if (c >= tree_nodes(ctr)) return;   // no groups from an overflowed build
     const double bl = frame[4];
     const int4 ci = nc[c];   // (first child, children, first particle, particles)
     if (ci.w <= 0) return;

@@ -215,6 +215,43 @@ def test_group_walk_degenerate_and_unsoftened(lib, g, orc, wl):
     assert np.median(orc.rel_err(a2[rows2], exact2)) < 2e-3
 
 
+@pytest.mark.parametrize("method", [3, 13, 5, 6])
+def test_node_capacity_overflow(lib, g, orc, wl, method):
+    """2,048 coincident pairs with one particle per leaf: each pair splits
+    down to the depth limit, 36,951 nodes (the oracle's count) against a
+    capacity of 4N + 4096 = 20,480.  The build stops at the capacity, the
+    kernels after it do no work, and the call reports GRAV_MEMORY_ERROR;
+    the same engine then serves a normal input."""
+    rng = np.random.default_rng(6)
+    x = np.repeat(rng.random((2048, 3)), 2, axis=0)
+    m = np.full(4096, 1.0 / 4096)
+    assert orc.build_tree(x, m, 1, False)["num_nodes"] > 4 * 4096 + 4096
+    gpu = method + 100
+    with pytest.raises(g.GravError) as e:
+        g.acceleration(lib, x, m, 1.0, gpu, opening_angle=0.5, softening_length=0.01,
+                       max_num_particles_per_leaf=1)
+    assert e.value.code == g.GRAV_MEMORY_ERROR
+    if method == 3:
+        system, keep = g.make_system(x, m, 1.0)
+        t = g.LinearOctree()
+        p = g.AccelerationParam(3, 1.0, 0.0, 1)
+        st = lib.construct_octree(ctypes.byref(t), ctypes.byref(system), ctypes.byref(p),
+                                  None, -1.0)
+        assert st.return_code == g.GRAV_MEMORY_ERROR
+        g.take_traceback(lib, st)
+    x2, _, m2 = wl.plummer(4096, 3)
+    a = g.acceleration(lib, x2, m2, 1.0, gpu, opening_angle=0.5, softening_length=0.01,
+                       max_num_particles_per_leaf=1)
+    assert np.isfinite(a).all()
+    if method in (3, 13):   # the oracle's walk, term for term
+        a_o, cnt, mag = orc.bh_counts(x2, m2, 1.0, 0.01, 0.5, 1, method == 13)
+        check_terms(a, a_o, mag)
+    else:
+        rows = np.arange(0, 4096, 16, dtype=np.int32)
+        err = orc.rel_err(a[rows], orc.direct_rows(x2, m2, 1.0, 0.01, rows))
+        assert np.median(err) < 5e-3
+
+
 def test_group_walk_in_simulation(lib, g, wl):
     """The group walk drives launch_simulation (graph-captured leapfrog)."""
     x, v, m = wl.galaxy_pair(32768, 8)
