@@ -26,9 +26,11 @@
 //   multipoles     bottom-up in one launch (arrival counters): an internal
 //                  node adds, child by child in octant order, the particles
 //                  of leaf children (sorted order) and the running sums of
-//                  internal children -- the reference's order (:652-735).  Leaves keep
-//                  mass 0 and centre of mass 0 in compat mode (the
-//                  reference's behaviour); otherwise they get their own sums.
+//                  internal children -- the reference's order (:652-735).
+//                  Leaves keep mass 0 and centre of mass 0 in compat mode
+//                  (the reference's behaviour); otherwise they get their own
+//                  sums.  The same kernels write the walk's node records and,
+//                  for the quadrupole walks, FP32 quadrupoles.
 // Every count the kernels need is read from device memory, so a whole build
 // is graph-capturable.  Node-capacity overflow sets ST_TREE_OVERFLOW, which
 // stays set until the host reports it; the kernels after the expansion then do
