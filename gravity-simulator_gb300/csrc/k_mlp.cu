@@ -24,6 +24,7 @@
 
 #include <cuda_bf16.h>
 
+#include <atomic>
 #include <cmath>
 #include <random>
 #include <vector>
@@ -499,11 +500,12 @@ ErrorStatus MlpDevice::forward(const float *feat, int n, float *pred, cudaStream
     if (n <= 0) return ok();
     const DeviceInfo *dev = nullptr;
     GS_TRY(device_info(&dev));
-    static bool attr = false;
-    if (!attr) {
+    // set once per process; a concurrent first call repeats the same setting
+    static std::atomic<bool> attr{false};
+    if (!attr.load(std::memory_order_acquire)) {
         GS_CUDA(cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)SM_FWD_END));
-        attr = true;
+        attr.store(true, std::memory_order_release);
     }
     const int tiles = (n + MLP_TILE - 1) / MLP_TILE;
     const int grid = std::min(tiles, dev->sm_count * 2);
@@ -518,11 +520,12 @@ ErrorStatus MlpDevice::gradients(const float *feat, const float *target, int n, 
     if (n <= 0) return ok();
     const DeviceInfo *dev = nullptr;
     GS_TRY(device_info(&dev));
-    static bool attr = false;
-    if (!attr) {
+    // set once per process; a concurrent first call repeats the same setting
+    static std::atomic<bool> attr{false};
+    if (!attr.load(std::memory_order_acquire)) {
         GS_CUDA(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)SM_TRAIN_END));
-        attr = true;
+        attr.store(true, std::memory_order_release);
     }
     const int tiles = (n + MLP_TILE - 1) / MLP_TILE;
     const int grid = std::min(tiles, dev->sm_count);
