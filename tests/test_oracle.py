@@ -157,6 +157,26 @@ def test_fixed_mode_tree_is_more_accurate(orc, wl):
     assert e_fix < 5e-3 < e_ref
 
 
+def test_octree_node_capacity_margin(orc, wl):
+    """The GPU octree holds 4N + 4096 nodes.  The bench's distributions
+    need about 1.5 N nodes with one particle per leaf and 0.43 N with eight.
+    2,048 coincident pairs need about 9 N: each pair splits down to the depth
+    limit.  The GPU answers that input with GRAV_MEMORY_ERROR
+    (tests/test_gpu_barnes_hut.py::test_node_capacity_overflow)."""
+    n = 65536
+    for gen in (wl.plummer, wl.galaxy_pair):
+        x, v, m = gen(n, 3)
+        assert orc.build_tree(x, m, 1, False)["num_nodes"] < 1.6 * n
+        assert orc.build_tree(x, m, 8, False)["num_nodes"] < 0.5 * n
+    rng = np.random.default_rng(6)
+    x = np.repeat(rng.random((2048, 3)), 2, axis=0)
+    m = np.full(4096, 1.0 / 4096)
+    nodes = orc.build_tree(x, m, 1, False)["num_nodes"]
+    assert nodes > 4 * 4096 + 4096 and nodes > 8 * 4096
+    # eight or more per leaf: a coincident pair stays in one leaf
+    assert orc.build_tree(x, m, 8, False)["num_nodes"] < 4096
+
+
 def _snapshot_rows(ids, m, x, v, fm, fx, fv):
     rows = []
     for i in range(len(m)):
