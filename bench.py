@@ -7,19 +7,32 @@ Prints ONE JSON line (rank 0).  A step is one integrator step of the
 workload (drift + force evaluation + kick) over the whole particle set.
 
 Workloads (seeded synthetic inputs -- grav_sim publishes no dataset):
+  galaxy1048576_learned -- the default and the headline line: the two-galaxy
+                    collision (exponential disk, Hernquist bulge and halo;
+                    equal masses) at N = 1,048,576, run as the theta = 1.0
+                    group walk plus the learned residual, judged every step
+                    by a 4,096-particle direct sum with the theta = 0.5 walk
+                    as fallback (method 104; collection and GPU training
+                    happen before the timed region).  The same line times
+                    the plain Barnes-Hut comparators on the same GPU: the
+                    group walk at theta = 0.5 (method 106) and the
+                    reference-style monopole walk (method 103) at theta =
+                    0.5 and at theta = 0.3, where it meets the 1e-3 median
+                    error bound.
   plummer1024_fp64 -- the reference's CPU-sized case: Plummer N = 1,024, the
                     FP64 direct sum in the reference's order (bit-exact),
                     leapfrog dt = 1e-3; every step is one CUDA-graph replay.
   plummer262144  -- equal-mass Plummer sphere, N = 262,144, G = M = a = 1,
                     compensated-FP32 direct sum, eps = 0.01, leapfrog,
-                    dt = 1e-3 (the mixed-precision direct-sum workload; the
-                    default and the headline line).
-  galaxy2097152 / galaxy1048576 -- two-galaxy collision (disk, bulge, halo;
-                    equal masses), Barnes-Hut with monopole + quadrupole
-                    cells, theta = 0.5, eps = 0.01, leapfrog dt = 1e-3.
+                    dt = 1e-3 (the mixed-precision direct-sum workload).
+  galaxy2097152 / galaxy1048576 -- the galaxy pair, Barnes-Hut with monopole
+                    + quadrupole cells, theta = 0.5, eps = 0.01, leapfrog
+                    dt = 1e-3.
   galaxy1048576_plain -- the same at N = 1,048,576 with the monopole walk.
   galaxy2097152_group / galaxy1048576_group -- the group walk with
-                    interaction lists (quadrupole cells), theta = 0.5.
+                    interaction lists (quadrupole cells), theta = 0.5; the
+                    2,097,152-particle one is the Barnes-Hut galaxy-collision
+                    workload (200 steps in the original brief).
   galaxy16777216_group -- the group walk at N = 16,777,216 (about 4 GB of
                     state and tree in HBM).
   galaxy2097152_group_leaf1 / _t065, galaxy1048576_group_leaf1 -- with one
@@ -29,9 +42,6 @@ Workloads (seeded synthetic inputs -- grav_sim publishes no dataset):
                     library's default for methods 106 and 107.
   galaxy1048576_group_mono[_t035] -- the group walk with monopole cells
                     only, theta = 0.5 (0.35).
-  galaxy1048576_learned -- theta = 1.0 walk + learned residual, judged by a
-                    4,096-particle direct sum per step (training before the
-                    timed region).
   ensemble8192 / ensemble8192_leapfrog -- 8,192 planetary systems (Sun, 8
                     planets, 0-4,096 massless test particles each), WHFast or
                     leapfrog with the massless accelerations, dt = 1 day.
@@ -48,13 +58,22 @@ value      particle-steps/s over all ranks, state resident in HBM, device
 e2e        the same metric through launch_simulation_python with host numpy
            buffers: allocation, host->device copy of x, v, m, K steps and the
            device->host copy of x, v inside the timed region.
-roofline   dominant kernel (k_direct_sum): 20 FLOP per pair interaction x
-           N(N-1) interactions per launch / mean launch time (CUDA events
-           around the kernel on its stream), against the FP32 FMA peak
-           measured on this GPU by the library's probe.
-cpu_baseline  grav_sim's symmetric pairwise loop (oracle restatement, one
-           thread -- the reference's pairwise has no OpenMP) timed on a
-           bounded slice of rows, extrapolated to a full step.
+roofline   dominant kernel: the direct sum (20 FLOP per pair interaction x
+           N(N-1) per launch) or the Barnes-Hut walk (20 FLOP per accepted
+           cell or leaf pair term, counted on the device) / mean launch time
+           (CUDA events around the kernel on its stream), against the FP32
+           FMA peak measured on this GPU by the library's probe.
+accuracy   median / p99 relative acceleration error of the last step's
+           forces against an FP64 direct sum of 4,096 sampled particles
+           (512 for the direct-sum workloads), computed on the GPU in FP64.
+cpu_baseline  the reference's algorithm restated by the oracle, timed on
+           this machine's host cores: the symmetric pairwise loop (one
+           thread: the reference's pairwise sum has no OpenMP) for the
+           direct-sum workloads; Barnes-Hut at theta = 0.5 as the reference
+           computes it (serial octree build, OpenMP walk over all cores) for
+           the galaxy workloads; the per-system WHFast or leapfrog loop (one
+           system per thread) for the ensembles.  Each on a bounded sample,
+           extrapolated to a full step.
 Multi-GPU: replicas only (each rank runs the whole workload); value sums
 ranks; time is the max over ranks.
 """
@@ -108,9 +127,18 @@ WORKLOADS = {
     "galaxy1048576_plain": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01, dt=1e-3,
                                 integrator=4, method=103, theta=0.5, leaf=1,
                                 flop_per_interaction=20),
+    # the headline: theta = 1.0 walk + learned residual against plain
+    # Barnes-Hut on the same GPU (the group walk, and the reference-style
+    # monopole walk at theta = 0.5 and at the theta where it meets 1e-3)
     "galaxy1048576_learned": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01, dt=1e-3,
                                   integrator=4, method=104, theta=1.0, leaf=8,
-                                  flop_per_interaction=20),
+                                  flop_per_interaction=20, plain_key="plain_group_theta0.5",
+                                  compare=[("plain_group_theta0.5",
+                                            dict(method=106, theta=0.5, leaf=8)),
+                                           ("plain_monopole_theta0.5",
+                                            dict(method=103, theta=0.5, leaf=1)),
+                                           ("plain_monopole_theta0.3",
+                                            dict(method=103, theta=0.3, leaf=1))]),
     "galaxy2097152_group": dict(ic="galaxy", n=2097152, seed=4, G=1.0, eps=0.01, dt=1e-3,
                                 integrator=4, method=106, theta=0.5, leaf=8,
                                 flop_per_interaction=20),
@@ -256,20 +284,197 @@ def cpu_baseline_pairwise(wk, x, m, target_s=12.0):
             "pair_evals_per_s": pair_rate}
 
 
-def accuracy_sample(a_gpu, x, m, G, eps, rows=1024, seed=0):
+# The reference's Barnes-Hut as the CPU baseline of the galaxy workloads:
+# opening angle 0.5, one particle per leaf (its default tree), its own cell
+# membership test and leaf multipoles (compat mode), serial octree build and
+# an OpenMP walk (src/acceleration_barnes_hut.c:33-248).
+CPU_BH_THETA = 0.5
+CPU_BH_LEAF = 1
+
+
+def cpu_baseline_bh(wk, x, m, target_s=10.0):
+    """Time grav_sim's Barnes-Hut (oracle restatement: serial build, OpenMP
+    walk over the host's cores) on a strided sample of the sorted particles;
+    a step is the build plus N walks (kick/drift, O(N), neglected)."""
+    sys.path.insert(0, str(ROOT))
+    from oracle import restatement as orc
+    n = wk["n"]
+    r = orc.bh_cpu_timing(x, m, wk["G"], wk["eps"], CPU_BH_THETA, CPU_BH_LEAF, True,
+                          target_s=target_s)
+    step_s = r["build_s"] + n * r["walk_s_per_particle"]
+    return {"value": n / step_s, "unit": "particle-steps/s", "cores": r["threads"],
+            "kind": "port",
+            "sample": f"grav_sim Barnes-Hut (theta={CPU_BH_THETA}, {CPU_BH_LEAF} particle per leaf, "
+                      f"the reference's membership test and leaf multipoles) at N={n}: octree "
+                      f"build {r['build_s']:.2f} s (serial, as the reference), walk of "
+                      f"{r['sample']} strided sorted particles in {r['walk_s']:.1f} s on "
+                      f"{r['threads']} OpenMP threads, extrapolated to N walks per step",
+            "step_s": step_s}
+
+
+def fp64_rows(x, m, rows, G, eps):
+    """FP64 direct-sum accelerations of the given rows (numpy in, numpy
+    out), computed with torch in FP64 on the current GPU."""
+    import torch
+    X = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    M = torch.from_numpy(np.ascontiguousarray(m)).cuda()
+    out = torch.empty((len(rows), 3), dtype=torch.float64, device="cuda")
+    idx = torch.from_numpy(np.asarray(rows, dtype=np.int64)).cuda()
+    chunk = max(1, int(2 ** 27 // max(x.shape[0], 1)))
+    for b in range(0, len(rows), chunk):
+        r = idx[b:b + chunk]
+        d = X[None, :, :] - X[r][:, None, :]              # x_j - x_i
+        r2 = (d * d).sum(-1) + eps * eps
+        w = M[None, :] / (r2 * torch.sqrt(r2))
+        w[torch.arange(len(r), device="cuda"), r] = 0.0    # no self term
+        out[b:b + chunk] = G * (w[:, :, None] * d).sum(1)
+        del d, r2, w
+    res = out.cpu().numpy()
+    del X, M, out, idx
+    torch.cuda.empty_cache()
+    return res
+
+
+def accuracy_sample(a_gpu, x, m, G, eps, rows=4096, seed=0):
     """Median / p99 relative error of GPU accelerations on sampled particles
-    against an FP64 direct sum (numpy, this process)."""
+    against an FP64 direct sum."""
     rng = np.random.default_rng(seed)
-    idx = rng.choice(x.shape[0], min(rows, x.shape[0]), replace=False)
-    errs = []
-    for i in idx:
-        d = x - x[i]
-        r2 = (d * d).sum(1) + eps * eps
-        r2[i] = np.inf
-        ai = G * (m[:, None] * d / (r2 * np.sqrt(r2))[:, None]).sum(0)
-        errs.append(np.linalg.norm(a_gpu[i] - ai) / np.linalg.norm(ai))
-    errs = np.array(errs)
+    idx = np.sort(rng.choice(x.shape[0], min(rows, x.shape[0]), replace=False))
+    ref = fp64_rows(x, m, idx, G, eps)
+    errs = np.linalg.norm(a_gpu[idx] - ref, axis=1) / np.linalg.norm(ref, axis=1)
     return float(np.median(errs)), float(np.quantile(errs, 0.99))
+
+
+BH_METHODS = (103, 104, 105, 106, 107, 113)
+
+
+def _bind_sim(lib, g):
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.gsgpu_sim_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                                     ctypes.c_double, ctypes.POINTER(g.AccelerationParam),
+                                     ctypes.c_int, ctypes.c_double, ctypes.c_void_p]
+    lib.gsgpu_sim_upload.argtypes = [ctypes.c_void_p, dp, dp, dp]
+    lib.gsgpu_sim_run.argtypes = [ctypes.c_void_p, ctypes.c_int64]
+    lib.gsgpu_sim_download.argtypes = [ctypes.c_void_p, dp, dp]
+    lib.gsgpu_sim_set_force_timing.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.gsgpu_sim_force_timing.argtypes = [ctypes.c_void_p, dp, ctypes.POINTER(ctypes.c_int64)]
+    lib.gsgpu_sim_kernels_per_step.argtypes = [ctypes.c_void_p]
+    lib.gsgpu_sim_destroy.argtypes = [ctypes.c_void_p]
+    lib.gsgpu_sim_download_acceleration.argtypes = [ctypes.c_void_p, dp]
+    lib.gsgpu_measure_fma_peak.argtypes = [ctypes.c_int, dp, dp]
+    lib.gsgpu_sim_interaction_counts.argtypes = [ctypes.c_void_p,
+                                                 ctypes.POINTER(ctypes.c_longlong)]
+    lib.gsgpu_sim_warmup_until_ready.argtypes = [ctypes.c_void_p, ctypes.c_int64,
+                                                 ctypes.POINTER(ctypes.c_int64)]
+    lib.gsgpu_sim_report.argtypes = [ctypes.c_void_p, dp, ctypes.c_int]
+    return dp
+
+
+def sim_arm(args, lib, g, wk, x, v, m, stream, flush, world, local, sample_clocks=False,
+            acc_rows=4096):
+    """One method on the device-resident loop: (training), W warm-up steps,
+    K timed steps (CUDA events on the simulation's stream, L2 flushed before
+    each), K more steps with events around the dominant kernel, then the
+    accuracy of the last step's forces."""
+    import torch
+    dp = _bind_sim(lib, g)
+    n = x.shape[0]
+    sim = ctypes.c_void_p()
+    p = g.AccelerationParam(wk["method"], wk.get("theta", 1.0), wk["eps"], wk.get("leaf", -1))
+    rc = lib.gsgpu_sim_create(ctypes.byref(sim), n, wk["G"], ctypes.byref(p), wk["integrator"],
+                              wk["dt"], ctypes.c_void_p(stream.cuda_stream))
+    assert rc == 0, rc
+    out = {}
+    try:
+        assert lib.gsgpu_sim_upload(sim, x.ctypes.data_as(dp), v.ctypes.data_as(dp),
+                                    m.ctypes.data_as(dp)) == 0
+        if wk["method"] == 104:
+            # collection snapshots and GPU training happen before the timed region
+            t0 = time.perf_counter()
+            spent = ctypes.c_int64()
+            assert lib.gsgpu_sim_warmup_until_ready(sim, 1000, ctypes.byref(spent)) == 0
+            out["training_s"] = time.perf_counter() - t0
+            out["training_steps"] = spent.value
+        # warm-up (includes the leapfrog half kick and graph capture)
+        assert lib.gsgpu_sim_run(sim, args.warmup) == 0
+        torch.cuda.synchronize()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        clocks = ClockSampler(local) if sample_clocks else None
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        if clocks:
+            clocks.start()
+            time.sleep(0.3)
+        wall0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.fill_(k & 0xFF)                 # evict L2 between steps (not timed)
+                starts[k].record(stream)
+                assert lib.gsgpu_sim_run(sim, 1) == 0
+                ends[k].record(stream)
+        torch.cuda.synchronize()
+        out["wall_s"] = time.perf_counter() - wall0
+        if clocks:
+            out["clocks"] = clocks.stop()
+        if world > 1:
+            torch.distributed.barrier()
+        total_ms = float(sum(s_.elapsed_time(e_) for s_, e_ in zip(starts, ends)))
+        total_ms, = max_over_ranks([total_ms], world)
+        out["total_ms"] = total_ms
+        out["ms_per_step"] = total_ms / args.steps
+        out["kernels_per_step"] = lib.gsgpu_sim_kernels_per_step(sim)
+        # The dominant kernel's duration, for the roofline: K more steps with
+        # CUDA events around each force kernel (launched directly, not from
+        # the graph; outside the timed region).
+        lib.gsgpu_sim_set_force_timing(sim, 1)
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.fill_(k & 0xFF)
+                assert lib.gsgpu_sim_run(sim, 1) == 0
+        torch.cuda.synchronize()
+        force_ms = ctypes.c_double()
+        force_n = ctypes.c_int64()
+        lib.gsgpu_sim_force_timing(sim, ctypes.byref(force_ms), ctypes.byref(force_n))
+        lib.gsgpu_sim_set_force_timing(sim, 0)
+        out["mean_force_ms"] = force_ms.value / max(force_n.value, 1)
+        interactions = float(n) * (n - 1)
+        if wk["method"] in BH_METHODS:
+            cnt = (ctypes.c_longlong * 2)()
+            lib.gsgpu_sim_interaction_counts(sim, cnt)
+            interactions = float(cnt[0] + cnt[1])
+        out["interactions"] = interactions
+        if wk["method"] == 104:
+            rep = np.zeros(13)
+            k = lib.gsgpu_sim_report(sim, rep.ctypes.data_as(dp), 13)
+            rep = rep[:max(k, 0)].tolist()
+            names = ["trained", "snapshots", "loss_first_epoch", "loss_last_epoch",
+                     "heldout_median_residual_before", "heldout_median_residual_after",
+                     "last_judged_median_err", "steps_judged", "steps_fallen_back",
+                     "theta_cheap", "training_seconds", "adam_steps", "network_in_use"]
+            out["learned_report"] = dict(zip(names, rep))
+        a_host = np.empty((n, 3))
+        torch.cuda.synchronize()
+        assert lib.gsgpu_sim_download_acceleration(sim, a_host.ctypes.data_as(dp)) == 0
+        xs = np.empty((n, 3))
+        vs = np.empty((n, 3))
+        lib.gsgpu_sim_download(sim, xs.ctypes.data_as(dp), vs.ctypes.data_as(dp))
+    finally:
+        lib.gsgpu_sim_destroy(sim)
+    med, p99 = accuracy_sample(a_host, xs, m, wk["G"], wk["eps"], rows=acc_rows)
+    out["median_rel_err"] = med
+    out["p99_rel_err"] = p99
+    out["xs"], out["vs"] = xs, vs
+    return out
+
+
+def _arm_summary(wk, r, n):
+    d = {"method": wk["method"], "theta": wk.get("theta"), "leaf": wk.get("leaf"),
+         "ms_per_step": r["ms_per_step"], "particle_steps_per_s": n / (r["ms_per_step"] / 1e3),
+         "median_rel_err": r["median_rel_err"], "p99_rel_err": r["p99_rel_err"],
+         "walk_ms": r["mean_force_ms"], "interactions": r["interactions"]}
+    return d
 
 
 def run_ours(args, world, rank, local):
@@ -285,111 +490,39 @@ def run_ours(args, world, rank, local):
         return run_cosmo(args, world, rank, local, wk, g, lib)
     n = wk["n"]
     x, v, m = (wl.plummer if wk["ic"] == "plummer" else wl.galaxy_pair)(n, wk["seed"])
-    bh = wk["method"] in (103, 104, 105, 106, 107, 113)
-
-    dp = ctypes.POINTER(ctypes.c_double)
-    lib.gsgpu_sim_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
-                                     ctypes.c_double, ctypes.POINTER(g.AccelerationParam),
-                                     ctypes.c_int, ctypes.c_double, ctypes.c_void_p]
-    lib.gsgpu_sim_upload.argtypes = [ctypes.c_void_p, dp, dp, dp]
-    lib.gsgpu_sim_run.argtypes = [ctypes.c_void_p, ctypes.c_int64]
-    lib.gsgpu_sim_download.argtypes = [ctypes.c_void_p, dp, dp]
-    lib.gsgpu_sim_set_force_timing.argtypes = [ctypes.c_void_p, ctypes.c_int]
-    lib.gsgpu_sim_force_timing.argtypes = [ctypes.c_void_p, dp, ctypes.POINTER(ctypes.c_int64)]
-    lib.gsgpu_sim_kernels_per_step.argtypes = [ctypes.c_void_p]
-    lib.gsgpu_sim_destroy.argtypes = [ctypes.c_void_p]
-    lib.gsgpu_sim_download_acceleration.argtypes = [ctypes.c_void_p, dp]
-    lib.gsgpu_measure_fma_peak.argtypes = [ctypes.c_int, dp, dp]
-    lib.gsgpu_sim_interaction_counts.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]
-    lib.gsgpu_sim_warmup_until_ready.argtypes = [ctypes.c_void_p, ctypes.c_int64,
-                                                 ctypes.POINTER(ctypes.c_int64)]
-    lib.gsgpu_sim_report.argtypes = [ctypes.c_void_p, dp, ctypes.c_int]
-
+    bh = wk["method"] in BH_METHODS
     stream = torch.cuda.Stream()
-    sim = ctypes.c_void_p()
-    p = g.AccelerationParam(wk["method"], wk.get("theta", 1.0), wk["eps"], wk.get("leaf", -1))
-    rc = lib.gsgpu_sim_create(ctypes.byref(sim), n, wk["G"], ctypes.byref(p), wk["integrator"],
-                              wk["dt"], ctypes.c_void_p(stream.cuda_stream))
-    assert rc == 0, rc
-    assert lib.gsgpu_sim_upload(sim, x.ctypes.data_as(dp), v.ctypes.data_as(dp),
-                                m.ctypes.data_as(dp)) == 0
-    training_s = None
-    if wk["method"] == 104:
-        # collection snapshots and GPU training happen before the timed region
-        t0 = time.perf_counter()
-        spent = ctypes.c_int64()
-        assert lib.gsgpu_sim_warmup_until_ready(sim, 1000, ctypes.byref(spent)) == 0
-        training_s = time.perf_counter() - t0
-    # warm-up (includes the leapfrog half kick and graph capture)
-    assert lib.gsgpu_sim_run(sim, args.warmup) == 0
-    torch.cuda.synchronize()
-
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    clocks = ClockSampler(local)
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    time.sleep(0.3)
-    wall0 = time.perf_counter()
-    with torch.cuda.stream(stream):
-        for k in range(args.steps):
-            flush.fill_(k & 0xFF)                 # evict L2 between steps (not timed)
-            starts[k].record(stream)
-            assert lib.gsgpu_sim_run(sim, 1) == 0
-            ends[k].record(stream)
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - wall0
-    clk = clocks.stop()
-    if world > 1:
-        torch.distributed.barrier()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = float(sum(step_ms))
-    total_ms, = max_over_ranks([total_ms], world)
-    kernels_per_step = lib.gsgpu_sim_kernels_per_step(sim)
-    # The dominant kernel's duration, for the roofline: K more steps with CUDA
-    # events around each force evaluation (launched directly, not from the
-    # graph; outside the timed region).
-    lib.gsgpu_sim_set_force_timing(sim, 1)
-    with torch.cuda.stream(stream):
-        for k in range(args.steps):
-            flush.fill_(k & 0xFF)
-            assert lib.gsgpu_sim_run(sim, 1) == 0
-    torch.cuda.synchronize()
-    force_ms = ctypes.c_double()
-    force_n = ctypes.c_int64()
-    lib.gsgpu_sim_force_timing(sim, ctypes.byref(force_ms), ctypes.byref(force_n))
-    lib.gsgpu_sim_set_force_timing(sim, 0)
-
-    value = world * n * args.steps / (total_ms / 1e3)
-    interactions = float(n) * (n - 1)
-    if bh:
-        cnt = (ctypes.c_longlong * 2)()
-        lib.gsgpu_sim_interaction_counts(sim, cnt)
-        interactions = float(cnt[0] + cnt[1])
-    report = None
-    if wk["method"] == 104:
-        rep = np.zeros(13)
-        k = lib.gsgpu_sim_report(sim, rep.ctypes.data_as(dp), 13)
-        report = rep[:max(k, 0)].tolist()
-    mean_force_ms = force_ms.value / max(force_n.value, 1)
+    acc_rows = 4096 if bh else 512
+    r = sim_arm(args, lib, g, wk, x, v, m, stream, flush, world, local, sample_clocks=True,
+                acc_rows=acc_rows)
+    value = world * n * args.steps / (r["total_ms"] / 1e3)
+    interactions = r["interactions"]
+    mean_force_ms = r["mean_force_ms"]
     achieved_tflops = wk["flop_per_interaction"] * interactions / (mean_force_ms / 1e3) / 1e12
-
     fp64 = wk["method"] == 111   # the FP64 reference-order direct sum
+    dp = ctypes.POINTER(ctypes.c_double)
     peak = ctypes.c_double()
     lib.gsgpu_measure_fma_peak(1 if fp64 else 0, ctypes.byref(peak), None)
 
-    # accuracy of the forces of the last step
-    a_host = np.empty((n, 3))
-    torch.cuda.synchronize()
-    assert lib.gsgpu_sim_download_acceleration(sim, a_host.ctypes.data_as(dp)) == 0
-    xs = np.empty((n, 3))
-    vs = np.empty((n, 3))
-    lib.gsgpu_sim_download(sim, xs.ctypes.data_as(dp), vs.ctypes.data_as(dp))
-    med, p99 = accuracy_sample(a_host, xs, m, wk["G"], wk["eps"], rows=512)
-    lib.gsgpu_sim_destroy(sim)
+    # the comparators of this workload, on the same GPU
+    comparison = None
+    if wk.get("compare"):
+        comparison = {"this_line": _arm_summary(wk, r, n)}
+        if wk["method"] == 104:
+            comparison["this_line"]["training_s"] = r.get("training_s")
+            comparison["this_line"]["network_in_use"] = bool(
+                r.get("learned_report", {}).get("network_in_use", 0))
+        for name, over in wk["compare"]:
+            wc = dict(wk, **over)
+            rc_ = sim_arm(args, lib, g, wc, x, v, m, stream, flush, world, local,
+                          acc_rows=acc_rows)
+            comparison[name] = _arm_summary(wc, rc_, n)
+        plain = comparison.get(wk.get("plain_key"))
+        if plain:
+            comparison["this_over_plain_speed"] = (comparison["this_line"]["particle_steps_per_s"]
+                                                  / plain["particle_steps_per_s"])
+
     energy = None
     if wk["ic"] == "plummer":
         # FP64 energies (unsoftened potential, src/utils.c:27-59) of the initial
@@ -397,7 +530,7 @@ def run_ours(args, world, rank, local):
         state = np.zeros((2, n, 7))
         state[:, :, 0] = m
         state[0, :, 1:4], state[0, :, 4:7] = x, v
-        state[1, :, 1:4], state[1, :, 4:7] = xs, vs
+        state[1, :, 1:4], state[1, :, 4:7] = r["xs"], r["vs"]
         e = np.zeros(2)
         lib.compute_energy_python.argtypes = [dp, ctypes.c_double, dp, ctypes.c_int32,
                                               ctypes.c_int32]
@@ -421,7 +554,7 @@ def run_ours(args, world, rank, local):
     e2e_val = world * n * args.steps / e2e_s
 
     traffic = None
-    kernel = ("k_bh_group" if wk["method"] in (106, 107) else "k_bh_walk") if bh else \
+    kernel = ("k_bh_group" if wk["method"] in (104, 106, 107) else "k_bh_walk") if bh else \
         ("k_direct_fp64_reference_order" if fp64 else "k_direct_sum")
     prof = ROOT / "profiles" / f"{kernel}_{args.workload}.md"
     if prof.exists():
@@ -431,6 +564,9 @@ def run_ours(args, world, rank, local):
     if bh:
         desc = (f"{args.workload}: galaxy pair N={n}, Barnes-Hut method {wk['method']} "
                 f"theta={wk['theta']} leaf={wk['leaf']}, eps={wk['eps']}, leapfrog dt={wk['dt']}")
+        if wk["method"] == 104:
+            desc += (" (theta=1.0 group walk + learned residual, judged by a 4096-particle "
+                     "direct sum per step, theta=0.5 group walk as fallback)")
         data = "synthetic (seeded two-galaxy model: exponential disk, Hernquist bulge and halo)"
         dtype = "f32 walk terms (Kahan), f64 tree multipoles and state"
     elif fp64:
@@ -451,7 +587,7 @@ def run_ours(args, world, rank, local):
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": total_ms / args.steps,
+        "ms_per_step": r["total_ms"] / args.steps,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
@@ -460,8 +596,9 @@ def run_ours(args, world, rank, local):
         "config": {"workload": desc,
                    "parallelism": f"replicas x{world}", "l2": "flushed between steps (256 MiB write)",
                    "interactions_per_s": value / n * interactions,
-                   "accuracy": {"median_rel_err": med, "p99_rel_err": p99,
-                                "sample": "512 particles vs FP64 direct sum"},
+                   "accuracy": {"median_rel_err": r["median_rel_err"],
+                                "p99_rel_err": r["p99_rel_err"],
+                                "sample": f"{acc_rows} particles vs FP64 direct sum"},
                    "energy": energy},
         "roofline": {"bound": "fp64" if fp64 else "fp32", "achieved": achieved_tflops,
                      "peak": peak.value,
@@ -476,20 +613,72 @@ def run_ours(args, world, rank, local):
                 "d2h_bytes_per_step": (6 * n * 8) / args.steps,
                 "note": "one launch_simulation_python call of K steps; its copies and setup "
                         "amortised over the K steps"},
-        "gpu_launches": args.steps * kernels_per_step,
-        "clocks": clk,
-        "wall_s": wall,
+        "gpu_launches": args.steps * r["kernels_per_step"],
+        "clocks": r.get("clocks"),
+        "wall_s": r["wall_s"],
     }
     if bh:
         out["config"]["interactions"] = "accepted cells + leaf pair terms of the last step "\
                                         "(device counters), 20 FLOP each"
-    if training_s is not None:
-        out["config"]["training_s"] = training_s
-        out["config"]["learned_report"] = report
+    if wk["method"] == 104:
+        out["config"]["training_s"] = r.get("training_s")
+        out["config"]["learned_report"] = r.get("learned_report")
+        out["e2e"]["note"] += ("; with method 104 a call of K < 64 steps runs only collection "
+                               "steps (fallback walk + training samples): the network is "
+                               "trained after the 64th force evaluation of a call")
+    if comparison:
+        out["config"]["comparison"] = comparison
     if rank == 0:
         if wk["ic"] == "plummer":
             out["cpu_baseline"] = cpu_baseline_pairwise(wk, x, m)
+        else:
+            out["cpu_baseline"] = cpu_baseline_bh(wk, x, m)
         print(json.dumps(out), flush=True)
+
+
+def cpu_baseline_ensemble(wk, systems, target_s=10.0, sample_systems=128):
+    """The reference's per-system loop (oracle restatement of WHFast or
+    leapfrog with the massless acceleration) on a stratified sample of the
+    systems -- every (S / sample)-th system in order of size -- one system
+    per OpenMP thread (the fair-share baseline of one system per core),
+    for a number of steps sized to about target_s seconds."""
+    sys.path.insert(0, str(ROOT))
+    from oracle import restatement as orc
+    G = _module("workloads").G_AU_MSUN_DAY
+    order = np.argsort([s_[2].size for s_ in systems], kind="stable")
+    pick = order[np.linspace(0, len(systems) - 1, min(sample_systems, len(systems))).astype(int)]
+    sample = [systems[i] for i in pick]
+    P = int(sum(s_[2].size for s_ in sample))
+    steps = 4
+    el, threads = orc.ensemble_cpu_timing(sample, G, wk["dt"], steps, wk["integrator"])
+    steps = max(4, min(10000, int(steps * target_s / max(el, 1e-3))))
+    el, threads = orc.ensemble_cpu_timing(sample, G, wk["dt"], steps, wk["integrator"])
+    name = "WHFast" if wk["integrator"] == 10 else "leapfrog"
+    return {"value": P * steps / el, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+            "sample": f"grav_sim {name} + massless acceleration, each system alone as "
+                      f"launch_simulation_python runs it: {len(sample)} of {len(systems)} systems "
+                      f"stratified by size ({P} particles), {steps} steps each, {el:.1f} s on "
+                      f"{threads} threads (one system per thread); particle-steps/s of the "
+                      f"sample, whose size distribution is the ensemble's"}
+
+
+def reference_ensemble(args, wk, wl):
+    systems = wl.planetary_ensemble(wk["systems"], wk["seed"], max_test=wk["max_test"])
+    for _ in range(args.warmup):
+        cpu_baseline_ensemble(wk, systems, target_s=0.5)
+    vals = [cpu_baseline_ensemble(wk, systems, target_s=3.0) for _ in range(args.steps)]
+    value = statistics.median(r["value"] for r in vals)
+    P = int(sum(s_[2].size for s_ in systems))
+    name = "WHFast" if wk["integrator"] == 10 else "leapfrog"
+    return {"value": value, "ms_per_step": 1e3 * P / value,
+            "data": "synthetic (seeded planetary systems)",
+            "config": {"workload": f"{args.workload}: {wk['systems']} systems, {P} particles, "
+                                   f"grav_sim {name} + massless accelerations, dt={wk['dt']} day"},
+            "cpu_baseline": {"value": value, "unit": "particle-steps/s",
+                             "cores": vals[-1]["cores"], "kind": "port",
+                             "sample": vals[-1]["sample"]},
+            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
 
 
 def run_ensemble(args, world, rank, local, wk, g, wl, lib):
@@ -551,6 +740,7 @@ def run_ensemble(args, world, rank, local, wk, g, wl, lib):
         "clocks": clk,
     }
     if rank == 0:
+        out["cpu_baseline"] = cpu_baseline_ensemble(wk, systems)
         print(json.dumps(out), flush=True)
 
 
@@ -640,29 +830,55 @@ def run_cosmo(args, world, rank, local, wk, g, lib):
 
 
 def run_reference(args, world, rank, local):
+    """The reference's CPU implementation of the workload's path (the
+    oracle's restatement of grav_sim, built on this machine), on the host
+    cores, each step a bounded sample of the workload extrapolated to a
+    full step.  Rank 0 alone runs it."""
     if rank != 0:
         return
     wl = _module("workloads")
     wk = WORKLOADS[args.workload]
-    x, v, m = wl.plummer(wk["n"], wk["seed"])
-    vals = []
-    for _ in range(args.warmup):
-        cpu_baseline_pairwise(wk, x, m, target_s=1.0)
-    for _ in range(args.steps):
-        vals.append(cpu_baseline_pairwise(wk, x, m, target_s=4.0))
+    base = {"metric": METRIC, "unit": "particle-steps/s", "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64"}
+    if wk["ic"] == "ensemble":
+        out = dict(base, **reference_ensemble(args, wk, wl))
+        print(json.dumps(out), flush=True)
+        return
+    if wk["ic"] == "cosmo":
+        print(json.dumps({"impl": "reference", "unavailable":
+                          "the reference's particle-mesh path needs FFTW 3, absent on this "
+                          "machine; its restatement runs a direct DFT, far too slow for a "
+                          "256^3 mesh"}), flush=True)
+        return
+    if wk["ic"] == "plummer":
+        x, v, m = wl.plummer(wk["n"], wk["seed"])
+        for _ in range(args.warmup):
+            cpu_baseline_pairwise(wk, x, m, target_s=1.0)
+        vals = [cpu_baseline_pairwise(wk, x, m, target_s=4.0) for _ in range(args.steps)]
+        desc = (f"{args.workload}: Plummer N={wk['n']}, grav_sim pairwise "
+                f"(acceleration.c:177-234) + leapfrog dt={wk['dt']}")
+        data = "synthetic (seeded Plummer sphere)"
+        cores = 1
+    else:
+        x, v, m = wl.galaxy_pair(wk["n"], wk["seed"])
+        for _ in range(args.warmup):
+            cpu_baseline_bh(wk, x, m, target_s=0.5)
+        vals = [cpu_baseline_bh(wk, x, m, target_s=3.0) for _ in range(args.steps)]
+        desc = (f"{args.workload}: galaxy pair N={wk['n']}, grav_sim Barnes-Hut "
+                f"(acceleration_barnes_hut.c:33-248, linear_octree.c) theta={CPU_BH_THETA} "
+                f"leaf={CPU_BH_LEAF}, eps={wk['eps']}, leapfrog dt={wk['dt']}")
+        data = "synthetic (seeded two-galaxy model: exponential disk, Hernquist bulge and halo)"
+        cores = vals[-1]["cores"]
     value = statistics.median(r["value"] for r in vals)
-    out = {
-        "metric": METRIC, "value": value, "unit": "particle-steps/s", "impl": "reference",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * wk["n"] / value, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Plummer sphere)",
-        "config": {"workload": f"{args.workload}: Plummer N={wk['n']}, grav_sim pairwise "
-                               f"(acceleration.c:177-234) + leapfrog dt={wk['dt']}"},
-        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": 1, "kind": "port",
-                         "sample": vals[-1]["sample"]},
+    out = dict(base, **{
+        "value": value, "ms_per_step": 1e3 * wk["n"] / value, "data": data,
+        "config": {"workload": desc},
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores,
+                         "kind": "port", "sample": vals[-1]["sample"]},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
-    }
+    })
     print(json.dumps(out), flush=True)
 
 
@@ -672,7 +888,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="plummer262144", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="galaxy1048576_learned", choices=sorted(WORKLOADS))
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()

@@ -80,7 +80,9 @@ struct DeviceInfo {
     int cc_minor = 0;
     char name[256] = {0};
 };
-// Queries the current device once per process; fails when no usable GPU.
+// Properties of the current device (queried once per device); fails when
+// there is no usable GPU.
+constexpr int kMaxDevices = 64;
 ErrorStatus device_info(const DeviceInfo **out);
 
 // Records CUDA events around the dominant kernel of each force evaluation.

@@ -123,29 +123,35 @@ ErrorStatus DBuf::reserve(size_t b)
 ErrorStatus device_info(const DeviceInfo **out)
 {
     static std::mutex mu;
-    static DeviceInfo info;
-    static bool done = false;
+    static DeviceInfo info[kMaxDevices];
+    static bool done[kMaxDevices] = {};
     std::lock_guard<std::mutex> lock(mu);
-    if (!done) {
-        int count = 0;
-        cudaError_t e = cudaGetDeviceCount(&count);
-        if (e != cudaSuccess || count < 1) {
-            (void)cudaGetLastError();
-            return GS_RAISE(GRAV_FAILURE, "no CUDA device available (%s)", cudaGetErrorString(e));
-        }
-        GS_CUDA(cudaGetDevice(&info.id));
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count < 1) {
+        (void)cudaGetLastError();
+        return GS_RAISE(GRAV_FAILURE, "no CUDA device available (%s)", cudaGetErrorString(e));
+    }
+    int dev = 0;
+    GS_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices)
+        return GS_RAISE(GRAV_FAILURE, "device ordinal %d is beyond the %d this library tracks", dev,
+                        kMaxDevices);
+    if (!done[dev]) {
+        DeviceInfo &d = info[dev];
+        d.id = dev;
         cudaDeviceProp prop;
-        GS_CUDA(cudaGetDeviceProperties(&prop, info.id));
-        info.sm_count = prop.multiProcessorCount;
-        info.cc_major = prop.major;
-        info.cc_minor = prop.minor;
-        std::snprintf(info.name, sizeof(info.name), "%s", prop.name);
+        GS_CUDA(cudaGetDeviceProperties(&prop, dev));
+        d.sm_count = prop.multiProcessorCount;
+        d.cc_major = prop.major;
+        d.cc_minor = prop.minor;
+        std::snprintf(d.name, sizeof(d.name), "%s", prop.name);
         if (prop.major < 10)
             return GS_RAISE(GRAV_FAILURE, "device %s (sm_%d%d) is not a Blackwell GPU; this "
                             "library is built for sm_103a only", prop.name, prop.major, prop.minor);
-        done = true;
+        done[dev] = true;
     }
-    *out = &info;
+    *out = &info[dev];
     return ok();
 }
 

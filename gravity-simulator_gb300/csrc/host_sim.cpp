@@ -734,6 +734,10 @@ ErrorStatus sim_run_until(gsgpu_sim *s, double tf, SimulationStatus *status, con
         ++steps;
         t = (double)steps * dt;
         if (oc && oc->due(t)) {
+            // A force that failed on the device (node-capacity overflow, a
+            // wait that ran out) is reported before its state reaches a file.
+            GS_CUDA(cudaStreamSynchronize(s->stream));
+            GS_TRY(s->engine->check_status(s->stream));
             // leapfrog writes v at integer time, v - 0.5 a dt (src/integrator.c:1043-1071)
             const double *dv = s->v.as<double>();
             if (s->integrator == INTEGRATOR_LEAPFROG) {
@@ -757,6 +761,7 @@ ErrorStatus sim_run_until(gsgpu_sim *s, double tf, SimulationStatus *status, con
         status->num_steps = steps;
     }
     GS_CUDA(cudaStreamSynchronize(s->stream));
+    GS_TRY(s->engine->check_status(s->stream));
     if (oc) GS_TRY(oc->finish());
     return ok();
 }

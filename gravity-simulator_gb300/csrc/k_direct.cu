@@ -576,10 +576,17 @@ ErrorStatus DirectRows::compute(const double *d_x, const double *d_m, const doub
 // allocator at all.  This entry point computes the same accelerations as
 // acceleration() with GRAV_GPU_PAIRWISE, from device arrays the caller
 // owns, using the same kernels; its scratch (the packed float4 particles,
-// the per-split partial sums and the status word) lives in one file-scope
-// device array instead of memory the library allocates.  That array is part
-// of the library image: every GPU that loads the library holds its
-// NOALLOC_BYTES (about 6.5 MiB) until the process exits.
+// the per-split partial sums, the status word and the frame centre) lives
+// in one file-scope device array instead of memory the library allocates.
+// That array is part of the library image: every GPU that loads the library
+// holds its NOALLOC_BYTES (about 6.5 MiB) until the process exits.
+//
+// Like acceleration(), it takes positions relative to the centre of their
+// bounding box before rounding them to FP32; here that centre is reduced on
+// the device (k_noalloc_frame) into the scratch array, so that systems far
+// from the origin keep their accuracy.  A bulk-copy wait that runs out in
+// k_direct_sum sets the status word, and the reduction then writes NaN into
+// every output row instead of partial sums.
 constexpr int NOALLOC_MAX_N = 32768;      // largest particle count accepted
 constexpr int NOALLOC_MAX_SPLITS = 8;
 constexpr size_t NOALLOC_PJ_BYTES = (size_t)NOALLOC_MAX_N * sizeof(float4);
@@ -587,8 +594,81 @@ constexpr size_t NOALLOC_PARTIAL_BYTES =
     (size_t)NOALLOC_MAX_SPLITS * 3 * NOALLOC_MAX_N * sizeof(double);
 constexpr size_t NOALLOC_BYTES = NOALLOC_PJ_BYTES + NOALLOC_PARTIAL_BYTES + 256;
 static_assert(NOALLOC_MAX_N % DS_JTILE == 0, "capacity must be whole tiles");
+// The last 256 bytes: the status word at offset 0, the FP64 frame centre at 64.
+constexpr size_t NOALLOC_STATUS_OFF = NOALLOC_PJ_BYTES + NOALLOC_PARTIAL_BYTES;
+constexpr size_t NOALLOC_FRAME_OFF = NOALLOC_STATUS_OFF + 64;
+static_assert(NOALLOC_FRAME_OFF + 3 * sizeof(double) <= NOALLOC_BYTES, "tail holds the frame");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+// Centre of the bounding box of x [n] (one CTA), formed as acceleration()
+// forms it on the host: per axis the exact minimum and maximum, then
+// 0.5 (lo + hi).
+constexpr int NA_FRAME_THREADS = 1024;
+__global__ void __launch_bounds__(NA_FRAME_THREADS)
+k_noalloc_frame(const double *__restrict__ x, int n, double *__restrict__ frame)
+{
+    __shared__ double lo_s[3][NA_FRAME_THREADS / 32], hi_s[3][NA_FRAME_THREADS / 32];
+    double lo[3] = {x[0], x[1], x[2]}, hi[3] = {x[0], x[1], x[2]};
+    for (int i = threadIdx.x; i < n; i += NA_FRAME_THREADS)
+        for (int k = 0; k < 3; ++k) {
+            const double q = x[3 * i + k];
+            lo[k] = q < lo[k] ? q : lo[k];
+            hi[k] = q > hi[k] ? q : hi[k];
+        }
+    for (int k = 0; k < 3; ++k)
+        for (int o = 16; o > 0; o >>= 1) {
+            const double l = __shfl_xor_sync(0xffffffffu, lo[k], o);
+            const double h = __shfl_xor_sync(0xffffffffu, hi[k], o);
+            lo[k] = l < lo[k] ? l : lo[k];
+            hi[k] = h > hi[k] ? h : hi[k];
+        }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 3; ++k) {
+            lo_s[k][w] = lo[k];
+            hi_s[k][w] = hi[k];
+        }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int k = threadIdx.x;
+        double l = lo_s[k][0], h = hi_s[k][0];
+        for (int v = 1; v < NA_FRAME_THREADS / 32; ++v) {
+            l = lo_s[k][v] < l ? lo_s[k][v] : l;
+            h = hi_s[k][v] > h ? hi_s[k][v] : h;
+        }
+        frame[k] = 0.5 * (l + h);
+    }
+}
+
+// k_reduce_splits for this entry point: when a tile wait of k_direct_sum
+// ran out (status bit ST_WAIT_TIMEOUT), some partial sums were never
+// written, and every row gets NaN instead of a wrong finite value.
+__global__ void k_noalloc_reduce(const double *__restrict__ partial, int splits, int n, int n_pad,
+                                 double G, const unsigned *__restrict__ status,
+                                 double *__restrict__ a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (*status & ST_WAIT_TIMEOUT) {
+        const double nan = __longlong_as_double(0x7ff8000000000000LL);
+        a[3 * i + 0] = nan;
+        a[3 * i + 1] = nan;
+        a[3 * i + 2] = nan;
+        return;
+    }
+    const size_t plane = (size_t)n_pad;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int s = 0; s < splits; ++s) {
+        const double *p = partial + (size_t)s * 3 * plane;
+        s0 += p[i];
+        s1 += p[plane + i];
+        s2 += p[2 * plane + i];
+    }
+    a[3 * i + 0] = G * s0;
+    a[3 * i + 1] = G * s1;
+    a[3 * i + 2] = G * s2;
+}
 
 namespace {
 
@@ -665,8 +745,8 @@ extern "C" int gsgpu_pairwise_acceleration_noalloc(const double *d_x, const doub
     unsigned char *scratch = static_cast<unsigned char *>(base);
     float4 *pj = reinterpret_cast<float4 *>(scratch);
     double *partial = reinterpret_cast<double *>(scratch + NOALLOC_PJ_BYTES);
-    unsigned *status = reinterpret_cast<unsigned *>(scratch + NOALLOC_PJ_BYTES +
-                                                    NOALLOC_PARTIAL_BYTES);
+    unsigned *status = reinterpret_cast<unsigned *>(scratch + NOALLOC_STATUS_OFF);
+    double *frame = reinterpret_cast<double *>(scratch + NOALLOC_FRAME_OFF);
 
     // Same work split as the allocating engine, with at most 8 j-chunks.
     const int n_pad = ((num_particles + DS_JTILE - 1) / DS_JTILE) * DS_JTILE;
@@ -687,12 +767,13 @@ extern "C" int gsgpu_pairwise_acceleration_noalloc(const double *d_x, const doub
         }
     }
 
-    // The status word must start at zero; the packed array and the partial
-    // sums are fully rewritten by every call.
+    // The status word must start at zero; the frame centre, the packed array
+    // and the partial sums are fully rewritten by every call.
     e = cudaMemsetAsync(status, 0, sizeof(unsigned), s);
     if (e == cudaSuccess) {
-        k_pack_float4<<<(n_pad + 255) / 256, 256, 0, s>>>(d_x, d_m, num_particles, n_pad, 0.0,
-                                                          0.0, 0.0, pj);
+        k_noalloc_frame<<<1, NA_FRAME_THREADS, 0, s>>>(d_x, num_particles, frame);
+        k_pack_frame<<<(n_pad + 255) / 256, 256, 0, s>>>(d_x, d_m, num_particles, n_pad, frame,
+                                                         pj);
         const float eps2 = (float)(softening_length * softening_length);
         if (eps2 > 0.0f)
             k_direct_sum<true><<<i_tiles * splits, DS_THREADS, DS_SMEM, s>>>(
@@ -700,8 +781,8 @@ extern "C" int gsgpu_pairwise_acceleration_noalloc(const double *d_x, const doub
         else
             k_direct_sum<false><<<i_tiles * splits, DS_THREADS, DS_SMEM, s>>>(
                 pj, n_pad, i_tiles, jt_per_chunk, jt_total, eps2, partial, status);
-        k_reduce_splits<<<(num_particles + 255) / 256, 256, 0, s>>>(partial, splits,
-                                                                    num_particles, n_pad, G, d_a);
+        k_noalloc_reduce<<<(num_particles + 255) / 256, 256, 0, s>>>(
+            partial, splits, num_particles, n_pad, G, status, d_a);
         e = cudaGetLastError();
     }
     if (e != cudaSuccess) {

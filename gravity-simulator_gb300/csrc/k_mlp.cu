@@ -500,13 +500,9 @@ ErrorStatus MlpDevice::forward(const float *feat, int n, float *pred, cudaStream
     if (n <= 0) return ok();
     const DeviceInfo *dev = nullptr;
     GS_TRY(device_info(&dev));
-    // set once per process; a concurrent first call repeats the same setting
-    static std::atomic<bool> attr{false};
-    if (!attr.load(std::memory_order_acquire)) {
-        GS_CUDA(cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)SM_FWD_END));
-        attr.store(true, std::memory_order_release);
-    }
+    // the attribute belongs to the current device: set on every call
+    GS_CUDA(cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)SM_FWD_END));
     const int tiles = (n + MLP_TILE - 1) / MLP_TILE;
     const int grid = std::min(tiles, dev->sm_count * 2);
     k_mlp_forward<<<grid, 128, SM_FWD_END, s>>>(params.as<float>(), feat, n, pred,
@@ -520,13 +516,9 @@ ErrorStatus MlpDevice::gradients(const float *feat, const float *target, int n, 
     if (n <= 0) return ok();
     const DeviceInfo *dev = nullptr;
     GS_TRY(device_info(&dev));
-    // set once per process; a concurrent first call repeats the same setting
-    static std::atomic<bool> attr{false};
-    if (!attr.load(std::memory_order_acquire)) {
-        GS_CUDA(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)SM_TRAIN_END));
-        attr.store(true, std::memory_order_release);
-    }
+    // the attribute belongs to the current device: set on every call
+    GS_CUDA(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)SM_TRAIN_END));
     const int tiles = (n + MLP_TILE - 1) / MLP_TILE;
     const int grid = std::min(tiles, dev->sm_count);
     // mean over samples of the squared error summed over the 3 outputs

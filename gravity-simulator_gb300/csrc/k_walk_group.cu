@@ -543,15 +543,12 @@ ErrorStatus launch_bh_group_walk(const OctreeDevice &t, double theta, double eps
 {
     static_assert(sizeof(GroupShared) % 16 == 0, "group shared block alignment");
     const size_t smem = sizeof(GroupShared) * GW_WARPS;
-    // set once per process; a concurrent first call repeats the same setting
-    static std::atomic<bool> attr_set{false};
-    if (!attr_set.load(std::memory_order_acquire)) {
-        GS_CUDA(cudaFuncSetAttribute(k_bh_group<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
-        GS_CUDA(cudaFuncSetAttribute(k_bh_group<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
-        attr_set.store(true, std::memory_order_release);
-    }
+    // The attribute belongs to the current device: set on every call (cheap,
+    // host-side only, allowed during stream capture).
+    GS_CUDA(cudaFuncSetAttribute(k_bh_group<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    GS_CUDA(cudaFuncSetAttribute(k_bh_group<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
     GroupWalkArgs w;
     w.na = t.w_na.as<float4>();
     w.nb = t.w_nb.as<float4>();
@@ -576,17 +573,17 @@ ErrorStatus launch_bh_group_walk(const OctreeDevice &t, double theta, double eps
     k_group_list<<<(t.cap_nodes + 255) / 256, 256, 0, s>>>(
         t.ctr.as<int>(), t.w_nc.as<int4>(), t.t_depth.as<int>(), t.w_pa.as<float4>(),
         t.w_pb.as<float4>(), t.frame.as<double>(), t.g_list.as<int2>(), w.gctr);
-    // persistent: every SM filled once (computed once per process)
-    static std::atomic<int> grid_once{0};
-    int grid = grid_once.load(std::memory_order_acquire);
+    // persistent: every SM filled once (computed once per device)
+    const DeviceInfo *dev = nullptr;
+    GS_TRY(device_info(&dev));
+    static std::atomic<int> grid_cache[kMaxDevices];
+    int grid = grid_cache[dev->id].load(std::memory_order_acquire);
     if (grid == 0) {
-        const DeviceInfo *dev = nullptr;
-        GS_TRY(device_info(&dev));
         int per_sm = 0;
         GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bh_group<true>,
                                                               32 * GW_WARPS, smem));
         grid = dev->sm_count * (per_sm > 0 ? per_sm : 1);
-        grid_once.store(grid, std::memory_order_release);
+        grid_cache[dev->id].store(grid, std::memory_order_release);
     }
     if (t.quad)
         k_bh_group<true><<<grid, 32 * GW_WARPS, smem, s>>>(w);

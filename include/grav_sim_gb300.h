@@ -413,9 +413,12 @@ int gsgpu_device_info(char *name, int len, int *sm_count, int *cc_major,
  * embedders whose device memory is a pool they manage; real-time loops that
  * may not touch the allocator.  Computes the accelerations of
  * acceleration() with GRAV_GPU_PAIRWISE (positions taken relative to the
- * origin) from caller-owned device arrays d_x [3N], d_m [N] into d_a [3N],
- * enqueued on `stream` (a cudaStream_t; NULL = legacy default stream) and not
- * synchronised.  It calls no cudaMalloc, cudaFree or allocating library
+ * centre of their bounding box, which is found on the device) from
+ * caller-owned device arrays d_x [3N], d_m [N] into d_a [3N], enqueued on
+ * `stream` (a cudaStream_t; NULL = legacy default stream) and not
+ * synchronised.  Errors found on the device cannot be returned by a call
+ * that does not wait for the GPU: if a shared-memory tile wait of the
+ * kernel runs out, every element of d_a is NaN, never partial sums.  It calls no cudaMalloc, cudaFree or allocating library
  * routine: its scratch is a fixed device array in the library image of about
  * 6.5 MiB, which every GPU that loads the library keeps until the process
  * exits, so num_particles is limited to 1..32768 (larger counts return

@@ -7,6 +7,10 @@
  */
 #include "grav_oracle.h"
 
+#ifdef ORC_OPENMP
+#include <omp.h>
+#endif
+
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -357,79 +361,111 @@ void orc_free_tree(OrcTree *t)
  * not contain the particle and satisfies (w_c)^2 < theta^2 |R|^2 adds its
  * monopole; otherwise a leaf adds its particles (skipping the particle
  * itself) and an internal node is opened. */
+/* One particle (sorted position s) of the walk of src/acceleration_barnes_hut.c:117-247. */
+static void bh_walk_particle(int s, const double *x, const double *m, double G,
+                             double eps2, double th2, double box_length,
+                             const OrcTree *t, int compat, double *a,
+                             int64_t *counts, double *absum)
+{
+    const int id = t->sorted_indices[s];
+    const int64_t key_i = compat ? t->keys[id] : t->keys[s];
+    const double xi0 = x[3 * id + 0], xi1 = x[3 * id + 1], xi2 = x[3 * id + 2];
+    double ax = 0.0, ay = 0.0, az = 0.0, mag = 0.0;
+    int64_t n_cell = 0, n_pp = 0;
+    struct { int node; int next; } st[ORC_MORTON_MAX_LEVEL + 2];
+    int top = 0;
+    st[0].node = 0; st[0].next = 0;
+    int level = 1;
+    for (;;) {
+        const int nd = st[top].node;
+        if (st[top].next < t->num_children[nd]) {
+            const int c = t->first_child[nd] + st[top].next;
+            const int first = t->first_particle[c];
+            const int64_t key_c = compat ? t->keys[t->sorted_indices[first]]
+                                         : t->keys[first];
+            const int sh = 3 * (ORC_MORTON_MAX_LEVEL - level);
+            const int inside = (key_i >> sh) == (key_c >> sh);
+            if (!inside) {
+                const double r0 = xi0 - t->com[3 * c + 0];
+                const double r1 = xi1 - t->com[3 * c + 1];
+                const double r2 = xi2 - t->com[3 * c + 2];
+                const double bl = box_length / (double)(2 << level);
+                const double ns = r0 * r0 + r1 * r1 + r2 * r2;
+                if (bl * bl < th2 * ns) {
+                    const double rn = sqrt(ns + eps2);
+                    const double tv = G * t->mass[c] / (rn * rn * rn);
+                    ax -= tv * r0; ay -= tv * r1; az -= tv * r2;
+                    mag += fabs(tv) * sqrt(ns);
+                    ++n_cell;
+                    st[top].next++;
+                    continue;
+                }
+            }
+            if (t->num_children[c] <= 0) {
+                const int cnt = t->num_particles[c];
+                for (int q = 0; q < cnt; ++q) {
+                    const int pj = t->sorted_indices[first + q];
+                    if (pj == id) continue;
+                    const double r0 = xi0 - x[3 * pj + 0];
+                    const double r1 = xi1 - x[3 * pj + 1];
+                    const double r2 = xi2 - x[3 * pj + 2];
+                    const double rn = sqrt(r0 * r0 + r1 * r1 + r2 * r2 + eps2);
+                    const double tv = G * m[pj] / (rn * rn * rn);
+                    ax -= tv * r0; ay -= tv * r1; az -= tv * r2;
+                    mag += fabs(tv) * sqrt(r0 * r0 + r1 * r1 + r2 * r2);
+                    ++n_pp;
+                }
+                st[top].next++;
+                continue;
+            }
+            ++top;
+            st[top].node = c; st[top].next = 0;
+            ++level;
+            continue;
+        }
+        if (top == 0) break;
+        --top;
+        st[top].next++;
+        --level;
+    }
+    a[3 * id + 0] = ax; a[3 * id + 1] = ay; a[3 * id + 2] = az;
+    if (counts) { counts[2 * id] = n_cell; counts[2 * id + 1] = n_pp; }
+    if (absum) absum[id] = mag;
+}
+
 void orc_bh_walk(int n, const double *x, const double *m, double G,
                  double eps, double theta, const OrcTree *t, int compat,
                  double *a, int64_t *counts, double *absum)
 {
-    const double eps2 = eps * eps;
-    const double th2 = theta * theta;
-    const double box_length = t->box_width * 2.0;
-    for (int s = 0; s < n; ++s) {
-        const int id = t->sorted_indices[s];
-        const int64_t key_i = compat ? t->keys[id] : t->keys[s];
-        const double xi0 = x[3 * id + 0], xi1 = x[3 * id + 1], xi2 = x[3 * id + 2];
-        double ax = 0.0, ay = 0.0, az = 0.0, mag = 0.0;
-        int64_t n_cell = 0, n_pp = 0;
-        struct { int node; int next; } st[ORC_MORTON_MAX_LEVEL + 2];
-        int top = 0;
-        st[0].node = 0; st[0].next = 0;
-        int level = 1;
-        for (;;) {
-            const int nd = st[top].node;
-            if (st[top].next < t->num_children[nd]) {
-                const int c = t->first_child[nd] + st[top].next;
-                const int first = t->first_particle[c];
-                const int64_t key_c = compat ? t->keys[t->sorted_indices[first]]
-                                             : t->keys[first];
-                const int sh = 3 * (ORC_MORTON_MAX_LEVEL - level);
-                const int inside = (key_i >> sh) == (key_c >> sh);
-                if (!inside) {
-                    const double r0 = xi0 - t->com[3 * c + 0];
-                    const double r1 = xi1 - t->com[3 * c + 1];
-                    const double r2 = xi2 - t->com[3 * c + 2];
-                    const double bl = box_length / (double)(2 << level);
-                    const double ns = r0 * r0 + r1 * r1 + r2 * r2;
-                    if (bl * bl < th2 * ns) {
-                        const double rn = sqrt(ns + eps2);
-                        const double tv = G * t->mass[c] / (rn * rn * rn);
-                        ax -= tv * r0; ay -= tv * r1; az -= tv * r2;
-                        mag += fabs(tv) * sqrt(ns);
-                        ++n_cell;
-                        st[top].next++;
-                        continue;
-                    }
-                }
-                if (t->num_children[c] <= 0) {
-                    const int cnt = t->num_particles[c];
-                    for (int q = 0; q < cnt; ++q) {
-                        const int pj = t->sorted_indices[first + q];
-                        if (pj == id) continue;
-                        const double r0 = xi0 - x[3 * pj + 0];
-                        const double r1 = xi1 - x[3 * pj + 1];
-                        const double r2 = xi2 - x[3 * pj + 2];
-                        const double rn = sqrt(r0 * r0 + r1 * r1 + r2 * r2 + eps2);
-                        const double tv = G * m[pj] / (rn * rn * rn);
-                        ax -= tv * r0; ay -= tv * r1; az -= tv * r2;
-                        mag += fabs(tv) * sqrt(r0 * r0 + r1 * r1 + r2 * r2);
-                        ++n_pp;
-                    }
-                    st[top].next++;
-                    continue;
-                }
-                ++top;
-                st[top].node = c; st[top].next = 0;
-                ++level;
-                continue;
-            }
-            if (top == 0) break;
-            --top;
-            st[top].next++;
-            --level;
-        }
-        a[3 * id + 0] = ax; a[3 * id + 1] = ay; a[3 * id + 2] = az;
-        if (counts) { counts[2 * id] = n_cell; counts[2 * id + 1] = n_pp; }
-        if (absum) absum[id] = mag;
-    }
+    for (int s = 0; s < n; ++s)
+        bh_walk_particle(s, x, m, G, eps * eps, theta * theta, t->box_width * 2.0, t, compat, a,
+                         counts, absum);
+}
+
+/* The walk for `count` sorted positions offset + k * stride (a strided
+ * sample of the particles), the loop over them parallel as the reference's
+ * (`#pragma omp parallel for`, src/acceleration_barnes_hut.c:114-117) when
+ * built with ORC_OPENMP. */
+void orc_bh_walk_sample(const double *x, const double *m, double G, double eps,
+                        double theta, const OrcTree *t, int compat, int64_t offset,
+                        int64_t stride, int count, double *a)
+{
+    const double eps2 = eps * eps, th2 = theta * theta, bl = t->box_width * 2.0;
+#ifdef ORC_OPENMP
+    #pragma omp parallel for
+#endif
+    for (int k = 0; k < count; ++k)
+        bh_walk_particle((int)(offset + (int64_t)k * stride), x, m, G, eps2, th2, bl, t, compat,
+                         a, NULL, NULL);
+}
+
+int orc_num_threads(void)
+{
+#ifdef ORC_OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
 }
 
 /* Traceless quadrupole moment of every node about its centre of mass,
@@ -1496,4 +1532,38 @@ void orc_direct_rows(int n, const double *x, const double *m, double G,
         }
         a_rows[3 * r + 0] = G * ax; a_rows[3 * r + 1] = G * ay; a_rows[3 * r + 2] = G * az;
     }
+}
+
+/* Independent planetary systems run as the reference runs each alone through
+ * launch_simulation_python: WHFast (integrator 10, src/integrator_whfast.c:
+ * 200-407, invalid particles removed) or leapfrog (integrator 4,
+ * src/integrator.c:894-1121) with the massless acceleration, no softening.
+ * System s owns rows [off[s], off[s] + counts[s]); counts[s] receives its
+ * final count.  In the OpenMP build one system runs per thread at a time
+ * (the fair-share baseline of one system per core).  Returns 0, or the
+ * first non-zero code of a system. */
+int orc_ensemble_run(int S, int *counts, const int64_t *off, int *ids, double *x,
+                     double *v, double *m, double G, double dt, double tf,
+                     int integrator)
+{
+    int rc_all = 0;
+#ifdef ORC_OPENMP
+    #pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int s = 0; s < S; ++s) {
+        const int64_t o = off[s];
+        int rc;
+        if (integrator == 10)
+            rc = orc_whfast_run(&counts[s], ids + o, x + 3 * o, v + 3 * o, m + o, G, 0.0, dt, tf,
+                                1, 0);
+        else
+            rc = orc_fixed_step_run(4, 2, counts[s], x + 3 * o, v + 3 * o, m + o, G, 0.0, dt, tf);
+        if (rc) {
+#ifdef ORC_OPENMP
+            #pragma omp critical
+#endif
+            if (!rc_all) rc_all = rc;
+        }
+    }
+    return rc_all;
 }

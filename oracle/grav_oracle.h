@@ -80,6 +80,15 @@ void orc_bh_walk(int n, const double *x, const double *m, double G,
                  double eps, double theta, const OrcTree *tree, int compat,
                  double *a, int64_t *counts, double *absum);
 
+/* The walk for the sorted positions offset + k * stride, k < count (a strided
+ * sample); in the OpenMP build (liboracle_omp.so) the loop over them is
+ * parallel as the reference's (src/acceleration_barnes_hut.c:114-117). */
+void orc_bh_walk_sample(const double *x, const double *m, double G, double eps,
+                        double theta, const OrcTree *tree, int compat, int64_t offset,
+                        int64_t stride, int count, double *a);
+/* Threads the build uses (1 without OpenMP). */
+int orc_num_threads(void);
+
 /* Quadrupole extension (not in grav_sim): traceless node quadrupoles about
  * the centre of mass, q[6*node] = (xx, xy, xz, yy, yz, zz), and the
  * corrected walk with monopole + quadrupole cell terms. */
@@ -171,5 +180,12 @@ void orc_direct_rows(int n, const double *x, const double *m, double G,
  * the scale against which the rounding of FP32 pair terms is bounded. */
 void orc_abs_sum_rows(int n, const double *x, const double *m, double G,
                       double eps, int nrows, const int *rows, double *out);
+
+/* Independent systems, each run as the reference runs it alone (WHFast with
+ * removal, integrator 10, or leapfrog, integrator 4; massless acceleration,
+ * no softening); one system per thread in the OpenMP build. */
+int orc_ensemble_run(int S, int *counts, const int64_t *off, int *ids, double *x,
+                     double *v, double *m, double G, double dt, double tf,
+                     int integrator);
 
 #endif

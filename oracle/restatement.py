@@ -13,12 +13,14 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
+LIB_OMP = HERE / "_build" / "liboracle_omp.so"
 
 dp = ctypes.POINTER(ctypes.c_double)
 ip = ctypes.POINTER(ctypes.c_int32)
 lp = ctypes.POINTER(ctypes.c_int64)
 
 _lib = None
+_omp = None
 
 
 def build() -> Path:
@@ -358,3 +360,80 @@ def rel_err(a, b):
     num = np.linalg.norm(np.asarray(a) - np.asarray(b), axis=1)
     den = np.linalg.norm(np.asarray(b), axis=1)
     return num / np.where(den > 0, den, 1.0)
+
+
+def load_omp():
+    """The OpenMP build of the restatement (timing baselines only)."""
+    global _omp
+    if _omp is not None:
+        return _omp
+    load()
+    if not LIB_OMP.exists() or LIB_OMP.stat().st_mtime < LIB.stat().st_mtime:
+        build()
+    lib = ctypes.CDLL(str(LIB_OMP))
+    lib.orc_build_tree.argtypes = [ctypes.c_int, dp, dp, ctypes.c_int, ctypes.c_int,
+                                   ctypes.POINTER(OrcTree)]
+    lib.orc_free_tree.argtypes = [ctypes.POINTER(OrcTree)]
+    lib.orc_bh_walk_sample.argtypes = [dp, dp, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_double, ctypes.POINTER(OrcTree), ctypes.c_int,
+                                       ctypes.c_int64, ctypes.c_int64, ctypes.c_int, dp]
+    lib.orc_num_threads.restype = ctypes.c_int
+    lib.orc_ensemble_run.argtypes = [ctypes.c_int, ip, lp, ip, dp, dp, dp, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_double, ctypes.c_int]
+    _omp = lib
+    return lib
+
+
+def bh_cpu_timing(x, m, G, eps, theta, leaf_max, compat, target_s=10.0):
+    """Time grav_sim's Barnes-Hut (src/acceleration_barnes_hut.c:33-248) as
+    the reference runs it: the octree built serially, the walk over sorted
+    particles OpenMP-parallel.  The walk is timed on a strided sample of the
+    sorted particles sized to take about target_s seconds; returns a dict
+    with the build time, the walk time per particle, the sample size and the
+    threads used."""
+    import time
+    x, m = _c(x), _c(m)
+    n = m.size
+    lib = load_omp()
+    t = OrcTree()
+    t0 = time.perf_counter()
+    assert lib.orc_build_tree(n, _d(x), _d(m), leaf_max, int(compat), ctypes.byref(t)) == 0
+    build_s = time.perf_counter() - t0
+    a = np.zeros((n, 3))
+    try:
+        count = min(n, 4096)
+        while True:
+            stride = max(1, n // count)
+            count = min(count, (n + stride - 1) // stride)
+            t0 = time.perf_counter()
+            lib.orc_bh_walk_sample(_d(x), _d(m), G, eps, theta, ctypes.byref(t), int(compat),
+                                   stride // 2, stride, count, _d(a))
+            walk_s = time.perf_counter() - t0
+            if walk_s >= 0.25 * target_s or count >= n:
+                break
+            count = min(n, int(count * min(64.0, max(2.0, target_s / max(walk_s, 1e-3)))))
+    finally:
+        lib.orc_free_tree(ctypes.byref(t))
+    return {"build_s": build_s, "walk_s_per_particle": walk_s / count, "sample": count,
+            "walk_s": walk_s, "threads": int(lib.orc_num_threads())}
+
+
+def ensemble_cpu_timing(systems, G, dt, steps, integrator):
+    """Run the given systems (list of (x, v, m)) for `steps` steps each as
+    the reference runs each alone, one system per OpenMP thread; returns
+    (seconds, threads)."""
+    import time
+    lib = load_omp()
+    counts = np.array([s_[2].size for s_ in systems], dtype=np.int32)
+    off = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.int64)
+    ids = np.concatenate([np.arange(c, dtype=np.int32) for c in counts])
+    x = _c(np.concatenate([s_[0] for s_ in systems]))
+    v = _c(np.concatenate([s_[1] for s_ in systems]))
+    m = _c(np.concatenate([s_[2] for s_ in systems]))
+    t0 = time.perf_counter()
+    rc = lib.orc_ensemble_run(counts.size, counts.ctypes.data_as(ip), off.ctypes.data_as(lp),
+                              ids.ctypes.data_as(ip), _d(x), _d(v), _d(m), G, dt,
+                              dt * steps * (1 - 1e-9), integrator)
+    el = time.perf_counter() - t0
+    assert rc == 0, rc
+    return el, int(lib.orc_num_threads())

@@ -2,7 +2,6 @@
 include/grav_sim_gb300.h declares, lays its structs out exactly like
 grav_sim, and applies grav_sim's parameter validation on the host."""
 import ctypes
-import os
 import subprocess
 import sys
 import textwrap
@@ -68,7 +67,8 @@ def _layout(tmp_path, include_line: str, extra_flags=()):
 def test_struct_layout_matches_reference(tmp_path):
     ours = _layout(tmp_path, f'"{HEADER}"')
     assert "System 48" in ours and "AccelerationParam 32" in ours and "ErrorStatus 24" in ours
-    refsrc = Path(os.environ.get("GRAV_SIM_REFERENCE_DIR", "/root/reference")) / "src"
+    from oracle.reference import REF_DIR
+    refsrc = REF_DIR / "src"
     if not (refsrc / "linear_octree.h").exists():
         pytest.skip("reference headers not present")
     shim = tmp_path / "ref_all.h"

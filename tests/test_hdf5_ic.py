@@ -6,14 +6,13 @@ examples/galaxy_collision/galaxy_collision_IC.hdf5 through libhdf5
 parses the file itself; these tests read that file where the reference is
 present, and check that damaged or foreign files give errors, never a crash.
 """
-import os
-from pathlib import Path
 
 import numpy as np
 import pytest
 
-IC = Path(os.environ.get("GRAV_SIM_REFERENCE_DIR", "/root/reference")) / \
-    "examples" / "galaxy_collision" / "galaxy_collision_IC.hdf5"
+from oracle.reference import REF_DIR
+
+IC = REF_DIR / "examples" / "galaxy_collision" / "galaxy_collision_IC.hdf5"
 
 
 @pytest.mark.skipif(not IC.exists(), reason="reference initial conditions not present")

@@ -12,15 +12,13 @@ stops at the device check with the library's traceback; with one it must
 equal the oracle bit for bit.
 """
 import ctypes
-import os
 import sys
 import types
-from pathlib import Path
 
 import numpy as np
 import pytest
 
-REF = Path(os.environ.get("GRAV_SIM_REFERENCE_DIR", "/root/reference"))
+from oracle.reference import REF_DIR as REF
 pytestmark = pytest.mark.skipif(not (REF / "grav_sim" / "api.py").exists(),
                                 reason="grav_sim's Python package not present")
 
