@@ -154,10 +154,18 @@ class DirectRows {
     ErrorStatus compute(const double *d_x, const double *d_m, const double *d_frame,
                         const int *d_rows, int nrows, double G, double eps, double *d_a_rows,
                         cudaStream_t s, ForceTimer *timer = nullptr);
+    // Reports (and clears) a shared-memory tile wait that ran out.
+    ErrorStatus check(cudaStream_t s);
     static constexpr int kernels() { return 4; }
 
   private:
-    int nj_ = 0, nj_pad_ = 0, ni_pad_ = 0, splits_ = 1, jt_per_chunk_ = 1;
+    // j-split of a launch over i_tiles row tiles: the whole number of waves
+    // of resident CTAs that needs the fewest tiles per CTA, with at most
+    // max_splits chunks.
+    void split_for(int i_tiles, int max_splits, int *splits, int *chunk) const;
+    int nj_ = 0, nj_pad_ = 0, ni_pad_ = 0, jt_total_ = 0;
+    long slots_ = 1;
+    size_t partial_rows_ = 0;   // capacity of partial_ in (split, row) pairs
     DBuf pj_, pi_, partial_, status_;
 };
 

@@ -498,6 +498,24 @@ __global__ void k_gather_rows(const float4 *__restrict__ pj, const int *__restri
     pi[r] = r < nrows ? pj[rows[r]] : make_float4(kPadPos, kPadPos, kPadPos, 0.0f);
 }
 
+void DirectRows::split_for(int i_tiles, int max_splits, int *splits, int *chunk) const
+{
+    double best = 1e300;
+    *splits = 1;
+    *chunk = jt_total_;
+    for (int s = 1; s <= std::min(jt_total_, max_splits); ++s) {
+        const int c = (jt_total_ + s - 1) / s;
+        const int used = (jt_total_ + c - 1) / c;
+        const long units = (long)i_tiles * used;
+        const double cost = (double)((units + slots_ - 1) / slots_) * (c + 0.25);
+        if (cost < best - 1e-9) {
+            best = cost;
+            *splits = used;
+            *chunk = c;
+        }
+    }
+}
+
 ErrorStatus DirectRows::setup(int nj, int max_rows)
 {
     const DeviceInfo *dev = nullptr;
@@ -505,8 +523,7 @@ ErrorStatus DirectRows::setup(int nj, int max_rows)
     nj_ = nj;
     nj_pad_ = ((nj + DS_JTILE - 1) / DS_JTILE) * DS_JTILE;
     ni_pad_ = ((max_rows + DS_ITILE - 1) / DS_ITILE) * DS_ITILE;
-    const int jt_total = nj_pad_ / DS_JTILE;
-    const int i_tiles = ni_pad_ / DS_ITILE;
+    jt_total_ = nj_pad_ / DS_JTILE;
     int per_sm = 0;
     GS_CUDA(cudaFuncSetAttribute(k_direct_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  DS_SMEM));
@@ -514,22 +531,17 @@ ErrorStatus DirectRows::setup(int nj, int max_rows)
                                  DS_SMEM));
     GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_direct_rows<true>, DS_THREADS,
                                                           DS_SMEM));
-    const long slots = (long)dev->sm_count * std::max(per_sm, 1);
-    double best = 1e300;
-    for (int s = 1; s <= std::min(jt_total, 128); ++s) {
-        const int chunk = (jt_total + s - 1) / s;
-        const int used = (jt_total + chunk - 1) / chunk;
-        const long units = (long)i_tiles * used;
-        const double cost = (double)((units + slots - 1) / slots) * (chunk + 0.25);
-        if (cost < best - 1e-9) {
-            best = cost;
-            splits_ = used;
-            jt_per_chunk_ = chunk;
-        }
-    }
+    slots_ = (long)dev->sm_count * std::max(per_sm, 1);
+    // Partial sums sized for the largest launch and for a launch of a single
+    // row tile, which splits the j range most finely.
+    int sp = 1, ch = 1;
+    split_for(ni_pad_ / DS_ITILE, 128, &sp, &ch);
+    partial_rows_ = (size_t)sp * ni_pad_;
+    split_for(1, 128, &sp, &ch);
+    partial_rows_ = std::max(partial_rows_, (size_t)sp * DS_ITILE);
     GS_TRY(pj_.reserve((size_t)nj_pad_ * sizeof(float4)));
     GS_TRY(pi_.reserve((size_t)ni_pad_ * sizeof(float4)));
-    GS_TRY(partial_.reserve((size_t)splits_ * 3 * ni_pad_ * sizeof(double)));
+    GS_TRY(partial_.reserve(partial_rows_ * 3 * sizeof(double)));
     GS_TRY(status_.reserve(sizeof(unsigned)));
     GS_CUDA(cudaMemset(status_.p, 0, sizeof(unsigned)));
     return ok();
@@ -549,20 +561,36 @@ ErrorStatus DirectRows::compute(const double *d_x, const double *d_m, const doub
                                                        pi_.as<float4>());
     const float eps2 = (float)(eps * eps);
     const int i_tiles = nr_pad / DS_ITILE;
-    const int jt_total = nj_pad_ / DS_JTILE;
+    // the split is chosen for this launch's row count (few rows: many
+    // j-chunks, so that the launch still fills every SM)
+    int splits = 1, chunk = jt_total_;
+    split_for(i_tiles, (int)std::min<size_t>(128, partial_rows_ / nr_pad), &splits, &chunk);
     if (timer) GS_TRY(timer->begin(s));
     if (eps2 > 0.0f)
-        k_direct_rows<true><<<i_tiles * splits_, DS_THREADS, DS_SMEM, s>>>(
-            pi_.as<float4>(), ni_pad_, pj_.as<float4>(), i_tiles, jt_per_chunk_, jt_total, eps2,
+        k_direct_rows<true><<<i_tiles * splits, DS_THREADS, DS_SMEM, s>>>(
+            pi_.as<float4>(), nr_pad, pj_.as<float4>(), i_tiles, chunk, jt_total_, eps2,
             partial_.as<double>(), status_.as<unsigned>());
     else
-        k_direct_rows<false><<<i_tiles * splits_, DS_THREADS, DS_SMEM, s>>>(
-            pi_.as<float4>(), ni_pad_, pj_.as<float4>(), i_tiles, jt_per_chunk_, jt_total, eps2,
+        k_direct_rows<false><<<i_tiles * splits, DS_THREADS, DS_SMEM, s>>>(
+            pi_.as<float4>(), nr_pad, pj_.as<float4>(), i_tiles, chunk, jt_total_, eps2,
             partial_.as<double>(), status_.as<unsigned>());
     if (timer) GS_TRY(timer->end(s));
-    k_reduce_splits<<<(nrows + 255) / 256, 256, 0, s>>>(partial_.as<double>(), splits_, nrows,
-                                                        ni_pad_, G, d_a_rows);
+    k_reduce_splits<<<(nrows + 255) / 256, 256, 0, s>>>(partial_.as<double>(), splits, nrows,
+                                                        nr_pad, G, d_a_rows);
     GS_CUDA(cudaGetLastError());
+    return ok();
+}
+
+ErrorStatus DirectRows::check(cudaStream_t s)
+{
+    unsigned h = 0;
+    GS_CUDA(cudaMemcpyAsync(&h, status_.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    GS_CUDA(cudaStreamSynchronize(s));
+    if (h) {
+        GS_CUDA(cudaMemsetAsync(status_.p, 0, sizeof(unsigned), s));
+        if (h & ST_WAIT_TIMEOUT)
+            return GS_RAISE(GRAV_FAILURE, "direct-sum rows kernel: shared-memory tile wait timed out");
+    }
     return ok();
 }
 

@@ -15,6 +15,9 @@
 //   training     after the last snapshot, the network is trained on the GPU
 //                by its own tcgen05 forward / backward kernels and Adam; the
 //                last snapshot is held out to measure what the network gains;
+//                the network is used only if it cuts the held-out median
+//                residual by 20 % and brings it within the judge's bound,
+//                else every step runs the judged fallback walk;
 //   inference    cheap walk + features + network + correction, then a judge:
 //                the direct sum of 4,096 particles (a different sample each
 //                step) gives their exact accelerations; when the median
@@ -24,13 +27,23 @@
 // Inference is graph-capturable (the fallback is a gated launch, not a host
 // decision).
 //
-// Features (sorted particle s, its leaf L and the leaf's parent P, cell
-// widths hL and hP = 2 hL, x the particle position, c / M / Q the centre of
-// mass, mass and traceless quadrupole of a node):
-//   0-2  (x - c_L) / hL           3  M_L / M_P          4-6  (c_L - c_P) / hP
-//   7-12 Q_L / (M_L hL^2)        13  ln(M_P / m) / 10  14-16 (x - c_P) / hP
+// Features (sorted particle s, its leaf L, the leaf's parent P and
+// grandparent GP, cell widths hL and hP = 2 hL, x the particle position,
+// c / M / Q the centre of mass, mass and traceless quadrupole of a node,
+// a_c the cheap walk's acceleration of the particle):
+//   0-2  (x - c_L) / hL           3  M_L / M_P          4-6  a_c / |a_c|
+//   7-12 Q_L / (M_L hL^2)        13  ln(M_P / m) / 10
+//  14    log10(|a_c| hP^2 / (G M_P)) / 5     (far field against the parent's)
+//  15    log10(M_GP / M_P) / 3               (density change one level up)
+//  16    log10(|a_c| W^2 / (G M_root)) / 5   (far field in units of the box
+//                                             width W and the total mass)
 //  17-22 Q_P / (M_P hP^2)        23  log10(M_P / hP^3) / 5
-//  24-31 |x - c_k| / hP for the children k of P in octant order (0 if absent)
+//  24-31 distances |x - c_k| / hP to the 8 nearest cells k, ascending: the
+//        cells are the nodes under GP at the leaf's depth, and the leaves
+//        under GP one level above it, other than L itself (4 where there
+//        are fewer than 8).
+// Features 4-6, 14 and 16 carry the far field (the cheap walk's force, its
+// direction and its size against the local and the global scale).
 #include "gs_mlp.h"
 #include "gs_octree.h"
 #include "gs_ptx.cuh"
@@ -57,6 +70,9 @@ constexpr int kEpochs = 24;
 // The network is used only if it brings the held-out median residual below
 // this fraction of the cheap walk's; otherwise the engine runs the fallback.
 constexpr double kMinGain = 0.8;
+// Training targets are clamped to +-1 % of |a_cheap| (in target units); the
+// held-out snapshot keeps its exact residuals.
+constexpr float kTargetClip = 1.0f;
 
 }  // namespace
 
@@ -67,7 +83,8 @@ __global__ void k_features(const int *__restrict__ ctr, int count, const int *__
                            const int *__restrict__ t_depth, const double *__restrict__ t_mass,
                            const double *__restrict__ t_com, const float4 *__restrict__ nq,
                            const double *__restrict__ frame, const double *__restrict__ x,
-                           const double *__restrict__ m, float *__restrict__ feat)
+                           const double *__restrict__ m, const double *__restrict__ a_cheap,
+                           double G, float *__restrict__ feat)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= count || tree_failed(ctr)) return;
@@ -76,7 +93,10 @@ __global__ void k_features(const int *__restrict__ ctr, int count, const int *__
     const int L = leaf_of[s];
     int P = t_parent[L];
     if (P < 0) P = L;
-    const double hL = frame[3] / (double)(1 << min(t_depth[L], 30));
+    int GP = t_parent[P];
+    if (GP < 0) GP = P;
+    const int dL = t_depth[L];
+    const double hL = frame[3] / (double)(1 << min(dL, 30));
     const double hP = 2.0 * hL;
     const double x0 = x[3 * id], x1 = x[3 * id + 1], x2 = x[3 * id + 2];
     const double *cL = t_com + 3 * (size_t)L;
@@ -91,27 +111,54 @@ __global__ void k_features(const int *__restrict__ ctr, int count, const int *__
     f[1] = (float)((x1 - cL[1]) / hL);
     f[2] = (float)((x2 - cL[2]) / hL);
     f[3] = (float)(ML / MP);
-    f[4] = (float)((cL[0] - cP[0]) / hP);
-    f[5] = (float)((cL[1] - cP[1]) / hP);
-    f[6] = (float)((cL[2] - cP[2]) / hP);
+    const double a0 = a_cheap[3 * id], a1 = a_cheap[3 * id + 1], a2 = a_cheap[3 * id + 2];
+    const double am = sqrt(a0 * a0 + a1 * a1 + a2 * a2);
+    const double ia = am > 0.0 ? 1.0 / am : 0.0;
+    f[4] = (float)(a0 * ia);
+    f[5] = (float)(a1 * ia);
+    f[6] = (float)(a2 * ia);
     const double nL = 1.0 / (ML * hL * hL), nP = 1.0 / (MP * hP * hP);
     for (int q = 0; q < 6; ++q) f[7 + q] = (float)(QL[q] * nL);
     f[13] = m[id] > 0.0 ? (float)(log(MP / m[id]) / 10.0) : 0.0f;
-    f[14] = (float)((x0 - cP[0]) / hP);
-    f[15] = (float)((x1 - cP[1]) / hP);
-    f[16] = (float)((x2 - cP[2]) / hP);
+    const double tiny = 1e-300;
+    const double W = frame[3], Mroot = fmax(t_mass[0], tiny);
+    f[14] = (float)(log10(fmax(am * hP * hP / (G * MP), tiny)) / 5.0);
+    f[15] = GP != P ? (float)(log10(fmax(t_mass[GP], tiny) / MP) / 3.0) : 0.0f;
+    f[16] = (float)(log10(fmax(am * W * W / (G * Mroot), tiny)) / 5.0);
     for (int q = 0; q < 6; ++q) f[17 + q] = (float)(QP[q] * nP);
     f[23] = (float)(log10(MP / (hP * hP * hP)) / 5.0);
-    const int nc = t_nc[P], fc = t_fc[P];
-    for (int c = 0; c < 8; ++c) {
-        float d = 0.0f;
-        if (c < nc) {
-            const double *cc = t_com + 3 * (size_t)(fc + c);
-            const double d0 = x0 - cc[0], d1 = x1 - cc[1], d2 = x2 - cc[2];
-            d = (float)(sqrt(d0 * d0 + d1 * d1 + d2 * d2) / hP);
+    // the 8 nearest cells under GP (insertion into an ascending list)
+    float near[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) near[c] = 4.0f;
+    const double ihP = 1.0 / hP;
+    auto consider = [&](int node) {
+        if (node == L) return;
+        const double *cc = t_com + 3 * (size_t)node;
+        const double d0 = x0 - cc[0], d1 = x1 - cc[1], d2 = x2 - cc[2];
+        const float d = (float)(sqrt(d0 * d0 + d1 * d1 + d2 * d2) * ihP);
+        if (!(d < near[7])) return;
+        // slots above the insertion point shift up, the slot at it takes d
+#pragma unroll
+        for (int c = 7; c > 0; --c)
+            near[c] = d < near[c - 1] ? near[c - 1] : (d < near[c] ? d : near[c]);
+        near[0] = d < near[0] ? d : near[0];
+    };
+    if (GP != L) {
+        const int nc = t_nc[GP], fc = t_fc[GP];
+        for (int c = 0; c < nc; ++c) {
+            const int u = fc + c;
+            const int nu = t_nc[u];
+            if (nu <= 0 || t_depth[u] >= dL) {
+                consider(u);
+                continue;
+            }
+            const int fu = t_fc[u];
+            for (int q = 0; q < nu; ++q) consider(fu + q);
         }
-        f[24 + c] = d;
     }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) f[24 + c] = near[c];
     float4 *out = reinterpret_cast<float4 *>(feat + (size_t)k * MLP_IN);
 #pragma unroll
     for (int q = 0; q < MLP_IN / 4; ++q)
@@ -133,9 +180,11 @@ __global__ void k_sample(int count, int n, long long offset, long long stride,
     ids[k] = sidx[s];
 }
 
-// target = 100 (a_direct - a_cheap) / |a_cheap|
+// target = 100 (a_direct - a_cheap) / |a_cheap|, each component clamped to
+// [-clip, clip]: the squared loss is then not dominated by the few particles
+// whose residual is far above the median the method is judged on.
 __global__ void k_targets(int count, const int *__restrict__ ids, const double *__restrict__ a_cheap,
-                          const double *__restrict__ a_exact, float *__restrict__ target)
+                          const double *__restrict__ a_exact, float clip, float *__restrict__ target)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= count) return;
@@ -143,9 +192,9 @@ __global__ void k_targets(int count, const int *__restrict__ ids, const double *
     const double c0 = a_cheap[3 * id], c1 = a_cheap[3 * id + 1], c2 = a_cheap[3 * id + 2];
     const double mag = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
     const double inv = mag > 0.0 ? kResidualScale / mag : 0.0;
-    target[3 * k] = (float)((a_exact[3 * k] - c0) * inv);
-    target[3 * k + 1] = (float)((a_exact[3 * k + 1] - c1) * inv);
-    target[3 * k + 2] = (float)((a_exact[3 * k + 2] - c2) * inv);
+    target[3 * k] = fminf(fmaxf((float)((a_exact[3 * k] - c0) * inv), -clip), clip);
+    target[3 * k + 1] = fminf(fmaxf((float)((a_exact[3 * k + 1] - c1) * inv), -clip), clip);
+    target[3 * k + 2] = fminf(fmaxf((float)((a_exact[3 * k + 2] - c2) * inv), -clip), clip);
 }
 
 // a += |a| pred / 100 (pred in sorted order)
@@ -290,7 +339,7 @@ class LearnedEngine final : public Engine {
         if (timer) GS_TRY(timer->begin(s));
         GS_TRY(launch_bh_group_walk(tree_, theta_, eps_, G_, d_a, cnt, s));
         if (timer) GS_TRY(timer->end(s));
-        GS_TRY(features(nullptr, n_, feat_.as<float>(), d_x, d_m, s));
+        GS_TRY(features(nullptr, n_, feat_.as<float>(), d_x, d_m, d_a, s));
         GS_TRY(mlp_.forward(feat_.as<float>(), n_, pred_.as<float>(), s));
         k_correct<<<(n_ + 255) / 256, 256, 0, s>>>(n_, tree_.sidx.as<int>(), pred_.as<float>(), d_a);
         GS_TRY(judge(d_x, d_m, d_a, s));
@@ -319,6 +368,7 @@ class LearnedEngine final : public Engine {
         if (st & ST_STACK_OVERFLOW)
             return GS_RAISE(GRAV_FAILURE, "tree walk deeper than the octree depth limit");
         GS_TRY(mlp_.check(s));
+        GS_TRY(rows_.check(s));
         return ok();
     }
 
@@ -380,13 +430,13 @@ class LearnedEngine final : public Engine {
     }
 
     ErrorStatus features(const int *pos, int count, float *out, const double *d_x,
-                         const double *d_m, cudaStream_t s)
+                         const double *d_m, const double *a_cheap, cudaStream_t s)
     {
         k_features<<<(count + 127) / 128, 128, 0, s>>>(
             tree_.ctr.as<int>(), count, pos, tree_.sidx.as<int>(), tree_.leaf_of.as<int>(), tree_.t_parent.as<int>(),
             tree_.t_nc.as<int>(), tree_.t_fc.as<int>(), tree_.t_depth.as<int>(),
             tree_.t_mass.as<double>(), tree_.t_com.as<double>(), tree_.w_nq.as<float4>(),
-            tree_.frame.as<double>(), d_x, d_m, out);
+            tree_.frame.as<double>(), d_x, d_m, a_cheap, G_, out);
         GS_CUDA(cudaGetLastError());
         return ok();
     }
@@ -407,9 +457,10 @@ class LearnedEngine final : public Engine {
                              a_rows_.as<double>(), s));
         float *f = data_feat_.as<float>() + (size_t)snapshots_ * K_ * MLP_IN;
         float *t = data_target_.as<float>() + (size_t)snapshots_ * K_ * MLP_OUT;
-        GS_TRY(features(pos_.as<int>(), K_, f, d_x, d_m, s));
+        GS_TRY(features(pos_.as<int>(), K_, f, d_x, d_m, a_cheap_.as<double>(), s));
+        const float clip = snapshots_ + 1 < kSnapshots ? kTargetClip : 3.0e38f;
         k_targets<<<(K_ + 255) / 256, 256, 0, s>>>(K_, ids_.as<int>(), a_cheap_.as<double>(),
-                                                   a_rows_.as<double>(), t);
+                                                   a_rows_.as<double>(), clip, t);
         GS_CUDA(cudaGetLastError());
         ++snapshots_;
         return ok();
@@ -473,7 +524,11 @@ class LearnedEngine final : public Engine {
         adam_steps_ = step;
         GS_TRY(mlp_.check(s));
         GS_TRY(holdout(s, &hold_before_, &hold_after_));
-        useful_ = hold_after_ < kMinGain * hold_before_;
+        // Use the network only where it can pay: it must cut the held-out
+        // median residual by at least 1 - kMinGain, and the corrected median
+        // must pass the judge's bound (else every step would fall back after
+        // paying for the cheap walk and the network as well).
+        useful_ = hold_after_ < kMinGain * hold_before_ && hold_after_ <= kJudgeTol;
         train_seconds_ =
             std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         trained_ = true;
@@ -490,7 +545,7 @@ class LearnedEngine final : public Engine {
         counters_;
     int snapshots_ = 0;
     bool trained_ = false;
-    bool useful_ = false;   // network kept: it cut the held-out residual by >= 1 - kMinGain
+    bool useful_ = false;   // network kept (gain >= 1 - kMinGain, corrected median <= 1e-3)
     int adam_steps_ = 0;
     double loss_first_ = 0.0, loss_last_ = 0.0, hold_before_ = 0.0, hold_after_ = 0.0;
     double train_seconds_ = 0.0;

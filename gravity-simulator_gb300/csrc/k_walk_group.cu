@@ -142,47 +142,68 @@ struct GroupWalkArgs {
     int *gctr;              // [0] groups, [1] work-queue head
 };
 
-// Lists as structure of arrays, so that entries (j, j+1) load as float2
-// pairs and are evaluated together by paired FP32 operations.
+// Lists hold their entries in pairs: pair k is entries (2k, 2k+1), and each
+// float4 carries two fields of both entries side by side, so that one
+// 16-byte shared load gives two fields of the pair in the register pairs the
+// paired FP32 operations read (half the loads of one float2 per field).
 struct GroupShared {
     int stack[GW_STACK];
-    float cx[GW_CELLS], cy[GW_CELLS], cz[GW_CELLS], cm[GW_CELLS];
-    float qxx[GW_CELLS], qxy[GW_CELLS], qxz[GW_CELLS], qyy[GW_CELLS], qyz[GW_CELLS], qzz[GW_CELLS];
-    float px[GW_PARTS], py[GW_PARTS], pz[GW_PARTS], pm[GW_PARTS];
+    float4 cA[GW_CELLS / 2];   // (x, x', y, y')        cell centre of mass
+    float4 cB[GW_CELLS / 2];   // (z, z', m, m')        and mass
+    float4 qA[GW_CELLS / 2];   // (xx, xx', xy, xy')    negated quadrupole
+    float4 qB[GW_CELLS / 2];   // (xz, xz', yy, yy')
+    float4 qC[GW_CELLS / 2];   // (yz, yz', zz, zz')
+    float4 pA[GW_PARTS / 2];   // (x, x', y, y')        leaf particles
+    float4 pB[GW_PARTS / 2];   // (z, z', m, m')
 };
+static_assert(GW_CELLS % 2 == 0 && GW_PARTS % 2 == 0, "lists hold whole pairs");
 
-__device__ __forceinline__ float2 ld2(const float *a, int j)
+// Field f (0: the float4's first two lanes, 1: its last two) of entry j.
+__device__ __forceinline__ void put(float4 *arr, int j, int f, float v)
 {
-    return *reinterpret_cast<const float2 *>(a + j);
+    reinterpret_cast<float *>(arr)[(j >> 1) * 4 + 2 * f + (j & 1)] = v;
 }
+
+__device__ __forceinline__ float get(const float4 *arr, int j, int f)
+{
+    return reinterpret_cast<const float *>(arr)[(j >> 1) * 4 + 2 * f + (j & 1)];
+}
+
+__device__ __forceinline__ float2 lo2(const float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(const float4 v) { return make_float2(v.z, v.w); }
 
 __device__ __forceinline__ float2 splat(float v) { return make_float2(v, v); }
 
 // One cell term (monopole + optional quadrupole) for a lane's particle.
+// The lists hold the negated quadrupole P = -Q; with d = com - x:
+//     a = d [m / r^3 - 2.5 (d.P.d) / r^7] + P d / r^5
+// (the monopole plus G [-Q d / r^5 + 2.5 (d.Q.d) d / r^7], G applied last).
 template <bool QUAD>
 __device__ __forceinline__ void cell_term1(const GroupShared &g, int j, float rx, float ry, float rz,
                                            float eps2, float &ax, float &ay, float &az)
 {
-    const float dx = g.cx[j] - rx, dy = g.cy[j] - ry, dz = g.cz[j] - rz;
+    const float dx = get(g.cA, j, 0) - rx, dy = get(g.cA, j, 1) - ry, dz = get(g.cB, j, 0) - rz;
     const float ns = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     const float ri = rsqrt_approx(ns + eps2);
     const float ri2 = ri * ri;
     const float ri3 = ri2 * ri;
-    const float sc = g.cm[j] * ri3;
-    ax = fmaf(dx, sc, ax);
-    ay = fmaf(dy, sc, ay);
-    az = fmaf(dz, sc, az);
+    float sc = get(g.cB, j, 1) * ri3;
     if (QUAD) {
-        // d = com - x:  G [-Q d / r^5 + 2.5 (d.Q.d) d / r^7]
-        const float qx = fmaf(g.qxx[j], dx, fmaf(g.qxy[j], dy, g.qxz[j] * dz));
-        const float qy = fmaf(g.qxy[j], dx, fmaf(g.qyy[j], dy, g.qyz[j] * dz));
-        const float qz = fmaf(g.qxz[j], dx, fmaf(g.qyz[j], dy, g.qzz[j] * dz));
-        const float dqd = fmaf(dx, qx, fmaf(dy, qy, dz * qz));
+        const float xx = get(g.qA, j, 0), xy = get(g.qA, j, 1), xz = get(g.qB, j, 0);
+        const float yy = get(g.qB, j, 1), yz = get(g.qC, j, 0), zz = get(g.qC, j, 1);
+        const float px = fmaf(xx, dx, fmaf(xy, dy, xz * dz));
+        const float py = fmaf(xy, dx, fmaf(yy, dy, yz * dz));
+        const float pz = fmaf(xz, dx, fmaf(yz, dy, zz * dz));
+        const float dpd = fmaf(dx, px, fmaf(dy, py, dz * pz));
         const float ri5 = ri3 * ri2;
-        const float f = 2.5f * dqd * (ri5 * ri2);
-        ax = fmaf(f, dx, fmaf(-qx, ri5, ax));
-        ay = fmaf(f, dy, fmaf(-qy, ri5, ay));
-        az = fmaf(f, dz, fmaf(-qz, ri5, az));
+        sc = fmaf(-2.5f, dpd * (ri5 * ri2), sc);
+        ax = fmaf(dx, sc, fmaf(px, ri5, ax));
+        ay = fmaf(dy, sc, fmaf(py, ri5, ay));
+        az = fmaf(dz, sc, fmaf(pz, ri5, az));
+    } else {
+        ax = fmaf(dx, sc, ax);
+        ay = fmaf(dy, sc, ay);
+        az = fmaf(dz, sc, az);
     }
 }
 
@@ -196,30 +217,33 @@ __device__ __forceinline__ void flush_cells(const GroupShared &g, int count, flo
     int j = 0;
 #pragma unroll 4
     for (; j + 1 < count; j += 2) {
-        const float2 dx = __fadd2_rn(ld2(g.cx, j), nrx);
-        const float2 dy = __fadd2_rn(ld2(g.cy, j), nry);
-        const float2 dz = __fadd2_rn(ld2(g.cz, j), nrz);
+        const float4 ca = g.cA[j >> 1], cb = g.cB[j >> 1];
+        const float2 dx = __fadd2_rn(lo2(ca), nrx);
+        const float2 dy = __fadd2_rn(hi2(ca), nry);
+        const float2 dz = __fadd2_rn(lo2(cb), nrz);
         const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
         const float2 ri = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
         const float2 ri2 = __fmul2_rn(ri, ri);
         const float2 ri3 = __fmul2_rn(ri2, ri);
-        const float2 sc = __fmul2_rn(ld2(g.cm, j), ri3);
-        ax = __ffma2_rn(dx, sc, ax);
-        ay = __ffma2_rn(dy, sc, ay);
-        az = __ffma2_rn(dz, sc, az);
+        float2 sc = __fmul2_rn(hi2(cb), ri3);
         if (QUAD) {
-            const float2 xx = ld2(g.qxx, j), xy = ld2(g.qxy, j), xz = ld2(g.qxz, j);
-            const float2 yy = ld2(g.qyy, j), yz = ld2(g.qyz, j), zz = ld2(g.qzz, j);
-            const float2 qx = __ffma2_rn(xx, dx, __ffma2_rn(xy, dy, __fmul2_rn(xz, dz)));
-            const float2 qy = __ffma2_rn(xy, dx, __ffma2_rn(yy, dy, __fmul2_rn(yz, dz)));
-            const float2 qz = __ffma2_rn(xz, dx, __ffma2_rn(yz, dy, __fmul2_rn(zz, dz)));
-            const float2 dqd = __ffma2_rn(dx, qx, __ffma2_rn(dy, qy, __fmul2_rn(dz, qz)));
+            // negated quadrupole P (see cell_term1)
+            const float4 qa = g.qA[j >> 1], qb = g.qB[j >> 1], qc = g.qC[j >> 1];
+            const float2 xx = lo2(qa), xy = hi2(qa), xz = lo2(qb);
+            const float2 yy = hi2(qb), yz = lo2(qc), zz = hi2(qc);
+            const float2 px = __ffma2_rn(xx, dx, __ffma2_rn(xy, dy, __fmul2_rn(xz, dz)));
+            const float2 py = __ffma2_rn(xy, dx, __ffma2_rn(yy, dy, __fmul2_rn(yz, dz)));
+            const float2 pz = __ffma2_rn(xz, dx, __ffma2_rn(yz, dy, __fmul2_rn(zz, dz)));
+            const float2 dpd = __ffma2_rn(dx, px, __ffma2_rn(dy, py, __fmul2_rn(dz, pz)));
             const float2 ri5 = __fmul2_rn(ri3, ri2);
-            const float2 nri5 = __fmul2_rn(ri5, splat(-1.0f));
-            const float2 f = __fmul2_rn(__fmul2_rn(splat(2.5f), dqd), __fmul2_rn(ri5, ri2));
-            ax = __ffma2_rn(f, dx, __ffma2_rn(qx, nri5, ax));
-            ay = __ffma2_rn(f, dy, __ffma2_rn(qy, nri5, ay));
-            az = __ffma2_rn(f, dz, __ffma2_rn(qz, nri5, az));
+            sc = __ffma2_rn(splat(-2.5f), __fmul2_rn(dpd, __fmul2_rn(ri5, ri2)), sc);
+            ax = __ffma2_rn(dx, sc, __ffma2_rn(px, ri5, ax));
+            ay = __ffma2_rn(dy, sc, __ffma2_rn(py, ri5, ay));
+            az = __ffma2_rn(dz, sc, __ffma2_rn(pz, ri5, az));
+        } else {
+            ax = __ffma2_rn(dx, sc, ax);
+            ay = __ffma2_rn(dy, sc, ay);
+            az = __ffma2_rn(dz, sc, az);
         }
     }
     float tx = ax.x + ax.y, ty = ay.x + ay.y, tz = az.x + az.y;
@@ -229,6 +253,10 @@ __device__ __forceinline__ void flush_cells(const GroupShared &g, int count, flo
     kahan_add(sz, cz, tz);
 }
 
+// Leaf particles.  With softening every r^2 >= eps^2 > 0 and the particle's
+// own term is 0 by its zero offset; without it the own term (r^2 = 0) is
+// skipped explicitly.
+template <bool SOFT>
 __device__ __forceinline__ void flush_parts(const GroupShared &g, int count, float rx, float ry,
                                             float rz, float eps2, float &sx, float &cx, float &sy,
                                             float &cy, float &sz, float &cz)
@@ -238,24 +266,27 @@ __device__ __forceinline__ void flush_parts(const GroupShared &g, int count, flo
     int j = 0;
 #pragma unroll 4
     for (; j + 1 < count; j += 2) {
-        const float2 dx = __fadd2_rn(ld2(g.px, j), nrx);
-        const float2 dy = __fadd2_rn(ld2(g.py, j), nry);
-        const float2 dz = __fadd2_rn(ld2(g.pz, j), nrz);
+        const float4 pa = g.pA[j >> 1], pb = g.pB[j >> 1];
+        const float2 dx = __fadd2_rn(lo2(pa), nrx);
+        const float2 dy = __fadd2_rn(hi2(pa), nry);
+        const float2 dz = __fadd2_rn(lo2(pb), nrz);
         const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, e2)));
-        // own term without softening: r2 = 0 contributes nothing
-        const float2 ri = make_float2(r2.x > 0.0f ? rsqrt_approx(r2.x) : 0.0f,
-                                      r2.y > 0.0f ? rsqrt_approx(r2.y) : 0.0f);
-        const float2 sc = __fmul2_rn(ld2(g.pm, j), __fmul2_rn(__fmul2_rn(ri, ri), ri));
+        float2 ri = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+        if (!SOFT) {   // own term without softening: r2 = 0 contributes nothing
+            ri.x = r2.x > 0.0f ? ri.x : 0.0f;
+            ri.y = r2.y > 0.0f ? ri.y : 0.0f;
+        }
+        const float2 sc = __fmul2_rn(hi2(pb), __fmul2_rn(__fmul2_rn(ri, ri), ri));
         ax = __ffma2_rn(dx, sc, ax);
         ay = __ffma2_rn(dy, sc, ay);
         az = __ffma2_rn(dz, sc, az);
     }
     float tx = ax.x + ax.y, ty = ay.x + ay.y, tz = az.x + az.y;
     if (j < count) {
-        const float dx = g.px[j] - rx, dy = g.py[j] - ry, dz = g.pz[j] - rz;
+        const float dx = get(g.pA, j, 0) - rx, dy = get(g.pA, j, 1) - ry, dz = get(g.pB, j, 0) - rz;
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-        const float ri = r2 > 0.0f ? rsqrt_approx(r2) : 0.0f;
-        const float sc = g.pm[j] * ri * ri * ri;
+        const float ri = (SOFT || r2 > 0.0f) ? rsqrt_approx(r2) : 0.0f;
+        const float sc = get(g.pB, j, 1) * ri * ri * ri;
         tx = fmaf(dx, sc, tx);
         ty = fmaf(dy, sc, ty);
         tz = fmaf(dz, sc, tz);
@@ -266,7 +297,7 @@ __device__ __forceinline__ void flush_parts(const GroupShared &g, int count, flo
 }
 
 // Walk of one group: sorted particles [g0, gend) on lanes 0..gend-g0-1.
-template <bool QUAD>
+template <bool QUAD, bool SOFT>
 __device__ void walk_group(const GroupWalkArgs &A, GroupShared &g, const float *s_w2, int lane,
                            int g0, int gend)
 {
@@ -348,17 +379,17 @@ __device__ void walk_group(const GroupWalkArgs &A, GroupShared &g, const float *
             }
             if (act == 1) {
                 const int at = ncell + __popc(acc & ((1u << lane) - 1u));
-                g.cx[at] = crel.x;
-                g.cy[at] = crel.y;
-                g.cz[at] = crel.z;
-                g.cm[at] = crel.w;
-                if (QUAD) {
-                    g.qxx[at] = q0.x;
-                    g.qxy[at] = q0.y;
-                    g.qxz[at] = q0.z;
-                    g.qyy[at] = q0.w;
-                    g.qyz[at] = q1.x;
-                    g.qzz[at] = q1.y;
+                put(g.cA, at, 0, crel.x);
+                put(g.cA, at, 1, crel.y);
+                put(g.cB, at, 0, crel.z);
+                put(g.cB, at, 1, crel.w);
+                if (QUAD) {   // negated, as the evaluation expects
+                    put(g.qA, at, 0, -q0.x);
+                    put(g.qA, at, 1, -q0.y);
+                    put(g.qB, at, 0, -q0.z);
+                    put(g.qB, at, 1, -q0.w);
+                    put(g.qC, at, 0, -q1.x);
+                    put(g.qC, at, 1, -q1.y);
                 }
             }
             ncell += __popc(acc);
@@ -375,7 +406,7 @@ __device__ void walk_group(const GroupWalkArgs &A, GroupShared &g, const float *
             if (total <= GW_PARTS) {
                 if (npart + total > GW_PARTS) {
                     __syncwarp();
-                    if (valid) flush_parts(g, npart, rx, ry, rz, A.eps2, sx, cx, sy, cy, sz, cz);
+                    if (valid) flush_parts<SOFT>(g, npart, rx, ry, rz, A.eps2, sx, cx, sy, cy, sz, cz);
                     n_pp += valid ? npart : 0;
                     npart = 0;
                     __syncwarp();
@@ -399,10 +430,10 @@ __device__ void walk_group(const GroupWalkArgs &A, GroupShared &g, const float *
                         const int p = first + off;
                         const float4 qa = A.pa[p], qb = A.pb[p];
                         const int at = npart + t;
-                        g.px[at] = (qa.x - oh.x) + (qb.x - ol.x);
-                        g.py[at] = (qa.y - oh.y) + (qb.y - ol.y);
-                        g.pz[at] = (qa.z - oh.z) + (qb.z - ol.z);
-                        g.pm[at] = qa.w;
+                        put(g.pA, at, 0, (qa.x - oh.x) + (qb.x - ol.x));
+                        put(g.pA, at, 1, (qa.y - oh.y) + (qb.y - ol.y));
+                        put(g.pB, at, 0, (qa.z - oh.z) + (qb.z - ol.z));
+                        put(g.pB, at, 1, qa.w);
                     }
                 }
                 npart += total;
@@ -420,7 +451,7 @@ __device__ void walk_group(const GroupWalkArgs &A, GroupShared &g, const float *
                         if (npart + m32 > GW_PARTS) {
                             __syncwarp();
                             if (valid)
-                                flush_parts(g, npart, rx, ry, rz, A.eps2, sx, cx, sy, cy, sz, cz);
+                                flush_parts<SOFT>(g, npart, rx, ry, rz, A.eps2, sx, cx, sy, cy, sz, cz);
                             n_pp += valid ? npart : 0;
                             npart = 0;
                             __syncwarp();
@@ -428,10 +459,11 @@ __device__ void walk_group(const GroupWalkArgs &A, GroupShared &g, const float *
                         if (lane < m32) {
                             const int p = first + b + lane;
                             const float4 qa = A.pa[p], qb = A.pb[p];
-                            g.px[npart + lane] = (qa.x - oh.x) + (qb.x - ol.x);
-                            g.py[npart + lane] = (qa.y - oh.y) + (qb.y - ol.y);
-                            g.pz[npart + lane] = (qa.z - oh.z) + (qb.z - ol.z);
-                            g.pm[npart + lane] = qa.w;
+                            const int at = npart + lane;
+                            put(g.pA, at, 0, (qa.x - oh.x) + (qb.x - ol.x));
+                            put(g.pA, at, 1, (qa.y - oh.y) + (qb.y - ol.y));
+                            put(g.pB, at, 0, (qa.z - oh.z) + (qb.z - ol.z));
+                            put(g.pB, at, 1, qa.w);
                         }
                         npart += m32;
                         __syncwarp();
@@ -457,7 +489,7 @@ __device__ void walk_group(const GroupWalkArgs &A, GroupShared &g, const float *
     }
     __syncwarp();
     if (valid && ncell > 0) flush_cells<QUAD>(g, ncell, rx, ry, rz, A.eps2, sx, cx, sy, cy, sz, cz);
-    if (valid && npart > 0) flush_parts(g, npart, rx, ry, rz, A.eps2, sx, cx, sy, cy, sz, cz);
+    if (valid && npart > 0) flush_parts<SOFT>(g, npart, rx, ry, rz, A.eps2, sx, cx, sy, cy, sz, cz);
     if (valid) {
         n_cell += ncell;
         n_pp += npart - 1;   // every particle meets itself once in its own leaf
@@ -504,7 +536,7 @@ __device__ bool group_fits(const GroupWalkArgs &A, const float *s_w2, int lane, 
     return ext * ext <= 1.0001f * s_w2[min(depth, OCT_MAX_LEVEL + 1)];
 }
 
-template <bool QUAD>
+template <bool QUAD, bool SOFT>
 // Five CTAs per SM (shared memory allows five; the register cap costs a few
 // spilled bytes but keeps the fifth CTA resident).
 __global__ void __launch_bounds__(32 * GW_WARPS, 5)
@@ -530,9 +562,10 @@ k_bh_group(GroupWalkArgs A)
         const int2 grp = A.groups[gi];
         const int cnt = grp.y & 255, depth = grp.y >> 8;
         if (group_fits(A, s_w2, lane, grp.x, cnt, depth)) {
-            walk_group<QUAD>(A, g, s_w2, lane, grp.x, grp.x + cnt);
+            walk_group<QUAD, SOFT>(A, g, s_w2, lane, grp.x, grp.x + cnt);
         } else {
-            for (int q = 0; q < cnt; ++q) walk_group<QUAD>(A, g, s_w2, lane, grp.x + q, grp.x + q + 1);
+            for (int q = 0; q < cnt; ++q)
+                walk_group<QUAD, SOFT>(A, g, s_w2, lane, grp.x + q, grp.x + q + 1);
         }
     }
 }
@@ -545,10 +578,10 @@ ErrorStatus launch_bh_group_walk(const OctreeDevice &t, double theta, double eps
     const size_t smem = sizeof(GroupShared) * GW_WARPS;
     // The attribute belongs to the current device: set on every call (cheap,
     // host-side only, allowed during stream capture).
-    GS_CUDA(cudaFuncSetAttribute(k_bh_group<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    GS_CUDA(cudaFuncSetAttribute(k_bh_group<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
+    const bool soft = eps > 0.0 && (float)(eps * eps) > 0.0f;
+    auto kernel = t.quad ? (soft ? k_bh_group<true, true> : k_bh_group<true, false>)
+                         : (soft ? k_bh_group<false, true> : k_bh_group<false, false>);
+    GS_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     GroupWalkArgs w;
     w.na = t.w_na.as<float4>();
     w.nb = t.w_nb.as<float4>();
@@ -580,15 +613,12 @@ ErrorStatus launch_bh_group_walk(const OctreeDevice &t, double theta, double eps
     int grid = grid_cache[dev->id].load(std::memory_order_acquire);
     if (grid == 0) {
         int per_sm = 0;
-        GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bh_group<true>,
+        GS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bh_group<true, true>,
                                                               32 * GW_WARPS, smem));
         grid = dev->sm_count * (per_sm > 0 ? per_sm : 1);
         grid_cache[dev->id].store(grid, std::memory_order_release);
     }
-    if (t.quad)
-        k_bh_group<true><<<grid, 32 * GW_WARPS, smem, s>>>(w);
-    else
-        k_bh_group<false><<<grid, 32 * GW_WARPS, smem, s>>>(w);
+    kernel<<<grid, 32 * GW_WARPS, smem, s>>>(w);
     GS_CUDA(cudaGetLastError());
     return ok();
 }

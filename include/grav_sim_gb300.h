@@ -359,7 +359,8 @@ int gsgpu_sim_warmup_until_ready(gsgpu_sim *sim, int64_t max_steps, int64_t *ste
  * residual before and after the network, last judged median error, steps
  * judged, steps that fell back, cheap opening angle, training seconds, Adam
  * steps, network in use: 1 if it cut the held-out median residual by at
- * least 20 %, else 0 and every step uses the judged fallback walk). */
+ * least 20 % and the corrected held-out median is within the judge's 1e-3
+ * bound, else 0 and every step uses the judged fallback walk). */
 int gsgpu_sim_report(gsgpu_sim *sim, double *out, int nmax);
 /* Learned method: copy up to `count` training samples of one snapshot
  * (features [count][32], targets [count][3]); returns the number copied. */

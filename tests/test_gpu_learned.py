@@ -4,10 +4,13 @@ A simulation of the galaxy-collision model collects its 64 training
 snapshots during its first steps (forces from the fallback walk), trains the
 network on the GPU, and then runs the cheap walk (theta 1.0, monopole +
 quadrupole) plus the network -- if the network cut the held-out median
-residual by at least 20 %; otherwise every step uses the judged fallback
-walk.  Checks:
-  * training converged (last-epoch loss below first); what the network
-    gains on the held-out snapshot is printed and decides the mode;
+residual by at least 20 % and the corrected median is within the judge's
+1e-3 bound; otherwise every step uses the judged fallback walk.  Checks:
+  * training converged (last-epoch loss below first);
+  * the trained network gains on the held-out snapshot: its median residual
+    after the correction is below the cheap walk's (and at least 20 % below
+    whenever the engine reports the network in use); the gain is printed
+    and the mode follows the rule above;
   * against an FP64 direct sum on sampled particles, the accelerations meet
     the 1e-3 median bound and beat the cheap walk without the network
     (GRAV_GPU_BARNES_HUT_QUAD at theta 1.0 on the same positions);
@@ -39,7 +42,7 @@ def _bind(lib, g):
     lib.gsgpu_sim_destroy.argtypes = [ctypes.c_void_p]
 
 
-def test_learned_correction_trains_and_gains(lib, g, orc, wl):
+def test_learned_correction_trains_gains_and_is_judged(lib, g, orc, wl):
     _bind(lib, g)
     n = 65536
     x, v, m = wl.galaxy_pair(n, 21)
@@ -59,7 +62,8 @@ def test_learned_correction_trains_and_gains(lib, g, orc, wl):
         gain = 1.0 - rep[5] / rep[4]
         print(f"held-out median residual {rep[4]:.4g} -> {rep[5]:.4g} (gain {100 * gain:.1f} %), "
               f"network {'in use' if rep[12] else 'disabled'}")
-        assert rep[12] == (1.0 if rep[5] < 0.8 * rep[4] else 0.0)
+        assert rep[5] < rep[4]                     # the network gains on held-out data
+        assert rep[12] == (1.0 if (rep[5] < 0.8 * rep[4] and rep[5] <= 1e-3) else 0.0)
         assert lib.gsgpu_sim_run(sim, 2) == 0
         xs, vs, a = np.empty((n, 3)), np.empty((n, 3)), np.empty((n, 3))
         assert lib.gsgpu_sim_download(sim, xs.ctypes.data_as(dp), vs.ctypes.data_as(dp)) == 0
