@@ -273,6 +273,7 @@ void print_and_free_traceback(ErrorStatus *error_status)
     free_traceback(error_status);
 }
 
+// src/system.c:26-36: G defaults to its value in AU^3 day^-2 Msun^-1.
 System get_new_system(void)
 {
     System s;
@@ -281,7 +282,7 @@ System get_new_system(void)
     s.x = nullptr;
     s.v = nullptr;
     s.m = nullptr;
-    s.G = 0.0;
+    s.G = 0.000295912208284119496676630;
     return s;
 }
 

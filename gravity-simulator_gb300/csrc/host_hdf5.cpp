@@ -471,7 +471,7 @@ ErrorStatus load_gadget2_ic(const char *path, System *system, double *unit_lengt
         st = read_part_type(f, "/PartType2", n2, s.m + n1, s.x + 3 * n1, s.v + 3 * n1);
     if (st.return_code != GRAV_SUCCESS) {
         free_system(&s);
-        return traceback(st, "read_part_type(...)", __FILE__, __LINE__, __func__);
+        return gs::traceback(st, "read_part_type(...)", __FILE__, __LINE__, __func__);
     }
     for (int k = 0; k < 3; ++k)
         if (unit_out[k]) *unit_out[k] = units_v[k];

@@ -43,6 +43,20 @@ ErrorStatus make_success_error_status(void);
 void free_traceback(ErrorStatus *error_status);
 /* src/error.h:202 */
 void print_and_free_traceback(ErrorStatus *error_status);
+/* src/error.h:105-127 (behind WRAP_RAISE_WARNING / WRAP_RAISE_WARNING_FMT) */
+void raise_warning(const char *warning_file, const int warning_line, const char *warning_func,
+                   const char *warning_msg);
+ErrorStatus raise_warning_fmt(const char *warning_file, const int warning_line,
+                              const char *warning_func, const char *format, ...);
+/* src/error.h:146-172 (behind WRAP_RAISE_ERROR / WRAP_RAISE_ERROR_FMT) */
+ErrorStatus raise_error(const char *error_file, const int error_line, const char *error_func,
+                        const int error_code, const char *error_msg);
+ErrorStatus raise_error_fmt(const char *error_file, const int error_line, const char *error_func,
+                            const int error_code, const char *format, ...);
+/* src/error.h:186-192 (behind WRAP_TRACEBACK): prepends the caller's frame
+ * to the traceback of a failed status; a success passes through. */
+ErrorStatus traceback(ErrorStatus error_status, const char *function_call_source_code,
+                      const char *error_file, const int error_line, const char *error_func);
 
 /* ---- system / parameters (src/system.h:12-20, src/acceleration.h:16-26,
  *      src/common.h:29-56, src/settings.h:11-16) --------------------- */
@@ -128,6 +142,9 @@ typedef struct Settings {
 
 /* src/system.h:28 */
 System get_new_system(void);
+/* src/system.h:55-58: arrays of num_particles (ids 0..n-1, x, v, m zeroed)
+ * allocated with malloc; release with free_system. */
+ErrorStatus get_initialized_system(System *system, const int num_particles);
 /* src/system.h:125 */
 void free_system(System *system);
 
@@ -150,6 +167,19 @@ OutputParam get_new_output_param(void);
 /* src/settings.h:23 */
 Settings get_new_settings(void);
 
+/* ---- utilities (src/utils.h:19-48, pcg/pcg_basic.h:58) -------------- */
+/* PCG32 generator state (the layout of pcg_basic.h's pcg32_random_t). */
+typedef struct pcg_state_setseq_64 {
+    uint64_t state;
+    uint64_t inc;
+} pcg32_random_t;
+/* src/utils.h:19: CLOCK_MONOTONIC seconds. */
+double grav_get_current_time(void);
+/* src/utils.h:35: a PCG32 generator seeded from the clock. */
+pcg32_random_t init_pcg_rng(void);
+/* src/utils.h:44-48: uniform in [min, max) from one 32-bit PCG32 draw. */
+double grav_randrange(const double min, const double max, pcg32_random_t *rng);
+
 /* ---- acceleration (src/acceleration.h:53-70) ----------------------- */
 
 /* src/acceleration.h:53-57.  a: host array [3N]; system->x, ->m host.  The
@@ -162,6 +192,17 @@ ErrorStatus acceleration(double *a, const System *system,
  * GRAV_GPU_BARNES_HUT_COMPAT, else GRAV_GPU_BARNES_HUT. */
 ErrorStatus acceleration_barnes_hut(double *a, const System *system,
                                     const AccelerationParam *acceleration_param);
+
+/* src/acceleration.h:98-103 (src/acceleration.c:369-506): runs
+ * acceleration() num_times_acceleration_param[i] times for each parameter
+ * set, timing each call with CLOCK_MONOTONIC, and prints per set the mean
+ * and sample standard deviation of the run times and the mean absolute
+ * error (three components summed, divided by N) of its first call against
+ * the first call of set 0.  Accepts the GPU method codes. */
+ErrorStatus benchmark_acceleration(const System *system,
+                                   const AccelerationParam *acceleration_params,
+                                   const int num_acceleration_params,
+                                   const int *num_times_acceleration_param);
 
 /* ---- linear octree (src/linear_octree.h:14-101) -------------------- */
 #define MORTON_MAX_LEVEL 21

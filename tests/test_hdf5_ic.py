@@ -5,6 +5,14 @@ examples/galaxy_collision/galaxy_collision_IC.hdf5 through libhdf5
 (examples/galaxy_collision/c/galaxy_collision.c:109-293).  load_gadget2_ic
 parses the file itself; these tests read that file where the reference is
 present, and check that damaged or foreign files give errors, never a crash.
+
+The values are pinned two ways: known entries of the file (first and last
+particles of each species, the two masses, the unit attributes), and a
+second read path that does not walk the HDF5 structures at all -- each array
+the parser returns, written back as the little-endian FP32 the file stores,
+must occur verbatim as one contiguous block of the file's bytes, and so must
+the header attribute NumPart_ThisFile = (0, 40000, 20000, 0, 0, 0) as
+uint32 (the counts the example reads, galaxy_collision.c:146-160).
 """
 
 import numpy as np
@@ -28,6 +36,36 @@ def test_reads_reference_galaxy_collision_ic(lib, g):
     assert (m[:40000] == m[0]).all() and (m[40000:] == m[-1]).all()
     # two galaxies on either side of the origin
     assert x[:, 0].min() < -50 and x[:, 0].max() > 50
+    # known entries (the file stores FP32; every value is exactly an FP32)
+    f32 = np.float32
+    assert np.array_equal(x[0], f32([-94.13385009765625, -10.240921974182129, -7.942867279052734]))
+    assert np.array_equal(v[0], f32([8.424066543579102, -51.35950469970703, -13.023665428161621]))
+    assert np.array_equal(x[39999], f32([85.55107116699219, 36.82402038574219, -0.637717604637146]))
+    assert np.array_equal(x[40000],
+                          f32([-90.04521179199219, -33.32984161376953, -0.02418774925172329]))
+    assert np.array_equal(v[40000], f32([45.37849044799805, 165.9688720703125, 50.6060791015625]))
+    assert np.array_equal(x[-1], f32([92.15531921386719, 41.02614974975586, 6.769761085510254]))
+    assert np.array_equal(v[-1], f32([-84.47198486328125, -73.0508041381836, 92.56161499023438]))
+    assert m[0] == f32(0.0010463387006893754) and m[-1] == f32(0.00023251971288118511)
+
+
+@pytest.mark.skipif(not IC.exists(), reason="reference initial conditions not present")
+def test_values_occur_verbatim_in_the_file(lib, g):
+    x, v, m, units = g.load_gadget2_ic(lib, IC)
+    data = IC.read_bytes()
+    blocks = [m[:40000], x[:40000], v[:40000], m[40000:], x[40000:], v[40000:]]
+    offsets = []
+    for arr in blocks:
+        f32 = np.ascontiguousarray(arr, dtype="<f4")
+        assert np.array_equal(f32.astype(np.float64), arr)     # exact FP32 values
+        raw = f32.tobytes()
+        off = data.find(raw[:64])
+        assert off >= 0 and data[off:off + len(raw)] == raw
+        offsets.append(off)
+    assert len(set(offsets)) == len(offsets)                    # six distinct datasets
+    assert data.find(np.array([0, 40000, 20000, 0, 0, 0], "<u4").tobytes()) >= 0
+    for u in units:
+        assert data.find(np.array([u], "<f8").tobytes()) >= 0
 
 
 @pytest.mark.skipif(not IC.exists(), reason="reference initial conditions not present")
