@@ -24,7 +24,6 @@
 // reference's expression order, so each system evolves exactly as the
 // reference evolves it (where the reference is not FMA-contracted and does
 // not read its uninitialised a[0] / aux, taken as zero here).
-#include "gs_div.cuh"
 #include "gs_internal.h"
 #include "gs_ptx.cuh"
 
@@ -288,10 +287,9 @@ __device__ __forceinline__ void jac_step(double xc[3], double vc[3], double mi, 
                                          double ep, const double *jxi, const double *jvi,
                                          double *xi, double *vi, double y[6])
 {
-    const double yei = __drcp_rn(ei);   // six quotients by ei share it
     for (int k = 0; k < 3; ++k) {
-        xc[k] = div_rcp(__dsub_rn(xc[k], __dmul_rn(mi, jxi[k])), ei, yei);
-        vc[k] = div_rcp(__dsub_rn(vc[k], __dmul_rn(mi, jvi[k])), ei, yei);
+        xc[k] = __ddiv_rn(__dsub_rn(xc[k], __dmul_rn(mi, jxi[k])), ei);
+        vc[k] = __ddiv_rn(__dsub_rn(vc[k], __dmul_rn(mi, jvi[k])), ei);
         y[k] = xc[k];
         y[3 + k] = vc[k];
         xi[k] = __dadd_rn(jxi[k], xc[k]);
@@ -379,11 +377,11 @@ __global__ void __launch_bounds__(32 * SEQ_WARPS) k_wh_seq(EnsDev E, int mode)
                         i = next_mass;
                         continue;
                     }
-                    const double ie = eta[i - 1], yie = __drcp_rn(ie);
-                    const double f = __dadd_rn(1.0, div_rcp(m[i], ie, yie));
+                    const double ie = eta[i - 1];
                     for (int k = 0; k < 3; ++k) {
-                        jx[3 * i + k] = __dsub_rn(x[3 * i + k], div_rcp(xc[k], ie, yie));
-                        jv[3 * i + k] = __dsub_rn(v[3 * i + k], div_rcp(vc[k], ie, yie));
+                        jx[3 * i + k] = __dsub_rn(x[3 * i + k], __ddiv_rn(xc[k], ie));
+                        jv[3 * i + k] = __dsub_rn(v[3 * i + k], __ddiv_rn(vc[k], ie));
+                        const double f = __dadd_rn(1.0, __ddiv_rn(m[i], ie));
                         xc[k] = __dadd_rn(__dmul_rn(xc[k], f), __dmul_rn(m[i], jx[3 * i + k]));
                         vc[k] = __dadd_rn(__dmul_rn(vc[k], f), __dmul_rn(m[i], jv[3 * i + k]));
                     }
@@ -417,11 +415,11 @@ __global__ void __launch_bounds__(32 * SEQ_WARPS) k_wh_seq(EnsDev E, int mode)
                 vc[k] = __dmul_rn(m[0], v[k]);
             }
             for (int i = 1; i < n; ++i) {
-                const double ie = eta[i - 1], yie = __drcp_rn(ie);
-                const double f = __dadd_rn(1.0, div_rcp(m[i], ie, yie));
+                const double ie = eta[i - 1];
                 for (int k = 0; k < 3; ++k) {
-                    jx[3 * i + k] = __dsub_rn(x[3 * i + k], div_rcp(xc[k], ie, yie));
-                    jv[3 * i + k] = __dsub_rn(v[3 * i + k], div_rcp(vc[k], ie, yie));
+                    jx[3 * i + k] = __dsub_rn(x[3 * i + k], __ddiv_rn(xc[k], ie));
+                    jv[3 * i + k] = __dsub_rn(v[3 * i + k], __ddiv_rn(vc[k], ie));
+                    const double f = __dadd_rn(1.0, __ddiv_rn(m[i], ie));
                     xc[k] = __dadd_rn(__dmul_rn(xc[k], f), __dmul_rn(m[i], jx[3 * i + k]));
                     vc[k] = __dadd_rn(__dmul_rn(vc[k], f), __dmul_rn(m[i], jv[3 * i + k]));
                 }
@@ -567,11 +565,10 @@ __global__ void __launch_bounds__(32 * SEQ_WARPS) k_wh_seq(EnsDev E, int mode)
         if (lane == 0) {
             for (int q = c - 1; q >= 0; --q) {
                 const double mi = st.m[q], ei = st.eta[q + 1], ep = st.eta[q];
-                const double yei = __drcp_rn(ei);
                 for (int k = 0; k < 3; ++k) {
                     const double jxq = st.jx[3 * q + k], jvq = st.jv[3 * q + k];
-                    xc[k] = div_rcp(__dsub_rn(xc[k], __dmul_rn(mi, jxq)), ei, yei);
-                    vc[k] = div_rcp(__dsub_rn(vc[k], __dmul_rn(mi, jvq)), ei, yei);
+                    xc[k] = __ddiv_rn(__dsub_rn(xc[k], __dmul_rn(mi, jxq)), ei);
+                    vc[k] = __ddiv_rn(__dsub_rn(vc[k], __dmul_rn(mi, jvq)), ei);
                     st.x[3 * q + k] = __dadd_rn(jxq, xc[k]);
                     st.v[3 * q + k] = __dadd_rn(jvq, vc[k]);
                     xc[k] = __dmul_rn(ep, xc[k]);
@@ -638,8 +635,7 @@ __global__ void __launch_bounds__(32 * PAIR_WARPS) k_wh_pairs(EnsDev E)
         const double dn = norm3d(d);
         const double dc = __dadd_rn(__dmul_rn(__dmul_rn(dn, dn), dn), e3);
         const double Gmm = __dmul_rn(__dmul_rn(E.G, m[j]), m[kk]);
-        const double ydc = __drcp_rn(dc);
-        for (int k = 0; k < 3; ++k) terms[t][k] = div_rcp(__dmul_rn(Gmm, d[k]), dc, ydc);
+        for (int k = 0; k < 3; ++k) terms[t][k] = __ddiv_rn(__dmul_rn(Gmm, d[k]), dc);
     }
     __syncwarp();
     for (int slot = lane; slot < 2 * kPairSlots; slot += 32) {
@@ -668,40 +664,33 @@ __global__ void __launch_bounds__(32 * PAIR_WARPS) k_wh_pairs(EnsDev E)
 }
 
 // ---- Kepler drift -------------------------------------------------------------
-// src/integrator_whfast.c:774-815.  The series' fixed divisors go through
-// div_rcp with their compile-time reciprocals, the divisions by 2 and 4 are
-// the exact multiplications they equal: the same bits as dividing.
-__device__ __forceinline__ double div_const(double a, double c, double rc)
-{
-    return div_rcp(a, c, rc);
-}
-
+// src/integrator_whfast.c:774-815
 __device__ __forceinline__ void stumpff(double z, double &c0, double &c1, double &c2, double &c3)
 {
     int q = 0;
     while (fabs(z) > 0.1) {
-        z = __dmul_rn(z, 0.25);
+        z = __ddiv_rn(z, 4.0);
         ++q;
     }
-    double t = __dsub_rn(1.0, div_const(z, 210.0, 1.0 / 210.0));
-    t = __dsub_rn(1.0, __dmul_rn(div_const(z, 156.0, 1.0 / 156.0), t));
-    t = __dsub_rn(1.0, __dmul_rn(div_const(z, 110.0, 1.0 / 110.0), t));
-    t = __dsub_rn(1.0, __dmul_rn(div_const(z, 72.0, 1.0 / 72.0), t));
-    t = __dsub_rn(1.0, __dmul_rn(div_const(z, 42.0, 1.0 / 42.0), t));
-    t = __dsub_rn(1.0, __dmul_rn(div_const(z, 20.0, 1.0 / 20.0), t));
-    double s3 = div_const(t, 6.0, 1.0 / 6.0);
-    double u = __dsub_rn(1.0, div_const(z, 182.0, 1.0 / 182.0));
-    u = __dsub_rn(1.0, __dmul_rn(div_const(z, 132.0, 1.0 / 132.0), u));
-    u = __dsub_rn(1.0, __dmul_rn(div_const(z, 90.0, 1.0 / 90.0), u));
-    u = __dsub_rn(1.0, __dmul_rn(div_const(z, 56.0, 1.0 / 56.0), u));
-    u = __dsub_rn(1.0, __dmul_rn(div_const(z, 30.0, 1.0 / 30.0), u));
-    u = __dsub_rn(1.0, __dmul_rn(div_const(z, 12.0, 1.0 / 12.0), u));
-    double s2 = __dmul_rn(u, 0.5);
+    double t = __dsub_rn(1.0, __ddiv_rn(z, 210.0));
+    t = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 156.0), t));
+    t = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 110.0), t));
+    t = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 72.0), t));
+    t = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 42.0), t));
+    t = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 20.0), t));
+    double s3 = __ddiv_rn(t, 6.0);
+    double u = __dsub_rn(1.0, __ddiv_rn(z, 182.0));
+    u = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 132.0), u));
+    u = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 90.0), u));
+    u = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 56.0), u));
+    u = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 30.0), u));
+    u = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 12.0), u));
+    double s2 = __ddiv_rn(u, 2.0);
     double s1 = __dsub_rn(1.0, __dmul_rn(z, s3));
     double s0 = __dsub_rn(1.0, __dmul_rn(z, s2));
     while (q > 0) {
-        s3 = __dmul_rn(__dadd_rn(s2, __dmul_rn(s0, s3)), 0.25);
-        s2 = __dmul_rn(__dmul_rn(s1, s1), 0.5);
+        s3 = __ddiv_rn(__dadd_rn(s2, __dmul_rn(s0, s3)), 4.0);
+        s2 = __ddiv_rn(__dmul_rn(s1, s1), 2.0);
         s1 = __dmul_rn(s0, s1);
         s0 = __dsub_rn(__dmul_rn(__dmul_rn(2.0, s0), s0), 1.0);
         --q;
@@ -720,10 +709,9 @@ __device__ bool kepler_drift(double *jx, double *jv, double gm, double dt)
     const double vv[3] = {jv[0], jv[1], jv[2]};
     const double xn = norm3d(xx);
     const double vn = norm3d(vv);
-    const double yxn = __drcp_rn(xn);   // four quotients by xn share it
-    const double rv = div_rcp(dot3(xx, vv), xn, yxn);
-    const double alpha = __dsub_rn(div_rcp(__dmul_rn(2.0, gm), xn, yxn), __dmul_rn(vn, vn));
-    double s = div_rcp(dt, xn, yxn);
+    const double rv = __ddiv_rn(dot3(xx, vv), xn);
+    const double alpha = __dsub_rn(__ddiv_rn(__dmul_rn(2.0, gm), xn), __dmul_rn(vn, vn));
+    double s = __ddiv_rn(dt, xn);
     double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0;
     bool conv = false, bad_z = false;
     const double xrv = __dmul_rn(xn, rv);
@@ -762,7 +750,7 @@ __device__ bool kepler_drift(double *jx, double *jv, double gm, double dt)
         const double err = __ddiv_rn(F, r);
         remove = (err > 1e-5) || bad_z;
     }
-    const double f = __dsub_rn(1.0, div_rcp(__dmul_rn(__dmul_rn(gm, ss), c2), xn, yxn));
+    const double f = __dsub_rn(1.0, __ddiv_rn(__dmul_rn(__dmul_rn(gm, ss), c2), xn));
     const double g = __dsub_rn(dt, __dmul_rn(__dmul_rn(gm, sss), c3));
     const double df = __ddiv_rn(__dmul_rn(__dmul_rn(-gm, s), c1), __dmul_rn(r, xn));
     const double dg = __dsub_rn(1.0, __ddiv_rn(__dmul_rn(__dmul_rn(gm, ss), c2), r));
@@ -821,12 +809,10 @@ __global__ void k_wh_accel(EnsDev E, int P)
     const double jn = norm3d(jxi);
     const double jc = __dadd_rn(__dmul_rn(__dmul_rn(jn, jn), jn), e3);
     const double Gm0 = __dmul_rn(G, m[0]);
-    // quotients sharing a denominator share its reciprocal (gs_div.cuh)
-    const double ye = __drcp_rn(eta[i - 1]), yjc = __drcp_rn(jc), ytc = __drcp_rn(tc);
-    const double pre = massive ? div_rcp(__dmul_rn(Gm0, eta[i]), eta[i - 1], ye) : Gm0;
+    const double pre = massive ? __ddiv_rn(__dmul_rn(Gm0, eta[i]), eta[i - 1]) : Gm0;
     double acc[3];
     for (int k = 0; k < 3; ++k)
-        acc[k] = __dmul_rn(pre, __dsub_rn(div_rcp(jxi[k], jc, yjc), div_rcp(tv[k], tc, ytc)));
+        acc[k] = __dmul_rn(pre, __dsub_rn(__ddiv_rn(jxi[k], jc), __ddiv_rn(tv[k], tc)));
     double aux[3] = {0.0, 0.0, 0.0};
     for (int q = 1; q < nh; ++q) {
         const int j = hv[q];
@@ -836,13 +822,11 @@ __global__ void k_wh_accel(EnsDev E, int P)
         const double dn = norm3d(d);
         const double dc = __dadd_rn(__dmul_rn(__dmul_rn(dn, dn), dn), e3);
         const double Gm = __dmul_rn(G, m[j]);
-        const double ydc = __drcp_rn(dc);
-        for (int k = 0; k < 3; ++k)
-            aux[k] = __dadd_rn(aux[k], div_rcp(__dmul_rn(Gm, d[k]), dc, ydc));
+        for (int k = 0; k < 3; ++k) aux[k] = __dadd_rn(aux[k], __ddiv_rn(__dmul_rn(Gm, d[k]), dc));
     }
     for (int k = 0; k < 3; ++k)
         acc[k] = __dsub_rn(acc[k],
-                           massive ? div_rcp(__dmul_rn(aux[k], eta[i]), eta[i - 1], ye) : aux[k]);
+                           massive ? __ddiv_rn(__dmul_rn(aux[k], eta[i]), eta[i - 1]) : aux[k]);
     aux[0] = aux[1] = aux[2] = 0.0;
     for (int q = 1; q < nh; ++q) {
         const int j = hv[q];
@@ -852,9 +836,7 @@ __global__ void k_wh_accel(EnsDev E, int P)
         const double dn = norm3d(d);
         const double dc = __dadd_rn(__dmul_rn(__dmul_rn(dn, dn), dn), e3);
         const double Gm = __dmul_rn(G, m[j]);
-        const double ydc = __drcp_rn(dc);
-        for (int k = 0; k < 3; ++k)
-            aux[k] = __dadd_rn(aux[k], div_rcp(__dmul_rn(Gm, d[k]), dc, ydc));
+        for (int k = 0; k < 3; ++k) aux[k] = __dadd_rn(aux[k], __ddiv_rn(__dmul_rn(Gm, d[k]), dc));
     }
     for (int k = 0; k < 3; ++k) acc[k] = __dadd_rn(acc[k], aux[k]);
     aux[0] = aux[1] = aux[2] = 0.0;
@@ -867,7 +849,7 @@ __global__ void k_wh_accel(EnsDev E, int P)
         }
         const int slot = rank >= 0 ? kPairSlots + rank : g;
         const double *pr = E.pairs + ((size_t)s * 2 * kPairSlots + slot) * 3;
-        for (int k = 0; k < 3; ++k) a[k] = __dsub_rn(acc[k], div_rcp(pr[k], eta[i - 1], ye));
+        for (int k = 0; k < 3; ++k) a[k] = __dsub_rn(acc[k], __ddiv_rn(pr[k], eta[i - 1]));
         return;
     }
     for (int q0 = 0; q0 < nh; ++q0) {
@@ -882,12 +864,11 @@ __global__ void k_wh_accel(EnsDev E, int P)
             const double dn = norm3d(d);
             const double dc = __dadd_rn(__dmul_rn(__dmul_rn(dn, dn), dn), e3);
             const double Gmm = __dmul_rn(Gmj, m[kk]);
-            const double ydc = __drcp_rn(dc);
             for (int k = 0; k < 3; ++k)
-                aux[k] = __dadd_rn(aux[k], div_rcp(__dmul_rn(Gmm, d[k]), dc, ydc));
+                aux[k] = __dadd_rn(aux[k], __ddiv_rn(__dmul_rn(Gmm, d[k]), dc));
         }
     }
-    for (int k = 0; k < 3; ++k) a[k] = __dsub_rn(acc[k], div_rcp(aux[k], eta[i - 1], ye));
+    for (int k = 0; k < 3; ++k) a[k] = __dsub_rn(acc[k], __ddiv_rn(aux[k], eta[i - 1]));
 }
 
 __global__ void k_wh_kick(EnsDev E, int P, double h)

@@ -504,13 +504,6 @@ int gsgpu_mlp_gradients(gsgpu_mlp *mlp, const float *features, const float *targ
 int gsgpu_mlp_train_step(gsgpu_mlp *mlp, const float *features, const float *target, int n,
                          float lr, double *loss_sum);
 
-/* Test entry point (no counterpart in the reference): forms 3 n quotients
- * from seeded random operands both by the library's reciprocal-based FP64
- * division (gs_div.cuh: Markstein's correction steps from a correctly
- * rounded reciprocal, used by the ensemble kernels) and by __ddiv_rn, and
- * stores in *mismatches how many differ in any bit. */
-int gsgpu_fp64_division_selftest(long long n, unsigned long long seed, long long *mismatches);
-
 /* FMA-throughput probe of the running GPU (fp64 = 0: FP32, 1: FP64):
  * TFLOP/s at 2 FLOP per FMA, best of 5 launches.  No counterpart in the
  * reference; it supplies the FP32/FP64 pipe peaks of the rooflines. */

@@ -185,19 +185,3 @@ def test_whfast_planar_systems_match_oracle(g, lib, wl, orc, negzero):
         assert np.array_equal(i_s, ri), s
         assert x_s.tobytes() == rx.tobytes() and v_s.tobytes() == rv.tobytes(), s
     ens.close()
-
-
-def test_reciprocal_division_equals_ddiv_rn(lib):
-    """The ensemble kernels form quotients that share a denominator, and the
-    Stumpff series' fixed divisions, from a correctly rounded reciprocal by
-    two Markstein correction steps; every quotient must equal __ddiv_rn's bit
-    for bit: 3 x 2^25 quotients of random bit patterns (every exponent,
-    subnormals, zeros, infinities, NaNs) and of the series' range."""
-    import ctypes
-    f = lib.gsgpu_fp64_division_selftest
-    f.argtypes = [ctypes.c_longlong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_longlong)]
-    f.restype = ctypes.c_int
-    for seed in (1, 20261204):
-        bad = ctypes.c_longlong(-1)
-        assert f(1 << 25, seed, ctypes.byref(bad)) == 0
-        assert bad.value == 0
