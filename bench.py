@@ -444,6 +444,14 @@ def sim_arm(args, lib, g, wk, x, v, m, stream, flush, world, local, sample_clock
         force_ms = ctypes.c_double()
         force_n = ctypes.c_int64()
         lib.gsgpu_sim_force_timing(sim, ctypes.byref(force_ms), ctypes.byref(force_n))
+        if wk["method"] in BH_METHODS:
+            mo_ms, so_ms, builds = ctypes.c_double(), ctypes.c_double(), ctypes.c_int64()
+            lib.gsgpu_sim_build_timing.argtypes = [ctypes.c_void_p, dp, dp,
+                                                   ctypes.POINTER(ctypes.c_int64)]
+            lib.gsgpu_sim_build_timing(sim, ctypes.byref(mo_ms), ctypes.byref(so_ms),
+                                       ctypes.byref(builds))
+            out["morton_ms"] = mo_ms.value / max(builds.value, 1)
+            out["sort_ms"] = so_ms.value / max(builds.value, 1)
         lib.gsgpu_sim_set_force_timing(sim, 0)
         out["mean_force_ms"] = force_ms.value / max(force_n.value, 1)
         interactions = float(n) * (n - 1)
@@ -641,7 +649,23 @@ def run_ours(args, world, rank, local):
     }
     if bh:
         out["config"]["interactions"] = "accepted cells + leaf pair terms of the last step "\
-                                        "(device counters), 20 FLOP each"
+                                        "(device counters); FLOP per term in roofline"
+        # Tree build against HBM: algorithmic bytes per particle of the Morton
+        # keys (24 B of positions read, 8 B of key written) and of the key
+        # sort (grav_sim's 7 radix passes of 9 bits, each reading and writing
+        # an 8 B key and a 4 B index: 168 B), over the kernels' event times.
+        hbm = measured_peaks().get("hbm_gbs")
+        mo_gbs = 32.0 * n / (r["morton_ms"] / 1e3) / 1e9 if r.get("morton_ms") else None
+        so_gbs = 168.0 * n / (r["sort_ms"] / 1e3) / 1e9 if r.get("sort_ms") else None
+        out["roofline"]["tree_build"] = {
+            "bound": "hbm", "unit": "GB/s", "peak": hbm,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs",
+            "morton": {"ms": r.get("morton_ms"), "achieved": mo_gbs,
+                       "frac": mo_gbs / hbm if mo_gbs and hbm else None,
+                       "bytes_per_particle": 32},
+            "sort": {"ms": r.get("sort_ms"), "achieved": so_gbs,
+                     "frac": so_gbs / hbm if so_gbs and hbm else None,
+                     "bytes_per_particle": 168}}
     if wk["method"] == 104:
         out["config"]["training_s"] = r.get("training_s")
         out["config"]["learned_report"] = r.get("learned_report")
@@ -725,14 +749,44 @@ def run_ensemble(args, world, rank, local, wk, g, wl, lib):
     torch.cuda.synchronize()
     clocks.start()
     time.sleep(0.3)
+    torch.cuda.profiler.start()   # the timed steps are the profiler range
     t0 = time.perf_counter()
     ens.run(args.steps)
     torch.cuda.synchronize()
     total_s = time.perf_counter() - t0
+    torch.cuda.profiler.stop()
     clk = clocks.stop()
     total_s, = max_over_ranks([total_s], world)
     kps = ens.kernels_per_step()
+    # the acceleration kernels' own time, for the roofline: K more steps
+    # launched directly with CUDA events around them (outside the timed region)
+    ens.set_kernel_timing(True)
+    ens.run(args.steps)
+    torch.cuda.synchronize()
+    drift_ms, accel_ms, timed = ens.kernel_timing()
+    ens.set_kernel_timing(False)
     ens.close()
+    # Algorithmic work of one acceleration step, at 20 FLOP per pair term:
+    # WHFast (src/integrator_whfast.c:959-1264) gives every particle but the
+    # primary its M - 1 interior / exterior massive terms and its 2 primary
+    # terms, and each system its M (M - 1) / 2 massive pair terms (summed once
+    # per system here); leapfrog's massless acceleration
+    # (src/acceleration.c:236-367) has L M + M (M - 1) / 2 terms per system
+    # (M massive bodies, L massless particles).
+    terms = 0
+    for s_ in systems:
+        n_s = s_[2].size
+        M = int(np.count_nonzero(s_[2]))
+        if wk["integrator"] == 10:
+            terms += (n_s - 1) * (M + 1) + M * (M - 1) // 2
+        else:
+            terms += (n_s - M) * M + M * (M - 1) // 2
+    lib.gsgpu_measure_fma_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_double)]
+    peak64 = ctypes.c_double()
+    lib.gsgpu_measure_fma_peak(1, ctypes.byref(peak64), None)
+    accel_launch_ms = accel_ms / max(timed, 1)
+    achieved = 20.0 * terms / (accel_launch_ms / 1e3) / 1e12
     value = world * P * args.steps / total_s
     # end to end: launch, upload, K steps, download through the ensemble API
     t0 = time.perf_counter()
@@ -760,6 +814,20 @@ def run_ensemble(args, world, rank, local, wk, g, wl, lib):
                 "note": "create + upload + K steps + download through gsgpu_ensemble_*"},
         "gpu_launches": args.steps * kps,
         "clocks": clk,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64.value,
+                     "unit": "TFLOP/s", "frac": achieved / peak64.value if peak64.value else None,
+                     "traffic": None,
+                     "kernel": "k_wh_pairs + k_wh_accel" if wk["integrator"] == 10
+                               else "k_ens_massless_accel",
+                     "mean_launch_ms": accel_launch_ms, "pair_terms_per_step": terms,
+                     "flop_per_pair_term": 20,
+                     "drift_ms_per_step": drift_ms / max(timed, 1) if wk["integrator"] == 10
+                                          else None,
+                     "peak_source": "FP64 FMA probe on this GPU (gsgpu_measure_fma_peak), "
+                                    "not in MEASURED_PEAKS.json",
+                     "note": "every pair term holds three correctly rounded FP64 divisions and a "
+                             "square root (bit-exact to the reference), which the 20-FLOP "
+                             "convention counts as single operations"},
     }
     if rank == 0:
         out["cpu_baseline"] = cpu_baseline_ensemble(wk, systems)

@@ -118,6 +118,13 @@ class Engine {
     {
         (void)cx; (void)cy; (void)cz;
     }
+    // Barnes-Hut engines: CUDA events around the Morton-key kernel and the
+    // key sort of each tree build (null: not timed).
+    virtual void set_build_timers(ForceTimer *morton, ForceTimer *sort)
+    {
+        (void)morton;
+        (void)sort;
+    }
     // false while the engine is still preparing itself (collecting training
     // data): its forces are then the fallback method's
     virtual bool ready() const { return true; }

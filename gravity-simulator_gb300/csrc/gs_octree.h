@@ -45,6 +45,7 @@ struct OctreeDevice {
     bool quad = false;   // traceless quadrupoles about the centre of mass
     DBuf w_nq;           // float4[2*cap]: (xx, xy, xz, yy), (yz, zz, 0, 0), FP32
     bool links = false;  // parent ids and particle -> leaf map
+    ForceTimer *tm_morton = nullptr, *tm_sort = nullptr;   // build timing (optional)
     DBuf t_parent;       // int[cap] (-1 for the root)
     DBuf leaf_of;        // int[n]: leaf id of sorted particle p
 
@@ -69,6 +70,7 @@ struct OctreeDevice {
     DBuf w_nc;                // int4[cap]: (first_child, num_children, first_particle, count)
     DBuf w_nkey;              // uint64[cap]: key used by the cell-membership test
     DBuf w_pa, w_pb;          // float4[n] in sorted order: (x_hi, m), (x_lo, 0)
+    DBuf xm;                  // double[4n] in sorted order: x, y, z, m (the multipole sums' input)
     DBuf g_list;              // int2[n]: particle groups of the group walk (first, count)
     DBuf g_ctr;               // int[4]: group count, work-queue head
     RadixSorter sorter;

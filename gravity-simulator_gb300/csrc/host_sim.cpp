@@ -154,6 +154,7 @@ struct gsgpu_sim {
     double graph_dt = 0.0;
     bool graph_failed = false;
     ForceTimer timer;
+    ForceTimer t_morton, t_sort;   // tree builds of Barnes-Hut engines
     int kernels_last = 0;
     // embedded Runge-Kutta (integrators 5-8) and IAS15 (9)
     double tolerance = -1.0, initial_dt = -1.0;
@@ -872,10 +873,30 @@ int gsgpu_sim_download_acceleration(gsgpu_sim *sim, double *a)
 int gsgpu_sim_set_force_timing(gsgpu_sim *sim, int enable)
 {
     if (!sim) return GRAV_POINTER_ERROR;
-    sim->timer.enabled = enable != 0;
-    sim->timer.total_ms = 0.0;
-    sim->timer.launches = 0;
-    sim->timer.used = 0;
+    for (gs::ForceTimer *t : {&sim->timer, &sim->t_morton, &sim->t_sort}) {
+        t->enabled = enable != 0;
+        t->total_ms = 0.0;
+        t->launches = 0;
+        t->used = 0;
+    }
+    sim->engine->set_build_timers(enable ? &sim->t_morton : nullptr, enable ? &sim->t_sort : nullptr);
+    return 0;
+}
+
+int gsgpu_sim_build_timing(const gsgpu_sim *sim, double *morton_ms, double *sort_ms,
+                           int64_t *builds)
+{
+    if (!sim) return GRAV_POINTER_ERROR;
+    gsgpu_sim *s = const_cast<gsgpu_sim *>(sim);
+    ErrorStatus st = s->t_morton.collect();
+    if (st.return_code == GRAV_SUCCESS) st = s->t_sort.collect();
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    if (morton_ms) *morton_ms = s->t_morton.total_ms;
+    if (sort_ms) *sort_ms = s->t_sort.total_ms;
+    if (builds) *builds = s->t_sort.launches;
     return 0;
 }
 

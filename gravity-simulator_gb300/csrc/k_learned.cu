@@ -372,6 +372,12 @@ class LearnedEngine final : public Engine {
         return ok();
     }
 
+    void set_build_timers(ForceTimer *morton, ForceTimer *sort) override
+    {
+        tree_.tm_morton = morton;
+        tree_.tm_sort = sort;
+    }
+
     ErrorStatus interaction_counts(cudaStream_t s, long long out[2]) override
     {
         unsigned long long h[2] = {0, 0};

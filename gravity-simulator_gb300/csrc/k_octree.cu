@@ -487,18 +487,21 @@ __global__ void k_tree_links(const int *__restrict__ ctr, const int *__restrict_
 }
 
 // Running sums of the particles of one leaf, sorted order (reference :667-674).
-__device__ __forceinline__ void add_particles(const double *__restrict__ x,
-                                              const double *__restrict__ m,
-                                              const int *__restrict__ sidx, int first, int count,
+// Mass and mass-weighted coordinate sums of sorted particles [first,
+// first + count) in sorted order (the reference's order), read from the
+// sorted (x, y, z, m) copy: contiguous 32-byte records instead of gathers
+// through the sorted ids into the caller's arrays; same values, same sums.
+__device__ __forceinline__ void add_particles(const double *__restrict__ xm, int first, int count,
                                               double &M, double &S0, double &S1, double &S2)
 {
     for (int p = first; p < first + count; ++p) {
-        const int pid = sidx[p];
-        const double mp = m[pid];
+        const double2 a = __ldg(reinterpret_cast<const double2 *>(xm + 4 * (size_t)p));
+        const double2 b = __ldg(reinterpret_cast<const double2 *>(xm + 4 * (size_t)p) + 1);
+        const double mp = b.y;
         M = __dadd_rn(M, mp);
-        S0 = __dadd_rn(S0, __dmul_rn(mp, x[3 * pid + 0]));
-        S1 = __dadd_rn(S1, __dmul_rn(mp, x[3 * pid + 1]));
-        S2 = __dadd_rn(S2, __dmul_rn(mp, x[3 * pid + 2]));
+        S0 = __dadd_rn(S0, __dmul_rn(mp, a.x));
+        S1 = __dadd_rn(S1, __dmul_rn(mp, a.y));
+        S2 = __dadd_rn(S2, __dmul_rn(mp, b.x));
     }
 }
 
@@ -560,7 +563,7 @@ __device__ __forceinline__ float df_offset(float ph, float pl, float ch, float c
 }
 
 struct MultipoleArgs {
-    const double *x, *m;
+    const double *xm;   // sorted (x, y, z, m) records
     const int *sidx, *in_node, *nd_parent, *in_id, *in_fc, *in_nchild;
     const int *t_np, *t_nc, *t_fp, *t_int, *t_depth;
     const double *frame;
@@ -590,7 +593,7 @@ __device__ void multipole_node(int ii, const MultipoleArgs &A)
             S1 = __dadd_rn(S1, __ldcg(cs + 2));
             S2 = __dadd_rn(S2, __ldcg(cs + 3));
         } else {
-            add_particles(A.x, A.m, A.sidx, A.t_fp[c], A.t_np[c], M, S0, S1, S2);
+            add_particles(A.xm, A.t_fp[c], A.t_np[c], M, S0, S1, S2);
         }
     }
     double *ws = A.in_sum + 4 * (size_t)ii;
@@ -669,7 +672,7 @@ __global__ void k_leaf_multipoles(const int *__restrict__ ctr, MultipoleArgs A,
         if (A.t_nc[id] > 0) continue;
         const int fp = A.t_fp[id], np = A.t_np[id];
         double M = 0.0, S0 = 0.0, S1 = 0.0, S2 = 0.0;
-        add_particles(A.x, A.m, A.sidx, fp, np, M, S0, S1, S2);
+        add_particles(A.xm, fp, np, M, S0, S1, S2);
         const double c0 = __ddiv_rn(S0, M), c1 = __ddiv_rn(S1, M), c2 = __ddiv_rn(S2, M);
         A.t_mass[id] = M;
         A.t_com[3 * id + 0] = c0;
@@ -719,11 +722,15 @@ __global__ void k_walk_nodes(const int *__restrict__ ctr, int compat, const doub
 
 __global__ void k_walk_particles(int n, const double *__restrict__ frame, const double *__restrict__ x,
                                  const double *__restrict__ m, const int *__restrict__ sidx,
-                                 float4 *__restrict__ pa, float4 *__restrict__ pb)
+                                 float4 *__restrict__ pa, float4 *__restrict__ pb,
+                                 double *__restrict__ xm)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     const int id = sidx[p];
+    double2 *xo = reinterpret_cast<double2 *>(xm + 4 * (size_t)p);
+    xo[0] = make_double2(x[3 * id + 0], x[3 * id + 1]);
+    xo[1] = make_double2(x[3 * id + 2], m[id]);
     float h0, l0, h1, l1, h2, l2;
     split_df(__dsub_rn(x[3 * id + 0], frame[0]), h0, l0);
     split_df(__dsub_rn(x[3 * id + 1], frame[1]), h1, l1);
@@ -765,6 +772,7 @@ ErrorStatus OctreeDevice::setup(int n_, int leaf_max_, bool compat_, bool quad_)
     GS_TRY(w_nkey.reserve((size_t)cap * sizeof(uint64_t)));
     GS_TRY(w_pa.reserve((size_t)n * sizeof(float4)));
     GS_TRY(w_pb.reserve((size_t)n * sizeof(float4)));
+    GS_TRY(xm.reserve((size_t)n * 4 * sizeof(double)));
     GS_TRY(g_list.reserve((size_t)n * sizeof(int2)));
     GS_TRY(g_ctr.reserve(4 * sizeof(int)));
     if (quad) GS_TRY(w_nq.reserve((size_t)cap * 2 * sizeof(float4)));
@@ -796,13 +804,17 @@ ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream
                                   own_box ? box_center[1] : 0.0, own_box ? box_center[2] : 0.0,
                                   own_box ? box_width : -1.0, frame.as<double>());
     const int pb = (n + OT_THREADS - 1) / OT_THREADS;
+    if (tm_morton) GS_TRY(tm_morton->begin(s));
     k_morton<<<pb, OT_THREADS, 0, s>>>(d_x, n, frame.as<double>(), keys.as<uint64_t>(),
                                        sidx.as<int>());
+    if (tm_morton) GS_TRY(tm_morton->end(s));
     k_tree_init<<<1, 32, 0, s>>>(ctr.as<int>(), n, nd_start.as<int>(), nd_count.as<int>(),
                                  nd_depth.as<int>(), nd_parent.as<int>(), nd_rank.as<int>(),
                                  nd_int.as<int>(), in_node.as<int>());
     GS_CUDA(cudaGetLastError());
+    if (tm_sort) GS_TRY(tm_sort->begin(s));
     GS_TRY(sorter.sort(keys.as<uint64_t>(), sidx.as<int>(), ctr.as<int>() + CTR_N, 63, s));
+    if (tm_sort) GS_TRY(tm_sort->end(s));
 
     const DeviceInfo *dev = nullptr;
     GS_TRY(device_info(&dev));
@@ -840,8 +852,7 @@ ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream
                                                  in_node.as<int>(), in_fc.as<int>(),
                                                  t_parent.as<int>(), leaf_of.as<int>());
     MultipoleArgs A;
-    A.x = d_x;
-    A.m = d_m;
+    A.xm = xm.as<double>();
     A.sidx = sidx.as<int>();
     A.in_node = in_node.as<int>();
     A.nd_parent = nd_parent.as<int>();
@@ -863,7 +874,8 @@ ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream
     A.nq = quad ? w_nq.as<float4>() : nullptr;
     // particle records first: the leaves' quadrupoles are formed from them
     k_walk_particles<<<pb, OT_THREADS, 0, s>>>(n, frame.as<double>(), d_x, d_m, sidx.as<int>(),
-                                               w_pa.as<float4>(), w_pb.as<float4>());
+                                               w_pa.as<float4>(), w_pb.as<float4>(),
+                                               xm.as<double>());
     if (!compat)
         k_leaf_multipoles<<<grid, OT_THREADS, 0, s>>>(ctr.as<int>(), A, w_pa.as<float4>(),
                                                       w_pb.as<float4>());

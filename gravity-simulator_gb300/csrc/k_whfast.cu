@@ -970,6 +970,11 @@ struct gsgpu_ensemble {
     double last_dt = 0.0;
     cudaGraphExec_t graph = nullptr;
     double graph_dt = 0.0;
+    // Kernel timing (gsgpu_ensemble_set_kernel_timing): steps launch
+    // directly, with CUDA events around the drift and around the
+    // interaction accelerations (pair sums + per-particle terms).
+    bool timing = false;
+    ForceTimer t_drift, t_accel;
 
     ~gsgpu_ensemble()
     {
@@ -1054,14 +1059,16 @@ struct gsgpu_ensemble {
 
     int seq_grid() const { return (S + SEQ_WARPS - 1) / SEQ_WARPS; }
 
-    ErrorStatus accel()
+    ErrorStatus accel(ForceTimer *timer = nullptr)
     {
+        if (timer) GS_TRY(timer->begin(stream));
         if (integrator == INTEGRATOR_WHFAST) {
             k_wh_pairs<<<(S + PAIR_WARPS - 1) / PAIR_WARPS, 32 * PAIR_WARPS, 0, stream>>>(E);
             k_wh_accel<<<grid_for(tpb_accel), tpb_accel, 0, stream>>>(E, P);
         }
         else
             k_ens_massless_accel<<<grid_for(tpb_accel), tpb_accel, 0, stream>>>(E, P);
+        if (timer) GS_TRY(timer->end(stream));
         GS_CUDA(cudaGetLastError());
         return ok();
     }
@@ -1092,16 +1099,19 @@ struct gsgpu_ensemble {
 
     ErrorStatus step(double h)
     {
+        ForceTimer *td = timing ? &t_drift : nullptr, *ta = timing ? &t_accel : nullptr;
         if (integrator == INTEGRATOR_WHFAST) {
             // src/integrator_whfast.c:290-343
             GS_TRY(sort(E.jx, E.jv));
+            if (td) GS_TRY(td->begin(stream));
             k_wh_drift<<<grid_for(tpb_drift), tpb_drift, 0, stream>>>(E, P, h);
+            if (td) GS_TRY(td->end(stream));
             k_wh_seq<<<seq_grid(), 32 * SEQ_WARPS, 0, stream>>>(E, 1);
-            GS_TRY(accel());
+            GS_TRY(accel(ta));
             k_wh_kick<<<pgrid(), 128, 0, stream>>>(E, P, h);
         } else {
             launch_comp_update(E.x, xe.as<double>(), E.v, h, 1.0, 3 * P, stream);
-            GS_TRY(accel());
+            GS_TRY(accel(ta));
             launch_comp_update(E.v, ve.as<double>(), E.a, h, 1.0, 3 * P, stream);
         }
         GS_CUDA(cudaGetLastError());
@@ -1141,6 +1151,12 @@ struct gsgpu_ensemble {
 
     ErrorStatus step_graph(double h)
     {
+        if (timing) {
+            GS_TRY(step(h));
+            GS_TRY(t_drift.collect());
+            GS_TRY(t_accel.collect());
+            return ok();
+        }
         if (!graph || graph_dt != h) {
             if (graph) {
                 cudaGraphExecDestroy(graph);
@@ -1465,6 +1481,26 @@ int gsgpu_ensemble_tuning(const gsgpu_ensemble *e, int *accel_threads, int *drif
     if (!e) return GRAV_POINTER_ERROR;
     if (accel_threads) *accel_threads = e->tuned ? e->tpb_accel : 0;
     if (drift_threads) *drift_threads = e->tuned ? e->tpb_drift : 0;
+    return 0;
+}
+
+int gsgpu_ensemble_set_kernel_timing(gsgpu_ensemble *e, int enable)
+{
+    if (!e) return GRAV_POINTER_ERROR;
+    e->timing = enable != 0;
+    e->t_drift.enabled = e->t_accel.enabled = e->timing;
+    e->t_drift.total_ms = e->t_accel.total_ms = 0.0;
+    e->t_drift.launches = e->t_accel.launches = 0;
+    return 0;
+}
+
+int gsgpu_ensemble_kernel_timing(const gsgpu_ensemble *e, double *drift_ms, double *accel_ms,
+                                 int64_t *steps)
+{
+    if (!e) return GRAV_POINTER_ERROR;
+    if (drift_ms) *drift_ms = e->t_drift.total_ms;
+    if (accel_ms) *accel_ms = e->t_accel.total_ms;
+    if (steps) *steps = e->t_accel.launches;
     return 0;
 }
 

@@ -486,6 +486,21 @@ class Ensemble:
                     "gsgpu_ensemble_tuning")
         return a.value, d.value
 
+    def set_kernel_timing(self, enable: bool) -> None:
+        """Direct launches with CUDA events around the drift and the
+        accelerations (instead of graph replays) while enabled."""
+        self._check(self.lib.gsgpu_ensemble_set_kernel_timing(self.handle, int(bool(enable))),
+                    "gsgpu_ensemble_set_kernel_timing")
+
+    def kernel_timing(self):
+        """(drift ms, acceleration ms, timed steps) summed since timing was
+        enabled."""
+        d, a, k = ctypes.c_double(), ctypes.c_double(), ctypes.c_int64()
+        self._check(self.lib.gsgpu_ensemble_kernel_timing(self.handle, ctypes.byref(d),
+                                                          ctypes.byref(a), ctypes.byref(k)),
+                    "gsgpu_ensemble_kernel_timing")
+        return d.value, a.value, k.value
+
     def close(self) -> None:
         if getattr(self, "handle", None):
             self.lib.gsgpu_ensemble_destroy(self.handle)
@@ -519,6 +534,11 @@ def _init_ensemble_api(lib: ctypes.CDLL) -> None:
     lib.gsgpu_ensemble_kernels_per_step.argtypes = [vp]
     lib.gsgpu_ensemble_tuning.restype = ctypes.c_int
     lib.gsgpu_ensemble_tuning.argtypes = [vp, c_int_p, c_int_p]
+    lib.gsgpu_ensemble_set_kernel_timing.restype = ctypes.c_int
+    lib.gsgpu_ensemble_set_kernel_timing.argtypes = [vp, ctypes.c_int]
+    lib.gsgpu_ensemble_kernel_timing.restype = ctypes.c_int
+    lib.gsgpu_ensemble_kernel_timing.argtypes = [vp, c_double_p, c_double_p,
+                                                 ctypes.POINTER(ctypes.c_int64)]
     lib.gsgpu_ensemble_destroy.restype = None
     lib.gsgpu_ensemble_destroy.argtypes = [vp]
     lib._ensemble_api = True

@@ -384,6 +384,11 @@ int gsgpu_sim_set_force_timing(gsgpu_sim *sim, int enable);
 int gsgpu_sim_force_timing(const gsgpu_sim *sim, double *total_ms,
                            int64_t *launches);
 /* Number of kernels launched by the most recent gsgpu_sim_run step. */
+/* Barnes-Hut methods, while force timing is on: summed milliseconds of the
+ * Morton-key kernel and of the particle key sort over the tree builds
+ * since it was turned on, and the number of builds. */
+int gsgpu_sim_build_timing(const gsgpu_sim *sim, double *morton_ms, double *sort_ms,
+                           int64_t *builds);
 int gsgpu_sim_kernels_per_step(const gsgpu_sim *sim);
 /* Interactions of the most recent force evaluation: counts[0] cell
  * (monopole) terms, counts[1] particle-particle terms (tree methods; both 0
@@ -442,6 +447,16 @@ int gsgpu_ensemble_num_particles(const gsgpu_ensemble *e);
  * acceleration and drift kernels (timed once after the first half kick;
  * 0 before that). */
 int gsgpu_ensemble_tuning(const gsgpu_ensemble *e, int *accel_threads, int *drift_threads);
+/* Kernel timing (no counterpart in the reference): while enabled, steps are
+ * launched directly instead of from the captured graph, with CUDA events
+ * around the Kepler drift and around the interaction accelerations (the
+ * pair sums and the per-particle terms; for leapfrog the massless
+ * accelerations).  gsgpu_ensemble_kernel_timing returns the summed
+ * milliseconds of each and the number of timed steps since timing was
+ * enabled. */
+int gsgpu_ensemble_set_kernel_timing(gsgpu_ensemble *e, int enable);
+int gsgpu_ensemble_kernel_timing(const gsgpu_ensemble *e, double *drift_ms, double *accel_ms,
+                                 int64_t *steps);
 void gsgpu_ensemble_destroy(gsgpu_ensemble *e);
 
 /* Library / device information: fills name (NUL-terminated, <= len). */
