@@ -180,6 +180,18 @@ __global__ void k_sample(int count, int n, long long offset, long long stride,
     ids[k] = sidx[s];
 }
 
+// Particle ids of the judge's strided sample (ids, not sorted positions, so
+// that the sample needs no tree); the offset moves with the device step
+// counter, so a replayed graph judges a different sample every step.
+__global__ void k_sample_ids(int count, int n, long long stride,
+                             const double *__restrict__ step_ctr, int *__restrict__ ids)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const long long offset = (long long)step_ctr[0] * 7919LL;
+    ids[k] = (int)((offset + (long long)k * stride) % n);
+}
+
 // target = 100 (a_direct - a_cheap) / |a_cheap|, each component clamped to
 // [-clip, clip]: the squared loss is then not dominated by the few particles
 // whose residual is far above the median the method is judged on.
@@ -299,14 +311,20 @@ class LearnedEngine final : public Engine {
         GS_TRY(flag_.reserve(sizeof(int)));
         GS_TRY(stats_.reserve(4 * sizeof(double)));
         GS_TRY(counters_.reserve(2 * sizeof(unsigned long long)));
+        GS_TRY(jframe_.reserve(8 * sizeof(double)));
         GS_CUDA(cudaMemset(flag_.p, 0, sizeof(int)));
         GS_CUDA(cudaMemset(stats_.p, 0, 4 * sizeof(double)));
         GS_CUDA(cudaMemset(counters_.p, 0, 2 * sizeof(unsigned long long)));
+        GS_CUDA(cudaMemset(jframe_.p, 0, 8 * sizeof(double)));
+        GS_CUDA(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
+        GS_CUDA(cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming));
         return ok();
     }
 
     ~LearnedEngine() override
     {
+        if (ev_fork_) cudaEventDestroy(ev_fork_);
+        if (ev_join_) cudaEventDestroy(ev_join_);
         if (own_) cudaStreamDestroy(own_);
     }
 
@@ -317,12 +335,20 @@ class LearnedEngine final : public Engine {
                         ForceTimer *timer) override
     {
         GS_CUDA(cudaMemsetAsync(counters_.p, 0, 2 * sizeof(unsigned long long), s));
-        GS_TRY(tree_.build(d_x, d_m, s));
         if (!trained_) {
+            GS_TRY(tree_.build(d_x, d_m, s));
             GS_TRY(collect(d_x, d_m, d_a, s));
             if (snapshots_ == kSnapshots) GS_TRY(train(s));
+            GS_TRY(keep_frame(s));
             return ok();
         }
+        // The judge's exact rows need only the positions: they run on the
+        // engine's own stream while this stream builds the tree and walks it
+        // (which leave most SMs idle for much of the build).  With a force
+        // timer the rows finish first, so that the walk is timed alone.
+        GS_TRY(judge_rows(d_x, d_m, s));
+        if (timer) GS_CUDA(cudaStreamWaitEvent(s, ev_join_, 0));
+        GS_TRY(tree_.build(d_x, d_m, s));
         unsigned long long *cnt = counters_.as<unsigned long long>();
         if (!useful_) {
             // The network did not earn its cost on the held-out snapshot:
@@ -330,10 +356,11 @@ class LearnedEngine final : public Engine {
             if (timer) GS_TRY(timer->begin(s));
             GS_TRY(launch_bh_group_walk(tree_, kThetaFallback, eps_, G_, d_a, cnt, s));
             if (timer) GS_TRY(timer->end(s));
-            GS_TRY(judge(d_x, d_m, d_a, s));
+            GS_TRY(judge(d_a, s));
             k_replace_rows<<<(J_ + 255) / 256, 256, 0, s>>>(J_, ids_.as<int>(),
                                                             a_rows_.as<double>(), d_a);
             GS_CUDA(cudaGetLastError());
+            GS_TRY(keep_frame(s));
             return ok();
         }
         if (timer) GS_TRY(timer->begin(s));
@@ -342,11 +369,12 @@ class LearnedEngine final : public Engine {
         GS_TRY(features(nullptr, n_, feat_.as<float>(), d_x, d_m, d_a, s));
         GS_TRY(mlp_.forward(feat_.as<float>(), n_, pred_.as<float>(), s));
         k_correct<<<(n_ + 255) / 256, 256, 0, s>>>(n_, tree_.sidx.as<int>(), pred_.as<float>(), d_a);
-        GS_TRY(judge(d_x, d_m, d_a, s));
+        GS_TRY(judge(d_a, s));
         GS_TRY(launch_bh_group_walk(tree_, kThetaFallback, eps_, G_, d_a, cnt, s, flag_.as<int>()));
         k_replace_rows<<<(J_ + 255) / 256, 256, 0, s>>>(J_, ids_.as<int>(), a_rows_.as<double>(),
                                                         d_a);
         GS_CUDA(cudaGetLastError());
+        GS_TRY(keep_frame(s));
         return ok();
     }
 
@@ -418,20 +446,42 @@ class LearnedEngine final : public Engine {
     }
 
   private:
-    // Direct sum of J_ particles (a rotating strided sample) against all;
-    // sets the fallback flag when their median relative error exceeds the
-    // tolerance and records the statistics.
-    ErrorStatus judge(const double *d_x, const double *d_m, const double *d_a, cudaStream_t s)
+    // The judge's exact accelerations: direct sum of J_ particles (a
+    // rotating strided sample of particle ids) against all, on own_, after
+    // everything enqueued on s so far (fork), packed relative to the frame
+    // centre of the previous step's tree (jframe_).  ev_join_ marks the end.
+    ErrorStatus judge_rows(const double *d_x, const double *d_m, cudaStream_t s)
     {
+        GS_CUDA(cudaEventRecord(ev_fork_, s));
+        GS_CUDA(cudaStreamWaitEvent(own_, ev_fork_, 0));
         const long long stride = std::max(1, n_ / J_);
-        k_sample<<<(J_ + 255) / 256, 256, 0, s>>>(J_, n_, 0, stride, stats_.as<double>() + 1,
-                                                  tree_.sidx.as<int>(), pos_.as<int>(),
-                                                  ids_.as<int>());
-        GS_TRY(rows_.compute(d_x, d_m, tree_.frame.as<double>(), ids_.as<int>(), J_, G_, eps_,
-                             a_rows_.as<double>(), s));
+        k_sample_ids<<<(J_ + 255) / 256, 256, 0, own_>>>(J_, n_, stride, stats_.as<double>() + 1,
+                                                         ids_.as<int>());
+        GS_CUDA(cudaGetLastError());
+        GS_TRY(rows_.compute(d_x, d_m, jframe_.as<double>(), ids_.as<int>(), J_, G_, eps_,
+                             a_rows_.as<double>(), own_));
+        GS_CUDA(cudaEventRecord(ev_join_, own_));
+        return ok();
+    }
+
+    // Joins the rows and compares: sets the fallback flag when the median
+    // relative error of the judged particles exceeds the tolerance, and
+    // records the statistics.
+    ErrorStatus judge(const double *d_a, cudaStream_t s)
+    {
+        GS_CUDA(cudaStreamWaitEvent(s, ev_join_, 0));
         k_judge<<<1, JG_THREADS, 0, s>>>(J_, ids_.as<int>(), d_a, a_rows_.as<double>(), kJudgeTol,
                                          flag_.as<int>(), stats_.as<double>());
         GS_CUDA(cudaGetLastError());
+        return ok();
+    }
+
+    // This step's tree frame centre becomes the next step's judge frame
+    // (after the join, so the rows that read jframe_ are done).
+    ErrorStatus keep_frame(cudaStream_t s)
+    {
+        GS_CUDA(cudaMemcpyAsync(jframe_.p, tree_.frame.p, 3 * sizeof(double),
+                                cudaMemcpyDeviceToDevice, s));
         return ok();
     }
 
@@ -548,7 +598,8 @@ class LearnedEngine final : public Engine {
     MlpDevice mlp_;
     DirectRows rows_;
     DBuf a_cheap_, feat_, pred_, pos_, ids_, a_rows_, data_feat_, data_target_, flag_, stats_,
-        counters_;
+        counters_, jframe_;
+    cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
     int snapshots_ = 0;
     bool trained_ = false;
     bool useful_ = false;   // network kept (gain >= 1 - kMinGain, corrected median <= 1e-3)
