@@ -395,6 +395,8 @@ class LearnedEngine final : public Engine {
             return GS_RAISE(GRAV_MEMORY_ERROR, "octree node capacity (%d) exceeded", tree_.cap_nodes);
         if (st & ST_STACK_OVERFLOW)
             return GS_RAISE(GRAV_FAILURE, "tree walk deeper than the octree depth limit");
+        if (st & ST_WAIT_TIMEOUT)
+            return GS_RAISE(GRAV_FAILURE, "octree key sort: a look-back wait ran out");
         GS_TRY(mlp_.check(s));
         GS_TRY(rows_.check(s));
         return ok();

@@ -9,7 +9,7 @@
 //   Morton keys    k_morton: (x - c)/w + 0.5 in FP64, truncation to int64,
 //                  21-bit mask (a coordinate at the box maximum wraps to 0,
 //                  as in the reference), bit interleave.
-//   sort           RadixSorter (stable LSD, 8-bit digits) of (key, id).
+//   sort           RadixSorter (stable LSD, 8-bit digits, one sweep per digit) of (key, id).
 //   topology       level-synchronous: k_tree_expand(d) splits every internal
 //                  node of depth d into its non-empty octants (binary search
 //                  on the sorted keys), appending children to an unordered
@@ -813,7 +813,8 @@ ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream
                                  nd_int.as<int>(), in_node.as<int>());
     GS_CUDA(cudaGetLastError());
     if (tm_sort) GS_TRY(tm_sort->begin(s));
-    GS_TRY(sorter.sort(keys.as<uint64_t>(), sidx.as<int>(), ctr.as<int>() + CTR_N, 63, s));
+    GS_TRY(sorter.sort(keys.as<uint64_t>(), sidx.as<int>(), ctr.as<int>() + CTR_N, n, 63,
+                       reinterpret_cast<unsigned *>(ctr.as<int>() + CTR_STATUS), s));
     if (tm_sort) GS_TRY(tm_sort->end(s));
 
     const DeviceInfo *dev = nullptr;
@@ -831,7 +832,8 @@ ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream
                                                 nd_depth.as<int>(), in_key.as<uint64_t>(),
                                                 in_order.as<int>(), in_arrive.as<int>());
     GS_TRY(sorter.sort(in_key.as<uint64_t>(), in_order.as<int>(), ctr.as<int>() + CTR_SAFE_INTERNAL,
-                       internal_key_bits(), s));
+                       cap_nodes, internal_key_bits(),
+                       reinterpret_cast<unsigned *>(ctr.as<int>() + CTR_STATUS), s));
     const int tiles = (cap_nodes + SCAN_TILE - 1) / SCAN_TILE;
     k_fc_tile_sums<<<tiles, OT_THREADS, 0, s>>>(ctr.as<int>(), in_order.as<int>(),
                                                 in_nchild.as<int>(), scan_tiles.as<unsigned>());

@@ -326,6 +326,8 @@ class BarnesHutEngine final : public Engine {
             return GS_RAISE(GRAV_MEMORY_ERROR, "octree node capacity (%d) exceeded", tree_.cap_nodes);
         if (st & ST_STACK_OVERFLOW)
             return GS_RAISE(GRAV_FAILURE, "tree walk deeper than the octree depth limit");
+        if (st & ST_WAIT_TIMEOUT)
+            return GS_RAISE(GRAV_FAILURE, "octree key sort: a look-back wait ran out");
         return ok();
     }
 
@@ -430,6 +432,8 @@ ErrorStatus octree_to_host(const AccelerationParam &p_in, const System *system,
     GS_TRY(t.read_counts(s, &nodes, &st));
     if (st & ST_TREE_OVERFLOW)
         return GS_RAISE(GRAV_MEMORY_ERROR, "octree node capacity (%d) exceeded", t.cap_nodes);
+    if (st & ST_WAIT_TIMEOUT)
+        return GS_RAISE(GRAV_FAILURE, "octree key sort: a look-back wait ran out");
     LinearOctree o;
     std::memset(&o, 0, sizeof(o));
     o.num_internal_nodes = nodes;
