@@ -345,6 +345,18 @@ def accuracy_sample(a_gpu, x, m, G, eps, rows=4096, seed=0):
     return float(np.median(errs)), float(np.quantile(errs, 0.99))
 
 
+def profile_traffic(kernel, workload, summary=None):
+    """DRAM bytes (read + write) per launch of `kernel` on `workload`, from
+    the ncu capture summarised in profiles/<kernel>_<workload>.md (or the
+    named summary), or None."""
+    prof = ROOT / "profiles" / f"{summary or kernel + '_' + workload}.md"
+    if prof.exists():
+        for ln in prof.read_text().splitlines():
+            if ln.startswith("traffic_bytes_per_launch:"):
+                return float(ln.split(":", 1)[1])
+    return None
+
+
 BH_METHODS = (103, 104, 105, 106, 107, 113)
 FLOP_QUAD_CELL = 56
 
@@ -579,14 +591,9 @@ def run_ours(args, world, rank, local):
     e2e_s, = max_over_ranks([time.perf_counter() - t0], world)
     e2e_val = world * n * args.steps / e2e_s
 
-    traffic = None
     kernel = ("k_bh_group" if wk["method"] in (104, 106, 107) else "k_bh_walk") if bh else \
         ("k_direct_fp64_reference_order" if fp64 else "k_direct_sum")
-    prof = ROOT / "profiles" / f"{kernel}_{args.workload}.md"
-    if prof.exists():
-        for ln in prof.read_text().splitlines():
-            if ln.startswith("traffic_bytes_per_launch:"):
-                traffic = float(ln.split(":", 1)[1])
+    traffic = profile_traffic(kernel, args.workload)
     if bh:
         desc = (f"{args.workload}: galaxy pair N={n}, Barnes-Hut method {wk['method']} "
                 f"theta={wk['theta']} leaf={wk['leaf']}, eps={wk['eps']}, leapfrog dt={wk['dt']}")
@@ -816,7 +823,9 @@ def run_ensemble(args, world, rank, local, wk, g, wl, lib):
         "clocks": clk,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak64.value,
                      "unit": "TFLOP/s", "frac": achieved / peak64.value if peak64.value else None,
-                     "traffic": None,
+                     "traffic": profile_traffic("k_wh_accel", args.workload,
+                                                "ensemble_whfast_" + args.workload)
+                                if wk["integrator"] == 10 else None,
                      "kernel": "k_wh_pairs + k_wh_accel" if wk["integrator"] == 10
                                else "k_ens_massless_accel",
                      "mean_launch_ms": accel_launch_ms, "pair_terms_per_step": terms,
