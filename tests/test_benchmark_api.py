@@ -154,3 +154,26 @@ def test_benchmark_acceleration_report(lib, g, wl, capfd):
     assert st.return_code == g.GRAV_VALUE_ERROR
     lib.free_traceback.argtypes = [ctypes.POINTER(g.ErrorStatus)]
     lib.free_traceback(ctypes.byref(st))
+
+
+def test_reference_benchmark_program_links_and_runs(tmp_path, lib):
+    """grav_sim's own examples/benchmark/c/benchmark.c, compiled against the
+    reference's headers, links this library and runs: its first set is
+    skipped (0 runs) and its second, the CPU Barnes-Hut code 3, is rejected
+    with the library's traceback (the program exits 1)."""
+    import subprocess
+    from oracle.reference import REF_DIR
+    src = REF_DIR / "examples" / "benchmark" / "c" / "benchmark.c"
+    if not src.exists():
+        pytest.skip("grav_sim's sources are not present")
+    libdir = str(__import__("pathlib").Path(lib._name).parent)
+    exe = tmp_path / "benchmark"
+    subprocess.run(["gcc", "-O2", "-std=gnu99", f"-I{REF_DIR / 'src'}", f"-I{REF_DIR / 'pcg'}",
+                    str(src), f"-L{libdir}", "-lgrav_sim_gb300", f"-Wl,-rpath,{libdir}", "-lm",
+                    "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 1
+    assert r.stdout.startswith("Benchmarking acceleration...\n")
+    assert "Test 0:    Skipped since num_times: 0 <= 0" in r.stdout
+    assert "Unknown acceleration method. Got: 3" in r.stderr
+    assert "benchmark_acceleration" in r.stderr
