@@ -765,6 +765,10 @@ def run_ensemble(args, world, rank, local, wk, g, wl, lib):
     clk = clocks.stop()
     total_s, = max_over_ranks([total_s], world)
     kps = ens.kernels_per_step()
+    accel_tpb, drift_tpb = ens.tuning()
+    tuning = {"accel_threads_per_block": accel_tpb, "drift_threads_per_block": drift_tpb,
+              "sort_threads_per_system": [{"class_capacity": c, "threads": t}
+                                          for c, t in ens.sort_tuning()]}
     # the acceleration kernels' own time, for the roofline: K more steps
     # launched directly with CUDA events around them (outside the timed region)
     ens.set_kernel_timing(True)
@@ -814,7 +818,8 @@ def run_ensemble(args, world, rank, local, wk, g, wl, lib):
                    "parallelism": f"replicas x{world}",
                    "l2": f"working set {P * 250 / 2**20:.0f} MiB > L2",
                    "accuracy": "bit-exact to the reference per system (tests/test_gpu_ensemble.py)",
-                   "timing": "host clock around K graph replays with device synchronisation"},
+                   "timing": "host clock around K graph replays with device synchronisation",
+                   "autotune": tuning},
         "e2e": {"value": world * P * args.steps / e2e_s, "unit": "particle-steps/s",
                 "h2d_bytes_per_step": (P * 60) / args.steps,
                 "d2h_bytes_per_step": (P * 60) / args.steps,

@@ -984,6 +984,9 @@ struct gsgpu_ensemble {
 
     int pgrid() const { return (P + 127) / 128; }
     int tpb_accel = 128, tpb_drift = 128;   // chosen by autotune()
+    // threads per system of the sort, per size class (0: the class's default,
+    // half its largest system's power of two); chosen by autotune()
+    int sort_tpb[kSortClasses] = {0, 0, 0};
     bool tuned = false;
     int grid_for(int t) const { return (P + t - 1) / t; }
 
@@ -1030,6 +1033,35 @@ struct gsgpu_ensemble {
                             stream);
             best_of([&](int t) { k_wh_drift<<<grid_for(t), t, 0, stream>>>(Es, P, dt); },
                     tpb_drift);
+            // Threads per system of the sort by distance, per size class.  The
+            // step starts with this sort of the Jacobi arrays, and sorting them
+            // again finds them in order, so these launches leave the step's
+            // result unchanged.
+            for (int c = 0; c < kSortClasses; ++c) {
+                const int count = sort_first[c + 1] - sort_first[c];
+                if (count == 0) continue;
+                const int p2 = sort_pow2[c];
+                float best = 1e30f;
+                for (int div : {2, 4, 8, 16}) {
+                    const int t = std::min(1024, std::max(32, p2 / div));
+                    auto launch = [&]() {
+                        k_wh_sort<<<count, t, (size_t)p2 * 12, stream>>>(
+                            E, E.jx, E.jv, p2, 0, sort_list.as<int>() + sort_first[c]);
+                    };
+                    launch();
+                    if (cudaEventRecord(e0, stream) != cudaSuccess) break;
+                    launch();
+                    launch();
+                    if (cudaEventRecord(e1, stream) != cudaSuccess) break;
+                    if (cudaEventSynchronize(e1) != cudaSuccess) break;
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (ms < best) {
+                        best = ms;
+                        sort_tpb[c] = t;
+                    }
+                }
+            }
         } else {
             best_of([&](int t) { k_ens_massless_accel<<<grid_for(t), t, 0, stream>>>(E, P); },
                     tpb_accel);
@@ -1048,8 +1080,9 @@ struct gsgpu_ensemble {
             if (count == 0) continue;
             const int p2 = sort_pow2[c];
             const size_t smem = (size_t)p2 * 12;
-            // one thread per pair of slots for the odd-even passes, 32..1024
-            const int threads = std::min(1024, std::max(32, p2 / 2));
+            // one thread per pair of slots for the odd-even passes, 32..1024,
+            // unless the autotuner chose fewer
+            const int threads = sort_tpb[c] > 0 ? sort_tpb[c] : std::min(1024, std::max(32, p2 / 2));
             k_wh_sort<<<count, threads, smem, stream>>>(E, vec, vel, p2, vec == E.x ? 1 : 0,
                                                         sort_list.as<int>() + sort_first[c]);
         }
@@ -1482,6 +1515,20 @@ int gsgpu_ensemble_tuning(const gsgpu_ensemble *e, int *accel_threads, int *drif
     if (accel_threads) *accel_threads = e->tuned ? e->tpb_accel : 0;
     if (drift_threads) *drift_threads = e->tuned ? e->tpb_drift : 0;
     return 0;
+}
+
+int gsgpu_ensemble_sort_tuning(const gsgpu_ensemble *e, int *pow2, int *threads, int n)
+{
+    if (!e || !pow2 || !threads) return GRAV_POINTER_ERROR;
+    int k = 0;
+    for (int c = 0; c < kSortClasses && k < n; ++c) {
+        if (e->sort_first[c + 1] == e->sort_first[c]) continue;
+        pow2[k] = e->sort_pow2[c];
+        threads[k] = e->sort_tpb[c] > 0 ? e->sort_tpb[c]
+                                        : std::min(1024, std::max(32, e->sort_pow2[c] / 2));
+        ++k;
+    }
+    return k;
 }
 
 int gsgpu_ensemble_set_kernel_timing(gsgpu_ensemble *e, int enable)

@@ -486,6 +486,13 @@ class Ensemble:
                     "gsgpu_ensemble_tuning")
         return a.value, d.value
 
+    def sort_tuning(self):
+        """[(size-class capacity, threads per system)] of the sort by distance."""
+        p2 = np.zeros(8, dtype=np.int32)
+        th = np.zeros(8, dtype=np.int32)
+        k = self.lib.gsgpu_ensemble_sort_tuning(self.handle, _ip(p2), _ip(th), 8)
+        return [(int(p2[i]), int(th[i])) for i in range(max(k, 0))]
+
     def set_kernel_timing(self, enable: bool) -> None:
         """Direct launches with CUDA events around the drift and the
         accelerations (instead of graph replays) while enabled."""
@@ -534,6 +541,8 @@ def _init_ensemble_api(lib: ctypes.CDLL) -> None:
     lib.gsgpu_ensemble_kernels_per_step.argtypes = [vp]
     lib.gsgpu_ensemble_tuning.restype = ctypes.c_int
     lib.gsgpu_ensemble_tuning.argtypes = [vp, c_int_p, c_int_p]
+    lib.gsgpu_ensemble_sort_tuning.restype = ctypes.c_int
+    lib.gsgpu_ensemble_sort_tuning.argtypes = [vp, c_int_p, c_int_p, ctypes.c_int]
     lib.gsgpu_ensemble_set_kernel_timing.restype = ctypes.c_int
     lib.gsgpu_ensemble_set_kernel_timing.argtypes = [vp, ctypes.c_int]
     lib.gsgpu_ensemble_kernel_timing.restype = ctypes.c_int

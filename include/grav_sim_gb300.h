@@ -447,6 +447,11 @@ int gsgpu_ensemble_num_particles(const gsgpu_ensemble *e);
  * acceleration and drift kernels (timed once after the first half kick;
  * 0 before that). */
 int gsgpu_ensemble_tuning(const gsgpu_ensemble *e, int *accel_threads, int *drift_threads);
+/* Threads per system the autotuner chose for the sort by distance, one
+ * entry per size class of systems present (the class's power-of-two
+ * capacity in pow2[k], its threads in threads[k]); returns the number of
+ * classes written (at most n). */
+int gsgpu_ensemble_sort_tuning(const gsgpu_ensemble *e, int *pow2, int *threads, int n);
 /* Kernel timing (no counterpart in the reference): while enabled, steps are
  * launched directly instead of from the captured graph, with CUDA events
  * around the Kepler drift and around the interaction accelerations (the
