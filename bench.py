@@ -38,8 +38,8 @@ Workloads (seeded synthetic inputs -- grav_sim publishes no dataset):
   galaxy2097152_group_leaf1 / _t065, galaxy1048576_group_leaf1 -- with one
                     particle per leaf (the reference's default tree), or at
                     theta = 0.65 (median error 6.4e-4, inside the 1e-3 bound).
-                    The group workloads use up to 8 particles per leaf, the
-                    library's default for methods 106 and 107.
+                    The group workloads use up to 16 particles per leaf, the
+                    library's default for methods 104, 106 and 107.
   galaxy1048576_group_mono[_t035] -- the group walk with monopole cells
                     only, theta = 0.5 (0.35).
   ensemble8192 / ensemble8192_leapfrog -- 8,192 planetary systems (Sun, 8
@@ -131,43 +131,43 @@ WORKLOADS = {
     # Barnes-Hut on the same GPU (the group walk, and the reference-style
     # monopole walk at theta = 0.5 and at the theta where it meets 1e-3)
     "galaxy1048576_learned": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01, dt=1e-3,
-                                  integrator=4, method=104, theta=1.0, leaf=8,
+                                  integrator=4, method=104, theta=1.0, leaf=16,
                                   flop_per_interaction=20, plain_key="plain_group_theta0.5",
                                   compare=[("plain_group_theta0.5",
-                                            dict(method=106, theta=0.5, leaf=8)),
+                                            dict(method=106, theta=0.5, leaf=16)),
                                            ("plain_monopole_theta0.5",
                                             dict(method=103, theta=0.5, leaf=1)),
                                            ("plain_monopole_theta0.3",
                                             dict(method=103, theta=0.3, leaf=1))]),
     "galaxy2097152_group": dict(ic="galaxy", n=2097152, seed=4, G=1.0, eps=0.01, dt=1e-3,
-                                integrator=4, method=106, theta=0.5, leaf=8,
+                                integrator=4, method=106, theta=0.5, leaf=16,
                                 flop_per_interaction=20),
     "galaxy16777216_group": dict(ic="galaxy", n=16777216, seed=8, G=1.0, eps=0.01, dt=1e-3,
-                                 integrator=4, method=106, theta=0.5, leaf=8,
+                                 integrator=4, method=106, theta=0.5, leaf=16,
                                  flop_per_interaction=20),
     "galaxy2097152_group_leaf1": dict(ic="galaxy", n=2097152, seed=4, G=1.0, eps=0.01, dt=1e-3,
                                       integrator=4, method=106, theta=0.5, leaf=1,
                                       flop_per_interaction=20),
     "galaxy2097152_group_t065": dict(ic="galaxy", n=2097152, seed=4, G=1.0, eps=0.01, dt=1e-3,
-                                     integrator=4, method=106, theta=0.65, leaf=8,
+                                     integrator=4, method=106, theta=0.65, leaf=16,
                                      flop_per_interaction=20),
     "galaxy1048576_group": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01, dt=1e-3,
-                                integrator=4, method=106, theta=0.5, leaf=8,
+                                integrator=4, method=106, theta=0.5, leaf=16,
                                 flop_per_interaction=20),
     "galaxy1048576_group_leaf1": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01, dt=1e-3,
                                       integrator=4, method=106, theta=0.5, leaf=1,
                                       flop_per_interaction=20),
     "galaxy1048576_group_mono": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01, dt=1e-3,
-                                     integrator=4, method=107, theta=0.5, leaf=8,
+                                     integrator=4, method=107, theta=0.5, leaf=16,
                                      flop_per_interaction=20),
     "galaxy1048576_group_mono_t035": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01,
                                           dt=1e-3, integrator=4, method=107, theta=0.35,
-                                          leaf=8, flop_per_interaction=20),
+                                          leaf=16, flop_per_interaction=20),
     # small cases of the walks, for profiler captures
     "galaxy262144": dict(ic="galaxy", n=262144, seed=6, G=1.0, eps=0.01, dt=1e-3, integrator=4,
                          method=105, theta=0.5, leaf=1, flop_per_interaction=20),
     "galaxy262144_group": dict(ic="galaxy", n=262144, seed=6, G=1.0, eps=0.01, dt=1e-3,
-                               integrator=4, method=106, theta=0.5, leaf=8,
+                               integrator=4, method=106, theta=0.5, leaf=16,
                                flop_per_interaction=20),
     "ensemble8192": dict(ic="ensemble", systems=8192, seed=3, max_test=4096, dt=1.0,
                          integrator=10, method=102),

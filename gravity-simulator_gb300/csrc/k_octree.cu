@@ -819,7 +819,9 @@ ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream
 
     const DeviceInfo *dev = nullptr;
     GS_TRY(device_info(&dev));
-    const int grid = dev->sm_count * 8;
+    // Grid-stride kernels: two CTAs per SM cover the largest levels, and a
+    // small grid keeps the launches of the many small levels cheap.
+    const int grid = dev->sm_count * 2;
     for (int d = 0; d < OCT_MAX_LEVEL; ++d) {
         k_tree_expand<<<grid, OT_THREADS, 0, s>>>(
             d, leaf_max, cap_nodes, keys.as<uint64_t>(), ctr.as<int>(), nd_start.as<int>(),

@@ -95,9 +95,9 @@ def test_finalize_acceleration_param_host_logic(lib, g):
     p = g.AccelerationParam(g.METHOD_GPU_BARNES_HUT, 0.5, 0.01, -1)
     st = f(ctypes.byref(p))
     assert st.return_code == 0 and p.max_num_particles_per_leaf == 1
-    p = g.AccelerationParam(106, 0.5, 0.01, -1)    # the group walks default to 8 per leaf
+    p = g.AccelerationParam(106, 0.5, 0.01, -1)    # the group walks default to 16 per leaf
     st = f(ctypes.byref(p))
-    assert st.return_code == 0 and p.max_num_particles_per_leaf == 8
+    assert st.return_code == 0 and p.max_num_particles_per_leaf == 16
     p = g.AccelerationParam(g.METHOD_GPU_BARNES_HUT, 0.5, 0.01, 0)
     st = f(ctypes.byref(p))
     assert st.return_code == g.GRAV_VALUE_ERROR
