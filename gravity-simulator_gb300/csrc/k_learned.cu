@@ -8,10 +8,11 @@
 // from 32 per-particle features of the tree around the particle.
 //
 // Life cycle of the engine (one engine per simulation):
-//   collection   the first kSnapshots force evaluations return the fallback
-//                walk (theta 0.5, monopole + quadrupole) and record one
-//                training snapshot each: features and direct-sum residuals of
-//                65,536 sampled particles (direct sum in compensated FP32);
+//   collection   the first kSnapshots * kCollectStride force evaluations
+//                return the fallback walk (theta 0.5, monopole + quadrupole),
+//                and every kCollectStride-th of them records a training
+//                snapshot: features and direct-sum residuals of 65,536
+//                sampled particles (direct sum in compensated FP32);
 //   training     after the last snapshot, the network is trained on the GPU
 //                by its own tcgen05 forward / backward kernels and Adam; the
 //                last snapshot is held out to measure what the network gains;
@@ -60,6 +61,11 @@ namespace gs {
 namespace {
 
 constexpr int kSnapshots = 64;
+// One training snapshot every kCollectStride force evaluations (the others
+// are the fallback walk alone): the snapshots' direct sums (65,536 rows
+// each) are spread over more steps, and the snapshots lie further apart in
+// time.
+constexpr int kCollectStride = 4;
 constexpr int kSamplesPerSnapshot = 65536;
 constexpr int kJudge = 4096;
 constexpr double kJudgeTol = 1e-3;
@@ -337,8 +343,13 @@ class LearnedEngine final : public Engine {
         GS_CUDA(cudaMemsetAsync(counters_.p, 0, 2 * sizeof(unsigned long long), s));
         if (!trained_) {
             GS_TRY(tree_.build(d_x, d_m, s));
-            GS_TRY(collect(d_x, d_m, d_a, s));
-            if (snapshots_ == kSnapshots) GS_TRY(train(s));
+            if (collect_steps_++ % kCollectStride == 0) {
+                GS_TRY(collect(d_x, d_m, d_a, s));
+                if (snapshots_ == kSnapshots) GS_TRY(train(s));
+            } else {
+                GS_TRY(launch_bh_group_walk(tree_, kThetaFallback, eps_, G_, d_a,
+                                            counters_.as<unsigned long long>(), s));
+            }
             GS_TRY(keep_frame(s));
             return ok();
         }
@@ -603,6 +614,7 @@ class LearnedEngine final : public Engine {
         counters_, jframe_;
     cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
     int snapshots_ = 0;
+    long long collect_steps_ = 0;
     bool trained_ = false;
     bool useful_ = false;   // network kept (gain >= 1 - kMinGain, corrected median <= 1e-3)
     int adam_steps_ = 0;

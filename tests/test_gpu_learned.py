@@ -53,7 +53,7 @@ def test_learned_correction_trains_gains_and_is_judged(lib, g, orc, wl):
         assert lib.gsgpu_sim_upload(sim, x.ctypes.data_as(dp), v.ctypes.data_as(dp),
                                     m.ctypes.data_as(dp)) == 0
         taken = ctypes.c_int64()
-        assert lib.gsgpu_sim_warmup_until_ready(sim, 200, ctypes.byref(taken)) == 0
+        assert lib.gsgpu_sim_warmup_until_ready(sim, 400, ctypes.byref(taken)) == 0
         rep = np.zeros(13)
         k = lib.gsgpu_sim_report(sim, rep.ctypes.data_as(dp), 13)
         assert k == 13 and rep[0] == 1.0 and rep[1] == 64
