@@ -247,17 +247,30 @@ ErrorStatus pm_acceleration_host(double *a, int n, const double *x, const double
                                  const double *box_center, double box_width, double H0,
                                  double omega_m, double mean_bkg_density, int pm_grid_size,
                                  double scale_factor);
+// op: snapshots as src/integrator_cosmology_leapfrog.c writes them (NULL or
+// disabled for none); at each one the host x and v are updated.
 ErrorStatus pm_leapfrog_cosmology(CosmologicalSystem *system, SimulationStatus *status,
-                                  const bool *is_exit, double dt, double a_begin, double a_final,
-                                  int pm_grid_size);
+                                  OutputParam *op, const bool *is_exit, double dt, double a_begin,
+                                  double a_final, int pm_grid_size);
 // Device time of the step loop of this thread's last cosmological run.
 ErrorStatus pm_last_timing(double *loop_ms, int64_t *steps);
 
 // ---- snapshots (host_output.cpp) ----------------------------------------
 ErrorStatus output_prepare(OutputParam *op, const Settings *settings);
 // Write snapshot number op->output_count_ from host arrays and count it.
-ErrorStatus output_snapshot_csv(OutputParam *op, int n, const int *ids, const double *x,
-                                const double *v, const double *m, double G, double t, double dt);
+ErrorStatus output_snapshot(OutputParam *op, int n, const int *ids, const double *x,
+                            const double *v, const double *m, double G, double t, double dt);
+// The header values a cosmological snapshot adds (src/output.c:697-900).
+struct CosmologyHeader {
+    double omega_m, omega_lambda, unit_length, unit_mass, unit_time;
+};
+ErrorStatus write_snapshot_hdf5(const char *path, int n, const int *ids, const double *x,
+                                const double *v, const double *m, double t, bool x_float,
+                                bool v_float, bool m_float, const CosmologyHeader *cosmo);
+// src/output.c:294-345: a cosmological snapshot of the host arrays (HDF5
+// only), numbered and counted like output_snapshot.
+ErrorStatus output_snapshot_cosmology(OutputParam *op, const CosmologicalSystem *system,
+                                      double t);
 
 class SnapshotWriter;
 
@@ -273,7 +286,10 @@ struct OutputContext {
 
     OutputContext();
     ~OutputContext();   // waits for the writer
-    bool active() const { return op && op->method == OUTPUT_METHOD_CSV; }
+    bool active() const
+    {
+        return op && (op->method == OUTPUT_METHOD_CSV || op->method == OUTPUT_METHOD_HDF5);
+    }
     // Start of a run: the first snapshot after the initial one is due at
     // one output interval (src/integrator.c:300-303).
     void begin() { next_time = op->output_interval; }

@@ -107,16 +107,12 @@ ErrorStatus leapfrog_cosmology(CosmologicalSystem *system, OutputParam *output_p
 {
     if (!system || !output_param || !simulation_status || !settings)
         return GS_RAISE(GRAV_POINTER_ERROR, "NULL argument");
-    // Cosmological snapshots are HDF5 only (src/output.c:294-337), which this
-    // library, like the reference built without libhdf5, does not write.
+    // Cosmological snapshots are HDF5 only (src/output.c:294-337).
     if (output_param->method == OUTPUT_METHOD_CSV)
         return GS_RAISE(GRAV_VALUE_ERROR,
                         "CSV output method is not supported for cosmological simulation.");
-    if (output_param->method != OUTPUT_METHOD_DISABLED)
-        return GS_RAISE(GRAV_VALUE_ERROR, "HDF5 output method is not available. Please "
-                                          "recompile with HDF5 support.");
-    return gs::pm_leapfrog_cosmology(system, simulation_status, settings->is_exit_ptr, dt, a_begin,
-                                     a_final, pm_grid_size);
+    return gs::pm_leapfrog_cosmology(system, simulation_status, output_param,
+                                     settings->is_exit_ptr, dt, a_begin, a_final, pm_grid_size);
 }
 
 // src/grav_sim.c:140-255

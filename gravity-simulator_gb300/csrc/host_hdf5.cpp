@@ -410,10 +410,376 @@ ErrorStatus read_part_type(const H5 &f, const char *group, uint64_t n, double *m
     return ok();
 }
 
+// ---- writer ----------------------------------------------------------
+// Snapshot files in the layout of grav_sim's HDF5 output
+// (src/output.c:483-695): group /Header with the int attributes
+// NumFilesPerSnapshot, NumPart_ThisFile, NumPart_Total and the double
+// attribute Time (each a one-element simple dataspace), and group
+// /PartType0 with the datasets ParticleIDs (int32 [N]), Masses ([N]),
+// Coordinates ([N][3]) and Velocities ([N][3]), FP32 or FP64 as the
+// output dtypes say.  The file is built in memory with the same structures
+// the reader above follows (version-0 superblock, version-1 object headers,
+// symbol-table groups with one B-tree node and one symbol table node each,
+// contiguous little-endian data) and written in one piece.
+
+constexpr uint64_t H5_UNDEF = ~0ull;
+constexpr int H5_LEAF_K = 4;       // symbol table node: 2K entries
+constexpr int H5_INTERNAL_K = 16;  // group B-tree node: 2K children
+
+class H5Builder {
+  public:
+    std::vector<unsigned char> b;
+
+    uint64_t alloc(size_t n)
+    {
+        const uint64_t at = (b.size() + 7) & ~(uint64_t)7;
+        b.resize(at + n, 0);
+        return at;
+    }
+    void put(uint64_t at, uint64_t v, int n)
+    {
+        for (int k = 0; k < n; ++k) b[at + k] = (unsigned char)(v >> (8 * k));
+    }
+    void put_bytes(uint64_t at, const void *src, size_t n) { std::memcpy(&b[at], src, n); }
+};
+
+using Bytes = std::vector<unsigned char>;
+
+void le(Bytes &o, uint64_t v, int n)
+{
+    for (int k = 0; k < n; ++k) o.push_back((unsigned char)(v >> (8 * k)));
+}
+
+void pad8(Bytes &o)
+{
+    while (o.size() % 8) o.push_back(0);
+}
+
+// Datatype message (version 1): little-endian int32, FP32 or FP64.
+Bytes h5_dtype(int kind)
+{
+    Bytes o;
+    if (kind == 0) {   // int32, signed
+        o = {0x10, 0x08, 0x00, 0x00};
+        le(o, 4, 4);
+        le(o, 0, 2);    // bit offset
+        le(o, 32, 2);   // precision
+    } else if (kind == 1) {   // IEEE binary32
+        o = {0x11, 0x20, 31, 0x00};
+        le(o, 4, 4);
+        le(o, 0, 2);
+        le(o, 32, 2);
+        o.push_back(23);   // exponent location
+        o.push_back(8);    // exponent size
+        o.push_back(0);    // mantissa location
+        o.push_back(23);   // mantissa size
+        le(o, 127, 4);     // exponent bias
+    } else {   // IEEE binary64
+        o = {0x11, 0x20, 63, 0x00};
+        le(o, 8, 4);
+        le(o, 0, 2);
+        le(o, 64, 2);
+        o.push_back(52);
+        o.push_back(11);
+        o.push_back(0);
+        o.push_back(52);
+        le(o, 1023, 4);
+    }
+    return o;
+}
+
+// Dataspace (version 1): simple with the given dimensions, scalar when none.
+Bytes h5_space(const std::vector<uint64_t> &dims)
+{
+    Bytes o = {1, (unsigned char)dims.size(), 0, 0, 0, 0, 0, 0};
+    for (uint64_t d : dims) le(o, d, 8);
+    return o;
+}
+
+struct H5Msg {
+    int type;
+    Bytes data;
+};
+
+// Version-1 object header holding the messages (each padded to 8 bytes).
+uint64_t h5_object_header(H5Builder &w, const std::vector<H5Msg> &msgs)
+{
+    size_t body = 0;
+    for (const H5Msg &m : msgs) body += 8 + ((m.data.size() + 7) & ~(size_t)7);
+    const uint64_t at = w.alloc(16 + body);
+    w.put(at, 1, 1);   // version
+    w.put(at + 2, msgs.size(), 2);
+    w.put(at + 4, 1, 4);   // reference count
+    w.put(at + 8, body, 4);
+    uint64_t p = at + 16;
+    for (const H5Msg &m : msgs) {
+        const size_t sz = (m.data.size() + 7) & ~(size_t)7;
+        w.put(p, (uint64_t)m.type, 2);
+        w.put(p + 2, sz, 2);
+        if (!m.data.empty()) w.put_bytes(p + 8, m.data.data(), m.data.size());
+        p += 8 + sz;
+    }
+    return at;
+}
+
+struct H5Child {
+    std::string name;   // children in ascending name order
+    uint64_t ohdr;
+    bool group;
+    uint64_t btree, heap;   // a group's symbol table
+};
+
+// A group's local heap, B-tree node and symbol table node; returns the
+// (B-tree, heap) addresses of its symbol table message.
+void h5_symbol_table(H5Builder &w, const std::vector<H5Child> &kids, uint64_t *btree,
+                     uint64_t *heap)
+{
+    Bytes data(8, 0);   // offset 0: the empty name
+    std::vector<uint64_t> name_off;
+    for (const H5Child &c : kids) {
+        name_off.push_back(data.size());
+        data.insert(data.end(), c.name.begin(), c.name.end());
+        data.push_back(0);
+        pad8(data);
+    }
+    const uint64_t hd = w.alloc(data.size());
+    w.put_bytes(hd, data.data(), data.size());
+    *heap = w.alloc(32);
+    w.put_bytes(*heap, "HEAP", 4);
+    w.put(*heap + 8, data.size(), 8);
+    w.put(*heap + 16, H5_UNDEF, 8);   // no free block
+    w.put(*heap + 24, hd, 8);
+    uint64_t snod = 0;
+    if (!kids.empty()) {
+        snod = w.alloc(8 + 2 * H5_LEAF_K * 40);
+        w.put_bytes(snod, "SNOD", 4);
+        w.put(snod + 4, 1, 1);
+        w.put(snod + 6, kids.size(), 2);
+        for (size_t k = 0; k < kids.size(); ++k) {
+            const uint64_t e = snod + 8 + 40 * k;
+            w.put(e, name_off[k], 8);
+            w.put(e + 8, kids[k].ohdr, 8);
+            if (kids[k].group) {
+                w.put(e + 16, 1, 4);   // cache type 1: the symbol table's addresses
+                w.put(e + 24, kids[k].btree, 8);
+                w.put(e + 32, kids[k].heap, 8);
+            }
+        }
+    }
+    *btree = w.alloc(24 + 8 * (2 * H5_INTERNAL_K + 1) + 8 * (2 * H5_INTERNAL_K));
+    w.put_bytes(*btree, "TREE", 4);
+    w.put(*btree + 4, 0, 1);   // group node
+    w.put(*btree + 5, 0, 1);   // leaf level
+    w.put(*btree + 6, kids.empty() ? 0 : 1, 2);
+    w.put(*btree + 8, H5_UNDEF, 8);
+    w.put(*btree + 16, H5_UNDEF, 8);
+    if (!kids.empty()) {
+        w.put(*btree + 24, 0, 8);                       // key 0: the empty name
+        w.put(*btree + 32, snod, 8);                    // child 0
+        w.put(*btree + 40, name_off.back(), 8);         // key 1: the last name
+    }
+}
+
+H5Msg h5_symbol_table_msg(uint64_t btree, uint64_t heap)
+{
+    Bytes o;
+    le(o, btree, 8);
+    le(o, heap, 8);
+    return {0x11, o};
+}
+
+// Attribute message (version 1) holding one value: a one-element simple
+// dataspace, or a scalar one.
+H5Msg h5_attribute(const char *name, int kind, const void *value, bool scalar = false)
+{
+    Bytes nm(name, name + std::strlen(name) + 1);
+    const Bytes t = h5_dtype(kind), sp = scalar ? h5_space({}) : h5_space({1});
+    Bytes o = {1, 0};
+    le(o, nm.size(), 2);
+    le(o, t.size(), 2);
+    le(o, sp.size(), 2);
+    o.insert(o.end(), nm.begin(), nm.end());
+    pad8(o);
+    o.insert(o.end(), t.begin(), t.end());
+    pad8(o);
+    o.insert(o.end(), sp.begin(), sp.end());
+    pad8(o);
+    const int vsize = kind == 2 ? 8 : 4;
+    const unsigned char *v = static_cast<const unsigned char *>(value);
+    o.insert(o.end(), v, v + vsize);
+    return {0x0c, o};
+}
+
+// A contiguous dataset: its raw data, then its object header.
+uint64_t h5_dataset(H5Builder &w, int kind, const std::vector<uint64_t> &dims, const void *raw,
+                    size_t raw_bytes)
+{
+    const uint64_t data = w.alloc(raw_bytes);
+    if (raw_bytes) w.put_bytes(data, raw, raw_bytes);
+    Bytes fill = {2, 2, 2, 0};   // fill value (v2): late allocation, never written, undefined
+    Bytes layout = {3, 1};       // data layout (v3): contiguous
+    le(layout, data, 8);
+    le(layout, raw_bytes, 8);
+    return h5_object_header(w, {{0x01, h5_space(dims)}, {0x03, h5_dtype(kind)}, {0x05, fill},
+                                {0x08, layout}});
+}
+
+}  // namespace
+
+ErrorStatus write_snapshot_hdf5(const char *path, int n, const int *ids, const double *x,
+                                const double *v, const double *m, double t, bool x_float,
+                                bool v_float, bool m_float, const CosmologyHeader *cosmo)
+{
+    if (n < 0) return GS_RAISE(GRAV_VALUE_ERROR, "negative particle count %d", n);
+    const size_t N = (size_t)n;
+    H5Builder w;
+    w.alloc(96);   // superblock, filled last
+    // /PartType0 datasets
+    std::vector<float> f32;
+    auto dataset = [&](bool as_float, const double *src, size_t count,
+                       std::vector<uint64_t> dims) -> uint64_t {
+        if (as_float) {
+            f32.resize(count);
+            for (size_t i = 0; i < count; ++i) f32[i] = (float)src[i];
+            return h5_dataset(w, 1, dims, f32.data(), count * 4);
+        }
+        return h5_dataset(w, 2, dims, src, count * 8);
+    };
+    const uint64_t d_coord = dataset(x_float, x, 3 * N, {N, 3});
+    const uint64_t d_mass = dataset(m_float, m, N, {N});
+    const uint64_t d_ids = h5_dataset(w, 0, {N}, ids, N * 4);
+    const uint64_t d_vel = dataset(v_float, v, 3 * N, {N, 3});
+    uint64_t pt_bt = 0, pt_heap = 0;
+    h5_symbol_table(w,
+                    {{"Coordinates", d_coord, false, 0, 0}, {"Masses", d_mass, false, 0, 0},
+                     {"ParticleIDs", d_ids, false, 0, 0}, {"Velocities", d_vel, false, 0, 0}},
+                    &pt_bt, &pt_heap);
+    const uint64_t pt = h5_object_header(w, {h5_symbol_table_msg(pt_bt, pt_heap)});
+    // /Header: an empty group with four attributes; a cosmological snapshot
+    // (src/output.c:697-900) has a scalar Time and Redshift = 1/a - 1,
+    // Omega0 and OmegaLambda besides
+    uint64_t hd_bt = 0, hd_heap = 0;
+    h5_symbol_table(w, {}, &hd_bt, &hd_heap);
+    const int one = 1;
+    std::vector<H5Msg> hmsg = {h5_symbol_table_msg(hd_bt, hd_heap),
+                               h5_attribute("NumFilesPerSnapshot", 0, &one),
+                               h5_attribute("NumPart_ThisFile", 0, &n),
+                               h5_attribute("NumPart_Total", 0, &n),
+                               h5_attribute("Time", 2, &t, cosmo != nullptr)};
+    const double z = 1.0 / t - 1.0;
+    if (cosmo) {
+        hmsg.push_back(h5_attribute("Redshift", 2, &z, true));
+        hmsg.push_back(h5_attribute("Omega0", 2, &cosmo->omega_m, true));
+        hmsg.push_back(h5_attribute("OmegaLambda", 2, &cosmo->omega_lambda, true));
+    }
+    const uint64_t hdr = h5_object_header(w, hmsg);
+    std::vector<H5Child> root_kids = {{"Header", hdr, true, hd_bt, hd_heap},
+                                      {"PartType0", pt, true, pt_bt, pt_heap}};
+    if (cosmo) {
+        // /Units: the cgs units, current and temperature 1
+        uint64_t un_bt = 0, un_heap = 0;
+        h5_symbol_table(w, {}, &un_bt, &un_heap);
+        const double unity = 1.0;
+        const uint64_t un = h5_object_header(
+            w, {h5_symbol_table_msg(un_bt, un_heap),
+                h5_attribute("Unit current in cgs (U_I)", 2, &unity, true),
+                h5_attribute("Unit length in cgs (U_L)", 2, &cosmo->unit_length, true),
+                h5_attribute("Unit mass in cgs (U_M)", 2, &cosmo->unit_mass, true),
+                h5_attribute("Unit time in cgs (U_t)", 2, &cosmo->unit_time, true),
+                h5_attribute("Unit temperature in cgs (U_T)", 2, &unity, true)});
+        root_kids.push_back({"Units", un, true, un_bt, un_heap});
+    }
+    // root group
+    uint64_t rt_bt = 0, rt_heap = 0;
+    h5_symbol_table(w, root_kids, &rt_bt, &rt_heap);
+    const uint64_t root = h5_object_header(w, {h5_symbol_table_msg(rt_bt, rt_heap)});
+    // superblock (version 0)
+    static const unsigned char sig[8] = {0x89, 'H', 'D', 'F', '\r', '\n', 0x1a, '\n'};
+    w.put_bytes(0, sig, 8);
+    w.put(13, 8, 1);   // size of offsets
+    w.put(14, 8, 1);   // size of lengths
+    w.put(16, H5_LEAF_K, 2);
+    w.put(18, H5_INTERNAL_K, 2);
+    w.put(24, 0, 8);          // base address
+    w.put(32, H5_UNDEF, 8);   // free-space info
+    w.put(40, w.b.size(), 8); // end of file
+    w.put(48, H5_UNDEF, 8);   // driver information
+    w.put(56, 0, 8);          // root entry: name offset
+    w.put(64, root, 8);
+    w.put(72, 1, 4);          // cache type 1
+    w.put(80, rt_bt, 8);
+    w.put(88, rt_heap, 8);
+    std::FILE *fp = std::fopen(path, "wb");
+    if (!fp)
+        return GS_RAISE(GRAV_OS_ERROR, "Failed to create HDF5 file for storing snapshots: \"%s\".",
+                        path);
+    const size_t wrote = std::fwrite(w.b.data(), 1, w.b.size(), fp);
+    const bool bad = wrote != w.b.size() || std::ferror(fp) != 0;
+    std::fclose(fp);
+    if (bad) return GS_RAISE(GRAV_OS_ERROR, "Failed to write snapshot file: \"%s\".", path);
+    return ok();
+}
+
+namespace {
+
+// The values of one dataset or attribute of a file, by path (a test and
+// reading aid for the snapshots above).
+ErrorStatus read_path(const char *path, const char *object, const char *attribute,
+                      std::vector<double> &out, std::vector<uint64_t> &dims)
+{
+    H5 f;
+    GS_TRY(open_h5(path, f));
+    uint64_t oh = 0;
+    GS_TRY(lookup(f, object, &oh));
+    if (attribute) {
+        dims.clear();
+        GS_TRY(read_attribute(f, oh, attribute, out));
+        dims.push_back(out.size());
+        return ok();
+    }
+    return read_dataset(f, oh, out, dims);
+}
+
 }  // namespace
 }  // namespace gs
 
 extern "C" {
+
+int gsgpu_hdf5_read(const char *path, const char *object, const char *attribute, double *out,
+                    long long capacity, long long *count)
+{
+    if (!path || !object || !count) return GRAV_POINTER_ERROR;
+    std::vector<double> v;
+    std::vector<uint64_t> dims;
+    ErrorStatus st = gs::read_path(path, object, attribute, v, dims);
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    *count = (long long)v.size();
+    if (out) {
+        if ((long long)v.size() > capacity) return GRAV_VALUE_ERROR;
+        std::memcpy(out, v.data(), v.size() * sizeof(double));
+    }
+    return GRAV_SUCCESS;
+}
+
+int gsgpu_write_snapshot_hdf5(const char *path, int num_particles, const int *ids,
+                              const double *x, const double *v, const double *m, double t,
+                              int coordinate_output_dtype, int velocity_output_dtype,
+                              int mass_output_dtype)
+{
+    if (!path || (num_particles > 0 && (!ids || !x || !v || !m))) return GRAV_POINTER_ERROR;
+    ErrorStatus st = gs::write_snapshot_hdf5(
+        path, num_particles, ids, x, v, m, t, coordinate_output_dtype == OUTPUT_DTYPE_FLOAT,
+        velocity_output_dtype == OUTPUT_DTYPE_FLOAT, mass_output_dtype == OUTPUT_DTYPE_FLOAT,
+        nullptr);
+    if (st.return_code != GRAV_SUCCESS) {
+        print_and_free_traceback(&st);
+        return st.return_code;
+    }
+    return GRAV_SUCCESS;
+}
 
 // src/system.c: free_system releases the four arrays of a System.
 void free_system(System *system)

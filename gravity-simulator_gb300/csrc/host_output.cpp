@@ -1,4 +1,4 @@
-// host_output.cpp -- CSV snapshots written by launch_simulation.
+// host_output.cpp -- CSV and HDF5 snapshots written by launch_simulation.
 //
 // The output parameters are checked as src/output.c:100-239 checks them
 // (method, positive interval, a directory path ending in '/', or
@@ -6,7 +6,9 @@
 // snapshot is the reference's CSV file (src/output.c:380-470): the path
 // "<dir>snapshot_%05d.csv" numbered by OutputParam.output_count_, four
 // metadata lines, the header line, then one line per particle with "%.17g"
-// (double) or "%.8g" (float output dtype) fields.
+// (double) or "%.8g" (float output dtype) fields.  An HDF5 snapshot
+// (src/output.c:483-695) is "<dir>snapshot_%05d.hdf5", written by
+// write_snapshot_hdf5 (host_hdf5.cpp).
 //
 // Snapshots inside the step loop are asynchronous: the state is copied
 // device->host on the run's stream into one of two pinned slots, an event
@@ -36,10 +38,8 @@ ErrorStatus output_prepare(OutputParam *op, const Settings *settings)
     case OUTPUT_METHOD_DISABLED:
         return ok();
     case OUTPUT_METHOD_CSV:
-        break;
     case OUTPUT_METHOD_HDF5:
-        // the reference's build without HDF5 (no libhdf5 on the path)
-        return GS_RAISE(GRAV_MEMORY_ERROR, "HDF5 output method is not available");
+        break;
     default:
         return GS_RAISE(GRAV_VALUE_ERROR, "Unknown output method. Got: %d", op->method);
     }
@@ -113,6 +113,22 @@ ErrorStatus write_csv(const OutputParam *op, int index, int n, const int *ids, c
     return ok();
 }
 
+// src/output.c:241-290: the snapshot in the file format the method names.
+ErrorStatus write_snapshot(const OutputParam *op, int index, int n, const int *ids,
+                           const double *x, const double *v, const double *m, double G, double t,
+                           double dt)
+{
+    if (op->method != OUTPUT_METHOD_HDF5) return write_csv(op, index, n, ids, x, v, m, G, t, dt);
+    char path[4096];
+    const int len = std::snprintf(path, sizeof(path), "%ssnapshot_%05d.hdf5", op->output_dir, index);
+    if (len < 0) return GS_RAISE(GRAV_VALUE_ERROR, "Failed to get storing file path string");
+    if (len >= (int)sizeof(path)) return GS_RAISE(GRAV_VALUE_ERROR, "Storing file path string is truncated.");
+    return write_snapshot_hdf5(path, n, ids, x, v, m, t,
+                               op->coordinate_output_dtype == OUTPUT_DTYPE_FLOAT,
+                               op->velocity_output_dtype == OUTPUT_DTYPE_FLOAT,
+                               op->mass_output_dtype == OUTPUT_DTYPE_FLOAT, nullptr);
+}
+
 template <class T> ErrorStatus pinned(T *&p, size_t count)
 {
     GS_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&p), count * sizeof(T), cudaHostAllocDefault));
@@ -121,10 +137,41 @@ template <class T> ErrorStatus pinned(T *&p, size_t count)
 
 }  // namespace
 
-ErrorStatus output_snapshot_csv(OutputParam *op, int n, const int *ids, const double *x,
-                                const double *v, const double *m, double G, double t, double dt)
+ErrorStatus output_snapshot(OutputParam *op, int n, const int *ids, const double *x,
+                            const double *v, const double *m, double G, double t, double dt)
 {
-    GS_TRY(write_csv(op, op->output_count_, n, ids, x, v, m, G, t, dt));
+    GS_TRY(write_snapshot(op, op->output_count_, n, ids, x, v, m, G, t, dt));
+    ++op->output_count_;
+    return ok();
+}
+
+ErrorStatus output_snapshot_cosmology(OutputParam *op, const CosmologicalSystem *system, double t)
+{
+    switch (op->method) {
+    case OUTPUT_METHOD_DISABLED:
+        break;
+    case OUTPUT_METHOD_CSV:
+        return GS_RAISE(GRAV_VALUE_ERROR,
+                        "CSV output method is not supported for cosmological simulation.");
+    case OUTPUT_METHOD_HDF5: {
+        char path[4096];
+        const int len = std::snprintf(path, sizeof(path), "%ssnapshot_%05d.hdf5", op->output_dir,
+                                      op->output_count_);
+        if (len < 0) return GS_RAISE(GRAV_VALUE_ERROR, "Failed to get storing file path string");
+        if (len >= (int)sizeof(path))
+            return GS_RAISE(GRAV_VALUE_ERROR, "Storing file path string is truncated.");
+        const CosmologyHeader h = {system->omega_m, system->omega_lambda, system->unit_length,
+                                   system->unit_mass, system->unit_time};
+        GS_TRY(write_snapshot_hdf5(path, system->num_particles, system->particle_ids, system->x,
+                                   system->v, system->m, t,
+                                   op->coordinate_output_dtype == OUTPUT_DTYPE_FLOAT,
+                                   op->velocity_output_dtype == OUTPUT_DTYPE_FLOAT,
+                                   op->mass_output_dtype == OUTPUT_DTYPE_FLOAT, &h));
+        break;
+    }
+    default:
+        return GS_RAISE(GRAV_VALUE_ERROR, "Unknown output method. Got: %d", op->method);
+    }
     ++op->output_count_;
     return ok();
 }
@@ -258,8 +305,8 @@ class SnapshotWriter {
             } else {
                 int n = s.n;
                 if (s.dev_cnt) n = *s.cnt < n ? *s.cnt : n;
-                e = write_csv(op_, s.index, n, s.dev_ids ? s.ids : system_->particle_ids, s.x, s.v,
-                              s.dev_m ? s.m : system_->m, system_->G, s.t, s.dt);
+                e = write_snapshot(op_, s.index, n, s.dev_ids ? s.ids : system_->particle_ids,
+                                   s.x, s.v, s.dev_m ? s.m : system_->m, system_->G, s.t, s.dt);
             }
             std::lock_guard<std::mutex> lk(mu_);
             if (e.return_code != GRAV_SUCCESS) {

@@ -463,8 +463,8 @@ struct gsgpu_sim {
         oc->begin();
         if (!oc->initial()) return ok();
         const System *sys = oc->system;
-        return output_snapshot_csv(oc->op, n, sys->particle_ids, sys->x, sys->v, sys->m, G,
-                                   status ? status->t : 0.0, status ? status->dt : 0.0);
+        return output_snapshot(oc->op, n, sys->particle_ids, sys->x, sys->v, sys->m, G,
+                               status ? status->t : 0.0, status ? status->dt : 0.0);
     }
 
     // A snapshot of x and the velocity array dv at time t after a step of h

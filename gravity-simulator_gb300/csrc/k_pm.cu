@@ -248,6 +248,15 @@ __global__ void k_cosmo_momentum(double *__restrict__ p, const double *__restric
     p[k] = t * t * v[k];
 }
 
+// velocity = momentum / a^2 at a snapshot (:200-209)
+__global__ void k_cosmo_velocity(double *__restrict__ v, const double *__restrict__ p, int len,
+                                 double t)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= len) return;
+    v[k] = p[k] / (t * t);
+}
+
 // momentum -= (0.5 dt) a / da (:142-149, :176-183); c = 0.5 dt / da
 __global__ void k_cosmo_kick(double *__restrict__ p, const double *__restrict__ a, int len,
                              double c)
@@ -414,12 +423,12 @@ ErrorStatus pm_acceleration_host(double *a, int n, const double *x, const double
     return ok();
 }
 
-// src/integrator_cosmology_leapfrog.c:24-255, output disabled (the
-// reference writes cosmological snapshots as HDF5 only).  x is advanced in
-// HBM; v is left as given, as the reference leaves it.
+// src/integrator_cosmology_leapfrog.c:24-255.  x is advanced in HBM; the
+// host v is written only at snapshots (v = p / a^2), as the reference
+// writes it, and is otherwise left as given.
 ErrorStatus pm_leapfrog_cosmology(CosmologicalSystem *system, SimulationStatus *status,
-                                  const bool *is_exit, double dt, double a_begin, double a_final,
-                                  int g)
+                                  OutputParam *op, const bool *is_exit, double dt, double a_begin,
+                                  double a_final, int g)
 {
     const int n = system->num_particles;
     GS_TRY(pm_check(n, system->x, system->m, system->box_center, g));
@@ -444,6 +453,10 @@ ErrorStatus pm_leapfrog_cosmology(CosmologicalSystem *system, SimulationStatus *
 
     double t = a_begin;
     if (status) status->t = t;
+    // snapshots (:49-52, :76-88): the initial one of the caller's arrays
+    const bool is_output = op && op->method != OUTPUT_METHOD_DISABLED;
+    double next_output_time = is_output ? op->output_interval : 0.0;
+    if (is_output && op->output_initial) GS_TRY(output_snapshot_cosmology(op, system, t));
     double msum = 0.0;   // vec_sum (src/math_functions.c:13-21), in order
     for (int i = 0; i < n; ++i) msum += system->m[i];
     const double mean_bkg_density = msum / ((bw * 2) * (bw * 2) * (bw * 2));
@@ -479,6 +492,16 @@ ErrorStatus pm_leapfrog_cosmology(CosmologicalSystem *system, SimulationStatus *
         if (status) {
             status->t = t;
             status->num_steps = steps;
+        }
+        if (is_output && t >= next_output_time) {
+            // the host arrays get x and v = p / a^2, then the snapshot (:198-221)
+            k_cosmo_velocity<<<blocks(L), TPB, 0, s>>>(v.as<double>(), p.as<double>(), L, t);
+            GS_CUDA(cudaGetLastError());
+            GS_CUDA(cudaMemcpyAsync(system->x, x.p, b3, cudaMemcpyDeviceToHost, s));
+            GS_CUDA(cudaMemcpyAsync(system->v, v.p, b3, cudaMemcpyDeviceToHost, s));
+            GS_CUDA(cudaStreamSynchronize(s));
+            GS_TRY(output_snapshot_cosmology(op, system, t));
+            next_output_time = op->output_count_ * op->output_interval;
         }
         if (is_exit && *is_exit) break;
     }

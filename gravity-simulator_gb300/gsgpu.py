@@ -256,10 +256,17 @@ def launch_cosmological_simulation(lib: ctypes.CDLL, x: np.ndarray, v: np.ndarra
                                    *, h: float, omega_m: float, omega_lambda: float, box_center,
                                    box_width: float, dt: float, a_begin: float, a_final: float,
                                    pm_grid_size: int, output_method: int = OUTPUT_METHOD_DISABLED,
-                                   ids: Optional[np.ndarray] = None):
+                                   ids: Optional[np.ndarray] = None,
+                                   output_dir: Optional[str] = None, output_interval: float = 1.0,
+                                   output_initial: bool = False,
+                                   output_dtypes=(OUTPUT_DTYPE_DOUBLE,) * 3,
+                                   units=(1.0, 1.0, 1.0)):
     """launch_cosmological_simulation (src/grav_sim.c:140-255).  x is advanced
-    in place (v is left as the reference leaves it); returns the status
-    (t = final scale factor, dt, num_steps)."""
+    in place; v changes only at HDF5 snapshots (output_method 3, written to
+    output_dir every output_interval of scale factor), where it becomes
+    momentum / a^2 as in the reference.  output_dtypes: coordinates,
+    velocities, masses; units: mass, length, time in cgs.  Returns the
+    status (t = final scale factor, dt, num_steps)."""
     lib.launch_cosmological_simulation.restype = ErrorStatus
     lib.launch_cosmological_simulation.argtypes = [
         ctypes.POINTER(CosmologicalSystem), ctypes.POINTER(OutputParam),
@@ -272,9 +279,10 @@ def launch_cosmological_simulation(lib: ctypes.CDLL, x: np.ndarray, v: np.ndarra
     sysc = CosmologicalSystem(n, _ip(ids), _dp(x), _dp(v), _dp(m), float(h), float(omega_m),
                               float(omega_lambda), 1.0 - omega_m - omega_lambda,
                               (ctypes.c_double * 3)(*[float(q) for q in box_center]),
-                              float(box_width), 1.0, 1.0, 1.0)
-    op = OutputParam(int(output_method), None, False, 1.0, OUTPUT_DTYPE_DOUBLE,
-                     OUTPUT_DTYPE_DOUBLE, OUTPUT_DTYPE_DOUBLE, 0)
+                              float(box_width), *[float(u) for u in units])
+    out_dir = output_dir.encode() if output_dir is not None else None
+    op = OutputParam(int(output_method), out_dir, bool(output_initial), float(output_interval),
+                     *[int(d) for d in output_dtypes], 0)
     status = SimulationStatus(0.0, 0.0, 0)
     flag = ctypes.c_bool(False)
     settings = Settings(0, False, ctypes.pointer(flag))
@@ -285,6 +293,44 @@ def launch_cosmological_simulation(lib: ctypes.CDLL, x: np.ndarray, v: np.ndarra
     if st.return_code != 0:
         raise GravError(st.return_code, take_traceback(lib, st))
     return status
+
+
+def write_snapshot_hdf5(lib: ctypes.CDLL, path, ids, x, v, m, t: float,
+                        output_dtypes=(OUTPUT_DTYPE_DOUBLE,) * 3):
+    """One HDF5 snapshot file in grav_sim's layout (gsgpu_write_snapshot_hdf5);
+    output_dtypes: coordinates, velocities, masses."""
+    lib.gsgpu_write_snapshot_hdf5.restype = ctypes.c_int
+    lib.gsgpu_write_snapshot_hdf5.argtypes = [ctypes.c_char_p, ctypes.c_int, c_int_p, c_double_p,
+                                              c_double_p, c_double_p, ctypes.c_double,
+                                              ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    ids = np.ascontiguousarray(ids, dtype=np.int32)
+    x, v, m = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, v, m))
+    n = int(m.shape[0])
+    assert ids.shape == (n,) and x.size == 3 * n and v.size == 3 * n
+    rc = lib.gsgpu_write_snapshot_hdf5(str(path).encode(), n, _ip(ids), _dp(x), _dp(v), _dp(m),
+                                       float(t), *[int(d) for d in output_dtypes])
+    if rc != 0:
+        raise GravError(rc, f"gsgpu_write_snapshot_hdf5({path})")
+
+
+def hdf5_read(lib: ctypes.CDLL, path, obj: str, attribute: Optional[str] = None) -> np.ndarray:
+    """The values of a dataset (or of one attribute of an object) of an HDF5
+    file as float64 (gsgpu_hdf5_read)."""
+    lib.gsgpu_hdf5_read.restype = ctypes.c_int
+    lib.gsgpu_hdf5_read.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
+                                    c_double_p, ctypes.c_longlong,
+                                    ctypes.POINTER(ctypes.c_longlong)]
+    count = ctypes.c_longlong()
+    attr = attribute.encode() if attribute is not None else None
+    rc = lib.gsgpu_hdf5_read(str(path).encode(), obj.encode(), attr, None, 0, ctypes.byref(count))
+    if rc != 0:
+        raise GravError(rc, f"gsgpu_hdf5_read({path}, {obj}, {attribute})")
+    out = np.empty(count.value, dtype=np.float64)
+    rc = lib.gsgpu_hdf5_read(str(path).encode(), obj.encode(), attr, _dp(out), out.size,
+                             ctypes.byref(count))
+    if rc != 0:
+        raise GravError(rc, f"gsgpu_hdf5_read({path}, {obj}, {attribute})")
+    return out
 
 
 def load_gadget2_ic(lib: ctypes.CDLL, path):

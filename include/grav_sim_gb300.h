@@ -142,6 +142,23 @@ typedef struct Settings {
 
 /* src/system.h:28 */
 System get_new_system(void);
+/* An HDF5 snapshot in the layout of grav_sim's output method 3
+ * (src/output.c:483-695): /Header attributes NumFilesPerSnapshot,
+ * NumPart_ThisFile, NumPart_Total and Time, /PartType0 datasets ParticleIDs,
+ * Masses, Coordinates and Velocities in the given output dtypes
+ * (OUTPUT_DTYPE_FLOAT or _DOUBLE).  Written without libhdf5.  Returns a
+ * GRAV_* code. */
+int gsgpu_write_snapshot_hdf5(const char *path, int num_particles, const int *ids,
+                              const double *x, const double *v, const double *m, double t,
+                              int coordinate_output_dtype, int velocity_output_dtype,
+                              int mass_output_dtype);
+/* The values of a dataset (attribute NULL) or of an attribute of the object
+ * at the path `object` ("/PartType0/Masses", "/Header") of an HDF5 file, as
+ * doubles.  *count receives the number of values; out (capacity values) may
+ * be NULL to ask for the count only.  Returns a GRAV_* code. */
+int gsgpu_hdf5_read(const char *path, const char *object, const char *attribute, double *out,
+                    long long capacity, long long *count);
+
 /* src/system.h:55-58: arrays of num_particles (ids 0..n-1, x, v, m zeroed)
  * allocated with malloc; release with free_system. */
 ErrorStatus get_initialized_system(System *system, const int num_particles);
@@ -285,9 +302,9 @@ ErrorStatus acceleration_PM(double *a, int num_particles, const double *x, const
                             double omega_m, double mean_bkg_density, int pm_grid_size,
                             double scale_factor);
 
-/* src/integrator.h:155-164.  Output must be disabled: cosmological
- * snapshots are HDF5, which is not available (as in the reference built
- * without libhdf5).  x advances in place; v is left as given. */
+/* src/integrator.h:155-164.  Snapshots are HDF5 (src/output.c:697-900; CSV
+ * is refused as the reference refuses it).  x advances in place; v is
+ * written only at snapshots, as momentum / a^2. */
 ErrorStatus leapfrog_cosmology(CosmologicalSystem *system, OutputParam *output_param,
                                SimulationStatus *simulation_status, Settings *settings, double dt,
                                double a_begin, double a_final, int pm_grid_size);

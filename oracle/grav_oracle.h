@@ -156,11 +156,12 @@ void orc_acceleration_pm(double *a, int n, const double *x, const double *m,
 double orc_compute_da(double a, double H0, double omega_m, double omega_lambda);
 /* src/system.c:1337-1375 */
 void orc_periodic_boundary(int n, double *x, const double *box_center, double box_width);
-/* src/integrator_cosmology_leapfrog.c:24-255, output disabled. */
+/* src/integrator_cosmology_leapfrog.c:24-255, output disabled; v_last (may
+ * be NULL) gets momentum / a^2 after the last step. */
 void orc_leapfrog_cosmology(int n, double *x, const double *v, const double *m, double h,
                             double omega_m, double omega_lambda, const double *box_center,
                             double box_width, double dt, double a_begin, double a_final,
-                            int pm_grid_size, int64_t *num_steps, double *t_out);
+                            int pm_grid_size, int64_t *num_steps, double *t_out, double *v_last);
 
 /* src/utils.c:27-59 (kinetic + unsoftened pairwise potential energy). */
 double orc_energy(int n, const double *x, const double *v, const double *m,

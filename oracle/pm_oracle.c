@@ -180,11 +180,13 @@ void orc_periodic_boundary(int n, double *x, const double *box_center, double bo
 
 /* src/integrator_cosmology_leapfrog.c:24-255 with output disabled.  x is
  * advanced in place; v is left as given (the reference converts momenta
- * back to velocities only for snapshots). */
+ * back to velocities only for snapshots).  v_last (3n, may be NULL)
+ * receives the velocities a snapshot after the last step would hold,
+ * momentum / a^2 (:200-209). */
 void orc_leapfrog_cosmology(int n, double *x, const double *v, const double *m, double h,
                             double omega_m, double omega_lambda, const double *box_center,
                             double box_width, double dt, double a_begin, double a_final,
-                            int pm_grid_size, int64_t *num_steps, double *t_out)
+                            int pm_grid_size, int64_t *num_steps, double *t_out, double *v_last)
 {
     const double H0 = h * 100.0;
     double t = a_begin;
@@ -217,6 +219,8 @@ void orc_leapfrog_cosmology(int n, double *x, const double *v, const double *m, 
     }
     if (num_steps) *num_steps = steps;
     if (t_out) *t_out = t;
+    if (v_last)
+        for (int i = 0; i < 3 * n; i++) v_last[i] = p[i] / (t * t);
     free(p);
     free(acc);
 }

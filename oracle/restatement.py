@@ -304,20 +304,25 @@ def acceleration_pm(x, m, box_center, box_width, H0, omega_m, mean_bkg_density, 
 
 
 def leapfrog_cosmology(x, v, m, h, omega_m, omega_lambda, box_center, box_width, dt, a_begin,
-                       a_final, grid):
+                       a_final, grid, velocities=False):
     """src/integrator_cosmology_leapfrog.c with output disabled; returns
-    (x, steps, t): v is left unchanged, as by the reference."""
+    (x, steps, t): v is left unchanged, as by the reference.  With
+    velocities=True also the velocities a snapshot after the last step
+    holds (momentum / a^2): (x, steps, t, v_last)."""
     lib = load()
     lib.orc_leapfrog_cosmology.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_double, dp, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
-                                           ctypes.POINTER(ctypes.c_double)]
+                                           ctypes.POINTER(ctypes.c_double), dp]
     x, v, m, c = _c(x).copy(), _c(v), _c(m), _c(box_center)
     steps, t = ctypes.c_int64(), ctypes.c_double()
+    v_last = np.empty_like(x)
     lib.orc_leapfrog_cosmology(m.size, _d(x), _d(v), _d(m), h, omega_m, omega_lambda, _d(c),
                                box_width, dt, a_begin, a_final, grid, ctypes.byref(steps),
-                               ctypes.byref(t))
+                               ctypes.byref(t), _d(v_last))
+    if velocities:
+        return x.reshape(-1, 3), steps.value, t.value, v_last.reshape(-1, 3)
     return x.reshape(-1, 3), steps.value, t.value
 
 

@@ -142,8 +142,8 @@ def test_output_param_checks_on_host(lib, g, tmp_path, capfd):
          "must end with a trailing slash"),
         (dict(output_method=2, output_dir=str(tmp_path / "b") + "/", output_interval=0.0),
          "Output interval must be positive"),
-        (dict(output_method=3, output_dir=str(tmp_path / "b") + "/", output_interval=1.0),
-         "HDF5 output method is not available"),
+        (dict(output_method=3, output_dir=str(tmp_path / "b") + "/", output_interval=-1.0),
+         "Output interval must be positive"),
         (dict(output_method=7, output_dir=str(tmp_path / "b") + "/", output_interval=1.0),
          "Unknown output method"),
     ]
@@ -161,6 +161,13 @@ def test_output_param_checks_on_host(lib, g, tmp_path, capfd):
     except RuntimeError:
         pass
     assert (tmp_path / "c").is_dir()
+    try:    # HDF5 output (method 3) is accepted as well
+        g.launch_simulation(lib, x.copy(), v.copy(), m, 1.0, integrator=4, dt=1e-3, tf=0.0,
+                            method=g.METHOD_GPU_PAIRWISE, output_method=3,
+                            output_dir=str(tmp_path / "d") + "/", output_interval=1.0)
+    except RuntimeError:
+        pass
+    assert (tmp_path / "d").is_dir()
 
 
 def test_check_if_included(lib):
@@ -171,7 +178,7 @@ def test_check_if_included(lib):
     assert not f(0b111000, 0b111111, 21)
 
 
-def test_cosmological_checks_on_host(lib, g, capfd):
+def test_cosmological_checks_on_host(lib, g, capfd, tmp_path):
     """launch_cosmological_simulation's checks (src/grav_sim.c:166-229) run
     before any device work, in the reference's order and words."""
     import numpy as np
@@ -182,7 +189,9 @@ def test_cosmological_checks_on_host(lib, g, capfd):
         (dict(h=-1.0), "Hubble parameter"),
         (dict(box_width=0.0), "Box width must be positive"),
         (dict(output_method=2), "CSV output is not supported"),
-        (dict(output_method=3), "HDF5 output method is not available"),
+        (dict(output_method=3, output_dir=str(tmp_path / "h")), "must end with a trailing slash"),
+        (dict(output_method=3, output_dir=str(tmp_path / "h") + "/", output_interval=0.0),
+         "Output interval must be positive"),
         (dict(dt=-1.0), "dt must be non=negative"),
         (dict(a_begin=0.0), "a_begin must be positive"),
         (dict(a_final=0.05), "a_final must be greater or equal"),
