@@ -13,7 +13,9 @@ Workloads (seeded synthetic inputs -- grav_sim publishes no dataset):
                     group walk plus the learned residual, judged every step
                     by a 4,096-particle direct sum with the theta = 0.5 walk
                     as fallback (method 104; collection and GPU training
-                    happen before the timed region).  The same line times
+                    happen before the timed region; when the network did not
+                    earn its place on the held-out snapshot, every step is
+                    the fallback walk alone, with nothing to judge).  The same line times
                     the plain Barnes-Hut comparators on the same GPU: the
                     group walk at theta = 0.5 (method 106) and the
                     reference-style monopole walk (method 103) at theta =
@@ -599,7 +601,8 @@ def run_ours(args, world, rank, local):
                 f"theta={wk['theta']} leaf={wk['leaf']}, eps={wk['eps']}, leapfrog dt={wk['dt']}")
         if wk["method"] == 104:
             desc += (" (theta=1.0 group walk + learned residual, judged by a 4096-particle "
-                     "direct sum per step, theta=0.5 group walk as fallback)")
+                     "direct sum per step, theta=0.5 group walk as fallback; a network that "
+                     "did not earn its place leaves the fallback walk alone)")
         data = "synthetic (seeded two-galaxy model: exponential disk, Hernquist bulge and halo)"
         dtype = "f32 walk terms (Kahan), f64 tree multipoles and state"
     elif fp64:

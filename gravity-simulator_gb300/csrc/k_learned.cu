@@ -18,7 +18,8 @@
 //                last snapshot is held out to measure what the network gains;
 //                the network is used only if it cuts the held-out median
 //                residual by 20 % and brings it within the judge's bound,
-//                else every step runs the judged fallback walk;
+//                else every step runs the fallback walk alone (no network
+//                output to judge: the step is the plain theta 0.5 walk);
 //   inference    cheap walk + features + network + correction, then a judge:
 //                the direct sum of 4,096 particles (a different sample each
 //                step) gives their exact accelerations; when the median
@@ -353,6 +354,18 @@ class LearnedEngine final : public Engine {
             GS_TRY(keep_frame(s));
             return ok();
         }
+        unsigned long long *cnt = counters_.as<unsigned long long>();
+        if (!useful_) {
+            // The network did not earn its cost on the held-out snapshot:
+            // the fallback walk gives every force.  No network output is
+            // applied, so there is nothing for the judge to check; the step
+            // is the plain theta 0.5 walk.
+            GS_TRY(tree_.build(d_x, d_m, s));
+            if (timer) GS_TRY(timer->begin(s));
+            GS_TRY(launch_bh_group_walk(tree_, kThetaFallback, eps_, G_, d_a, cnt, s));
+            if (timer) GS_TRY(timer->end(s));
+            return ok();
+        }
         // The judge's exact rows need only the positions: they run on the
         // engine's own stream while this stream builds the tree and walks it
         // (which leave most SMs idle for much of the build).  With a force
@@ -360,20 +373,6 @@ class LearnedEngine final : public Engine {
         GS_TRY(judge_rows(d_x, d_m, s));
         if (timer) GS_CUDA(cudaStreamWaitEvent(s, ev_join_, 0));
         GS_TRY(tree_.build(d_x, d_m, s));
-        unsigned long long *cnt = counters_.as<unsigned long long>();
-        if (!useful_) {
-            // The network did not earn its cost on the held-out snapshot:
-            // the fallback walk gives every force, still judged each step.
-            if (timer) GS_TRY(timer->begin(s));
-            GS_TRY(launch_bh_group_walk(tree_, kThetaFallback, eps_, G_, d_a, cnt, s));
-            if (timer) GS_TRY(timer->end(s));
-            GS_TRY(judge(d_a, s));
-            k_replace_rows<<<(J_ + 255) / 256, 256, 0, s>>>(J_, ids_.as<int>(),
-                                                            a_rows_.as<double>(), d_a);
-            GS_CUDA(cudaGetLastError());
-            GS_TRY(keep_frame(s));
-            return ok();
-        }
         if (timer) GS_TRY(timer->begin(s));
         GS_TRY(launch_bh_group_walk(tree_, theta_, eps_, G_, d_a, cnt, s));
         if (timer) GS_TRY(timer->end(s));
@@ -391,8 +390,8 @@ class LearnedEngine final : public Engine {
 
     int kernels_per_eval() const override
     {
-        if (trained_ && !useful_)   // fallback walk, sample, rows, judge, replace
-            return tree_.launches_per_build() + 1 + 1 + DirectRows::kernels() + 1 + 1;
+        if (trained_ && !useful_)   // the fallback walk alone
+            return tree_.launches_per_build() + 1;
         return tree_.launches_per_build() + 1 + 1 + 1 + 1 + 1 + DirectRows::kernels() + 1 + 1 + 1;
     }
 

@@ -13,8 +13,10 @@
 //   k_wh_sort       one CTA per system: sort by distance from the primary
 //                   (bitonic sort of (distance, index) in shared memory,
 //                   ties by index), permute, eta (sequential prefix);
-//   k_wh_seq        one thread per system: removals (compaction), eta,
-//                   Jacobi <-> Cartesian recurrences, massive-body list;
+//   k_wh_seq_*      removals (compaction), eta, Jacobi <-> Cartesian
+//                   recurrences, massive-body list: a warp per system for
+//                   the scans and fills, a thread per system for the
+//                   sequential steps of the recurrence;
 //   k_wh_drift      one thread per particle: universal-variable Kepler
 //                   solve (Newton, Stumpff series with argument quartering);
 //   k_wh_accel      one thread per particle: interaction accelerations in
@@ -56,6 +58,11 @@ struct EnsDev {
     int *rm;             // [P] removal marks
     int *nrm;            // [S]
     double *pairs;       // [S][2 * kPairSlots][3] shared pair sums
+    // Jacobi -> Cartesian pass (k_wh_seq_scan / _chain / _fill)
+    int *seq_nmass;      // [S] massive particles (run path), -1: whole chain, -2: empty
+    int *seq_runs;       // [S] massless runs recorded
+    int *run_lo, *run_hi;   // [S][kSeqMassMax + 1] first / last slot of a run
+    double *run_y;       // [S][kSeqMassMax + 1][6] offsets of a run's x and v
     // scratch for the permutation
     int *t_ids;
     double *t_x, *t_v, *t_m;
@@ -80,6 +87,41 @@ __device__ __forceinline__ double norm3d(const double *a) { return __dsqrt_rn(do
 __device__ __forceinline__ unsigned long long dist_key(double d)
 {
     return isnan(d) ? 0x7ff8000000000000ull : (unsigned long long)__double_as_longlong(fabs(d));
+}
+
+// eta_i = m_0 + m_1 + ... + m_i, added one by one in slot order
+// (src/integrator_whfast.c:1266-1279), from the masses in ms[0..n), by warp
+// 0 of the block.  The warp walks the slots 32 at a time and performs only
+// the adds that can change the running sum: adding +-0 to a sum that is
+// neither zero nor NaN returns the sum itself, so massless slots repeat the
+// sum of the last massive slot before them, and only the massive slots
+// (and every slot while the sum is zero or NaN) are added, in order, with
+// the reference's rounding.  The results are those of the one-by-one loop
+// bit for bit; a system of test particles costs a few adds instead of n.
+__device__ void sort_eta(const double *ms, double *eta, int n)
+{
+    if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    double e = ms[0];
+    if (lane == 0) eta[0] = e;
+    for (int c = 1; c < n; c += 32) {
+        const int i = c + lane;
+        const double mi = i < n ? ms[i] : 0.0;
+        const unsigned valid = __ballot_sync(0xffffffffu, i < n);
+        const unsigned nz = __ballot_sync(0xffffffffu, i < n && mi != 0.0);
+        double mine = e;   // the sum after the last slot added at or before this lane
+        int j = -1;
+        for (;;) {
+            const unsigned above = j < 0 ? 0xffffffffu : ~((2u << j) - 1u);   // lanes > j
+            const bool every = e == 0.0 || isnan(e);
+            const unsigned cand = (every ? valid : nz) & above;
+            if (!cand) break;
+            j = __ffs(cand) - 1;
+            e = __dadd_rn(e, __shfl_sync(0xffffffffu, mi, j));
+            if (lane >= j) mine = e;
+        }
+        if (i < n) eta[i] = mine;
+    }
 }
 
 // Sorts slots of one system by |vec_i - vec_prim| and permutes vec, vel, m,
@@ -156,13 +198,11 @@ __global__ void k_wh_sort(EnsDev E, double *vec, double *vel, int pow2_max, int 
             unsorted = unsorted || key[i] > key[i + 1];
     }
     if (!__syncthreads_or(unsorted)) {
-        if (need_eta && threadIdx.x == 0) {
-            double e = E.m[base];
-            E.eta[base] = e;
-            for (int i = 1; i < n; ++i) {
-                e = __dadd_rn(e, E.m[base + i]);
-                E.eta[base + i] = e;
-            }
+        if (need_eta) {   // the keys are done with: their space holds the masses
+            double *ms = reinterpret_cast<double *>(wh_smem);
+            for (int i = threadIdx.x; i < n; i += blockDim.x) ms[i] = E.m[base + i];
+            __syncthreads();
+            sort_eta(ms, E.eta + base, n);
         }
         return;
     }
@@ -221,24 +261,21 @@ __global__ void k_wh_sort(EnsDev E, double *vec, double *vel, int pow2_max, int 
         }
     }
     __syncthreads();
+    // the keys are done with: their space holds the permuted masses for eta
+    double *ms = reinterpret_cast<double *>(wh_smem);
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int d = base + i;
         E.ids[d] = E.t_ids[d];
-        E.m[d] = E.t_m[d];
+        const double md = E.t_m[d];
+        E.m[d] = md;
+        ms[i] = md;
         for (int c = 0; c < 3; ++c) {
             vec[3 * d + c] = E.t_x[3 * d + c];
             vel[3 * d + c] = E.t_v[3 * d + c];
         }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {   // src/integrator_whfast.c:1266-1279
-        double e = E.m[base];
-        E.eta[base] = e;
-        for (int i = 1; i < n; ++i) {
-            e = __dadd_rn(e, E.m[base + i]);
-            E.eta[base + i] = e;
-        }
-    }
+    sort_eta(ms, E.eta + base, n);   // src/integrator_whfast.c:1266-1279
 }
 
 // ---- per-system sequential work ---------------------------------------------
@@ -247,12 +284,6 @@ __global__ void k_wh_sort(EnsDev E, double *vec, double *vel, int pow2_max, int 
 // chunks of the system through shared memory with coalesced loads and
 // stores; the massive-body list is built by ballots.
 constexpr int SEQ_WARPS = 4;     // systems per CTA
-constexpr int SEQ_CHUNK = 96;    // particles staged per chunk (42 KiB per CTA)
-
-struct SeqStage {
-    double jx[3 * SEQ_CHUNK], jv[3 * SEQ_CHUNK], x[3 * SEQ_CHUNK], v[3 * SEQ_CHUNK];
-    double m[SEQ_CHUNK], eta[SEQ_CHUNK + 1];
-};
 
 // Massless runs of the Jacobi -> Cartesian chain.  For a particle with
 // m_i = 0 (finite Jacobi coordinates, eta_i = eta_{i-1} = e, and a centre
@@ -269,11 +300,6 @@ struct SeqRuns {
     int lo[kSeqMassMax + 1], hi[kSeqMassMax + 1];
     double y[kSeqMassMax + 1][6];
     int nruns;
-};
-
-union SeqShared {
-    SeqStage st;
-    SeqRuns runs;
 };
 
 __device__ __forceinline__ bool neg_zero(double v)
@@ -312,22 +338,21 @@ __device__ void wh_massive_list_warp(const EnsDev &E, int base, int n, int s, in
     if (lane == 0) E.nh[s] = k;
 }
 
-// mode 0: Cartesian -> Jacobi (initialisation); mode 1: removals, eta,
-// Jacobi -> Cartesian.  Both rebuild the massive-body list.
-__global__ void __launch_bounds__(32 * SEQ_WARPS) k_wh_seq(EnsDev E, int mode)
+// Cartesian -> Jacobi, once per run; rebuilds the massive-body list.
+__global__ void __launch_bounds__(32 * SEQ_WARPS) k_wh_seq_init(EnsDev E)
 {
-    __shared__ SeqShared shared_all[SEQ_WARPS];
+    __shared__ SeqRuns shared_all[SEQ_WARPS];
     const int lane = threadIdx.x & 31;
     const int s = blockIdx.x * SEQ_WARPS + (threadIdx.x >> 5);
     if (s >= E.S) return;   // warp-uniform
-    SeqStage &st = shared_all[threadIdx.x >> 5].st;
-    SeqRuns &rs = shared_all[threadIdx.x >> 5].runs;
+    SeqRuns &rs = shared_all[threadIdx.x >> 5];
     const int base = E.off[s];
-    int n = E.cnt[s];
+    const int n = E.cnt[s];
     if (n <= 0) return;
-    double *m = E.m + base, *eta = E.eta + base;
-    double *x = E.x + 3 * base, *v = E.v + 3 * base, *jx = E.jx + 3 * base, *jv = E.jv + 3 * base;
-    if (mode == 0) {
+    const double *m = E.m + base, *eta = E.eta + base;
+    const double *x = E.x + 3 * base, *v = E.v + 3 * base;
+    double *jx = E.jx + 3 * base, *jv = E.jv + 3 * base;
+    {
         // src/integrator_whfast.c:682-724 (once per run).  For a massless
         // particle the interior centre of mass is left exactly as it is
         // (factor 1 + 0/eta = 1, added term +-0), so with finite
@@ -431,12 +456,46 @@ __global__ void __launch_bounds__(32 * SEQ_WARPS) k_wh_seq(EnsDev E, int mode)
         }
         __syncwarp();
         wh_massive_list_warp(E, base, n, s, lane);
+    }
+}
+
+// ---- Jacobi -> Cartesian, every step (src/integrator_whfast.c:726-772) --------
+// The recurrence runs from the outermost particle inwards through the
+// interior centre of mass xc, one particle after another.  Only a few of
+// its steps are sequential work: a massless particle leaves the centre at a
+// fixed point of xc <- RN(e RN(xc / e)) after a step or two, from where
+// every particle of its massless run adds the same offset.  So the pass is
+//   k_wh_seq_scan   one CTA per system: removals (compaction, eta), then
+//                   finite Jacobi coordinates and the massive particles'
+//                   slots in order (the massive-body list, and at most
+//                   kSeqMassMax of them for the chain);
+//   k_wh_seq_chain  one thread per system: the sequential steps (massive
+//                   particles, and the first steps of each massless run until
+//                   the fixed point), recording each run's offsets; the whole
+//                   chain where the run path does not apply;
+//   k_wh_seq_fill   one thread per slot: the runs (x = jx + offset).
+// The chain is a lane's own work: FP64 instructions of a lane-0-only warp
+// cost the FP64 pipe as much as a full warp's, so a warp of 32 systems'
+// chains does 32 times the work of one system's chain in the same time.
+constexpr int SCAN_THREADS = 128;
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_wh_seq_scan(EnsDev E)
+{
+    const int s = blockIdx.x;
+    const int base = E.off[s];
+    int n = E.cnt[s];
+    if (n <= 0) {
+        if (threadIdx.x == 0) E.seq_nmass[s] = -2;
         return;
     }
-    if (E.nrm[s] > 0) {
+    double *m = E.m + base, *eta = E.eta + base;
+    double *x = E.x + 3 * base, *v = E.v + 3 * base, *jx = E.jx + 3 * base, *jv = E.jv + 3 * base;
+    const int nrm = E.nrm[s];
+    __syncthreads();   // every thread has read nrm before thread 0 clears it
+    if (nrm > 0) {
         // src/system.c:444-528 and :530-577: stable compaction of the
         // surviving slots (Cartesian x, v, m, ids, Jacobi x, v), then eta
-        if (lane == 0) {
+        if (threadIdx.x == 0) {
             int w = 0;
             for (int i = 0; i < n; ++i) {
                 if (E.rm[base + i]) {
@@ -464,132 +523,137 @@ __global__ void __launch_bounds__(32 * SEQ_WARPS) k_wh_seq(EnsDev E, int mode)
                 eta[i] = e;
             }
         }
-        __syncwarp();
+        __syncthreads();
         n = E.cnt[s];
     }
-    // src/integrator_whfast.c:726-772
-    double xc[3], vc[3];
-    if (lane == 0) {
+    // finite Jacobi coordinates (the run path needs them)
+    bool f = true;
+    for (int i = threadIdx.x; i < n; i += SCAN_THREADS)
+        for (int k = 0; k < 3; ++k) f = f && isfinite(jx[3 * i + k]) && isfinite(jv[3 * i + k]);
+    const bool finite = __syncthreads_and(f);
+    // the slots with m != 0 in order: counts over contiguous ranges, an
+    // exclusive scan over the block, then the writes
+    const int per = (n + SCAN_THREADS - 1) / SCAN_THREADS;
+    const int lo = min(n, (int)threadIdx.x * per), hi = min(n, lo + per);
+    int c = 0;
+    for (int i = lo; i < hi; ++i) c += m[i] != 0.0 ? 1 : 0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = c;
+    for (int d = 1; d < 32; d <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += t;
+    }
+    __shared__ int warp_tot[SCAN_THREADS / 32];
+    if (lane == 31) warp_tot[wid] = incl;
+    __syncthreads();
+    int at = incl - c, total = 0;
+    for (int w = 0; w < SCAN_THREADS / 32; ++w) {
+        if (w < wid) at += warp_tot[w];
+        total += warp_tot[w];
+    }
+    int *mass_idx = E.t_ids + base;
+    int *hv = E.hv + base;
+    const bool massless = E.variant != WH_PAIRWISE;
+    for (int i = lo; i < hi; ++i) {
+        if (m[i] == 0.0) continue;
+        if (at < kSeqMassMax) mass_idx[at] = i;
+        if (massless) hv[at] = i;   // the massive-body list
+        ++at;
+    }
+    if (!massless)
+        for (int i = threadIdx.x; i < n; i += SCAN_THREADS) hv[i] = i;
+    if (threadIdx.x == 0) {
+        E.nh[s] = massless ? total : n;
+        E.seq_nmass[s] = (finite && total <= kSeqMassMax) ? total : -1;
+    }
+}
+
+__global__ void k_wh_seq_chain(EnsDev E)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= E.S) return;
+    const int nmass = E.seq_nmass[s];
+    if (nmass == -2) return;   // empty system
+    const int base = E.off[s];
+    const int n = E.cnt[s];
+    const double *m = E.m + base, *eta = E.eta + base;
+    double *x = E.x + 3 * base, *v = E.v + 3 * base;
+    const double *jx = E.jx + 3 * base, *jv = E.jv + 3 * base;
+    double xc[3], vc[3], y[6];
+    for (int k = 0; k < 3; ++k) {
+        xc[k] = __dmul_rn(eta[n - 1], jx[k]);
+        vc[k] = __dmul_rn(eta[n - 1], jv[k]);
+    }
+    const size_t rb = (size_t)s * (kSeqMassMax + 1);
+    int nr = 0;
+    if (nmass >= 0) {
+        const int *mass_idx = E.t_ids + base;
+        int q = nmass - 1;   // highest massive particle not yet passed
+        int i = n - 1;
+        while (i >= 1) {
+            while (q >= 0 && mass_idx[q] > i) --q;
+            const int mtop = q >= 0 ? mass_idx[q] : -1;
+            if (mtop == i) {
+                jac_step(xc, vc, m[i], eta[i], eta[i - 1], jx + 3 * i, jv + 3 * i, x + 3 * i,
+                         v + 3 * i, y);
+                --i;
+                continue;
+            }
+            const int lo = mtop + 1 > 1 ? mtop + 1 : 1;
+            int j = i;
+            bool fixed = false;
+            while (j >= lo && !fixed) {
+                const double ox[3] = {xc[0], xc[1], xc[2]}, ov[3] = {vc[0], vc[1], vc[2]};
+                jac_step(xc, vc, m[j], eta[j], eta[j - 1], jx + 3 * j, jv + 3 * j, x + 3 * j,
+                         v + 3 * j, y);
+                fixed = true;
+                for (int k = 0; k < 3; ++k)
+                    fixed = fixed && __double_as_longlong(xc[k]) == __double_as_longlong(ox[k]) &&
+                            __double_as_longlong(vc[k]) == __double_as_longlong(ov[k]) &&
+                            isfinite(xc[k]) && isfinite(vc[k]) && !neg_zero(xc[k]) &&
+                            !neg_zero(vc[k]);
+                --j;
+            }
+            if (j >= lo) {
+                E.run_lo[rb + nr] = lo;
+                E.run_hi[rb + nr] = j;
+                for (int k = 0; k < 6; ++k) E.run_y[(rb + nr) * 6 + k] = y[k];
+                ++nr;
+            }
+            i = lo - 1;
+        }
+    } else {
+        // the whole chain, particle by particle
+        for (int i = n - 1; i >= 1; --i)
+            jac_step(xc, vc, m[i], eta[i], eta[i - 1], jx + 3 * i, jv + 3 * i, x + 3 * i, v + 3 * i,
+                     y);
+    }
+    E.seq_runs[s] = nr;
+    for (int k = 0; k < 3; ++k) {
+        x[k] = __ddiv_rn(xc[k], m[0]);
+        v[k] = __ddiv_rn(vc[k], m[0]);
+    }
+}
+
+// One thread per slot: a slot of a massless run takes the run's offsets.
+__global__ void k_wh_seq_fill(EnsDev E, int P)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int s = E.sys_of[p];
+    const int i = p - E.off[s];
+    if (i >= E.cnt[s]) return;
+    const int nr = E.seq_runs[s];
+    const size_t rb = (size_t)s * (kSeqMassMax + 1);
+    for (int r = 0; r < nr; ++r) {
+        if (i < E.run_lo[rb + r] || i > E.run_hi[rb + r]) continue;
+        const double *y = E.run_y + (rb + r) * 6;
         for (int k = 0; k < 3; ++k) {
-            xc[k] = __dmul_rn(eta[n - 1], jx[k]);
-            vc[k] = __dmul_rn(eta[n - 1], jv[k]);
+            E.x[3 * (size_t)p + k] = __dadd_rn(E.jx[3 * (size_t)p + k], y[k]);
+            E.v[3 * (size_t)p + k] = __dadd_rn(E.jv[3 * (size_t)p + k], y[3 + k]);
         }
-    }
-    // run path: needs finite Jacobi coordinates and few massive particles
-    bool finite = true;
-    int nmass = 0;
-    for (int c = 0; c < n; c += 32) {
-        const int i = c + lane;
-        bool f = true, h = false;
-        if (i < n) {
-            for (int k = 0; k < 3; ++k) f = f && isfinite(jx[3 * i + k]) && isfinite(jv[3 * i + k]);
-            h = m[i] != 0.0;
-        }
-        finite = __all_sync(0xffffffffu, f) && finite;
-        const unsigned b = __ballot_sync(0xffffffffu, h);
-        const int at = nmass + __popc(b & ((1u << lane) - 1u));
-        if (h && at < kSeqMassMax) rs.mass_idx[at] = i;
-        nmass += __popc(b);
-    }
-    if (finite && nmass <= kSeqMassMax) {
-        __syncwarp();
-        if (lane == 0) {
-            int nr = 0;
-            int q = nmass - 1;   // highest massive particle not yet passed
-            int i = n - 1;
-            double y[6];
-            while (i >= 1) {
-                while (q >= 0 && rs.mass_idx[q] > i) --q;
-                const int mtop = q >= 0 ? rs.mass_idx[q] : -1;
-                if (mtop == i) {
-                    jac_step(xc, vc, m[i], eta[i], eta[i - 1], jx + 3 * i, jv + 3 * i, x + 3 * i,
-                             v + 3 * i, y);
-                    --i;
-                    continue;
-                }
-                const int lo = mtop + 1 > 1 ? mtop + 1 : 1;
-                int j = i;
-                bool fixed = false;
-                while (j >= lo && !fixed) {
-                    const double ox[3] = {xc[0], xc[1], xc[2]}, ov[3] = {vc[0], vc[1], vc[2]};
-                    jac_step(xc, vc, m[j], eta[j], eta[j - 1], jx + 3 * j, jv + 3 * j, x + 3 * j,
-                             v + 3 * j, y);
-                    fixed = true;
-                    for (int k = 0; k < 3; ++k)
-                        fixed = fixed && __double_as_longlong(xc[k]) == __double_as_longlong(ox[k]) &&
-                                __double_as_longlong(vc[k]) == __double_as_longlong(ov[k]) &&
-                                isfinite(xc[k]) && isfinite(vc[k]) && !neg_zero(xc[k]) &&
-                                !neg_zero(vc[k]);
-                    --j;
-                }
-                if (j >= lo) {
-                    rs.lo[nr] = lo;
-                    rs.hi[nr] = j;
-                    for (int k = 0; k < 6; ++k) rs.y[nr][k] = y[k];
-                    ++nr;
-                }
-                i = lo - 1;
-            }
-            rs.nruns = nr;
-            for (int k = 0; k < 3; ++k) {
-                x[k] = __ddiv_rn(xc[k], m[0]);
-                v[k] = __ddiv_rn(vc[k], m[0]);
-            }
-        }
-        __syncwarp();
-        const int nr = rs.nruns;
-        for (int r = 0; r < nr; ++r) {
-            const int lo = rs.lo[r], cnt = 3 * (rs.hi[r] - lo + 1);
-            for (int t = lane; t < cnt; t += 32) {
-                const int k = t % 3;
-                x[3 * lo + t] = __dadd_rn(jx[3 * lo + t], rs.y[r][k]);
-                v[3 * lo + t] = __dadd_rn(jv[3 * lo + t], rs.y[r][3 + k]);
-            }
-        }
-        __syncwarp();
-        wh_massive_list_warp(E, base, n, s, lane);
         return;
     }
-    __syncwarp();
-    // general path: the whole chain, chunk by chunk from the outside in
-    for (int hi = n; hi > 1; hi -= SEQ_CHUNK) {
-        const int lo = hi - SEQ_CHUNK > 1 ? hi - SEQ_CHUNK : 1;
-        const int c = hi - lo;
-        for (int t = lane; t < 3 * c; t += 32) {
-            st.jx[t] = jx[3 * lo + t];
-            st.jv[t] = jv[3 * lo + t];
-        }
-        for (int t = lane; t < c; t += 32) st.m[t] = m[lo + t];
-        for (int t = lane; t <= c; t += 32) st.eta[t] = eta[lo - 1 + t];
-        __syncwarp();
-        if (lane == 0) {
-            for (int q = c - 1; q >= 0; --q) {
-                const double mi = st.m[q], ei = st.eta[q + 1], ep = st.eta[q];
-                for (int k = 0; k < 3; ++k) {
-                    const double jxq = st.jx[3 * q + k], jvq = st.jv[3 * q + k];
-                    xc[k] = __ddiv_rn(__dsub_rn(xc[k], __dmul_rn(mi, jxq)), ei);
-                    vc[k] = __ddiv_rn(__dsub_rn(vc[k], __dmul_rn(mi, jvq)), ei);
-                    st.x[3 * q + k] = __dadd_rn(jxq, xc[k]);
-                    st.v[3 * q + k] = __dadd_rn(jvq, vc[k]);
-                    xc[k] = __dmul_rn(ep, xc[k]);
-                    vc[k] = __dmul_rn(ep, vc[k]);
-                }
-            }
-        }
-        __syncwarp();
-        for (int t = lane; t < 3 * c; t += 32) {
-            x[3 * lo + t] = st.x[t];
-            v[3 * lo + t] = st.v[t];
-        }
-        __syncwarp();
-    }
-    if (lane == 0) {
-        for (int k = 0; k < 3; ++k) {
-            x[k] = __ddiv_rn(xc[k], m[0]);
-            v[k] = __ddiv_rn(vc[k], m[0]);
-        }
-    }
-    wh_massive_list_warp(E, base, n, s, lane);
 }
 
 // ---- shared interaction pair sums ---------------------------------------------
@@ -964,7 +1028,7 @@ struct gsgpu_ensemble {
     bool own_stream = false;
     std::vector<int> h_off;
     DBuf off, cnt, sys_of, ids, x, v, m, jx, jv, a, eta, hv, nh, rm, nrm, t_ids, t_x, t_v, t_m,
-        status, xe, ve, pairs;
+        status, xe, ve, pairs, seq_nmass, seq_runs, run_lo, run_hi, run_y;
     EnsDev E{};
     bool primed = false;
     double last_dt = 0.0;
@@ -1092,6 +1156,16 @@ struct gsgpu_ensemble {
 
     int seq_grid() const { return (S + SEQ_WARPS - 1) / SEQ_WARPS; }
 
+    // Removals, eta and Jacobi -> Cartesian (src/integrator_whfast.c:726-772)
+    ErrorStatus to_cartesian(const EnsDev &D)
+    {
+        k_wh_seq_scan<<<S, SCAN_THREADS, 0, stream>>>(D);
+        k_wh_seq_chain<<<(S + 63) / 64, 64, 0, stream>>>(D);
+        k_wh_seq_fill<<<pgrid(), 128, 0, stream>>>(D, P);
+        GS_CUDA(cudaGetLastError());
+        return ok();
+    }
+
     ErrorStatus accel(ForceTimer *timer = nullptr)
     {
         if (timer) GS_TRY(timer->begin(stream));
@@ -1116,7 +1190,7 @@ struct gsgpu_ensemble {
                 // the initial snapshot is of the system sorted by distance
                 GS_TRY(snapshot(oc, E.v, status ? status->t : 0.0, status ? status->dt : 0.0));
             }
-            k_wh_seq<<<seq_grid(), 32 * SEQ_WARPS, 0, stream>>>(E, 0);
+            k_wh_seq_init<<<seq_grid(), 32 * SEQ_WARPS, 0, stream>>>(E);
             GS_TRY(accel());
             k_wh_kick<<<pgrid(), 128, 0, stream>>>(E, P, 0.5 * dt);
         } else {
@@ -1139,7 +1213,7 @@ struct gsgpu_ensemble {
             if (td) GS_TRY(td->begin(stream));
             k_wh_drift<<<grid_for(tpb_drift), tpb_drift, 0, stream>>>(E, P, h);
             if (td) GS_TRY(td->end(stream));
-            k_wh_seq<<<seq_grid(), 32 * SEQ_WARPS, 0, stream>>>(E, 1);
+            GS_TRY(to_cartesian(E));
             GS_TRY(accel(ta));
             k_wh_kick<<<pgrid(), 128, 0, stream>>>(E, P, h);
         } else {
@@ -1158,7 +1232,7 @@ struct gsgpu_ensemble {
         for (int c = 0; c < kSortClasses; ++c) k += sort_first[c + 1] > sort_first[c] ? 1 : 0;
         return k;
     }
-    int kernels_per_step() const { return integrator == INTEGRATOR_WHFAST ? 5 + sort_launches() : 3; }
+    int kernels_per_step() const { return integrator == INTEGRATOR_WHFAST ? 7 + sort_launches() : 3; }
 
     // Snapshot of system 0 (a launch_simulation run holds one system): E.x
     // and the velocity array dv with the ids and masses of its live slots.
@@ -1177,7 +1251,7 @@ struct gsgpu_ensemble {
         EnsDev T = E;
         T.jv = E.t_v;
         k_wh_kick<<<pgrid(), 128, 0, stream>>>(T, P, -0.5 * h);
-        k_wh_seq<<<seq_grid(), 32 * SEQ_WARPS, 0, stream>>>(T, 1);
+        GS_TRY(to_cartesian(T));
         GS_CUDA(cudaGetLastError());
         return snapshot(oc, E.v, t, h);
     }
@@ -1294,6 +1368,11 @@ ErrorStatus ensemble_create(gsgpu_ensemble **out, int num_systems, const int *co
     GS_TRY(e->eta.reserve(P * sizeof(double)));
     GS_TRY(e->t_m.reserve(P * sizeof(double)));
     GS_TRY(e->status.reserve(sizeof(unsigned)));
+    GS_TRY(e->seq_nmass.reserve(S * sizeof(int)));
+    GS_TRY(e->seq_runs.reserve(S * sizeof(int)));
+    GS_TRY(e->run_lo.reserve(S * (kSeqMassMax + 1) * sizeof(int)));
+    GS_TRY(e->run_hi.reserve(S * (kSeqMassMax + 1) * sizeof(int)));
+    GS_TRY(e->run_y.reserve(S * (kSeqMassMax + 1) * 6 * sizeof(double)));
     GS_TRY(e->pairs.reserve(S * 2 * kPairSlots * 3 * sizeof(double)));
     std::vector<int> sys(P);
     for (int s = 0; s < num_systems; ++s)
@@ -1353,6 +1432,11 @@ ErrorStatus ensemble_create(gsgpu_ensemble **out, int num_systems, const int *co
     E.t_m = e->t_m.as<double>();
     E.status = e->status.as<unsigned>();
     E.pairs = e->pairs.as<double>();
+    E.seq_nmass = e->seq_nmass.as<int>();
+    E.seq_runs = e->seq_runs.as<int>();
+    E.run_lo = e->run_lo.as<int>();
+    E.run_hi = e->run_hi.as<int>();
+    E.run_y = e->run_y.as<double>();
     E.G = G;
     E.eps = eps;
     E.variant = method == GRAV_GPU_MASSLESS ? WH_MASSLESS : WH_PAIRWISE;

@@ -129,7 +129,7 @@ def test_ensemble_graph_replay_equals_run_until(g, lib, wl):
         else:
             ens.run_until(100.0)
         out.append(ens.download())
-        assert ens.kernels_per_step() == 6
+        assert ens.kernels_per_step() == 8   # one sort class, drift, 3 Jacobi -> Cartesian, pairs, accel, kick
         assert all(t in (64, 128, 256, 512) for t in ens.tuning())
         ens.close()
     for a, b in zip(*out):

@@ -5,7 +5,7 @@ snapshots during its first steps (forces from the fallback walk), trains the
 network on the GPU, and then runs the cheap walk (theta 1.0, monopole +
 quadrupole) plus the network -- if the network cut the held-out median
 residual by at least 20 % and the corrected median is within the judge's
-1e-3 bound; otherwise every step uses the judged fallback walk.  Checks:
+1e-3 bound; otherwise every step uses the fallback walk alone.  Checks:
   * training converged (last-epoch loss below first);
   * the trained network gains on the held-out snapshot: its median residual
     after the correction is below the cheap walk's (and at least 20 % below
@@ -14,7 +14,8 @@ residual by at least 20 % and the corrected median is within the judge's
   * against an FP64 direct sum on sampled particles, the accelerations meet
     the 1e-3 median bound and beat the cheap walk without the network
     (GRAV_GPU_BARNES_HUT_QUAD at theta 1.0 on the same positions);
-  * the per-step judge runs every step.
+  * the judge runs every step while the network is in use, and not at all
+    when the fallback walk alone gives the forces (no output to judge).
 The network's kernels themselves are checked against the CPU oracle in
 test_gpu_mlp.py.
 """
@@ -69,7 +70,10 @@ def test_learned_correction_trains_gains_and_is_judged(lib, g, orc, wl):
         assert lib.gsgpu_sim_download(sim, xs.ctypes.data_as(dp), vs.ctypes.data_as(dp)) == 0
         assert lib.gsgpu_sim_download_acceleration(sim, a.ctypes.data_as(dp)) == 0
         lib.gsgpu_sim_report(sim, rep.ctypes.data_as(dp), 13)
-        assert rep[7] >= 2                         # judged every step
+        if rep[12]:
+            assert rep[7] >= 2                     # judged every step
+        else:
+            assert rep[7] == 0                     # the fallback walk alone
     finally:
         lib.gsgpu_sim_destroy(sim)
     rows = np.random.default_rng(2).choice(n, 2048, replace=False).astype(np.int32)
