@@ -30,6 +30,7 @@
 #include "gs_ptx.cuh"
 
 #include <algorithm>
+#include <cstdio>
 #include <vector>
 
 namespace gs {
@@ -729,6 +730,48 @@ __global__ void __launch_bounds__(32 * PAIR_WARPS) k_wh_pairs(EnsDev E)
 
 // ---- Kepler drift -------------------------------------------------------------
 // src/integrator_whfast.c:774-815
+// Quotients x / d by the divisors d of the Stumpff series, correctly
+// rounded without a division.  zh = RN(1/d) and zl = RN(1/d - zh) (exact
+// rationals rounded once); q = RN(x zh + RN(x zl)) is within an ulp of x/d
+// (Brisebarre, Muller and Raina, "Accelerating correctly rounded
+// floating-point division when the divisor is known in advance", IEEE
+// Trans. Computers 53(8), 2004), and one correction with the exact remainder
+// r = x - q d gives RN(q + r zh) = RN(x/d) (Markstein, IBM J. Res. Dev.
+// 34(1), 1990: a faithful quotient and a correctly rounded reciprocal).
+// The remainder is exact while its last bit stays above the subnormal
+// range, so |x| outside [2^-960, 2^960] (zeros, subnormals, infinities,
+// NaN) takes the division itself.  Checked against __ddiv_rn bit for bit
+// by gsgpu_stumpff_division_selftest.
+struct StumpffDiv {
+    double d, zh, zl;
+};
+enum { SD6, SD12, SD20, SD30, SD42, SD56, SD72, SD90, SD110, SD132, SD156, SD182, SD210, kStumpffDivs };
+__constant__ StumpffDiv kStumpffDiv[kStumpffDivs] = {
+    {6.0, 0x1.5555555555555p-3, 0x1.5555555555555p-57},
+    {12.0, 0x1.5555555555555p-4, 0x1.5555555555555p-58},
+    {20.0, 0x1.999999999999ap-5, -0x1.999999999999ap-59},
+    {30.0, 0x1.1111111111111p-5, 0x1.1111111111111p-61},
+    {42.0, 0x1.8618618618618p-6, 0x1.8618618618618p-60},
+    {56.0, 0x1.2492492492492p-6, 0x1.2492492492492p-60},
+    {72.0, 0x1.c71c71c71c71cp-7, 0x1.c71c71c71c71cp-61},
+    {90.0, 0x1.6c16c16c16c17p-7, -0x1.f49f49f49f49fp-62},
+    {110.0, 0x1.29e4129e4129ep-7, 0x1.04a7904a7904ap-61},
+    {132.0, 0x1.f07c1f07c1f08p-8, -0x1.f07c1f07c1f08p-63},
+    {156.0, 0x1.a41a41a41a41ap-8, 0x1.0690690690690p-62},
+    {182.0, 0x1.6816816816817p-8, -0x1.fa5fa5fa5fa60p-62},
+    {210.0, 0x1.3813813813814p-8, -0x1.fb1fb1fb1fb20p-62},
+};
+
+template <int K> __device__ __forceinline__ double sdiv(double x)
+{
+    const double d = kStumpffDiv[K].d, zh = kStumpffDiv[K].zh, zl = kStumpffDiv[K].zl;
+    const double ax = fabs(x);
+    if (!(ax >= 0x1p-960 && ax <= 0x1p+960)) return __ddiv_rn(x, d);
+    const double q = __fma_rn(x, zh, __dmul_rn(x, zl));
+    const double r = __fma_rn(-q, d, x);
+    return __fma_rn(r, zh, q);
+}
+
 __device__ __forceinline__ void stumpff(double z, double &c0, double &c1, double &c2, double &c3)
 {
     int q = 0;
@@ -736,20 +779,20 @@ __device__ __forceinline__ void stumpff(double z, double &c0, double &c1, double
         z = __ddiv_rn(z, 4.0);
         ++q;
     }
-    double t = __dsub_rn(1.0, __ddiv_rn(z, 210.0));
-    t = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 156.0), t));
-    t = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 110.0), t));
-    t = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 72.0), t));
-    t = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 42.0), t));
-    t = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 20.0), t));
-    double s3 = __ddiv_rn(t, 6.0);
-    double u = __dsub_rn(1.0, __ddiv_rn(z, 182.0));
-    u = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 132.0), u));
-    u = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 90.0), u));
-    u = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 56.0), u));
-    u = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 30.0), u));
-    u = __dsub_rn(1.0, __dmul_rn(__ddiv_rn(z, 12.0), u));
-    double s2 = __ddiv_rn(u, 2.0);
+    double t = __dsub_rn(1.0, sdiv<SD210>(z));
+    t = __dsub_rn(1.0, __dmul_rn(sdiv<SD156>(z), t));
+    t = __dsub_rn(1.0, __dmul_rn(sdiv<SD110>(z), t));
+    t = __dsub_rn(1.0, __dmul_rn(sdiv<SD72>(z), t));
+    t = __dsub_rn(1.0, __dmul_rn(sdiv<SD42>(z), t));
+    t = __dsub_rn(1.0, __dmul_rn(sdiv<SD20>(z), t));
+    double s3 = sdiv<SD6>(t);
+    double u = __dsub_rn(1.0, sdiv<SD182>(z));
+    u = __dsub_rn(1.0, __dmul_rn(sdiv<SD132>(z), u));
+    u = __dsub_rn(1.0, __dmul_rn(sdiv<SD90>(z), u));
+    u = __dsub_rn(1.0, __dmul_rn(sdiv<SD56>(z), u));
+    u = __dsub_rn(1.0, __dmul_rn(sdiv<SD30>(z), u));
+    u = __dsub_rn(1.0, __dmul_rn(sdiv<SD12>(z), u));
+    double s2 = __dmul_rn(u, 0.5);   // u / 2, exact scaling: the same rounding
     double s1 = __dsub_rn(1.0, __dmul_rn(z, s3));
     double s0 = __dsub_rn(1.0, __dmul_rn(z, s2));
     while (q > 0) {
@@ -1004,7 +1047,92 @@ __global__ void __launch_bounds__(32 * SEQ_WARPS) k_ens_massive_list(EnsDev E)
     wh_massive_list_warp(E, E.off[s], E.cnt[s], s, threadIdx.x & 31);
 }
 
+// Self-check of sdiv against the division it replaces: sample k of the
+// n checked per divisor is a 64-bit pattern (every exponent, subnormals,
+// infinities, NaN) for even k, and for odd k a dividend whose exact
+// quotient lies halfway between two doubles (the hardest rounding case).
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z)
+{
+    z += 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+template <int K> __device__ bool sdiv_matches(double x)
+{
+    const double a = sdiv<K>(x), b = __ddiv_rn(x, kStumpffDiv[K].d);
+    return (isnan(a) && isnan(b)) || __double_as_longlong(a) == __double_as_longlong(b);
+}
+
+__global__ void k_sdiv_selftest(long long n, unsigned long long seed, unsigned long long *bad)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    unsigned long long local = 0;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += stride) {
+        const unsigned long long h = mix64(seed ^ mix64((unsigned long long)k));
+        double x;
+        const int which = (int)(h % kStumpffDivs);
+        if (k & 1) {
+            // x = RN((q0 + ulp(q0) / 2) d): the exact quotient x / d lies
+            // next to the midpoint of two neighbouring doubles
+            const unsigned long long m = (mix64(h) >> 11) | (1ull << 52);
+            const int e = (int)(mix64(h + 1) % 241) - 120;
+            const double q0 = scalbn((double)m, e - 52);
+            const double half_ulp_d = __dmul_rn(scalbn(1.0, e - 53), kStumpffDiv[which].d);
+            x = __fma_rn(q0, kStumpffDiv[which].d, half_ulp_d);
+        } else {
+            x = __longlong_as_double((long long)h);
+        }
+        bool ok = true;
+        switch (which) {
+        case SD6: ok = sdiv_matches<SD6>(x); break;
+        case SD12: ok = sdiv_matches<SD12>(x); break;
+        case SD20: ok = sdiv_matches<SD20>(x); break;
+        case SD30: ok = sdiv_matches<SD30>(x); break;
+        case SD42: ok = sdiv_matches<SD42>(x); break;
+        case SD56: ok = sdiv_matches<SD56>(x); break;
+        case SD72: ok = sdiv_matches<SD72>(x); break;
+        case SD90: ok = sdiv_matches<SD90>(x); break;
+        case SD110: ok = sdiv_matches<SD110>(x); break;
+        case SD132: ok = sdiv_matches<SD132>(x); break;
+        case SD156: ok = sdiv_matches<SD156>(x); break;
+        case SD182: ok = sdiv_matches<SD182>(x); break;
+        default: ok = sdiv_matches<SD210>(x); break;
+        }
+        local += ok ? 0 : 1;
+    }
+    if (local) atomicAdd(bad, local);
+}
+
 }  // namespace gs
+
+// Checks the division-free Stumpff quotients against __ddiv_rn on n
+// samples; *mismatches receives the count of differing results.
+extern "C" int gsgpu_stumpff_division_selftest(long long n, unsigned long long seed,
+                                               long long *mismatches)
+{
+    if (!mismatches || n < 0) return GRAV_POINTER_ERROR;
+    gs::DBuf bad;
+    ErrorStatus st = bad.reserve(sizeof(unsigned long long));
+    if (st.return_code != GRAV_SUCCESS) {
+        free_traceback(&st);
+        return GRAV_MEMORY_ERROR;
+    }
+    cudaError_t e = cudaMemset(bad.p, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+        gs::k_sdiv_selftest<<<1216, 256>>>(n, seed, bad.as<unsigned long long>());
+        e = cudaGetLastError();
+    }
+    unsigned long long h = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&h, bad.p, sizeof(h), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        std::fprintf(stderr, "gsgpu_stumpff_division_selftest: %s\n", cudaGetErrorString(e));
+        return GRAV_FAILURE;
+    }
+    *mismatches = (long long)h;
+    return GRAV_SUCCESS;
+}
 
 // ---------------------------------------------------------------------------
 // Host side: the ensemble object.

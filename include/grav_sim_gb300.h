@@ -469,6 +469,12 @@ int gsgpu_ensemble_tuning(const gsgpu_ensemble *e, int *accel_threads, int *drif
  * capacity in pow2[k], its threads in threads[k]); returns the number of
  * classes written (at most n). */
 int gsgpu_ensemble_sort_tuning(const gsgpu_ensemble *e, int *pow2, int *threads, int n);
+/* Self-check (no counterpart in the reference): the Kepler drift's Stumpff
+ * series divides by 13 small integer constants through a division-free
+ * correctly rounded quotient; this compares it with the division itself
+ * (__ddiv_rn) bit for bit on n samples (random bit patterns and quotients
+ * next to rounding ties).  *mismatches receives the number that differ. */
+int gsgpu_stumpff_division_selftest(long long n, unsigned long long seed, long long *mismatches);
 /* Kernel timing (no counterpart in the reference): while enabled, steps are
  * launched directly instead of from the captured graph, with CUDA events
  * around the Kepler drift and around the interaction accelerations (the

@@ -5,6 +5,8 @@ it alone: checked against the WHFast golden vectors (made by the reference
 itself) and, for many uneven systems at once, against the oracle's
 restatement system by system.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -185,3 +187,16 @@ def test_whfast_planar_systems_match_oracle(g, lib, wl, orc, negzero):
         assert np.array_equal(i_s, ri), s
         assert x_s.tobytes() == rx.tobytes() and v_s.tobytes() == rv.tobytes(), s
     ens.close()
+
+
+def test_stumpff_division_matches_ddiv(lib):
+    """The drift's division-free quotients by the Stumpff series' constants
+    equal __ddiv_rn bit for bit: 2^26 samples over every exponent class and
+    next to rounding ties."""
+    lib.gsgpu_stumpff_division_selftest.restype = ctypes.c_int
+    lib.gsgpu_stumpff_division_selftest.argtypes = [ctypes.c_longlong, ctypes.c_ulonglong,
+                                                    ctypes.POINTER(ctypes.c_longlong)]
+    bad = ctypes.c_longlong(-1)
+    for seed in (1, 2):
+        assert lib.gsgpu_stumpff_division_selftest(1 << 26, seed, ctypes.byref(bad)) == 0
+        assert bad.value == 0
