@@ -11,6 +11,7 @@
 // The "momentum" figures keep the reference's definition: sums of vector
 // components, m (vx + vy + vz) and m (L_x + L_y + L_z) per particle.
 #include "gs_internal.h"
+#include "gs_ptx.cuh"
 
 #include <algorithm>
 #include <cstdio>
@@ -102,11 +103,116 @@ static ErrorStatus diag(const double *h_state, int num_snapshots, int n, double 
     return ok();
 }
 
+// ---- softened potential energy for large N --------------------------------
+// phi_i = sum_{j != i} m_j / sqrt(|x_i - x_j|^2 + eps^2) for one i per
+// thread, with the j particles staged through shared memory 256 at a time.
+// Coordinates are double-float (hi + lo) relative to the bounding-box
+// centre, so each difference keeps about 48 bits; the terms are summed in
+// FP32 per 64 and the partial sums Kahan-compensated.
+constexpr int EN_THREADS = 256;
+constexpr int EN_PARTIAL = 64;
+
+__global__ void __launch_bounds__(EN_THREADS)
+k_softened_phi(const float4 *__restrict__ ph, const float4 *__restrict__ pl, int n, float eps2,
+               double *__restrict__ phi)
+{
+    __shared__ float4 sh[EN_THREADS], sl[EN_THREADS];
+    const int i = blockIdx.x * EN_THREADS + threadIdx.x;
+    const float4 xh = i < n ? ph[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 xl = i < n ? pl[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float s = 0.f, c = 0.f;
+    for (int t0 = 0; t0 < n; t0 += EN_THREADS) {
+        __syncthreads();
+        const int j = t0 + threadIdx.x;
+        sh[threadIdx.x] = j < n ? ph[j] : make_float4(0.f, 0.f, 0.f, 0.f);   // m = 0 pads
+        sl[threadIdx.x] = j < n ? pl[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        __syncthreads();
+        const int cnt = min(EN_THREADS, n - t0);
+        for (int k0 = 0; k0 < cnt; k0 += EN_PARTIAL) {
+            float part = 0.f;
+            const int k1 = min(cnt, k0 + EN_PARTIAL);
+#pragma unroll 4
+            for (int k = k0; k < k1; ++k) {
+                const float4 yh = sh[k], yl = sl[k];
+                const float dx = (yh.x - xh.x) + (yl.x - xl.x);
+                const float dy = (yh.y - xh.y) + (yl.y - xl.y);
+                const float dz = (yh.z - xh.z) + (yl.z - xl.z);
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+                const float w = (t0 + k == i) ? 0.f : yh.w;
+                part = fmaf(w, rsqrt_approx(r2), part);
+            }
+            kahan_add(s, c, part);
+        }
+    }
+    if (i < n) phi[i] = (double)s - (double)c;
+}
+
+ErrorStatus softened_energy(const double *x, const double *v, const double *m, int n, double G,
+                            double eps, double *energy)
+{
+    double ke = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double v2 = v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] +
+                          v[3 * i + 2] * v[3 * i + 2];
+        ke += 0.5 * m[i] * v2;
+    }
+    if (n < 2) {
+        *energy = ke;
+        return ok();
+    }
+    double lo[3] = {x[0], x[1], x[2]}, hi[3] = {x[0], x[1], x[2]};
+    for (int i = 1; i < n; ++i)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], x[3 * i + k]);
+            hi[k] = std::max(hi[k], x[3 * i + k]);
+        }
+    std::vector<float4> hph(n), hpl(n);
+    for (int i = 0; i < n; ++i) {
+        float h[3], l[3];
+        for (int k = 0; k < 3; ++k) {
+            const double d = x[3 * i + k] - 0.5 * (lo[k] + hi[k]);
+            h[k] = (float)d;
+            l[k] = (float)(d - (double)h[k]);
+        }
+        hph[i] = make_float4(h[0], h[1], h[2], (float)m[i]);
+        hpl[i] = make_float4(l[0], l[1], l[2], 0.f);
+    }
+    DBuf dph, dpl, dphi;
+    GS_TRY(dph.reserve((size_t)n * sizeof(float4)));
+    GS_TRY(dpl.reserve((size_t)n * sizeof(float4)));
+    GS_TRY(dphi.reserve((size_t)n * sizeof(double)));
+    GS_CUDA(cudaMemcpy(dph.p, hph.data(), (size_t)n * sizeof(float4), cudaMemcpyHostToDevice));
+    GS_CUDA(cudaMemcpy(dpl.p, hpl.data(), (size_t)n * sizeof(float4), cudaMemcpyHostToDevice));
+    k_softened_phi<<<(n + EN_THREADS - 1) / EN_THREADS, EN_THREADS>>>(
+        dph.as<float4>(), dpl.as<float4>(), n, (float)(eps * eps), dphi.as<double>());
+    GS_CUDA(cudaGetLastError());
+    std::vector<double> phi(n);
+    GS_CUDA(cudaMemcpy(phi.data(), dphi.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
+    double pe = 0.0;
+    for (int i = 0; i < n; ++i) pe += m[i] * phi[i];
+    *energy = ke - 0.5 * G * pe;
+    return ok();
+}
+
 }  // namespace gs
 
 using namespace gs;
 
 extern "C" {
+
+int gsgpu_softened_energy(const double *x, const double *v, const double *m, int n, double G,
+                          double eps, double *energy)
+{
+    if (!x || !v || !m || !energy) return GRAV_POINTER_ERROR;
+    if (n < 0) return GRAV_VALUE_ERROR;
+    ErrorStatus st = softened_energy(x, v, m, n, G, eps, energy);
+    if (st.return_code != GRAV_SUCCESS) {
+        const int rc = st.return_code;
+        print_and_free_traceback(&st);
+        return rc;
+    }
+    return GRAV_SUCCESS;
+}
 
 void compute_energy_python(double *energy, double G, const double *sol_state,
                            int32_t num_snapshots, int32_t num_particles)

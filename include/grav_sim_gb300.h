@@ -337,6 +337,15 @@ int launch_simulation_python(
 /* src/python_interface.c:195-201 (FP64 on the GPU) */
 void compute_energy_python(double *energy, double G, const double *sol_state,
                            int32_t num_snapshots, int32_t num_particles);
+/* Total energy with the softened potential (no counterpart in the reference,
+ * whose compute_energy uses the unsoftened one): sum_i m_i |v_i|^2 / 2 -
+ * G sum_{i<j} m_i m_j / sqrt(|x_i - x_j|^2 + eps^2) of n host particles.
+ * Kinetic part and the final sums in FP64; the potential's pair terms in
+ * compensated FP32 on double-float coordinates relative to the bounding-box
+ * centre (about 1e-7 relative), for energy drift at sizes where the FP64
+ * O(N^2) sum is too slow.  Returns a GRAV_* code. */
+int gsgpu_softened_energy(const double *x, const double *v, const double *m, int n, double G,
+                          double eps, double *energy);
 /* src/python_interface.c:245-250 */
 void compute_linear_momentum_python(double *linear_momentum,
                                     const double *sol_state,
