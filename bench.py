@@ -347,14 +347,15 @@ def accuracy_sample(a_gpu, x, m, G, eps, rows=4096, seed=0):
     return float(np.median(errs)), float(np.quantile(errs, 0.99))
 
 
-def profile_traffic(kernel, workload, summary=None):
+def profile_traffic(kernel, workload, summary=None, field="traffic_bytes_per_launch"):
     """DRAM bytes (read + write) per launch of `kernel` on `workload`, from
     the ncu capture summarised in profiles/<kernel>_<workload>.md (or the
-    named summary), or None."""
+    named summary), or None.  field="l2_bytes_per_launch" gives the L2
+    traffic (lts__t_bytes.sum) where the summary records it."""
     prof = ROOT / "profiles" / f"{summary or kernel + '_' + workload}.md"
     if prof.exists():
         for ln in prof.read_text().splitlines():
-            if ln.startswith("traffic_bytes_per_launch:"):
+            if ln.startswith(field + ":"):
                 return float(ln.split(":", 1)[1])
     return None
 
@@ -620,6 +621,7 @@ def run_ours(args, world, rank, local):
     kernel = ("k_bh_group" if wk["method"] in (104, 106, 107) else "k_bh_walk") if bh else \
         ("k_direct_fp64_reference_order" if fp64 else "k_direct_sum")
     traffic = profile_traffic(kernel, args.workload)
+    l2_bytes = profile_traffic(kernel, args.workload, field="l2_bytes_per_launch")
     if bh:
         desc = (f"{args.workload}: galaxy pair N={n}, Barnes-Hut method {wk['method']} "
                 f"theta={wk['theta']} leaf={wk['leaf']}, eps={wk['eps']}, leapfrog dt={wk['dt']}")
@@ -671,7 +673,11 @@ def run_ours(args, world, rank, local):
                                               "cell": flop_cell},
                      "interactions_per_launch": {"cells": r["interaction_cells"],
                                                  "pairs": r["interaction_pairs"]},
-                     "achieved_at_20_flop_per_interaction": achieved_20},
+                     "achieved_at_20_flop_per_interaction": achieved_20,
+                     "l2": ({"bytes_per_launch": l2_bytes,
+                             "achieved_gbs": l2_bytes / (mean_force_ms * 1e6),
+                             "source": "lts__t_bytes.sum of one launch (profiles/)"}
+                            if l2_bytes and mean_force_ms else None)},
         "e2e": {"value": e2e_val, "unit": "particle-steps/s",
                 "h2d_bytes_per_step": (7 * n * 8) / args.steps,
                 "d2h_bytes_per_step": (6 * n * 8) / args.steps,
