@@ -5,10 +5,11 @@
 // (src/acceleration_barnes_hut.c:78-248) one child at a time, which costs
 // about 200 instructions per accepted cell.  This walk trades identical
 // decisions for throughput:
-//   * groups come from the tree: the children of a cell with more than 32
-//     particles are merged in octant order into runs of at most 32
-//     particles (a leaf with more is cut into runs of 32), so a group lies
-//     in one cell and its box stays compact where the Morton curve jumps;
+//   * groups come from the tree: in a cell with more than 32 particles,
+//     each run of consecutive children of at most 32 particles is cut into
+//     pieces of 32 sorted particles (a leaf with more is cut the same way),
+//     so a group lies in one cell and its box stays compact where the
+//     Morton curve jumps, and groups fill the lanes;
 //     the one group that does not fit its cell (the particles whose Morton
 //     coordinate wraps at the box maximum) is walked particle by particle;
 //   * a persistent warp takes groups from a work queue and walks the tree
@@ -52,9 +53,9 @@ constexpr int GW_RESERVE = 8 * (OCT_MAX_LEVEL + 1);
 constexpr int GW_GROUP = 32;       // particles per group at most
 
 // Group list: one thread per node.  A cell with more than GW_GROUP
-// particles merges its children, in octant order, into runs of at most
-// GW_GROUP particles (a leaf with more is cut into runs); the root is one
-// group when it is small enough.  Entry: (first sorted particle,
+// particles cuts each run of consecutive children of at most GW_GROUP
+// particles into pieces of GW_GROUP (a leaf with more is cut the same way);
+// the root is one group when it is small enough.  Entry: (first sorted particle,
 // count | depth << 8) with depth that of the cell the group lies in.
 // A group whose particles do not fit within the side of its cell (the
 // particles whose Morton coordinate wraps at the box maximum sit in a cell
@@ -106,18 +107,24 @@ __global__ void k_group_list(const int *__restrict__ ctr, const int4 *__restrict
             put_group(groups, gctr, ci.z + b, min(GW_GROUP, ci.w - b), d, pa, pb, bl);
         return;
     }
+    // Runs of consecutive children of at most GW_GROUP particles each are
+    // contiguous in sorted order and lie in this cell: each run is cut into
+    // pieces of GW_GROUP particles (the last one shorter), so that groups
+    // fill the warp's lanes (children of 20, 20 and 20 particles make groups
+    // of 32 and 28, not three of 20).
     int first = 0, count = 0;
-    for (int k = 0; k < ci.y; ++k) {
-        const int4 ch = nc[ci.x + k];
-        if (ch.w > GW_GROUP || count + ch.w > GW_GROUP) {
-            if (count > 0) put_group(groups, gctr, first, count, d, pa, pb, bl);
+    for (int k = 0; k <= ci.y; ++k) {
+        const int4 ch = k < ci.y ? nc[ci.x + k] : make_int4(0, 0, 0, GW_GROUP + 1);
+        if (ch.w > GW_GROUP) {   // a child walked as its own cell, or the end
+            for (int b = 0; b < count; b += GW_GROUP)
+                put_group(groups, gctr, first + b, min(GW_GROUP, count - b), d, pa, pb, bl);
             count = 0;
+            continue;
         }
-        if (ch.w > GW_GROUP || ch.w <= 0) continue;
+        if (ch.w <= 0) continue;
         if (count == 0) first = ch.z;
         count += ch.w;
     }
-    if (count > 0) put_group(groups, gctr, first, count, d, pa, pb, bl);
 }
 
 struct GroupWalkArgs {
