@@ -38,6 +38,8 @@
 #include "gs_octree.h"
 #include "gs_ptx.cuh"
 
+#include <cstdio>
+
 namespace gs {
 
 constexpr int OT_THREADS = 256;
@@ -132,6 +134,32 @@ k_bbox_final(const double *__restrict__ part, int blocks, double ocx, double ocy
     frame[2] = c[2];
     frame[3] = w;
     frame[4] = __dmul_rn(w, 2.0);
+    // the width's double-word reciprocal for div_by_width: zh = RN(1/w) and
+    // zl = RN(1/w - zh), where 1 - zh w is exact (zh is correctly rounded)
+    const double zh = __ddiv_rn(1.0, w);
+    frame[5] = zh;
+    frame[6] = __ddiv_rn(__fma_rn(-zh, w, 1.0), w);
+    const double aw = fabs(w);
+    frame[7] = (aw >= 0x1p-100 && aw <= 0x1p+100) ? 1.0 : 0.0;
+}
+
+// RN(x / w) for the box width w = frame[3] without a division, from the
+// double-word reciprocal (frame[5], frame[6]) that k_bbox_final stored:
+// q = RN(x zh + RN(x zl)) is within an ulp of x / w (Brisebarre, Muller and
+// Raina, IEEE Trans. Computers 53(8), 2004), and the exact remainder
+// r = x - q w corrects it to RN(q + r zh) = RN(x / w) (Markstein, IBM J.
+// Res. Dev. 34(1), 1990).  The remainder is exact while its last bit stays
+// above the subnormal range: |w| in [2^-100, 2^100] (frame[7]) and |x| in
+// [2^-900, 2^900]; other operands (zeros, subnormals, infinities, NaN)
+// take the division itself.  Checked against __ddiv_rn bit for bit by
+// gsgpu_width_division_selftest.
+__device__ __forceinline__ double div_by_width(double x, const double *__restrict__ frame)
+{
+    const double ax = fabs(x);
+    if (frame[7] == 0.0 || !(ax >= 0x1p-900 && ax <= 0x1p+900)) return __ddiv_rn(x, frame[3]);
+    const double q = __fma_rn(x, frame[5], __dmul_rn(x, frame[6]));
+    const double r = __fma_rn(-q, frame[3], x);
+    return __fma_rn(r, frame[5], q);
 }
 
 // 21 low bits of v spread to every third bit (magic-number interleave).
@@ -152,10 +180,9 @@ __global__ void k_morton(const double *__restrict__ x, int n, const double *__re
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double w = frame[3];
     uint64_t k = 0;
     for (int d = 0; d < 3; ++d) {
-        const double u = __dadd_rn(__ddiv_rn(__dsub_rn(x[3 * i + d], frame[d]), w), 0.5);
+        const double u = __dadd_rn(div_by_width(__dsub_rn(x[3 * i + d], frame[d]), frame), 0.5);
         const long long q = __double2ll_rz(__dmul_rn(u, 2097152.0));
         k |= spread3((uint64_t)q) << d;
     }
@@ -910,4 +937,73 @@ ErrorStatus OctreeDevice::clear_status(cudaStream_t s)
     return ok();
 }
 
+// Self-check of div_by_width against the division it replaces: per sample,
+// a width w (a random significand, every tenth one all ones, an exponent in
+// [-100, 100]) and a dividend x (a random 64-bit pattern for even k: every
+// class of double; for odd k one whose quotient lies next to a midpoint of
+// two doubles), the frame built as k_bbox_final builds it.
+__device__ __forceinline__ unsigned long long wmix(unsigned long long z)
+{
+    z += 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+__global__ void k_width_div_selftest(long long n, unsigned long long seed, unsigned long long *bad)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    unsigned long long local = 0;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += stride) {
+        const unsigned long long h = wmix(seed ^ wmix((unsigned long long)k));
+        unsigned long long sig = wmix(h + 7) >> 12;
+        if (h % 10 == 0) sig = (1ull << 52) - 1ull;
+        const int ew = (int)(wmix(h + 3) % 201) - 100;
+        const double w = scalbn(__longlong_as_double((long long)(0x3ff0000000000000ull | sig)), ew);
+        double frame[8];
+        frame[3] = w;
+        frame[5] = __ddiv_rn(1.0, w);
+        frame[6] = __ddiv_rn(__fma_rn(-frame[5], w, 1.0), w);
+        frame[7] = 1.0;
+        double x;
+        if (k & 1) {
+            const unsigned long long m = (wmix(h + 11) >> 11) | (1ull << 52);
+            const int e = (int)(wmix(h + 13) % 241) - 120;
+            const double q0 = scalbn((double)m, e - 52);
+            x = __fma_rn(q0, w, __dmul_rn(scalbn(1.0, e - 53), w));
+        } else {
+            x = __longlong_as_double((long long)wmix(h + 17));
+        }
+        const double a = div_by_width(x, frame), b = __ddiv_rn(x, w);
+        const bool ok = (isnan(a) && isnan(b)) || __double_as_longlong(a) == __double_as_longlong(b);
+        local += ok ? 0 : 1;
+    }
+    if (local) atomicAdd(bad, local);
+}
+
 }  // namespace gs
+
+extern "C" int gsgpu_width_division_selftest(long long n, unsigned long long seed,
+                                             long long *mismatches)
+{
+    if (!mismatches || n < 0) return GRAV_POINTER_ERROR;
+    gs::DBuf bad;
+    ErrorStatus st = bad.reserve(sizeof(unsigned long long));
+    if (st.return_code != GRAV_SUCCESS) {
+        free_traceback(&st);
+        return GRAV_MEMORY_ERROR;
+    }
+    cudaError_t e = cudaMemset(bad.p, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+        gs::k_width_div_selftest<<<1216, 256>>>(n, seed, bad.as<unsigned long long>());
+        e = cudaGetLastError();
+    }
+    unsigned long long h = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&h, bad.p, sizeof(h), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        std::fprintf(stderr, "gsgpu_width_division_selftest: %s\n", cudaGetErrorString(e));
+        return GRAV_FAILURE;
+    }
+    *mismatches = (long long)h;
+    return GRAV_SUCCESS;
+}

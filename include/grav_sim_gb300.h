@@ -484,6 +484,12 @@ int gsgpu_ensemble_sort_tuning(const gsgpu_ensemble *e, int *pow2, int *threads,
  * (__ddiv_rn) bit for bit on n samples (random bit patterns and quotients
  * next to rounding ties).  *mismatches receives the number that differ. */
 int gsgpu_stumpff_division_selftest(long long n, unsigned long long seed, long long *mismatches);
+/* Self-check (no counterpart in the reference): the Morton keys divide the
+ * centred coordinates by the box width through a division-free correctly
+ * rounded quotient; this compares it with __ddiv_rn bit for bit on n samples
+ * (random widths and dividends, quotients next to rounding ties).
+ * *mismatches receives the number that differ. */
+int gsgpu_width_division_selftest(long long n, unsigned long long seed, long long *mismatches);
 /* Kernel timing (no counterpart in the reference): while enabled, steps are
  * launched directly instead of from the captured graph, with CUDA events
  * around the Kepler drift and around the interaction accelerations (the

@@ -306,3 +306,17 @@ def test_group_walk_monopole_vs_per_particle(lib, g, orc, wl):
                                 exact))
     print(f"monopole: group {e_g:.3g}, per-particle {e_p:.3g}")
     assert e_g <= 1.1 * e_p
+
+
+def test_width_division_matches_ddiv(lib):
+    """The Morton keys' division-free quotients by the box width equal
+    __ddiv_rn bit for bit: 2^26 samples of widths in [2^-100, 2^100] and
+    dividends of every class and next to rounding ties."""
+    import ctypes
+    lib.gsgpu_width_division_selftest.restype = ctypes.c_int
+    lib.gsgpu_width_division_selftest.argtypes = [ctypes.c_longlong, ctypes.c_ulonglong,
+                                                  ctypes.POINTER(ctypes.c_longlong)]
+    bad = ctypes.c_longlong(-1)
+    for seed in (1, 2):
+        assert lib.gsgpu_width_division_selftest(1 << 26, seed, ctypes.byref(bad)) == 0
+        assert bad.value == 0
