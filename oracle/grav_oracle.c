@@ -595,11 +595,27 @@ void orc_comp_update(int len, double *y, double *err, const double *d,
     }
 }
 
+/* Barnes-Hut parameters of method 3 (src/acceleration.h:16-26: opening
+ * angle, particles per leaf) for orc_fixed_step_run, and whether the tree
+ * keeps the reference's quirks Q1/Q2 (compat) or computes true leaf
+ * multipoles. */
+static double g_bh_theta = 0.5;
+static int g_bh_leaf = 1, g_bh_compat = 0;
+
+void orc_set_bh_params(double theta, int leaf_max, int compat)
+{
+    g_bh_theta = theta;
+    g_bh_leaf = leaf_max;
+    g_bh_compat = compat;
+}
+
 static int accel_of(int method, int n, const double *x, const double *m,
                     double G, double eps, double *a)
 {
     if (method == 1) { orc_pairwise(n, x, m, G, eps, a); return 0; }
     if (method == 2) return orc_massless(n, x, m, G, eps, a);
+    if (method == 3)
+        return orc_barnes_hut(n, x, m, G, eps, g_bh_theta, g_bh_leaf, g_bh_compat, a);
     return 2;
 }
 

@@ -112,6 +112,9 @@ void orc_comp_update(int len, double *y, double *err, const double *d,
  * sum (method 1) or the massless sum (method 2): integrator codes 1 euler,
  * 2 euler-cromer, 3 rk4, 4 leapfrog.  Reproduces total_num_steps =
  * ceil(tf/dt), the last-step dt clamp and t = steps*dt. */
+/* Opening angle, particles per leaf and quirk mode of method 3 (Barnes-Hut)
+ * in orc_fixed_step_run. */
+void orc_set_bh_params(double theta, int leaf_max, int compat);
 int orc_fixed_step_run(int integrator, int method, int n, double *x, double *v,
                        const double *m, double G, double eps, double dt,
                        double tf);

@@ -208,10 +208,17 @@ def bh_quad(x, m, G, eps, theta, leaf_max):
     return a, mag, q
 
 
-def fixed_step_run(integrator, method, x, v, m, G, eps, dt, tf):
+def fixed_step_run(integrator, method, x, v, m, G, eps, dt, tf, bh=None):
+    """Fixed-step integrators 1-4 of src/integrator.c with acceleration method
+    1 (pairwise), 2 (massless) or 3 (Barnes-Hut; bh = (theta, leaf_max,
+    compat)); returns (x, v)."""
     x, v, m = _c(x).copy(), _c(v).copy(), _c(m)
-    rc = load().orc_fixed_step_run(integrator, method, m.size, _d(x), _d(v), _d(m),
-                                   G, eps, dt, tf)
+    lib = load()
+    if bh is not None:
+        lib.orc_set_bh_params.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        lib.orc_set_bh_params(float(bh[0]), int(bh[1]), int(bh[2]))
+    rc = lib.orc_fixed_step_run(integrator, method, m.size, _d(x), _d(v), _d(m),
+                                G, eps, dt, tf)
     assert rc == 0, rc
     return x, v
 

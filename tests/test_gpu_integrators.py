@@ -162,3 +162,37 @@ def test_ias15_oracle_random(lib, g, orc, wl):
                                        tf=0.2, method=g.METHOD_GPU_PAIRWISE_FP64,
                                        softening_length=0.02, tolerance=1e-8)
     assert np.array_equal(xo, xo_ref) and np.array_equal(vo, vo_ref)
+
+
+def _softened_energy(x, v, m, G, eps):
+    ke = 0.5 * np.sum(m * np.sum(v * v, axis=1))
+    pe = 0.0
+    for i0 in range(0, len(m), 512):
+        d = x[i0:i0 + 512, None, :] - x[None, :, :]
+        w = m[i0:i0 + 512, None] * m[None, :] / np.sqrt(np.sum(d * d, axis=2) + eps * eps)
+        idx = np.arange(i0, min(i0 + 512, len(m)))
+        w[idx - i0, idx] = 0.0
+        pe += w.sum()
+    return ke - 0.5 * G * pe
+
+
+def test_energy_drift_against_reference_barnes_hut(lib, g, orc, wl):
+    """Relative drift of the softened energy over 200 leapfrog steps of a
+    galaxy pair (N = 2,048, eps = 0.01, dt = 1e-3): the group walk (106,
+    theta 0.5, quadrupole cells) against the same run with grav_sim's
+    Barnes-Hut as the oracle restates it (theta 0.5, true leaf multipoles,
+    monopole cells).  The GPU run may not drift more than the reference's
+    (with a floor for round-off)."""
+    x, v, m = wl.galaxy_pair(2048, 13)
+    G, eps, dt, tf = 1.0, 0.01, 1e-3, 0.2
+    e0 = _softened_energy(x, v, m, G, eps)
+    xg, vg = x.copy(), v.copy()
+    g.launch_simulation(lib, xg, vg, m.copy(), G, integrator=4, dt=dt, tf=tf,
+                        method=g.METHOD_GPU_BARNES_HUT_GROUP, opening_angle=0.5,
+                        softening_length=eps, max_num_particles_per_leaf=16)
+    xr, vr = orc.fixed_step_run(4, 3, x, v, m, G, eps, dt, tf, bh=(0.5, 1, 0))
+    drift_gpu = abs(_softened_energy(xg, vg, m, G, eps) - e0) / abs(e0)
+    drift_ref = abs(_softened_energy(xr, vr, m, G, eps) - e0) / abs(e0)
+    print(f"relative energy drift over 200 steps: GPU group walk {drift_gpu:.3g}, "
+          f"reference Barnes-Hut {drift_ref:.3g}")
+    assert drift_gpu <= max(drift_ref, 1e-7)
