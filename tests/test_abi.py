@@ -202,3 +202,23 @@ def test_cosmological_checks_on_host(lib, g, capfd, tmp_path):
         with pytest.raises(g.GravError) as e:
             g.launch_cosmological_simulation(lib, x.copy(), v.copy(), m, **kw)
         assert msg in str(e.value), (msg, str(e.value))
+
+
+def test_recorded_grav_sim_calls_match_the_abi():
+    """The launch_simulation_python calls recorded from grav_sim's Simulator
+    (tests/golden/dropin_calls.npz) have the 30 arguments of
+    src/python_interface.c:94-125 in grav_sim's types: the particle count and
+    exit flag by reference, four input arrays, four output pointers, one
+    output folder string and 19 scalars of the declared types."""
+    import json
+    import numpy as np
+    from conftest import cases, golden
+    for name, c in cases(golden("dropin_calls")).items():
+        spec = json.loads(bytes(c["spec.json"]).decode())
+        kinds = [a["kind"] for a in spec]
+        assert len(spec) == 30, name
+        assert kinds[0] == "byref" and kinds[28] == "byref", name
+        assert kinds[1:5] == ["array"] * 4 and kinds[5:9] == ["out_pointer"] * 4, name
+        assert kinds[20] == "bytes" and kinds.count("scalar") == 19, name
+        n = spec[0]["value"]
+        assert c["x"].shape == (n, 3) and c["m"].shape == (n,), name
