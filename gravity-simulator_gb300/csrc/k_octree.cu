@@ -521,6 +521,7 @@ __global__ void k_tree_links(const int *__restrict__ ctr, const int *__restrict_
 __device__ __forceinline__ void add_particles(const double *__restrict__ xm, int first, int count,
                                               double &M, double &S0, double &S1, double &S2)
 {
+#pragma unroll 4
     for (int p = first; p < first + count; ++p) {
         const double2 a = __ldg(reinterpret_cast<const double2 *>(xm + 4 * (size_t)p));
         const double2 b = __ldg(reinterpret_cast<const double2 *>(xm + 4 * (size_t)p) + 1);
@@ -709,6 +710,7 @@ __global__ void k_leaf_multipoles(const int *__restrict__ ctr, MultipoleArgs A,
         write_node_record(id, M, c0, c1, c2, A.t_depth[id], A.frame, A.na, A.nb, h, l);
         if (A.nq) {
             float Q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
             for (int p = fp; p < fp + np; ++p) {
                 const float4 a = pa[p], b = pb[p];
                 add_quad(Q, a.w, df_offset(a.x, b.x, h[0], l[0]), df_offset(a.y, b.y, h[1], l[1]),

@@ -67,6 +67,7 @@ __device__ void put_group(int2 *groups, int *gctr, int first, int count, int dep
 {
     const float4 oh = pa[first], ol = pb[first];
     float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f};
+#pragma unroll 8
     for (int p = first + 1; p < first + count; ++p) {
         const float4 ph = pa[p], pl = pb[p];
         const float r[3] = {(ph.x - oh.x) + (pl.x - ol.x), (ph.y - oh.y) + (pl.y - ol.y),
