@@ -147,6 +147,17 @@ def test_restatement_vs_reference_fresh(orc, wl):
                               reference.acceleration(x, m, 1.0, 3, theta=th, eps=0.01, leaf=leaf))
 
 
+@pytest.mark.skipif(not reference.available(), reason="reference library not built here")
+def test_restated_leapfrog_with_barnes_hut_vs_reference(orc, wl):
+    """The restated integrator with method 3 (Barnes-Hut, the reference's
+    quirks kept) against grav_sim's own launch_simulation with its Barnes-Hut:
+    the same state after 20 leapfrog steps, bit for bit."""
+    x, v, m = wl.galaxy_pair(1024, 17)
+    xo, vo = orc.fixed_step_run(4, 3, x, v, m, 1.0, 0.01, 1e-3, 0.02, bh=(0.5, 4, 1))
+    _, xr, vr, _ = reference.launch(x, v, m, 1.0, 4, 1e-3, 0.02, 3, theta=0.5, eps=0.01, leaf=4)
+    assert np.array_equal(xo, xr) and np.array_equal(vo, vr)
+
+
 def test_fixed_mode_tree_is_more_accurate(orc, wl):
     """With true leaf multipoles and own keys (fixed mode) the walk is far
     closer to the direct sum than the reference's walk (zero-mass leaves)."""
