@@ -2,6 +2,8 @@
 // small parameter helpers of grav_sim's C ABI.
 #include "gs_internal.h"
 
+#include <cufft.h>
+
 #include <atomic>
 
 #include <cmath>
@@ -384,6 +386,39 @@ int gsgpu_device_info(char *name, int len, int *sm_count, int *cc_major, int *cc
     if (cc_major) *cc_major = d->cc_major;
     if (cc_minor) *cc_minor = d->cc_minor;
     return 0;
+}
+
+// src/grav_sim.h:92 (src/grav_sim.c:630-700): what the library was built
+// with, in the reference's section layout (grav_sim's `python -m grav_sim`
+// and launch_simulation at normal verbosity print it).  This library's
+// facts: the device architecture, the CUDA runtime and cuFFT it was built
+// against, its own HDF5 snapshot writer.
+void print_compilation_info(void)
+{
+    const char *line = "-----------------------------------------------------------------\n";
+    std::fputs(line, stdout);
+    std::fputs("grav_sim force-evaluation path for GB300 (sm_103a)\n\n", stdout);
+#ifdef __linux__
+    std::fputs("Operating System: Linux\n", stdout);
+#else
+    std::fputs("Operating System: Unknown\n", stdout);
+#endif
+    std::fputs("Compilation Info:\n", stdout);
+    std::printf("  CUDA runtime: %d.%d\n", CUDART_VERSION / 1000, (CUDART_VERSION % 1000) / 10);
+    std::fputs("  Device code: sm_103a (no CPU fallback)\n", stdout);
+    std::fputs("  Compiled with OpenMP: false\n", stdout);
+    std::fputs("  HDF5 snapshots: true (written and read without libhdf5)\n", stdout);
+    int fft_version = 0;
+    if (cufftGetVersion(&fft_version) == CUFFT_SUCCESS)
+        std::printf("  Particle-mesh transforms: cuFFT %d\n", fft_version);
+    else
+        std::fputs("  Particle-mesh transforms: cuFFT\n", stdout);
+    std::fputs("\n", stdout);
+    std::printf("Build time: %s %s\n", __DATE__, __TIME__);
+#if defined(__GNUC__) && !defined(__clang__)
+    std::printf("Compiler: GCC (version: %d)\n", __GNUC__);
+#endif
+    std::fputs(line, stdout);
 }
 
 void free_memory_int32(int32_t *ptr) { std::free(ptr); }

@@ -1046,7 +1046,8 @@ ErrorStatus launch_simulation(System *system, IntegratorParam *integrator_param,
         return ok();
     }
 
-    if (settings->verbose >= 2) {
+    if (settings->verbose >= 2) {   // GRAV_VERBOSITY_NORMAL (src/grav_sim.c:111-121)
+        print_compilation_info();
         const DeviceInfo *d = nullptr;
         GS_TRY(device_info(&d));
         std::printf("grav_sim GB300 library: %s (%d SMs), method %d, integrator %d, N = %d\n",

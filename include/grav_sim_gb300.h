@@ -358,6 +358,9 @@ void compute_angular_momentum_python(double *angular_momentum,
 double compute_energy(const System *system);
 
 /* src/python_interface.c:8-16 */
+/* src/grav_sim.h:92: the build's facts (CUDA runtime, device code, cuFFT,
+ * the HDF5 writer), printed to stdout. */
+void print_compilation_info(void);
 void free_memory_int32(int32_t *ptr);
 void free_memory_double(double *ptr);
 /* src/python_interface.c:18-26.  Built-in initial conditions are host

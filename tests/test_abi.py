@@ -222,3 +222,15 @@ def test_recorded_grav_sim_calls_match_the_abi():
         assert kinds[20] == "bytes" and kinds.count("scalar") == 19, name
         n = spec[0]["value"]
         assert c["x"].shape == (n, 3) and c["m"].shape == (n,), name
+
+
+def test_print_compilation_info(lib, capfd):
+    """grav_sim's `python -m grav_sim` calls print_compilation_info
+    (grav_sim/__main__.py; src/grav_sim.h:92): it is exported and prints the
+    build's facts in the reference's sections, without touching a GPU."""
+    lib.print_compilation_info.restype = None
+    capfd.readouterr()
+    lib.print_compilation_info()
+    out = capfd.readouterr().out
+    assert "Operating System:" in out and "Compilation Info:" in out and "Build time:" in out
+    assert "sm_103a" in out
