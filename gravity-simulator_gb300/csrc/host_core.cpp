@@ -419,6 +419,7 @@ void print_compilation_info(void)
     std::printf("Compiler: GCC (version: %d)\n", __GNUC__);
 #endif
     std::fputs(line, stdout);
+    std::fflush(stdout);   // before any output of the caller's own runtime
 }
 
 void free_memory_int32(int32_t *ptr) { std::free(ptr); }
