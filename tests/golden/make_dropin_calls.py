@@ -5,7 +5,8 @@ grav_sim's package cannot travel to a machine without the reference sources,
 and a machine with them here has no GPU.  So this script runs grav_sim's
 unchanged ``GravitySimulatorAPI`` / ``Simulator.launch_simulation``
 (grav_sim/api.py, grav_sim/simulator.py:22-143) with this library loaded and
-the GPU method codes registered as INTEGRATION.md shows, and intercepts the
+the GPU method codes registered in grav_sim's method tables
+(grav_sim/parameters.py:21-35), and intercepts the
 one call it makes, ``launch_simulation_python`` (src/python_interface.c
 :94-192): every argument is recorded with the ctypes type grav_sim gave it,
 and the input arrays with their values.  The expected results come from the
