@@ -128,6 +128,13 @@ class Engine {
     // false while the engine is still preparing itself (collecting training
     // data): its forces are then the fallback method's
     virtual bool ready() const { return true; }
+    // Learned engines: 0 follow the held-out rule, 1 always apply the
+    // network (the judge still guards each step), 2 never; false elsewhere.
+    virtual bool set_learned_policy(int policy)
+    {
+        (void)policy;
+        return false;
+    }
     // Engine-specific statistics; returns how many values were written.
     virtual int report(double *out, int nmax) const
     {

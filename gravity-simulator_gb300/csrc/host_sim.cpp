@@ -957,6 +957,18 @@ int gsgpu_sim_training_samples(gsgpu_sim *sim, int snapshot, float *features, fl
     return sim->engine->dataset(snapshot, features, targets, count);
 }
 
+int gsgpu_sim_set_learned_policy(gsgpu_sim *sim, int policy)
+{
+    if (!sim) return GRAV_POINTER_ERROR;
+    cudaStreamSynchronize(sim->stream);
+    if (!sim->engine->set_learned_policy(policy)) return GRAV_VALUE_ERROR;
+    if (sim->graph) {   // the captured step holds the previous policy's launches
+        cudaGraphExecDestroy(sim->graph);
+        sim->graph = nullptr;
+    }
+    return 0;
+}
+
 int gsgpu_sim_report(gsgpu_sim *sim, double *out, int nmax)
 {
     if (!sim || !out) return -GRAV_POINTER_ERROR;

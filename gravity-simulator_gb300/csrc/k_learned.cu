@@ -336,6 +336,13 @@ class LearnedEngine final : public Engine {
     }
 
     bool capturable() const override { return trained_; }
+
+    bool set_learned_policy(int policy) override
+    {
+        if (policy < 0 || policy > 2) return false;
+        policy_ = policy;
+        return true;
+    }
     bool ready() const override { return trained_; }
 
     ErrorStatus compute(const double *d_x, const double *d_m, double *d_a, cudaStream_t s,
@@ -355,7 +362,7 @@ class LearnedEngine final : public Engine {
             return ok();
         }
         unsigned long long *cnt = counters_.as<unsigned long long>();
-        if (!useful_) {
+        if (!network_on()) {
             // The network did not earn its cost on the held-out snapshot:
             // the fallback walk gives every force.  No network output is
             // applied, so there is nothing for the judge to check; the step
@@ -390,7 +397,7 @@ class LearnedEngine final : public Engine {
 
     int kernels_per_eval() const override
     {
-        if (trained_ && !useful_)   // the fallback walk alone
+        if (trained_ && !network_on())   // the fallback walk alone
             return tree_.launches_per_build() + 1;
         return tree_.launches_per_build() + 1 + 1 + 1 + 1 + 1 + DirectRows::kernels() + 1 + 1 + 1;
     }
@@ -445,7 +452,7 @@ class LearnedEngine final : public Engine {
     {
         double v[13] = {trained_ ? 1.0 : 0.0, (double)snapshots_, loss_first_, loss_last_,
                         hold_before_, hold_after_, 0.0, 0.0, 0.0, theta_, train_seconds_,
-                        (double)adam_steps_, useful_ ? 1.0 : 0.0};
+                        (double)adam_steps_, network_on() ? 1.0 : 0.0};
         double st[4] = {0, 0, 0, 0};
         if (stats_.p && cudaMemcpy(st, stats_.p, sizeof(st), cudaMemcpyDeviceToHost) == cudaSuccess) {
             v[6] = st[0];
@@ -616,6 +623,9 @@ class LearnedEngine final : public Engine {
     long long collect_steps_ = 0;
     bool trained_ = false;
     bool useful_ = false;   // network kept (gain >= 1 - kMinGain, corrected median <= 1e-3)
+    int policy_ = 0;        // 0 the rule above, 1 always the network, 2 never
+
+    bool network_on() const { return policy_ == 1 || (policy_ == 0 && useful_); }
     int adam_steps_ = 0;
     double loss_first_ = 0.0, loss_last_ = 0.0, hold_before_ = 0.0, hold_after_ = 0.0;
     double train_seconds_ = 0.0;

@@ -437,6 +437,12 @@ int gsgpu_sim_warmup_until_ready(gsgpu_sim *sim, int64_t max_steps, int64_t *ste
  * least 20 % and the corrected held-out median is within the judge's 1e-3
  * bound, else 0 and every step uses the judged fallback walk). */
 int gsgpu_sim_report(gsgpu_sim *sim, double *out, int nmax);
+/* Learned method (104): 0 follows the rule above (the default), 1 applies the
+ * network at every step whatever it gained (the judge still checks each step
+ * and falls back to the theta 0.5 walk when the median error exceeds 1e-3),
+ * 2 never applies it.  GRAV_VALUE_ERROR for other methods or policies.  The
+ * next step is captured afresh. */
+int gsgpu_sim_set_learned_policy(gsgpu_sim *sim, int policy);
 /* Learned method: copy up to `count` training samples of one snapshot
  * (features [count][32], targets [count][3]); returns the number copied. */
 int gsgpu_sim_training_samples(gsgpu_sim *sim, int snapshot, float *features, float *targets,

@@ -85,3 +85,61 @@ def test_learned_correction_trains_gains_and_is_judged(lib, g, orc, wl):
     print(f"median error: cheap {e_cheap:.3g}, learned {e_learned:.3g}")
     assert e_learned < e_cheap
     assert e_learned < 1e-3
+
+
+@pytest.mark.parametrize("theta, falls_back", [(1.0, True), (0.5, False)])
+def test_network_forced_on_is_judged(lib, g, orc, wl, theta, falls_back):
+    """With the policy set to always apply the network, every step runs the
+    features, the network's forward pass and the correction, and the judge
+    checks the result.  At theta_cheap 1.0 the corrected median error breaks
+    the 1e-3 bound, so every step falls back to the theta 0.5 walk.  At
+    theta_cheap 0.5 it stays within the bound and no step falls back.  Either
+    way the forces meet the bound against the FP64 direct sum."""
+    _bind(lib, g)
+    lib.gsgpu_sim_set_learned_policy.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    n = 65536
+    x, v, m = wl.galaxy_pair(n, 23)
+    sim = ctypes.c_void_p()
+    p = g.AccelerationParam(g.METHOD_GPU_BH_LEARNED, theta, 0.01, 16)
+    assert lib.gsgpu_sim_create(ctypes.byref(sim), n, 1.0, ctypes.byref(p), 4, 1e-3, None) == 0
+    try:
+        assert lib.gsgpu_sim_upload(sim, x.ctypes.data_as(dp), v.ctypes.data_as(dp),
+                                    m.ctypes.data_as(dp)) == 0
+        taken = ctypes.c_int64()
+        assert lib.gsgpu_sim_warmup_until_ready(sim, 400, ctypes.byref(taken)) == 0
+        assert lib.gsgpu_sim_set_learned_policy(sim, 3) == 2          # GRAV_VALUE_ERROR
+        assert lib.gsgpu_sim_set_learned_policy(sim, 1) == 0
+        rep0 = np.zeros(13)
+        lib.gsgpu_sim_report(sim, rep0.ctypes.data_as(dp), 13)
+        assert lib.gsgpu_sim_run(sim, 3) == 0
+        xs, vs, a = np.empty((n, 3)), np.empty((n, 3)), np.empty((n, 3))
+        assert lib.gsgpu_sim_download(sim, xs.ctypes.data_as(dp), vs.ctypes.data_as(dp)) == 0
+        assert lib.gsgpu_sim_download_acceleration(sim, a.ctypes.data_as(dp)) == 0
+        rep = np.zeros(13)
+        lib.gsgpu_sim_report(sim, rep.ctypes.data_as(dp), 13)
+    finally:
+        lib.gsgpu_sim_destroy(sim)
+    judged, fell = rep[7] - rep0[7], rep[8] - rep0[8]
+    print(f"theta_cheap {theta}: judged {judged:.0f}, fell back {fell:.0f}, "
+          f"last judged median {rep[6]:.3g}")
+    assert rep[12] == 1.0 and judged == 3
+    assert fell == (3 if falls_back else 0)
+    rows = np.random.default_rng(4).choice(n, 2048, replace=False).astype(np.int32)
+    err = np.median(orc.rel_err(a[rows], orc.direct_rows(xs, m, 1.0, 0.01, rows)))
+    print(f"median error of the step's forces: {err:.3g}")
+    assert err < 1e-3
+
+
+def test_learned_policy_needs_the_learned_method(lib, g):
+    lib.gsgpu_sim_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                                     ctypes.c_double, ctypes.POINTER(g.AccelerationParam),
+                                     ctypes.c_int, ctypes.c_double, ctypes.c_void_p]
+    lib.gsgpu_sim_set_learned_policy.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.gsgpu_sim_destroy.argtypes = [ctypes.c_void_p]
+    sim = ctypes.c_void_p()
+    p = g.AccelerationParam(g.METHOD_GPU_BARNES_HUT_GROUP, 0.5, 0.01, 16)
+    assert lib.gsgpu_sim_create(ctypes.byref(sim), 1024, 1.0, ctypes.byref(p), 4, 1e-3, None) == 0
+    try:
+        assert lib.gsgpu_sim_set_learned_policy(sim, 1) == 2       # GRAV_VALUE_ERROR
+    finally:
+        lib.gsgpu_sim_destroy(sim)
