@@ -200,3 +200,38 @@ def test_stumpff_division_matches_ddiv(lib):
     for seed in (1, 2):
         assert lib.gsgpu_stumpff_division_selftest(1 << 26, seed, ctypes.byref(bad)) == 0
         assert bad.value == 0
+
+
+@pytest.mark.parametrize("pairwise", [False, True])
+def test_whfast_many_massive_bodies_match_oracle(g, lib, wl, orc, pairwise):
+    """Systems of 70 to 200 bodies that all have mass (the test particles of
+    the planetary model given masses of 1e-12 to 1e-10 Msun): the Jacobi ->
+    Cartesian recurrence has more than 64 massive slots, so it runs as one
+    whole chain per system (k_wh_seq_chain's general path), and eta after
+    each sort adds every slot.  Bit for bit against the oracle."""
+    G = wl.G_AU_MSUN_DAY
+    rng = np.random.default_rng(99 + int(pairwise))
+    systems = []
+    for x, v, m in wl.planetary_ensemble(60, 515 + int(pairwise), max_test=300):
+        if m.size < 70:
+            continue
+        m = m.copy()
+        m[9:] = 10.0 ** rng.uniform(-12, -10, m.size - 9)
+        systems.append((x[:200], v[:200], m[:200]))
+        if len(systems) == 8:
+            break
+    assert len(systems) >= 4
+    counts0, ids, x, v, m = _concat(systems)
+    dt, tf = 6.0, 120.0
+    ens = g.Ensemble(lib, counts0, G, integrator=WHFAST,
+                     method=GPU_PAIRWISE_FP64 if pairwise else GPU_MASSLESS, dt=dt)
+    ens.upload(ids, x, v, m)
+    ens.run_until(tf)
+    counts, ido, xo, vo, mo = ens.download()
+    assert np.array_equal(counts, counts0)
+    for s, (i_s, x_s, v_s, m_s) in enumerate(_blocks(counts0, counts, ido, xo, vo, mo)):
+        xs, vs, ms = systems[s]
+        ri, rx, rv, rm = orc.whfast_run(xs, vs, ms, G, 0.0, dt, tf, pairwise=pairwise)
+        assert np.array_equal(i_s, ri), s
+        assert np.array_equal(x_s, rx) and np.array_equal(v_s, rv), s
+    ens.close()
