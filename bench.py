@@ -20,7 +20,10 @@ Workloads (seeded synthetic inputs -- grav_sim publishes no dataset):
                     group walk at theta = 0.5 (method 106) and the
                     reference-style monopole walk (method 103) at theta =
                     0.5 and at theta = 0.3, where it meets the 1e-3 median
-                    error bound.
+                    error bound; and the learned pipeline at work: method
+                    104 at theta_cheap = 0.75 with the network forced on
+                    (features, forward pass, correction and judge every
+                    step) beside the plain group walk at theta = 0.75.
   plummer1024_fp64 -- the reference's CPU-sized case: Plummer N = 1,024, the
                     FP64 direct sum in the reference's order (bit-exact),
                     leapfrog dt = 1e-3; every step is one CUDA-graph replay.
@@ -140,7 +143,15 @@ WORKLOADS = {
                                            ("plain_monopole_theta0.5",
                                             dict(method=103, theta=0.5, leaf=1)),
                                            ("plain_monopole_theta0.3",
-                                            dict(method=103, theta=0.3, leaf=1))]),
+                                            dict(method=103, theta=0.3, leaf=1)),
+                                           # the learned pipeline at work: a cheap angle
+                                           # where the corrected error meets the bound,
+                                           # the network forced on, beside the plain walk
+                                           # at the same angle
+                                           ("learned_forced_theta0.75",
+                                            dict(method=104, theta=0.75, leaf=16, policy=1)),
+                                           ("plain_group_theta0.75",
+                                            dict(method=106, theta=0.75, leaf=16))]),
     "galaxy2097152_group": dict(ic="galaxy", n=2097152, seed=4, G=1.0, eps=0.01, dt=1e-3,
                                 integrator=4, method=106, theta=0.5, leaf=16,
                                 flop_per_interaction=20),
@@ -411,6 +422,9 @@ def sim_arm(args, lib, g, wk, x, v, m, stream, flush, world, local, sample_clock
             assert lib.gsgpu_sim_warmup_until_ready(sim, 1000, ctypes.byref(spent)) == 0
             out["training_s"] = time.perf_counter() - t0
             out["training_steps"] = spent.value
+            if wk.get("policy") is not None:   # 1: the network at every step, judged
+                lib.gsgpu_sim_set_learned_policy.argtypes = [ctypes.c_void_p, ctypes.c_int]
+                assert lib.gsgpu_sim_set_learned_policy(sim, int(wk["policy"])) == 0
         # warm-up (includes the leapfrog half kick and graph capture)
         assert lib.gsgpu_sim_run(sim, args.warmup) == 0
         torch.cuda.synchronize()
@@ -508,6 +522,13 @@ def _arm_summary(wk, r, n):
          "ms_per_step": r["ms_per_step"], "particle_steps_per_s": n / (r["ms_per_step"] / 1e3),
          "median_rel_err": r["median_rel_err"], "p99_rel_err": r["p99_rel_err"],
          "walk_ms": r["mean_force_ms"], "interactions": r["interactions"]}
+    if wk["method"] == 104:
+        lr = r.get("learned_report", {})
+        d.update({"policy": wk.get("policy", 0), "network_in_use": lr.get("network_in_use"),
+                  "steps_judged": lr.get("steps_judged"),
+                  "steps_fallen_back": lr.get("steps_fallen_back"),
+                  "heldout_median_residual_before": lr.get("heldout_median_residual_before"),
+                  "heldout_median_residual_after": lr.get("heldout_median_residual_after")})
     return d
 
 
