@@ -24,6 +24,9 @@ Workloads (seeded synthetic inputs -- grav_sim publishes no dataset):
                     104 at theta_cheap = 0.75 with the network forced on
                     (features, forward pass, correction and judge every
                     step) beside the plain group walk at theta = 0.75.
+  galaxy1048576_learned_t075 -- that learned arm alone (method 104 at
+                    theta_cheap = 0.75, the network forced on), for its
+                    launch list.
   plummer1024_fp64 -- the reference's CPU-sized case: Plummer N = 1,024, the
                     FP64 direct sum in the reference's order (bit-exact),
                     leapfrog dt = 1e-3; every step is one CUDA-graph replay.
@@ -152,6 +155,10 @@ WORKLOADS = {
                                             dict(method=104, theta=0.75, leaf=16, policy=1)),
                                            ("plain_group_theta0.75",
                                             dict(method=106, theta=0.75, leaf=16))]),
+    # the learned pipeline alone (the headline's learned_forced_theta0.75 arm)
+    "galaxy1048576_learned_t075": dict(ic="galaxy", n=1048576, seed=5, G=1.0, eps=0.01,
+                                       dt=1e-3, integrator=4, method=104, theta=0.75, leaf=16,
+                                       policy=1, flop_per_interaction=20),
     "galaxy2097152_group": dict(ic="galaxy", n=2097152, seed=4, G=1.0, eps=0.01, dt=1e-3,
                                 integrator=4, method=106, theta=0.5, leaf=16,
                                 flop_per_interaction=20),

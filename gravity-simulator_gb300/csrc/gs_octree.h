@@ -103,8 +103,10 @@ ErrorStatus launch_bh_walk(const OctreeDevice &t, const double *d_x, double thet
 
 // Group walk with interaction lists (k_walk_group.cu): same counters and
 // gate as launch_bh_walk; needs a tree with true leaf multipoles (not compat).
+// The groups depend on the tree alone: a second walk of the same tree (another
+// angle) passes reuse_groups and keeps the first walk's list.
 ErrorStatus launch_bh_group_walk(const OctreeDevice &t, double theta, double eps, double G,
                                  double *d_a, unsigned long long *counters, cudaStream_t s,
-                                 const int *gate = nullptr);
+                                 const int *gate = nullptr, bool reuse_groups = false);
 
 }  // namespace gs

@@ -51,6 +51,7 @@
 #include "gs_ptx.cuh"
 
 #include <algorithm>
+#include <cfloat>
 #include <chrono>
 #include <cmath>
 #include <numeric>
@@ -83,15 +84,22 @@ constexpr float kTargetClip = 1.0f;
 
 }  // namespace
 
+// One thread per sampled particle, in FP32: positions and centres of mass
+// are the walk's double-float records relative to the frame centre (pa/pb
+// per sorted particle, na/nb per node), so a difference x - c is
+// (x_hi - c_hi) + (x_lo - c_lo), accurate to FP32 rounding of the result;
+// the logarithms of products and quotients are sums and differences of
+// logarithms, so no intermediate leaves the FP32 range that the walk's own
+// records already live in.
 __global__ void k_features(const int *__restrict__ ctr, int count, const int *__restrict__ pos,
                            const int *__restrict__ sidx,
                            const int *__restrict__ leaf_of, const int *__restrict__ t_parent,
-                           const int *__restrict__ t_nc, const int *__restrict__ t_fc,
-                           const int *__restrict__ t_depth, const double *__restrict__ t_mass,
-                           const double *__restrict__ t_com, const float4 *__restrict__ nq,
-                           const double *__restrict__ frame, const double *__restrict__ x,
-                           const double *__restrict__ m, const double *__restrict__ a_cheap,
-                           double G, float *__restrict__ feat)
+                           const int4 *__restrict__ nc, const int *__restrict__ t_depth,
+                           const float4 *__restrict__ na, const float4 *__restrict__ nb,
+                           const float4 *__restrict__ nq, const float4 *__restrict__ pa,
+                           const float4 *__restrict__ pb, const double *__restrict__ frame,
+                           const double *__restrict__ a_cheap, float log10G,
+                           float *__restrict__ feat)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= count || tree_failed(ctr)) return;
@@ -103,47 +111,53 @@ __global__ void k_features(const int *__restrict__ ctr, int count, const int *__
     int GP = t_parent[P];
     if (GP < 0) GP = P;
     const int dL = t_depth[L];
-    const double hL = frame[3] / (double)(1 << min(dL, 30));
-    const double hP = 2.0 * hL;
-    const double x0 = x[3 * id], x1 = x[3 * id + 1], x2 = x[3 * id + 2];
-    const double *cL = t_com + 3 * (size_t)L;
-    const double *cP = t_com + 3 * (size_t)P;
-    const double ML = fmax(t_mass[L], 1e-300), MP = fmax(t_mass[P], 1e-300);
+    const float W = (float)frame[3];
+    const float hL = ldexpf(W, -min(dL, 30));
+    const float hP = 2.0f * hL;
+    const float4 xh = pa[s], xl = pb[s];
+    const float4 aL = na[L], bL = nb[L], aP = na[P];
+    const float ML = fmaxf(aL.w, FLT_MIN), MP = fmaxf(aP.w, FLT_MIN);
     const float4 qL0 = nq[2 * (size_t)L], qL1 = nq[2 * (size_t)L + 1];
     const float4 qP0 = nq[2 * (size_t)P], qP1 = nq[2 * (size_t)P + 1];
-    const float QL[6] = {qL0.x, qL0.y, qL0.z, qL0.w, qL1.x, qL1.y};
-    const float QP[6] = {qP0.x, qP0.y, qP0.z, qP0.w, qP1.x, qP1.y};
     float f[MLP_IN];
-    f[0] = (float)((x0 - cL[0]) / hL);
-    f[1] = (float)((x1 - cL[1]) / hL);
-    f[2] = (float)((x2 - cL[2]) / hL);
-    f[3] = (float)(ML / MP);
-    const double a0 = a_cheap[3 * id], a1 = a_cheap[3 * id + 1], a2 = a_cheap[3 * id + 2];
-    const double am = sqrt(a0 * a0 + a1 * a1 + a2 * a2);
-    const double ia = am > 0.0 ? 1.0 / am : 0.0;
-    f[4] = (float)(a0 * ia);
-    f[5] = (float)(a1 * ia);
-    f[6] = (float)(a2 * ia);
-    const double nL = 1.0 / (ML * hL * hL), nP = 1.0 / (MP * hP * hP);
-    for (int q = 0; q < 6; ++q) f[7 + q] = (float)(QL[q] * nL);
-    f[13] = m[id] > 0.0 ? (float)(log(MP / m[id]) / 10.0) : 0.0f;
-    const double tiny = 1e-300;
-    const double W = frame[3], Mroot = fmax(t_mass[0], tiny);
-    f[14] = (float)(log10(fmax(am * hP * hP / (G * MP), tiny)) / 5.0);
-    f[15] = GP != P ? (float)(log10(fmax(t_mass[GP], tiny) / MP) / 3.0) : 0.0f;
-    f[16] = (float)(log10(fmax(am * W * W / (G * Mroot), tiny)) / 5.0);
-    for (int q = 0; q < 6; ++q) f[17 + q] = (float)(QP[q] * nP);
-    f[23] = (float)(log10(MP / (hP * hP * hP)) / 5.0);
+    const float ihL = 1.0f / hL, ihP = 0.5f * ihL;
+    f[0] = ((xh.x - aL.x) + (xl.x - bL.x)) * ihL;
+    f[1] = ((xh.y - aL.y) + (xl.y - bL.y)) * ihL;
+    f[2] = ((xh.z - aL.z) + (xl.z - bL.z)) * ihL;
+    f[3] = ML / MP;
+    const float a0 = (float)a_cheap[3 * id], a1 = (float)a_cheap[3 * id + 1],
+                a2 = (float)a_cheap[3 * id + 2];
+    const float am = norm3df(a0, a1, a2);
+    const float ia = am > 0.0f ? 1.0f / am : 0.0f;
+    f[4] = a0 * ia;
+    f[5] = a1 * ia;
+    f[6] = a2 * ia;
+    // Q / (M h^2) with h^2 = (h * h) rounded once; the products stay in range
+    // as long as M h^2 does, which holds for the walk's FP32 cells
+    const float nL = ihL * ihL / ML, nP = ihP * ihP / MP;
+    f[7] = qL0.x * nL; f[8] = qL0.y * nL; f[9] = qL0.z * nL;
+    f[10] = qL0.w * nL; f[11] = qL1.x * nL; f[12] = qL1.y * nL;
+    const float m = xh.w;
+    const float lgMP = log10f(MP), lghP = log10f(hP), lgam = log10f(fmaxf(am, FLT_MIN));
+    f[13] = m > 0.0f ? (lgMP - log10f(m)) * (2.302585093f / 10.0f) : 0.0f;
+    f[14] = (lgam + 2.0f * lghP - log10G - lgMP) / 5.0f;
+    f[15] = GP != P ? (log10f(fmaxf(na[GP].w, FLT_MIN)) - lgMP) / 3.0f : 0.0f;
+    const float Mroot = fmaxf(na[0].w, FLT_MIN);
+    f[16] = (lgam + 2.0f * log10f(W) - log10G - log10f(Mroot)) / 5.0f;
+    f[17] = qP0.x * nP; f[18] = qP0.y * nP; f[19] = qP0.z * nP;
+    f[20] = qP0.w * nP; f[21] = qP1.x * nP; f[22] = qP1.y * nP;
+    f[23] = (lgMP - 3.0f * lghP) / 5.0f;
     // the 8 nearest cells under GP (insertion into an ascending list)
     float near[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) near[c] = 4.0f;
-    const double ihP = 1.0 / hP;
     auto consider = [&](int node) {
         if (node == L) return;
-        const double *cc = t_com + 3 * (size_t)node;
-        const double d0 = x0 - cc[0], d1 = x1 - cc[1], d2 = x2 - cc[2];
-        const float d = (float)(sqrt(d0 * d0 + d1 * d1 + d2 * d2) * ihP);
+        const float4 ca = na[node], cb = nb[node];
+        const float d0 = (xh.x - ca.x) + (xl.x - cb.x);
+        const float d1 = (xh.y - ca.y) + (xl.y - cb.y);
+        const float d2 = (xh.z - ca.z) + (xl.z - cb.z);
+        const float d = sqrtf(d0 * d0 + d1 * d1 + d2 * d2) * ihP;
         if (!(d < near[7])) return;
         // slots above the insertion point shift up, the slot at it takes d
 #pragma unroll
@@ -152,16 +166,15 @@ __global__ void k_features(const int *__restrict__ ctr, int count, const int *__
         near[0] = d < near[0] ? d : near[0];
     };
     if (GP != L) {
-        const int nc = t_nc[GP], fc = t_fc[GP];
-        for (int c = 0; c < nc; ++c) {
-            const int u = fc + c;
-            const int nu = t_nc[u];
-            if (nu <= 0 || t_depth[u] >= dL) {
+        const int4 g = nc[GP];
+        for (int c = 0; c < g.y; ++c) {
+            const int u = g.x + c;
+            const int4 cu = nc[u];
+            if (cu.y <= 0 || t_depth[u] >= dL) {
                 consider(u);
                 continue;
             }
-            const int fu = t_fc[u];
-            for (int q = 0; q < nu; ++q) consider(fu + q);
+            for (int q = 0; q < cu.y; ++q) consider(cu.x + q);
         }
     }
 #pragma unroll
@@ -383,11 +396,12 @@ class LearnedEngine final : public Engine {
         if (timer) GS_TRY(timer->begin(s));
         GS_TRY(launch_bh_group_walk(tree_, theta_, eps_, G_, d_a, cnt, s));
         if (timer) GS_TRY(timer->end(s));
-        GS_TRY(features(nullptr, n_, feat_.as<float>(), d_x, d_m, d_a, s));
+        GS_TRY(features(nullptr, n_, feat_.as<float>(), d_a, s));
         GS_TRY(mlp_.forward(feat_.as<float>(), n_, pred_.as<float>(), s));
         k_correct<<<(n_ + 255) / 256, 256, 0, s>>>(n_, tree_.sidx.as<int>(), pred_.as<float>(), d_a);
         GS_TRY(judge(d_a, s));
-        GS_TRY(launch_bh_group_walk(tree_, kThetaFallback, eps_, G_, d_a, cnt, s, flag_.as<int>()));
+        GS_TRY(launch_bh_group_walk(tree_, kThetaFallback, eps_, G_, d_a, cnt, s, flag_.as<int>(),
+                                    true));
         k_replace_rows<<<(J_ + 255) / 256, 256, 0, s>>>(J_, ids_.as<int>(), a_rows_.as<double>(),
                                                         d_a);
         GS_CUDA(cudaGetLastError());
@@ -397,9 +411,13 @@ class LearnedEngine final : public Engine {
 
     int kernels_per_eval() const override
     {
+        // a group walk is two launches (group list, walk); the gated
+        // fallback reuses the cheap walk's list
         if (trained_ && !network_on())   // the fallback walk alone
-            return tree_.launches_per_build() + 1;
-        return tree_.launches_per_build() + 1 + 1 + 1 + 1 + 1 + DirectRows::kernels() + 1 + 1 + 1;
+            return tree_.launches_per_build() + 2;
+        // sample ids, judge rows, cheap walk, features, network, correction,
+        // judge, gated fallback walk, judged rows replaced
+        return tree_.launches_per_build() + 1 + DirectRows::kernels() + 2 + 1 + 1 + 1 + 1 + 1 + 1;
     }
 
     ErrorStatus check_status(cudaStream_t s) override
@@ -504,14 +522,15 @@ class LearnedEngine final : public Engine {
         return ok();
     }
 
-    ErrorStatus features(const int *pos, int count, float *out, const double *d_x,
-                         const double *d_m, const double *a_cheap, cudaStream_t s)
+    ErrorStatus features(const int *pos, int count, float *out, const double *a_cheap,
+                         cudaStream_t s)
     {
         k_features<<<(count + 127) / 128, 128, 0, s>>>(
-            tree_.ctr.as<int>(), count, pos, tree_.sidx.as<int>(), tree_.leaf_of.as<int>(), tree_.t_parent.as<int>(),
-            tree_.t_nc.as<int>(), tree_.t_fc.as<int>(), tree_.t_depth.as<int>(),
-            tree_.t_mass.as<double>(), tree_.t_com.as<double>(), tree_.w_nq.as<float4>(),
-            tree_.frame.as<double>(), d_x, d_m, a_cheap, G_, out);
+            tree_.ctr.as<int>(), count, pos, tree_.sidx.as<int>(), tree_.leaf_of.as<int>(),
+            tree_.t_parent.as<int>(), tree_.w_nc.as<int4>(), tree_.t_depth.as<int>(),
+            tree_.w_na.as<float4>(), tree_.w_nb.as<float4>(), tree_.w_nq.as<float4>(),
+            tree_.w_pa.as<float4>(), tree_.w_pb.as<float4>(), tree_.frame.as<double>(), a_cheap,
+            (float)std::log10(G_), out);
         GS_CUDA(cudaGetLastError());
         return ok();
     }
@@ -521,7 +540,7 @@ class LearnedEngine final : public Engine {
     {
         unsigned long long *cnt = counters_.as<unsigned long long>();
         GS_TRY(launch_bh_group_walk(tree_, theta_, eps_, G_, a_cheap_.as<double>(), cnt, s));
-        GS_TRY(launch_bh_group_walk(tree_, kThetaFallback, eps_, G_, d_a, cnt, s));
+        GS_TRY(launch_bh_group_walk(tree_, kThetaFallback, eps_, G_, d_a, cnt, s, nullptr, true));
         const long long stride = std::max(1, n_ / K_);
         const long long offset = ((long long)snapshots_ * 104729LL) % std::max(1LL, stride) +
                                  (long long)snapshots_ * 31LL;
@@ -532,7 +551,7 @@ class LearnedEngine final : public Engine {
                              a_rows_.as<double>(), s));
         float *f = data_feat_.as<float>() + (size_t)snapshots_ * K_ * MLP_IN;
         float *t = data_target_.as<float>() + (size_t)snapshots_ * K_ * MLP_OUT;
-        GS_TRY(features(pos_.as<int>(), K_, f, d_x, d_m, a_cheap_.as<double>(), s));
+        GS_TRY(features(pos_.as<int>(), K_, f, a_cheap_.as<double>(), s));
         const float clip = snapshots_ + 1 < kSnapshots ? kTargetClip : 3.0e38f;
         k_targets<<<(K_ + 255) / 256, 256, 0, s>>>(K_, ids_.as<int>(), a_cheap_.as<double>(),
                                                    a_rows_.as<double>(), clip, t);

@@ -52,10 +52,14 @@ constexpr uint32_t SM_TRAIN_END = SM_D1 + MLP_TILE * DW * 2;    // 147456
 constexpr uint32_t TM_Z1 = 0, TM_Z2 = 64, TM_Z3 = 128, TM_OUT = 192;
 constexpr uint32_t TM_DW1 = 256, TM_DW2 = 288, TM_DW3 = 352, TM_DW4 = 416;
 
-__device__ __forceinline__ float silu(float v) { return v / (1.0f + __expf(-v)); }
+// The quotients use the fast reciprocal (__fdividef, about 2 ulp) rather than
+// the IEEE division's longer sequence: the activations are rounded to BF16
+// (8 significant bits) right after.  For v < -88, 1 + exp(-v) is infinite and
+// the quotient is -0, the limit of SiLU.
+__device__ __forceinline__ float silu(float v) { return __fdividef(v, 1.0f + __expf(-v)); }
 __device__ __forceinline__ float silu_grad(float v)
 {
-    const float s = 1.0f / (1.0f + __expf(-v));
+    const float s = __fdividef(1.0f, 1.0f + __expf(-v));
     return s * (1.0f + v * (1.0f - s));
 }
 
@@ -188,8 +192,37 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t tmem_row, uint32_t col,
 
 }  // namespace
 
-// ------------------------------------------------------------------------
-__global__ void __launch_bounds__(128)
+// Forward-only plan: each hidden layer's MMA has completed (read its input
+// tile) before the epilogue writes the next activations, so one hidden tile
+// serves all three layers, and one 64-column accumulator all three hidden
+// GEMMs: 46 KB of shared memory and 128 TMEM columns per CTA, four CTAs per SM.
+constexpr uint32_t SM_FWD_H = SM_H1;
+constexpr uint32_t SM_FWD_END1 = SM_FWD_H + MLP_TILE * MLP_H * 2;   // 47104
+constexpr uint32_t TM_FWD_Z = 0, TM_FWD_OUT = 64, TM_FWD_COLS = 128;
+constexpr int FWD_CTAS_PER_SM = 4;
+
+// Features of sample row r (FP32, 32 per sample) -> registers; rows past n are zero.
+__device__ __forceinline__ void load_features(float *v, const float *__restrict__ feat,
+                                              long long base, int n, int r)
+{
+    const long long i = base + r;
+    if (i < n) {
+        const float4 *src = reinterpret_cast<const float4 *>(feat + i * MLP_IN);
+#pragma unroll
+        for (int q = 0; q < MLP_IN / 4; ++q) {
+            const float4 t = __ldcs(src + q);
+            v[4 * q] = t.x;
+            v[4 * q + 1] = t.y;
+            v[4 * q + 2] = t.z;
+            v[4 * q + 3] = t.w;
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < MLP_IN; ++q) v[q] = 0.0f;
+    }
+}
+
+__global__ void __launch_bounds__(128, FWD_CTAS_PER_SM)
 k_mlp_forward(const float *__restrict__ P, const float *__restrict__ feat, int n,
               float *__restrict__ pred, unsigned *__restrict__ status)
 {
@@ -198,7 +231,7 @@ k_mlp_forward(const float *__restrict__ P, const float *__restrict__ feat, int n
     __shared__ uint32_t taddr_s;
     __shared__ float bias[3 * MLP_H + MLP_OUT_PAD];
     const int tid = threadIdx.x, warp = tid >> 5;
-    if (warp == 0) tmem_alloc(&taddr_s, 256);
+    if (warp == 0) tmem_alloc(&taddr_s, TM_FWD_COLS);
     if (tid == 0) {
         mbar_init(&bar, 1);
         mbar_fence_init();
@@ -217,42 +250,48 @@ k_mlp_forward(const float *__restrict__ P, const float *__restrict__ feat, int n
     uint32_t phase = 0;
     bool ok = true;
     const int tiles = (n + MLP_TILE - 1) / MLP_TILE;
+    float v[MLP_IN];
+    if (blockIdx.x < tiles) load_features(v, feat, (long long)blockIdx.x * MLP_TILE, n, tid);
     for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
         const long long base = (long long)t * MLP_TILE;
-        stage_features(sm, feat, base, n, tid);
+#pragma unroll
+        for (int f = 0; f < MLP_IN; f += 8) store8(sm + SM_X, tid, f, MLP_IN, v + f);
         tc_sync();
         if (tid == 0) {
-            mma_forward(tmem + TM_Z1, s0 + SM_X, s0 + SM_W1, MLP_IN, MLP_H);
+            mma_forward(tmem + TM_FWD_Z, s0 + SM_X, s0 + SM_W1, MLP_IN, MLP_H);
+            umma_commit(&bar);
+        }
+        // the next tile's features are in flight while this tile's layers run
+        if (t + (int)gridDim.x < tiles)
+            load_features(v, feat, (long long)(t + gridDim.x) * MLP_TILE, n, tid);
+        if (!(ok = wait_mma(&bar, phase, status))) break;
+        tc_fence_after();
+        hidden_epilogue(trow, TM_FWD_Z, bias, sm + SM_FWD_H, tid);
+        tc_sync();
+        if (tid == 0) {
+            mma_forward(tmem + TM_FWD_Z, s0 + SM_FWD_H, s0 + SM_W2, MLP_H, MLP_H);
             umma_commit(&bar);
         }
         if (!(ok = wait_mma(&bar, phase, status))) break;
         tc_fence_after();
-        hidden_epilogue(trow, TM_Z1, bias, sm + SM_H1, tid);
+        hidden_epilogue(trow, TM_FWD_Z, bias + MLP_H, sm + SM_FWD_H, tid);
         tc_sync();
         if (tid == 0) {
-            mma_forward(tmem + TM_Z2, s0 + SM_H1, s0 + SM_W2, MLP_H, MLP_H);
+            mma_forward(tmem + TM_FWD_Z, s0 + SM_FWD_H, s0 + SM_W3, MLP_H, MLP_H);
             umma_commit(&bar);
         }
         if (!(ok = wait_mma(&bar, phase, status))) break;
         tc_fence_after();
-        hidden_epilogue(trow, TM_Z2, bias + MLP_H, sm + SM_H2, tid);
+        hidden_epilogue(trow, TM_FWD_Z, bias + 2 * MLP_H, sm + SM_FWD_H, tid);
         tc_sync();
         if (tid == 0) {
-            mma_forward(tmem + TM_Z3, s0 + SM_H2, s0 + SM_W3, MLP_H, MLP_H);
-            umma_commit(&bar);
-        }
-        if (!(ok = wait_mma(&bar, phase, status))) break;
-        tc_fence_after();
-        hidden_epilogue(trow, TM_Z3, bias + 2 * MLP_H, sm + SM_H3, tid);
-        tc_sync();
-        if (tid == 0) {
-            mma_forward(tmem + TM_OUT, s0 + SM_H3, s0 + SM_W4, MLP_H, MLP_OUT_PAD);
+            mma_forward(tmem + TM_FWD_OUT, s0 + SM_FWD_H, s0 + SM_W4, MLP_H, MLP_OUT_PAD);
             umma_commit(&bar);
         }
         if (!(ok = wait_mma(&bar, phase, status))) break;
         tc_fence_after();
         float o[16];
-        tmem_ld16(trow + TM_OUT, o);
+        tmem_ld16(trow + TM_FWD_OUT, o);
         const long long i = base + tid;
         if (i < n) {
             pred[3 * i + 0] = o[0] + bias[3 * MLP_H + 0];
@@ -265,7 +304,7 @@ k_mlp_forward(const float *__restrict__ P, const float *__restrict__ feat, int n
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, 256);
+    if (warp == 0) tmem_dealloc(tmem, TM_FWD_COLS);
 }
 
 // ------------------------------------------------------------------------
@@ -502,10 +541,10 @@ ErrorStatus MlpDevice::forward(const float *feat, int n, float *pred, cudaStream
     GS_TRY(device_info(&dev));
     // the attribute belongs to the current device: set on every call
     GS_CUDA(cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)SM_FWD_END));
+                                 (int)SM_FWD_END1));
     const int tiles = (n + MLP_TILE - 1) / MLP_TILE;
-    const int grid = std::min(tiles, dev->sm_count * 2);
-    k_mlp_forward<<<grid, 128, SM_FWD_END, s>>>(params.as<float>(), feat, n, pred,
+    const int grid = std::min(tiles, dev->sm_count * FWD_CTAS_PER_SM);
+    k_mlp_forward<<<grid, 128, SM_FWD_END1, s>>>(params.as<float>(), feat, n, pred,
                                                 status.as<unsigned>());
     GS_CUDA(cudaGetLastError());
     return ok();

@@ -314,7 +314,8 @@ class BarnesHutEngine final : public Engine {
         return ok();
     }
 
-    int kernels_per_eval() const override { return tree_.launches_per_build() + 1; }
+    // the group walk is two launches (group list, walk)
+    int kernels_per_eval() const override { return tree_.launches_per_build() + (group_ ? 2 : 1); }
 
     ErrorStatus check_status(cudaStream_t s) override
     {

@@ -580,7 +580,7 @@ k_bh_group(GroupWalkArgs A)
 
 ErrorStatus launch_bh_group_walk(const OctreeDevice &t, double theta, double eps, double G,
                                  double *d_a, unsigned long long *counters, cudaStream_t s,
-                                 const int *gate)
+                                 const int *gate, bool reuse_groups)
 {
     static_assert(sizeof(GroupShared) % 16 == 0, "group shared block alignment");
     const size_t smem = sizeof(GroupShared) * GW_WARPS;
@@ -610,10 +610,15 @@ ErrorStatus launch_bh_group_walk(const OctreeDevice &t, double theta, double eps
     w.gate = gate;
     w.groups = t.g_list.as<int2>();
     w.gctr = t.g_ctr.as<int>();
-    GS_CUDA(cudaMemsetAsync(t.g_ctr.p, 0, 2 * sizeof(int), s));
-    k_group_list<<<(t.cap_nodes + 255) / 256, 256, 0, s>>>(
-        t.ctr.as<int>(), t.w_nc.as<int4>(), t.t_depth.as<int>(), t.w_pa.as<float4>(),
-        t.w_pb.as<float4>(), t.frame.as<double>(), t.g_list.as<int2>(), w.gctr);
+    if (reuse_groups) {
+        // the list and its count stay; only the work-queue head restarts
+        GS_CUDA(cudaMemsetAsync(w.gctr + 1, 0, sizeof(int), s));
+    } else {
+        GS_CUDA(cudaMemsetAsync(t.g_ctr.p, 0, 2 * sizeof(int), s));
+        k_group_list<<<(t.cap_nodes + 255) / 256, 256, 0, s>>>(
+            t.ctr.as<int>(), t.w_nc.as<int4>(), t.t_depth.as<int>(), t.w_pa.as<float4>(),
+            t.w_pb.as<float4>(), t.frame.as<double>(), t.g_list.as<int2>(), w.gctr);
+    }
     // persistent: every SM filled once (computed once per device)
     const DeviceInfo *dev = nullptr;
     GS_TRY(device_info(&dev));
