@@ -608,38 +608,60 @@ struct MultipoleArgs {
 // of the FP32 rate here, and the walk uses FP32 quadrupoles).  Children's
 // values written by other threads of the same launch are read through L2
 // (__ldcg), after the fence that follows the arrival counter.
-__device__ void multipole_node(int ii, const MultipoleArgs &A)
+//
+// A node is computed by the four lanes of a group: lane j keeps one of the
+// four ordered sums (j = 0 the mass, j = 1..3 the sums of m x, m y, m z), so
+// a particle costs one FP64 multiply and one add for all four sums (lane 0
+// multiplies the mass by 1.0, which is exact: its sum is the plain mass sum),
+// and the three quotients are one division.  An FP64 warp instruction costs
+// the pipe a whole warp's time however few lanes it carries, and near the
+// root a single group climbs alone: this cuts the FP64 instructions on that
+// path from 7 to 2 per particle.  Each sum sees the same operands in the same
+// order as a one-thread loop would, so the values are the same bit for bit.
+__device__ void multipole_node4(int ii, int j, unsigned gmask, const MultipoleArgs &A)
 {
-    double M = 0.0, S0 = 0.0, S1 = 0.0, S2 = 0.0;
     const int fc = A.in_fc[ii];
-    const int nch = A.in_nchild[ii];
-    for (int c = fc; c < fc + nch; ++c) {
+    const int end = fc + A.in_nchild[ii];
+    double acc = 0.0;
+    for (int c = fc; c < end; ++c) {
         if (A.t_nc[c] > 0) {
-            const double *cs = A.in_sum + 4 * (size_t)A.t_int[c];
-            M = __dadd_rn(M, __ldcg(cs + 0));
-            S0 = __dadd_rn(S0, __ldcg(cs + 1));
-            S1 = __dadd_rn(S1, __ldcg(cs + 2));
-            S2 = __dadd_rn(S2, __ldcg(cs + 3));
+            acc = __dadd_rn(acc, __ldcg(A.in_sum + 4 * (size_t)A.t_int[c] + j));
         } else {
-            add_particles(A.xm, A.t_fp[c], A.t_np[c], M, S0, S1, S2);
+            const int p1 = A.t_fp[c] + A.t_np[c];
+#pragma unroll 4
+            for (int p = A.t_fp[c]; p < p1; ++p) {
+                const double *r = A.xm + 4 * (size_t)p;
+                const double mp = __ldg(r + 3);
+                const double xv = j == 0 ? 1.0 : __ldg(r + j - 1);
+                acc = __dadd_rn(acc, __dmul_rn(mp, xv));
+            }
         }
     }
-    double *ws = A.in_sum + 4 * (size_t)ii;
-    ws[0] = M;
-    ws[1] = S0;
-    ws[2] = S1;
-    ws[3] = S2;
+    A.in_sum[4 * (size_t)ii + j] = acc;
+    const double M = __shfl_sync(gmask, acc, 0, 4);
+    const double cj = __ddiv_rn(acc, M);   // lanes 1..3: coordinate j - 1 of the centre
     const int id = A.in_id[ii];
-    const double c0 = __ddiv_rn(S0, M), c1 = __ddiv_rn(S1, M), c2 = __ddiv_rn(S2, M);
-    A.t_mass[id] = M;
-    A.t_com[3 * id + 0] = c0;
-    A.t_com[3 * id + 1] = c1;
-    A.t_com[3 * id + 2] = c2;
+    float hj = 0.0f, lj = 0.0f;
+    if (j == 0) {
+        A.t_mass[id] = M;
+    } else {
+        A.t_com[3 * id + j - 1] = cj;
+        split_df(__dsub_rn(cj, A.frame[j - 1]), hj, lj);
+    }
     float h[3], l[3];
-    write_node_record(id, M, c0, c1, c2, A.t_depth[id], A.frame, A.na, A.nb, h, l);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        h[k] = __shfl_sync(gmask, hj, k + 1, 4);
+        l[k] = __shfl_sync(gmask, lj, k + 1, 4);
+    }
+    if (j == 0) {
+        A.na[id] = make_float4(h[0], h[1], h[2], (float)M);
+        A.nb[id] = make_float4(l[0], l[1], l[2], cell_side2(A.frame, A.t_depth[id]));
+    }
     if (A.nq) {
+        // every lane of the group forms the same sums; lane 0 stores them
         float Q[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        for (int c = fc; c < fc + nch; ++c) {
+        for (int c = fc; c < end; ++c) {
             const float4 ca = __ldcg(A.na + c), cb = __ldcg(A.nb + c);
             const float4 qa = __ldcg(A.nq + 2 * (size_t)c), qb = __ldcg(A.nq + 2 * (size_t)c + 1);
             add_quad(Q, ca.w, df_offset(ca.x, cb.x, h[0], l[0]), df_offset(ca.y, cb.y, h[1], l[1]),
@@ -651,22 +673,27 @@ __device__ void multipole_node(int ii, const MultipoleArgs &A)
             Q[4] += qb.x;
             Q[5] += qb.y;
         }
-        store_quad(A.nq, id, Q);
+        if (j == 0) store_quad(A.nq, id, Q);
     }
 }
 
-// All internal nodes in one launch, bottom-up.  A thread starts at each
-// internal node none of whose children is internal, computes it, and climbs:
-// it counts itself in the parent's arrival counter, and the thread that
+// All internal nodes in one launch, bottom-up.  A group of four lanes starts
+// at each internal node none of whose children is internal, computes it, and
+// climbs: it counts itself in the parent's arrival counter, and the group that
 // completes the count (the last of the parent's internal children to finish)
-// computes the parent.  Nothing waits: a thread that is not last stops.  Every
+// computes the parent.  Nothing waits: a group that is not last stops.  Every
 // node is computed once, by the same arithmetic in the same child order as a
-// level-by-level pass, so the sums are identical to it.
+// level-by-level pass, so the sums are identical to it.  Every decision below
+// is the same for the four lanes of a group (they share the node), so the
+// group's shuffles and barriers see all four.
 __global__ void __launch_bounds__(OT_THREADS) k_multipole_up(const int *__restrict__ ctr,
                                                              MultipoleArgs A)
 {
     const int ni = ctr[CTR_SAFE_INTERNAL];
-    for (int i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < ni; i0 += gridDim.x * blockDim.x) {
+    const int j = threadIdx.x & 3;
+    const unsigned gmask = 0xFu << ((threadIdx.x & 31) & ~3);
+    const int groups = (gridDim.x * blockDim.x) >> 2;
+    for (int i0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 2; i0 < ni; i0 += groups) {
         const int fc0 = A.in_fc[i0];
         const int nch0 = A.in_nchild[i0];
         bool bottom = true;
@@ -674,15 +701,20 @@ __global__ void __launch_bounds__(OT_THREADS) k_multipole_up(const int *__restri
         if (!bottom) continue;
         int ii = i0;
         for (;;) {
-            multipole_node(ii, A);
+            multipole_node4(ii, j, gmask, A);
             const int p = A.nd_parent[A.in_node[ii]];
             if (p < 0) break;
             const int fc = A.in_fc[p];
             const int nch = A.in_nchild[p];
             int internal = 0;
             for (int c = fc; c < fc + nch; ++c) internal += A.t_nc[c] > 0 ? 1 : 0;
+            // each lane's writes are visible before lane 0 counts the group in
             __threadfence();
-            if (atomicAdd(&A.in_arrive[p], 1) != internal - 1) break;
+            __syncwarp(gmask);
+            int arrived = 0;
+            if (j == 0) arrived = atomicAdd(&A.in_arrive[p], 1);
+            arrived = __shfl_sync(gmask, arrived, 0, 4);
+            if (arrived != internal - 1) break;
             __threadfence();
             ii = p;
         }
@@ -912,7 +944,9 @@ ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream
     if (!compat)
         k_leaf_multipoles<<<grid, OT_THREADS, 0, s>>>(ctr.as<int>(), A, w_pa.as<float4>(),
                                                       w_pb.as<float4>());
-    k_multipole_up<<<grid, OT_THREADS, 0, s>>>(ctr.as<int>(), A);
+    // four lanes per internal node: a larger grid, so that every node of a
+    // tree of up to about 2^16 internal nodes starts at once
+    k_multipole_up<<<dev->sm_count * 8, OT_THREADS, 0, s>>>(ctr.as<int>(), A);
     k_walk_nodes<<<grid, OT_THREADS, 0, s>>>(
         ctr.as<int>(), compat ? 1 : 0, frame.as<double>(), keys.as<uint64_t>(), sidx.as<int>(),
         t_np.as<int>(), t_nc.as<int>(), t_fp.as<int>(), t_fc.as<int>(), t_depth.as<int>(),
