@@ -212,6 +212,11 @@ void launch_rk_emb_combine(const double *x, const double *v, const double *xe, c
                            double *txe, double *tve, double *terms, const double *w,
                            const double *dtdw, int stages, double dt, double abs_tol,
                            double rel_tol, int len, cudaStream_t s);
+// Sum of count error terms on the device, in a fixed grouping (not the
+// reference's order): scratch holds kErrorSumScratch doubles, the sum lands in
+// scratch[kErrorSumScratch - 1].
+constexpr int kErrorSumScratch = 257;
+void launch_error_sum(const double *terms, long long count, double *scratch, cudaStream_t s);
 
 // ---- IAS15 (k_ias15.cu) ------------------------------------------------
 extern const double kIas15H[8];   // Gauss-Radau spacings

@@ -10,6 +10,7 @@
 // graph and replayed; a clamped last step is launched directly.
 #include "gs_internal.h"
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -18,6 +19,11 @@
 
 namespace gs {
 namespace {
+
+// How embedded Runge-Kutta runs add their error terms: 0 on the host in the
+// reference's order (bit-exact step control, the default), 1 on the device
+// (gsgpu_set_rk_error_sum).
+std::atomic<int> g_rk_error_sum{0};
 
 struct Frame {
     double c[3];
@@ -158,7 +164,7 @@ struct gsgpu_sim {
     int kernels_last = 0;
     // embedded Runge-Kutta (integrators 5-8) and IAS15 (9)
     double tolerance = -1.0, initial_dt = -1.0;
-    DBuf e_vk, e_xk, e_x1, e_v1, e_txe, e_tve, e_xs, e_terms;
+    DBuf e_vk, e_xk, e_x1, e_v1, e_txe, e_tve, e_xs, e_terms, e_esum;
     double *h_terms = nullptr;   // pinned host copy of the 6N error terms
     DBuf i_b0, i_b, i_g, i_e, i_F, i_a1, i_d7, i_max;
     unsigned long long *h_max = nullptr;   // pinned: two maxima
@@ -399,6 +405,7 @@ struct gsgpu_sim {
             status->num_steps = 0;
         }
         double *vk = e_vk.as<double>(), *xk = e_xk.as<double>();
+        const bool device_sum = g_rk_error_sum.load(std::memory_order_relaxed) == 1;
         while (t < tf) {
             GS_TRY(force(vk));
             GS_CUDA(cudaMemcpyAsync(xk, v.p, bytes3(), cudaMemcpyDeviceToDevice, stream));
@@ -417,12 +424,24 @@ struct gsgpu_sim {
                                   e_txe.as<double>(), e_tve.as<double>(), e_terms.as<double>(),
                                   T->b, dtdw, S, h, tolerance, tolerance, L, stream);
             GS_CUDA(cudaGetLastError());
-            GS_CUDA(cudaMemcpyAsync(h_terms, e_terms.p, (size_t)2 * L * sizeof(double),
-                                    cudaMemcpyDeviceToHost, stream));
-            GS_CUDA(cudaStreamSynchronize(stream));
-            GS_TRY(engine->check_status(stream));
             double sum = 0.0;
-            for (int k = 0; k < 2 * L; ++k) sum += h_terms[k];
+            if (device_sum) {
+                // one double comes back instead of the 6N terms; not the
+                // reference's order, so the step control is not bit-exact
+                launch_error_sum(e_terms.as<double>(), 2LL * L, e_esum.as<double>(), stream);
+                GS_CUDA(cudaGetLastError());
+                GS_CUDA(cudaMemcpyAsync(h_terms, e_esum.as<double>() + kErrorSumScratch - 1,
+                                        sizeof(double), cudaMemcpyDeviceToHost, stream));
+                GS_CUDA(cudaStreamSynchronize(stream));
+                GS_TRY(engine->check_status(stream));
+                sum = h_terms[0];
+            } else {
+                GS_CUDA(cudaMemcpyAsync(h_terms, e_terms.p, (size_t)2 * L * sizeof(double),
+                                        cudaMemcpyDeviceToHost, stream));
+                GS_CUDA(cudaStreamSynchronize(stream));
+                GS_TRY(engine->check_status(stream));
+                for (int k = 0; k < 2 * L; ++k) sum += h_terms[k];
+            }
             double error = std::sqrt(sum / (n * 3 * 2));
             if (error <= 1 || h <= tf * 1e-12) {
                 ++steps;
@@ -652,6 +671,7 @@ ErrorStatus sim_create(gsgpu_sim **out, int n, double G, const AccelerationParam
         DBuf *bufs[] = {&s->e_x1, &s->e_v1, &s->e_txe, &s->e_tve, &s->e_xs};
         for (DBuf *b : bufs) GS_TRY(b->reserve(b3));
         GS_TRY(s->e_terms.reserve(2 * b3));
+        GS_TRY(s->e_esum.reserve(kErrorSumScratch * sizeof(double)));
         GS_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&s->h_terms), 2 * b3,
                               cudaHostAllocDefault));
     } else if (integrator != INTEGRATOR_EULER && integrator != INTEGRATOR_EULER_CROMER &&
@@ -955,6 +975,13 @@ int gsgpu_sim_training_samples(gsgpu_sim *sim, int snapshot, float *features, fl
     if (!sim) return -GRAV_POINTER_ERROR;
     cudaStreamSynchronize(sim->stream);
     return sim->engine->dataset(snapshot, features, targets, count);
+}
+
+int gsgpu_set_rk_error_sum(int mode)
+{
+    if (mode != 0 && mode != 1) return GRAV_VALUE_ERROR;
+    gs::g_rk_error_sum.store(mode, std::memory_order_relaxed);
+    return 0;
 }
 
 int gsgpu_sim_set_learned_policy(gsgpu_sim *sim, int policy)

@@ -254,4 +254,50 @@ void launch_rk_emb_combine(const double *x, const double *v, const double *xe, c
                                                  cf, stages, dt, abs_tol, rel_tol, len);
 }
 
+// Sum of the embedded Runge-Kutta error terms on the device: each of
+// ES_BLOCKS x ES_THREADS threads adds its strided share in index order, each
+// block adds its threads' sums in a fixed tree, and one block adds the block
+// sums the same way.  The grouping depends on the count alone, so the result
+// is the same on every run; it is not the reference's one-by-one order (that
+// sum is reproduced on the host), but its rounding error is smaller.
+constexpr int ES_BLOCKS = 256, ES_THREADS = 256;
+
+__device__ __forceinline__ double block_tree_sum(double v, double *sh)
+{
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = ES_THREADS / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] = __dadd_rn(sh[threadIdx.x], sh[threadIdx.x + w]);
+        __syncthreads();
+    }
+    return sh[0];
+}
+
+__global__ void __launch_bounds__(ES_THREADS)
+k_error_sum_blocks(const double *__restrict__ terms, long long count, double *__restrict__ part)
+{
+    __shared__ double sh[ES_THREADS];
+    double acc = 0.0;
+    const long long stride = (long long)ES_BLOCKS * ES_THREADS;
+    for (long long i = (long long)blockIdx.x * ES_THREADS + threadIdx.x; i < count; i += stride)
+        acc = __dadd_rn(acc, terms[i]);
+    const double b = block_tree_sum(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = b;
+}
+
+__global__ void __launch_bounds__(ES_THREADS)
+k_error_sum_final(const double *__restrict__ part, double *__restrict__ out)
+{
+    __shared__ double sh[ES_THREADS];
+    const double b = block_tree_sum(part[threadIdx.x], sh);
+    if (threadIdx.x == 0) out[0] = b;
+}
+
+void launch_error_sum(const double *terms, long long count, double *scratch, cudaStream_t s)
+{
+    static_assert(ES_BLOCKS == ES_THREADS, "the final block adds one partial per thread");
+    k_error_sum_blocks<<<ES_BLOCKS, ES_THREADS, 0, s>>>(terms, count, scratch);
+    k_error_sum_final<<<1, ES_THREADS, 0, s>>>(scratch, scratch + ES_BLOCKS);
+}
+
 }  // namespace gs

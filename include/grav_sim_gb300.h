@@ -443,6 +443,17 @@ int gsgpu_sim_report(gsgpu_sim *sim, double *out, int nmax);
  * 2 never applies it.  GRAV_VALUE_ERROR for other methods or policies.  The
  * next step is captured afresh. */
 int gsgpu_sim_set_learned_policy(gsgpu_sim *sim, int policy);
+
+/* How the embedded Runge-Kutta integrators (5-8; src/integrator_rk_embedded.c
+ * :522-987 is the loop this replaces) add the 6N error terms of an attempt,
+ * for every run started after the call: 0 (the default) copies the terms to
+ * the host and adds them one by one in the reference's order, so the step
+ * control -- and the run -- equal the reference's bit for bit; 1 adds them on
+ * the device in a fixed grouping and copies one double back (no 6N-double copy
+ * and host loop per attempt; the sum's rounding differs from the reference's
+ * in the last bits, so accepted steps and step sizes may differ slightly).
+ * GRAV_VALUE_ERROR for other modes. */
+int gsgpu_set_rk_error_sum(int mode);
 /* Learned method: copy up to `count` training samples of one snapshot
  * (features [count][32], targets [count][3]); returns the number copied. */
 int gsgpu_sim_training_samples(gsgpu_sim *sim, int snapshot, float *features, float *targets,

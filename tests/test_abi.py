@@ -234,3 +234,14 @@ def test_print_compilation_info(lib, capfd):
     out = capfd.readouterr().out
     assert "Operating System:" in out and "Compilation Info:" in out and "Build time:" in out
     assert "sm_103a" in out
+
+
+def test_rk_error_sum_switch(lib, g):
+    """gsgpu_set_rk_error_sum takes 0 (the reference's order on the host,
+    the default) or 1 (on the device) and rejects other modes; it only sets a
+    flag, so it runs without a GPU."""
+    lib.gsgpu_set_rk_error_sum.argtypes = [ctypes.c_int]
+    assert lib.gsgpu_set_rk_error_sum(2) == g.GRAV_VALUE_ERROR
+    assert lib.gsgpu_set_rk_error_sum(-1) == g.GRAV_VALUE_ERROR
+    assert lib.gsgpu_set_rk_error_sum(1) == 0
+    assert lib.gsgpu_set_rk_error_sum(0) == 0

@@ -131,6 +131,42 @@ def test_rk_embedded_oracle_random(lib, g, orc, wl):
     assert np.array_equal(xo, xo_ref) and np.array_equal(vo, vo_ref)
 
 
+@pytest.mark.parametrize("n, method, integ, tf", [(2048, "METHOD_GPU_PAIRWISE_FP64", 6, 0.3),
+                                                  (1048576, "METHOD_GPU_MASSLESS", 5, 0.02)])
+def test_rk_embedded_device_error_sum(lib, g, wl, n, method, integ, tf):
+    """The device-side error sum (gsgpu_set_rk_error_sum(1)) gives the run of
+    the reference's host-side order to within the last bits of the step sizes
+    (positions and velocities within 1e-12), without the 6N-term copy and host
+    loop per attempt.  The second case is a million test particles around
+    eight massive bodies, where the force is cheap and that loop is most of an
+    attempt (both wall times printed)."""
+    import time
+    lib.gsgpu_set_rk_error_sum.argtypes = [ctypes.c_int]
+    if n <= 4096:
+        x, v, m = wl.plummer(n, 4242)
+    else:
+        x, v, m = wl.plummer(n, 4243)
+        m = np.zeros(n)
+        m[:8] = 1.0 / 8
+    kw = dict(integrator=integ, dt=1e-3, tf=tf, method=getattr(g, method),
+              softening_length=0.01, tolerance=1e-6)
+    out, wall = {}, {}
+    try:
+        for mode in (0, 1, 0, 1):   # each mode twice: the second run is timed warm
+            assert lib.gsgpu_set_rk_error_sum(mode) == 0
+            xs, vs = x.copy(), v.copy()
+            t0 = time.perf_counter()
+            g.launch_simulation(lib, xs, vs, m, 1.0, **kw)
+            wall[mode] = time.perf_counter() - t0
+            out[mode] = (xs, vs)
+    finally:
+        lib.gsgpu_set_rk_error_sum(0)
+    (x0, v0), (x1, v1) = out[0], out[1]
+    print(f"N={n}: host-order sum {wall[0]:.3f} s, device sum {wall[1]:.3f} s")
+    assert np.abs(x1 - x0).max() <= 1e-12 * np.abs(x0).max()
+    assert np.abs(v1 - v0).max() <= 1e-12 * np.abs(v0).max()
+
+
 def test_ias15_bitexact_golden(lib, g):
     """IAS15: the GPU predictor / corrector kernels with the host-side
     convergence test and step control reproduce the reference's run bit for
