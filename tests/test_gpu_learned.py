@@ -87,6 +87,47 @@ def test_learned_correction_trains_gains_and_is_judged(lib, g, orc, wl):
     assert e_learned < 1e-3
 
 
+def test_features_match_fp64_restatement(lib, g, orc, wl):
+    """The first training snapshot is taken at the initial positions, and with
+    N = 65,536 its rows are every particle in sorted order.  Its 32 features
+    (FP32 on the GPU) equal the FP64 restatement of their definition
+    (tests/learned_features.py) on the oracle's tree of the same positions,
+    given the cheap walk's accelerations (the group walk, method 106, at
+    theta 1.0 with the same tree), to within 2e-6 (1 + |feature|): FP32
+    rounding (2.3e-7 measured), far below the BF16 rounding (4e-3) the
+    network's input gets."""
+    import learned_features as lf
+    _bind(lib, g)
+    fp = ctypes.POINTER(ctypes.c_float)
+    lib.gsgpu_sim_training_samples.argtypes = [ctypes.c_void_p, ctypes.c_int, fp, fp,
+                                               ctypes.c_int]
+    n = 65536
+    x, v, m = wl.galaxy_pair(n, 21)
+    sim = ctypes.c_void_p()
+    p = g.AccelerationParam(g.METHOD_GPU_BH_LEARNED, 1.0, 0.01, 16)
+    assert lib.gsgpu_sim_create(ctypes.byref(sim), n, 1.0, ctypes.byref(p), 4, 1e-3, None) == 0
+    feat = np.empty((n, 32), dtype=np.float32)
+    targ = np.empty((n, 3), dtype=np.float32)
+    try:
+        assert lib.gsgpu_sim_upload(sim, x.ctypes.data_as(dp), v.ctypes.data_as(dp),
+                                    m.ctypes.data_as(dp)) == 0
+        assert lib.gsgpu_sim_run(sim, 1) == 0   # the first force records snapshot 0
+        k = lib.gsgpu_sim_training_samples(sim, 0, feat.ctypes.data_as(fp),
+                                           targ.ctypes.data_as(fp), n)
+        assert k == n
+    finally:
+        lib.gsgpu_sim_destroy(sim)
+    a_cheap = g.acceleration(lib, x, m, 1.0, g.METHOD_GPU_BARNES_HUT_GROUP, opening_angle=1.0,
+                             softening_length=0.01, max_num_particles_per_leaf=16)
+    T = orc.build_tree(x, m, 16, False)
+    ref = lf.features(T, x, m, 1.0, a_cheap)
+    diff = np.abs(feat.astype(np.float64) - ref)
+    scaled = diff / (1.0 + np.abs(ref))
+    print("largest scaled difference per feature:", np.array2string(scaled.max(0), precision=1))
+    assert np.all(np.isfinite(feat))
+    assert scaled.max() <= 2e-6, int(np.argmax(scaled.max(0)))
+
+
 @pytest.mark.parametrize("theta, falls_back", [(1.0, True), (0.5, False)])
 def test_network_forced_on_is_judged(lib, g, orc, wl, theta, falls_back):
     """With the policy set to always apply the network, every step runs the
