@@ -737,10 +737,10 @@ def run_ours(args, world, rank, local):
     if wk["method"] == 104:
         out["config"]["training_s"] = r.get("training_s")
         out["config"]["learned_report"] = r.get("learned_report")
-        out["e2e"]["note"] += ("; with method 104 a call of fewer than 253 steps runs only the "
-                               "collection phase (the fallback walk, and every 4th step a "
-                               "65,536-row training snapshot): the network is trained after "
-                               "the 64th snapshot of a call")
+        out["e2e"]["note"] += ("; with method 104 a leapfrog call of at most 252 steps ends "
+                               "before its network could be trained (after the 64th "
+                               "65,536-row snapshot, the 253rd force evaluation) and applied, "
+                               "so it skips the collection: every step is the fallback walk")
     if comparison:
         out["config"]["comparison"] = comparison
     if rank == 0:

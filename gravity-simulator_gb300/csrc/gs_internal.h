@@ -128,6 +128,10 @@ class Engine {
     // false while the engine is still preparing itself (collecting training
     // data): its forces are then the fallback method's
     virtual bool ready() const { return true; }
+    // The run will ask for at most evals forces (a one-shot run with a fixed
+    // step); an engine whose preparation could not finish within them may
+    // skip it.  Not called: no limit.
+    virtual void set_evaluation_budget(long long evals) { (void)evals; }
     // Learned engines: 0 follow the held-out rule, 1 always apply the
     // network (the judge still guards each step), 2 never; false elsewhere.
     virtual bool set_learned_policy(int policy)

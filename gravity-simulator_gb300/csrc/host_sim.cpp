@@ -1102,6 +1102,15 @@ ErrorStatus launch_simulation(System *system, IntegratorParam *integrator_param,
     std::unique_ptr<gsgpu_sim> sim(raw);
     sim->tolerance = integrator_param->tolerance;
     sim->initial_dt = integrator_param->initial_dt;
+    if (integ == INTEGRATOR_EULER || integ == INTEGRATOR_EULER_CROMER || integ == INTEGRATOR_RK4 ||
+        integ == INTEGRATOR_LEAPFROG) {
+        // force evaluations of this run: ceil(tf / dt) steps (the last one
+        // clamped), four per RK4 step, one more for leapfrog's initial force
+        const double steps = std::ceil(tf / integrator_param->dt);
+        if (steps >= 0.0 && steps < 1e15)
+            sim->engine->set_evaluation_budget((long long)steps * (integ == INTEGRATOR_RK4 ? 4 : 1) +
+                                               (integ == INTEGRATOR_LEAPFROG ? 1 : 0));
+    }
     GS_TRY(gs::sim_upload(sim.get(), system->x, system->v, system->m));
     GS_TRY(gs::sim_run_until(sim.get(), tf, simulation_status, settings->is_exit_ptr, &oc));
     GS_TRY(gs::sim_download(sim.get(), system->x, system->v));

@@ -348,7 +348,19 @@ class LearnedEngine final : public Engine {
         if (own_) cudaStreamDestroy(own_);
     }
 
-    bool capturable() const override { return trained_; }
+    bool capturable() const override { return trained_ || skip_collection(); }
+
+    // A one-shot run of at most (kSnapshots - 1) * kCollectStride + 1 force
+    // evaluations ends before the network could be applied once (the 64th
+    // snapshot is the 253rd evaluation, and training follows it): such a run
+    // skips the collection, and every force is the fallback walk -- the
+    // forces the collection steps give as well.
+    void set_evaluation_budget(long long evals) override { budget_ = evals; }
+    bool skip_collection() const
+    {
+        return !trained_ && budget_ >= 0 &&
+               budget_ <= (long long)(kSnapshots - 1) * kCollectStride + 1;
+    }
 
     bool set_learned_policy(int policy) override
     {
@@ -364,7 +376,7 @@ class LearnedEngine final : public Engine {
         GS_CUDA(cudaMemsetAsync(counters_.p, 0, 2 * sizeof(unsigned long long), s));
         if (!trained_) {
             GS_TRY(tree_.build(d_x, d_m, s));
-            if (collect_steps_++ % kCollectStride == 0) {
+            if (!skip_collection() && collect_steps_++ % kCollectStride == 0) {
                 GS_TRY(collect(d_x, d_m, d_a, s));
                 if (snapshots_ == kSnapshots) GS_TRY(train(s));
             } else {
@@ -413,7 +425,7 @@ class LearnedEngine final : public Engine {
     {
         // a group walk is two launches (group list, walk); the gated
         // fallback reuses the cheap walk's list
-        if (trained_ && !network_on())   // the fallback walk alone
+        if ((trained_ && !network_on()) || skip_collection())   // the fallback walk alone
             return tree_.launches_per_build() + 2;
         // sample ids, judge rows, cheap walk, features, network, correction,
         // judge, gated fallback walk, judged rows replaced
@@ -640,6 +652,7 @@ class LearnedEngine final : public Engine {
     cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
     int snapshots_ = 0;
     long long collect_steps_ = 0;
+    long long budget_ = -1;   // force evaluations the run asks for at most (-1: unknown)
     bool trained_ = false;
     bool useful_ = false;   // network kept (gain >= 1 - kMinGain, corrected median <= 1e-3)
     int policy_ = 0;        // 0 the rule above, 1 always the network, 2 never

@@ -87,6 +87,23 @@ def test_learned_correction_trains_gains_and_is_judged(lib, g, orc, wl):
     assert e_learned < 1e-3
 
 
+def test_short_run_is_the_fallback_walk(lib, g, wl):
+    """A launch_simulation run that ends before the network could be trained
+    (here 40 leapfrog steps) skips the collection: its forces are the
+    fallback walk's at every step, so the run equals method 106 at theta 0.5
+    bit for bit."""
+    x, v, m = wl.galaxy_pair(4096, 33)
+    out = {}
+    for method, theta in ((g.METHOD_GPU_BH_LEARNED, 1.0), (g.METHOD_GPU_BARNES_HUT_GROUP, 0.5)):
+        xs, vs = x.copy(), v.copy()
+        g.launch_simulation(lib, xs, vs, m, 1.0, integrator=4, dt=1e-3, tf=0.04, method=method,
+                            opening_angle=theta, softening_length=0.01,
+                            max_num_particles_per_leaf=16)
+        out[method] = (xs, vs)
+    a, b = out[g.METHOD_GPU_BH_LEARNED], out[g.METHOD_GPU_BARNES_HUT_GROUP]
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
 def test_features_match_fp64_restatement(lib, g, orc, wl):
     """The first training snapshot is taken at the initial positions, and with
     N = 65,536 its rows are every particle in sorted order.  Its 32 features
