@@ -37,6 +37,8 @@ __device__ __forceinline__ int tree_nodes(const int *ctr)
 }
 #endif
 
+constexpr int kMisplacedCap = 64;
+
 struct OctreeDevice {
     int n = 0;
     int cap_nodes = 0;   // node capacity
@@ -73,6 +75,12 @@ struct OctreeDevice {
     DBuf xm;                  // double[4n] in sorted order: x, y, z, m (the multipole sums' input)
     DBuf g_list;              // int2[n]: particle groups of the group walk (first, count)
     DBuf g_ctr;               // int[4]: group count, work-queue head
+    // Particles whose Morton coordinate left [0, 2^21) and was masked (the
+    // coordinate at the box maximum wraps to 0; a particle outside a given
+    // box): their key cell is not where they are.  misplaced: uint8[n] by
+    // particle id; mlist: int[1 + kMisplacedCap], the count and the sorted
+    // positions of the first kMisplacedCap of them.
+    DBuf misplaced, mlist;
     RadixSorter sorter;
 
     ErrorStatus setup(int n, int leaf_max, bool compat, bool quad = false);

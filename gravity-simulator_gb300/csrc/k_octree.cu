@@ -176,18 +176,22 @@ __device__ __forceinline__ uint64_t spread3(uint64_t v)
 
 // src/linear_octree.c:159-202
 __global__ void k_morton(const double *__restrict__ x, int n, const double *__restrict__ frame,
-                         uint64_t *__restrict__ keys, int *__restrict__ sidx)
+                         uint64_t *__restrict__ keys, int *__restrict__ sidx,
+                         unsigned char *__restrict__ misplaced)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint64_t k = 0;
+    bool out = false;   // a coordinate outside [0, 2^21) is masked: the key cell is elsewhere
     for (int d = 0; d < 3; ++d) {
         const double u = __dadd_rn(div_by_width(__dsub_rn(x[3 * i + d], frame[d]), frame), 0.5);
         const long long q = __double2ll_rz(__dmul_rn(u, 2097152.0));
+        out = out || q < 0 || q > 0x1fffffll;
         k |= spread3((uint64_t)q) << d;
     }
     keys[i] = k;
     sidx[i] = i;
+    misplaced[i] = out ? 1 : 0;
 }
 
 __global__ void k_tree_init(int *__restrict__ ctr, int n, int *__restrict__ nd_start,
@@ -784,11 +788,17 @@ __global__ void k_walk_nodes(const int *__restrict__ ctr, int compat, const doub
 __global__ void k_walk_particles(int n, const double *__restrict__ frame, const double *__restrict__ x,
                                  const double *__restrict__ m, const int *__restrict__ sidx,
                                  float4 *__restrict__ pa, float4 *__restrict__ pb,
-                                 double *__restrict__ xm)
+                                 double *__restrict__ xm,
+                                 const unsigned char *__restrict__ misplaced,
+                                 int *__restrict__ mlist)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     const int id = sidx[p];
+    if (misplaced[id]) {   // rare: the count, and the sorted positions of the first ones
+        const int at = atomicAdd(&mlist[0], 1);
+        if (at < kMisplacedCap) mlist[1 + at] = p;
+    }
     double2 *xo = reinterpret_cast<double2 *>(xm + 4 * (size_t)p);
     xo[0] = make_double2(x[3 * id + 0], x[3 * id + 1]);
     xo[1] = make_double2(x[3 * id + 2], m[id]);
@@ -831,6 +841,8 @@ ErrorStatus OctreeDevice::setup(int n_, int leaf_max_, bool compat_, bool quad_)
     GS_TRY(w_nb.reserve((size_t)cap * sizeof(float4)));
     GS_TRY(w_nc.reserve((size_t)cap * sizeof(int4)));
     GS_TRY(w_nkey.reserve((size_t)cap * sizeof(uint64_t)));
+    GS_TRY(misplaced.reserve((size_t)n));
+    GS_TRY(mlist.reserve((size_t)(1 + kMisplacedCap) * sizeof(int)));
     GS_TRY(w_pa.reserve((size_t)n * sizeof(float4)));
     GS_TRY(w_pb.reserve((size_t)n * sizeof(float4)));
     GS_TRY(xm.reserve((size_t)n * 4 * sizeof(double)));
@@ -867,7 +879,7 @@ ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream
     const int pb = (n + OT_THREADS - 1) / OT_THREADS;
     if (tm_morton) GS_TRY(tm_morton->begin(s));
     k_morton<<<pb, OT_THREADS, 0, s>>>(d_x, n, frame.as<double>(), keys.as<uint64_t>(),
-                                       sidx.as<int>());
+                                       sidx.as<int>(), misplaced.as<unsigned char>());
     if (tm_morton) GS_TRY(tm_morton->end(s));
     k_tree_init<<<1, 32, 0, s>>>(ctr.as<int>(), n, nd_start.as<int>(), nd_count.as<int>(),
                                  nd_depth.as<int>(), nd_parent.as<int>(), nd_rank.as<int>(),
@@ -938,9 +950,11 @@ ErrorStatus OctreeDevice::build(const double *d_x, const double *d_m, cudaStream
     A.nb = w_nb.as<float4>();
     A.nq = quad ? w_nq.as<float4>() : nullptr;
     // particle records first: the leaves' quadrupoles are formed from them
+    GS_CUDA(cudaMemsetAsync(mlist.p, 0, sizeof(int), s));
     k_walk_particles<<<pb, OT_THREADS, 0, s>>>(n, frame.as<double>(), d_x, d_m, sidx.as<int>(),
                                                w_pa.as<float4>(), w_pb.as<float4>(),
-                                               xm.as<double>());
+                                               xm.as<double>(), misplaced.as<unsigned char>(),
+                                               mlist.as<int>());
     if (!compat)
         k_leaf_multipoles<<<grid, OT_THREADS, 0, s>>>(ctr.as<int>(), A, w_pa.as<float4>(),
                                                       w_pb.as<float4>());

@@ -52,18 +52,10 @@ constexpr int GW_RESERVE = 8 * (OCT_MAX_LEVEL + 1);
 
 constexpr int GW_GROUP = 32;       // particles per group at most
 
-// Group list: one thread per node.  A cell with more than GW_GROUP
-// particles cuts each run of consecutive children of at most GW_GROUP
-// particles into pieces of GW_GROUP (a leaf with more is cut the same way);
-// the root is one group when it is small enough.  Entry: (first sorted particle,
-// count | depth << 8) with depth that of the cell the group lies in.
-// A group whose particles do not fit within the side of its cell (the
-// particles whose Morton coordinate wraps at the box maximum sit in a cell
-// on the far side) goes to the queue as single particles, so that no warp
-// walks a box-wide group and its walks spread over the warps.
-__device__ void put_group(int2 *groups, int *gctr, int first, int count, int depth,
-                          const float4 *__restrict__ pa, const float4 *__restrict__ pb,
-                          double box_length)
+// Whether the particles of [first, first + count) lie within the side of a
+// depth-`depth` cell, from their positions.
+__device__ bool group_extent_fits(int first, int count, int depth, const float4 *__restrict__ pa,
+                                  const float4 *__restrict__ pb, double box_length)
 {
     const float4 oh = pa[first], ol = pb[first];
     float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f};
@@ -79,7 +71,35 @@ __device__ void put_group(int2 *groups, int *gctr, int first, int count, int dep
     }
     const float ext = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
     const double side = box_length / (double)(2 << min(depth, OCT_MAX_LEVEL + 1));
-    if ((double)ext * (double)ext <= 1.0001 * side * side) {
+    return (double)ext * (double)ext <= 1.0001 * side * side;
+}
+
+// Group list: one thread per node.  A cell with more than GW_GROUP
+// particles cuts each run of consecutive children of at most GW_GROUP
+// particles into pieces of GW_GROUP (a leaf with more is cut the same way);
+// the root is one group when it is small enough.  Entry: (first sorted particle,
+// count | depth << 8) with depth that of the cell the group lies in.
+// A group whose particles do not fit within the side of its cell (the
+// particles whose Morton coordinate wraps at the box maximum sit in a cell
+// on the far side) goes to the queue as single particles, so that no warp
+// walks a box-wide group and its walks spread over the warps.
+//
+// A group's particles lie in one key cell, so it fits the cell's side unless
+// it holds a particle whose key cell is not where it is (misplaced).  With at
+// most kMisplacedCap of those (their sorted positions in mlist), only a group
+// that holds one has its extent measured; the others fit without reading
+// their particles.  With more, every group is measured.
+__device__ void put_group(int2 *groups, int *gctr, int first, int count, int depth,
+                          const float4 *__restrict__ pa, const float4 *__restrict__ pb,
+                          double box_length, const int *__restrict__ mlist, int nmis)
+{
+    bool measure = nmis > kMisplacedCap;
+    for (int k = 0; k < nmis && !measure; ++k) {
+        const int q = mlist[1 + k];
+        measure = q >= first && q < first + count;
+    }
+    const bool fits = !measure || group_extent_fits(first, count, depth, pa, pb, box_length);
+    if (fits) {
         groups[atomicAdd(&gctr[0], 1)] = make_int2(first, count | (depth << 8));
     } else {
         const int at = atomicAdd(&gctr[0], count);
@@ -87,25 +107,28 @@ __device__ void put_group(int2 *groups, int *gctr, int first, int count, int dep
     }
 }
 
+
 __global__ void k_group_list(const int *__restrict__ ctr, const int4 *__restrict__ nc,
                              const int *__restrict__ depth, const float4 *__restrict__ pa,
                              const float4 *__restrict__ pb, const double *__restrict__ frame,
-                             int2 *__restrict__ groups, int *__restrict__ gctr)
+                             const int *__restrict__ mlist, int2 *__restrict__ groups,
+                             int *__restrict__ gctr)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= tree_nodes(ctr)) return;   // no groups from an overflowed build
     const double bl = frame[4];
+    const int nmis = mlist[0];
     const int4 ci = nc[c];   // (first child, children, first particle, particles)
     if (ci.w <= 0) return;
     const int d = depth[c];
     if (c == 0 && ci.w <= GW_GROUP) {
-        put_group(groups, gctr, ci.z, ci.w, d, pa, pb, bl);
+        put_group(groups, gctr, ci.z, ci.w, d, pa, pb, bl, mlist, nmis);
         return;
     }
     if (ci.w <= GW_GROUP) return;   // its own parent groups it
     if (ci.y <= 0) {                // oversized leaf (depth limit): runs of GW_GROUP
         for (int b = 0; b < ci.w; b += GW_GROUP)
-            put_group(groups, gctr, ci.z + b, min(GW_GROUP, ci.w - b), d, pa, pb, bl);
+            put_group(groups, gctr, ci.z + b, min(GW_GROUP, ci.w - b), d, pa, pb, bl, mlist, nmis);
         return;
     }
     // Runs of consecutive children of at most GW_GROUP particles each are
@@ -118,7 +141,8 @@ __global__ void k_group_list(const int *__restrict__ ctr, const int4 *__restrict
         const int4 ch = k < ci.y ? nc[ci.x + k] : make_int4(0, 0, 0, GW_GROUP + 1);
         if (ch.w > GW_GROUP) {   // a child walked as its own cell, or the end
             for (int b = 0; b < count; b += GW_GROUP)
-                put_group(groups, gctr, first + b, min(GW_GROUP, count - b), d, pa, pb, bl);
+                put_group(groups, gctr, first + b, min(GW_GROUP, count - b), d, pa, pb, bl, mlist,
+                          nmis);
             count = 0;
             continue;
         }
@@ -617,7 +641,8 @@ ErrorStatus launch_bh_group_walk(const OctreeDevice &t, double theta, double eps
         GS_CUDA(cudaMemsetAsync(t.g_ctr.p, 0, 2 * sizeof(int), s));
         k_group_list<<<(t.cap_nodes + 255) / 256, 256, 0, s>>>(
             t.ctr.as<int>(), t.w_nc.as<int4>(), t.t_depth.as<int>(), t.w_pa.as<float4>(),
-            t.w_pb.as<float4>(), t.frame.as<double>(), t.g_list.as<int2>(), w.gctr);
+            t.w_pb.as<float4>(), t.frame.as<double>(), t.mlist.as<int>(), t.g_list.as<int2>(),
+            w.gctr);
     }
     // persistent: every SM filled once (computed once per device)
     const DeviceInfo *dev = nullptr;
